@@ -1,0 +1,891 @@
+// gw_capi.cpp -- host runtime behind the C ABI (include/gw_gb300.h).
+//
+// Owns device memory for an ensemble of cells, converts between the reference's array layouts
+// and the engine's SoA planes, packs cells into thread-block clusters, and drives the engine
+// kernel in launches of up to steps_per_launch global steps.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gw_gb300.h"
+#include "gw_internal.h"
+
+using namespace gw;
+
+namespace {
+
+constexpr double kFaraday = 96.5;   // common.hpp:9
+constexpr double kGasConst = 8.314; // common.hpp:10
+
+thread_local std::string g_create_error;
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t n = 0;
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+    cudaError_t alloc(size_t bytes) {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = bytes;
+        if (bytes == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e == cudaSuccess) e = cudaMemset(p, 0, bytes);
+        return e;
+    }
+    template <typename T>
+    T *as() const {
+        return reinterpret_cast<T *>(p);
+    }
+};
+
+}  // namespace
+
+struct gw_ctx {
+    int device = 0;
+    int precision = GW_PRECISION_FP64;
+    bool ode64 = true;
+    int n_cells = 0;
+    uint64_t seed = 0;
+    int event_cap = 65536;
+    int steps_per_launch = 1000;
+    std::vector<int32_t> ncru;
+    std::vector<int64_t> slot0;
+    int64_t n_slots = 0;
+    std::vector<CellStatic> cs;
+    std::vector<CellDyn> dyn_host;  // staging copy
+    std::vector<CtaWork> work;
+    LaunchShape shape{};
+    int ssa_warps = 0, tile_cap = 0, max_cta_cell = 1, n_clusters = 0;
+    size_t rsize = 8;  // bytes per Real
+    DevBuf d_cs, d_dyn, d_slot0, d_work, d_lcc, d_flags, d_ryr, d_cass, d_jlcc, d_cajsr, d_cajsr_lo,
+        d_events, d_status;
+    std::vector<DevBuf *> stim_bufs;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    gw_stats stats{};
+    std::string err;
+    ~gw_ctx() {
+        for (auto *b : stim_bufs) delete b;
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+int fail(gw_ctx *c, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c)
+        c->err = buf;
+    else
+        g_create_error = buf;
+    return code;
+}
+
+#define CK(ctx, call)                                                                          \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? GW_ERR_OUT_OF_MEMORY : GW_ERR_CUDA, \
+                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);  \
+    } while (0)
+
+// Constants ctor (GW_utils.tpp:67-116), FP64, reference expression order.
+void make_static(const gw_params &p, int nCRU, CellStatic &c) {
+    std::memset(&c, 0, sizeof c);
+    c.p = p;
+    c.RT_F = kGasConst * p.T / kFaraday;
+    c.F_RT = 1.0 / c.RT_F;
+    c.CRU_factor = (double)p.NCaRU / (double)nCRU;
+    c.CSA_FVcyto = p.CSA / (1000 * p.Vcyto * kFaraday);
+    c.VSS_Vcyto = p.VSS / p.Vcyto;
+    c.Vcyto_VNSR = p.Vcyto / p.VNSR;
+    c.VJSR_VNSR = p.VJSR / p.VNSR;
+    c.a = p.a;
+    c.gamma0 = p.gamma0;
+    c.gamma0a = c.gamma0 * p.a;
+    c.gamma0a2 = c.gamma0a * p.a;
+    c.gamma0a3 = c.gamma0a2 * p.a;
+    c.gamma0a4 = c.gamma0a3 * p.a;
+    c.binv = 1.0 / p.b;
+    c.omega = p.omega;
+    c.omega_b = c.omega * c.binv;
+    c.omega_b2 = c.omega_b * c.binv;
+    c.omega_b3 = c.omega_b2 * c.binv;
+    c.omega_b4 = c.omega_b3 * c.binv;
+    c.BSR_const = p.KBSR * p.BSRT;
+    c.BSL_const = p.KBSL * p.BSLT;
+    c.VSS_VJSR = p.VSS / p.VJSR;
+    c.CSQN_const = p.KCSQN * p.CSQNT;
+    c.JLCC_const = 2.0e6 * p.PCaL / p.VSS;
+    c.Cao_scaled = 0.341 * p.Cao;
+    c.Nao3 = p.Nao * p.Nao * p.Nao;
+    c.INaCa_const = 5000.0 * p.kNaCa /
+                    ((p.KmNa * p.KmNa * p.KmNa + p.Nao * p.Nao * p.Nao) * (p.KmCa + p.Cao));
+    c.sigma = (std::exp(p.Nao / 67.3) - 1.0) / 7.0;
+    c.INaK_const = p.INaKmax * p.Ko / (p.Ko + p.KmKo);
+    c.sqrtKo = std::sqrt(p.Ko);
+    c.PKv14_Csc = p.PKv14 / p.Csc;
+    c.Ito2_const = 1.0e9 * p.Pto2 * kFaraday * c.CRU_factor / p.CSA;
+    c.IK1_const = p.Ko / (p.Ko + p.KmK1);
+    c.ICaL_const = -1000.0 * (2.0 * kFaraday * p.VSS) * c.CRU_factor / p.CSA;
+    c.CMDN_const = p.KCMDN * p.CMDNT;
+}
+
+int byte_of(int v) { return v & 0xFF; }
+
+// Flux carry of the reference's ctor (GW.hpp:73-74): initialise_Jxfer / initialise_Jtr from the
+// default GlobalState and the ctor's CRU constants, summed over CRUs in order.
+void ctor_carry(const gw_params &p, int n, double &sum_jtr, double &sum_jxfer) {
+    gw_globals g;
+    gw_globals_default(&g);
+    const double jx = p.rxfer * (1.45370e-4 - g.Cai);
+    const double jt = p.rtr * (g.CaNSR - 0.908408);
+    sum_jtr = 0.0;
+    sum_jxfer = 0.0;
+    for (int i = 0; i < n; ++i) sum_jtr += jt;
+    for (int i = 0; i < 4 * n; ++i) sum_jxfer += jx;
+}
+
+// Launch shape: cluster size C, CRU tile per CTA and SSA warps per CTA.  A cell needs
+// ceil(ncru / tile) <= C CTAs.
+int plan_shape(gw_ctx *c, int cluster_req, int tile_req) {
+    const int max_n = *std::max_element(c->ncru.begin(), c->ncru.end());
+    int C = cluster_req > 0 ? cluster_req : 0;
+    int tile = tile_req > 0 ? tile_req : 0;
+    if (C == 0 && tile == 0) {
+        // Default: one CRU per SSA thread where possible, at most 16 CTAs per cell.
+        C = 1;
+        while (C < kMaxClusterCtas && (max_n + C - 1) / C > 32 * 15) C *= 2;
+        tile = (max_n + C - 1) / C;
+    } else if (C == 0) {
+        C = std::max(1, (max_n + tile - 1) / tile);
+    } else if (tile == 0) {
+        tile = (max_n + C - 1) / C;
+    }
+    tile = std::max(32, ((tile + 31) / 32) * 32);
+    if (C > kMaxClusterCtas || C < 1) return fail(c, GW_ERR_UNSUPPORTED, "cluster size %d not in [1,16]", C);
+    const int need = (max_n + tile - 1) / tile;
+    if (need > C)
+        return fail(c, GW_ERR_UNSUPPORTED, "a cell of %d CRUs needs %d CTAs of %d CRUs but the cluster has %d",
+                    max_n, need, tile, C);
+    c->ssa_warps = std::min(15, tile / 32);
+    c->tile_cap = tile;
+    // Pack cells (first-fit decreasing on CTA count) into clusters of C CTAs.
+    std::vector<int> order(c->n_cells);
+    for (int i = 0; i < c->n_cells; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return c->ncru[a] > c->ncru[b]; });
+    std::vector<int> used;                   // CTAs used per cluster
+    std::vector<std::vector<int>> members;   // cells per cluster
+    c->max_cta_cell = 1;
+    for (int cell : order) {
+        const int k = std::max(1, (c->ncru[cell] + tile - 1) / tile);
+        c->max_cta_cell = std::max(c->max_cta_cell, k);
+        size_t q = 0;
+        for (; q < used.size(); ++q)
+            if (used[q] + k <= C) break;
+        if (q == used.size()) {
+            used.push_back(0);
+            members.emplace_back();
+        }
+        members[q].push_back(cell);
+        used[q] += k;
+    }
+    c->n_clusters = (int)used.size();
+    c->work.assign((size_t)c->n_clusters * C, CtaWork{-1, 0, 0, 0, 0, 0, 0, 0});
+    for (int q = 0; q < c->n_clusters; ++q) {
+        int rank = 0;
+        for (int cell : members[q]) {
+            const int n = c->ncru[cell];
+            const int k = std::max(1, (n + tile - 1) / tile);
+            for (int r = 0; r < k; ++r) {
+                CtaWork &w = c->work[(size_t)q * C + rank + r];
+                w.cell = cell;
+                w.cru_begin = (int)((int64_t)n * r / k);
+                w.cru_count = (int)((int64_t)n * (r + 1) / k) - w.cru_begin;
+                w.rank_in_cell = r;
+                w.first = rank;
+                w.n_cta_cell = k;
+            }
+            rank += k;
+        }
+    }
+    c->shape.cluster = C;
+    c->shape.threads = (c->ssa_warps + 1) * 32;
+    c->shape.ctas = c->n_clusters * C;
+    c->shape.smem = c->precision == GW_PRECISION_FP64
+                        ? smem_bytes_fp64(c->ssa_warps, c->tile_cap, c->max_cta_cell)
+                        : smem_bytes_fp32(c->ssa_warps, c->tile_cap, c->max_cta_cell);
+    int dev_smem = 0;
+    cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+    if ((int)c->shape.smem > dev_smem)
+        return fail(c, GW_ERR_UNSUPPORTED, "shared memory %zu B per CTA exceeds %d B", c->shape.smem, dev_smem);
+    return GW_OK;
+}
+
+KernelArgs base_args(gw_ctx *c) {
+    KernelArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.work = c->d_work.as<CtaWork>();
+    a.cs = c->d_cs.as<CellStatic>();
+    a.dyn = c->d_dyn.as<CellDyn>();
+    a.slot0 = c->d_slot0.as<int64_t>();
+    a.n_slots = c->n_slots;
+    a.lcc = c->d_lcc.as<uint32_t>();
+    a.flags = c->d_flags.as<uint32_t>();
+    a.ryr = c->d_ryr.as<uint32_t>();
+    a.cass = c->d_cass.p;
+    a.jlcc = c->d_jlcc.p;
+    a.cajsr = c->d_cajsr.p;
+    a.cajsr_lo = c->d_cajsr_lo.as<float>();
+    a.seed = c->seed;
+    a.event_cap = c->event_cap;
+    a.n_cells = c->n_cells;
+    a.events = c->d_events.as<unsigned long long>();
+    a.status = c->d_status.as<int>();
+    a.ssa_warps = c->ssa_warps;
+    a.tile_cap = c->tile_cap;
+    a.max_cta_cell = c->max_cta_cell;
+    a.tr_cell = -1;
+    return a;
+}
+
+int check_cell(gw_ctx *c, int cell) {
+    if (!c) return GW_ERR_INVALID_ARGUMENT;
+    if (cell < 0 || cell >= c->n_cells) return fail(c, GW_ERR_INVALID_ARGUMENT, "cell %d out of range", cell);
+    return GW_OK;
+}
+
+int pull_dyn(gw_ctx *c) {
+    CK(c, cudaMemcpy(c->dyn_host.data(), c->d_dyn.p, sizeof(CellDyn) * c->n_cells, cudaMemcpyDeviceToHost));
+    return GW_OK;
+}
+int push_dyn(gw_ctx *c) {
+    CK(c, cudaMemcpy(c->d_dyn.p, c->dyn_host.data(), sizeof(CellDyn) * c->n_cells, cudaMemcpyHostToDevice));
+    return GW_OK;
+}
+
+// Copy one plane region [slot0, slot0 + n) of a device plane array (plane stride n_slots).
+template <typename T>
+int plane_get(gw_ctx *c, const DevBuf &b, int plane, int64_t s0, int64_t n, T *out) {
+    CK(c, cudaMemcpy(out, b.as<T>() + plane * c->n_slots + s0, sizeof(T) * n, cudaMemcpyDeviceToHost));
+    return GW_OK;
+}
+template <typename T>
+int plane_put(gw_ctx *c, DevBuf &b, int plane, int64_t s0, int64_t n, const T *in) {
+    CK(c, cudaMemcpy(b.as<T>() + plane * c->n_slots + s0, in, sizeof(T) * n, cudaMemcpyHostToDevice));
+    return GW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gw_abi_version(void) { return GW_ABI_VERSION; }
+
+void gw_params_default(gw_params *p) {
+    // GW_utils.hpp:40-156
+    *p = gw_params{310.0, 153.4, 25.84, 1.113, 22.26e-6, 0.2303e-6, 12500, 4.0, 138.0, 2.0, 150.0,
+                   20.0, 0.85, 2.0, 0.005, 7.0, 2.0, 1.9356, 0.44, 0.02158, 9.13e-13, 13.3156, 2.0,
+                   2.65e-15, 877.5, 250.0, 2.358e8, 9.6, 1.415e6, 13.65, 0.07, 93.385, 1.887e7,
+                   30.0, 2.358e6, 0.001235, 3.92, 200.0, 0.333, 20.0, 0.047, 0.00087, 1.124,
+                   0.0087, 13.5, 0.63, 0.05, 0.00238, 12.8, 0.024, 0.0266, 0.1348, 0.00271, 0.1389,
+                   0.5437, 0.02898, 0.08019, 0.04684, 0.04984, 3.37302e-4, 8.1948e-4, 5.374e-8,
+                   1.8936, 14.225, 158.574, 142.937, 6.7735, 15.621, 28.753, 524.576, 1.989e-7,
+                   1.8931, 0.006950, 0.01179, 0.08527, 0.002963, 0.0, 1.0571e-4, 0.0, 0.2001,
+                   0.3203, 13.509, 1151.765, 2.230, 12.0, 5.370, 5.240, 1.0e6, 3.0, 13.0, 0.002659,
+                   0.27, 87.5, 1.38, 0.2, 0.35, 0.901, 10.0, 1.5, 0.03, 0.0005, 0.0002536, 0.00264,
+                   20.0, 6.60e-5, 40.0, 0.04, 0.140, 0.070, 0.0002096, 0.0002096, 0.000260, 1.8,
+                   0.75, 0.75};
+}
+
+void gw_globals_default(gw_globals *g) {
+    // GW_utils.hpp:231-247
+    *g = gw_globals{-91.382, 10.0, 131.84, 1.45273e-4, 0.908882, 8.98282e-3, 0.137617, 5.33837e-4,
+                    0.996345, 0.997315, 2.04171e-4,
+                    {0.999503, 4.13720e-4, 7.27568e-5, 8.73984e-6, 1.36159e-6},
+                    {0.953060, 0.0253906, 2.53848e-4, 1.12796e-6, 1.87950e-9, 0.0151370,
+                     0.00517622, 8.96600e-4, 8.17569e-5, 2.24032e-6},
+                    {0.722328, 0.101971, 0.00539932, 1.27081e-4, 1.82742e-6, 0.152769, 0.00962328,
+                     0.00439043, 0.00195348, 0.00143629}};
+}
+
+void gw_globals_py_default(gw_globals *g) {
+    gw_globals_default(g);
+    g->CaLTRPN = 8.9282e-3;  // pyGW.cpp:37
+}
+
+int gw_create(const gw_ensemble_desc *d, gw_ctx **out) {
+    if (!d || !out) return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "null descriptor or output");
+    *out = nullptr;
+    if (d->n_cells <= 0 || !d->ncru || !d->params)
+        return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "n_cells must be > 0 with ncru and params");
+    if (d->precision != GW_PRECISION_FP64 && d->precision != GW_PRECISION_FP32)
+        return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "unknown precision %d", d->precision);
+    for (int i = 0; i < d->n_cells; ++i)
+        if (d->ncru[i] <= 0) return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "cell %d: nCRU must be > 0", i);
+    if (d->n_cells > (1 << 28)) return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "too many cells");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(nullptr, GW_ERR_NO_DEVICE, "no CUDA device");
+    if (d->device < 0 || d->device >= ndev) return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "bad device %d", d->device);
+    int major = 0, minor = 0;
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, d->device);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, d->device);
+    if (major != 10 || minor != 3)
+        return fail(nullptr, GW_ERR_NO_DEVICE, "device %d is sm_%d%d; this build targets sm_103a", d->device, major, minor);
+    gw_ctx *c = new gw_ctx;
+    c->device = d->device;
+    c->precision = d->precision;
+    c->ode64 = d->precision == GW_PRECISION_FP64 || d->ode_fp32_rhs == 0;
+    c->n_cells = d->n_cells;
+    c->seed = d->seed;
+    c->event_cap = d->event_cap > 0 ? d->event_cap : 65536;
+    c->steps_per_launch = d->steps_per_launch > 0 ? d->steps_per_launch : 1000;
+    c->rsize = c->precision == GW_PRECISION_FP64 ? 8 : 4;
+    c->ncru.assign(d->ncru, d->ncru + d->n_cells);
+    if (cudaSetDevice(c->device) != cudaSuccess) {
+        delete c;
+        return fail(nullptr, GW_ERR_CUDA, "cudaSetDevice failed");
+    }
+    int rc = plan_shape(c, d->cluster_ctas, d->cta_crus);
+    if (rc != GW_OK) {
+        g_create_error = c->err;
+        delete c;
+        return rc;
+    }
+    c->slot0.resize(c->n_cells);
+    int64_t s = 0;
+    for (int i = 0; i < c->n_cells; ++i) {
+        c->slot0[i] = s;
+        s += ((int64_t)c->ncru[i] + 31) / 32 * 32;
+    }
+    c->n_slots = s;
+    c->cs.resize(c->n_cells);
+    c->dyn_host.assign(c->n_cells, CellDyn{});
+    for (int i = 0; i < c->n_cells; ++i) {
+        const gw_params &p = d->params[d->params_per_cell ? i : 0];
+        make_static(p, c->ncru[i], c->cs[i]);
+        CellDyn &y = c->dyn_host[i];
+        std::memset(&y, 0, sizeof y);
+        gw_globals g;
+        gw_globals_default(&g);
+        std::memcpy(y.g, &g, sizeof g);
+        ctor_carry(p, c->ncru[i], y.sum_jtr, y.sum_jxfer);
+    }
+    auto alloc_all = [&]() -> int {
+        CK(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        CK(c, cudaEventCreate(&c->ev0));
+        CK(c, cudaEventCreate(&c->ev1));
+        CK(c, c->d_cs.alloc(sizeof(CellStatic) * c->n_cells));
+        CK(c, c->d_dyn.alloc(sizeof(CellDyn) * c->n_cells));
+        CK(c, c->d_slot0.alloc(sizeof(int64_t) * c->n_cells));
+        CK(c, c->d_work.alloc(sizeof(CtaWork) * c->work.size()));
+        CK(c, c->d_lcc.alloc(4 * c->n_slots));
+        CK(c, c->d_flags.alloc(4 * c->n_slots));
+        CK(c, c->d_ryr.alloc(4 * 6 * c->n_slots));
+        CK(c, c->d_cass.alloc(c->rsize * 4 * c->n_slots));
+        CK(c, c->d_jlcc.alloc(c->rsize * 4 * c->n_slots));
+        CK(c, c->d_cajsr.alloc(c->rsize * c->n_slots));
+        CK(c, c->d_cajsr_lo.alloc(4 * c->n_slots));
+        CK(c, c->d_events.alloc(sizeof(unsigned long long)));
+        CK(c, c->d_status.alloc(sizeof(int) * c->n_cells));
+        CK(c, cudaMemcpy(c->d_cs.p, c->cs.data(), sizeof(CellStatic) * c->n_cells, cudaMemcpyHostToDevice));
+        CK(c, cudaMemcpy(c->d_slot0.p, c->slot0.data(), sizeof(int64_t) * c->n_cells, cudaMemcpyHostToDevice));
+        CK(c, cudaMemcpy(c->d_work.p, c->work.data(), sizeof(CtaWork) * c->work.size(), cudaMemcpyHostToDevice));
+        return GW_OK;
+    };
+    rc = alloc_all();
+    if (rc == GW_OK) rc = push_dyn(c);
+    // The reference's ctor draws a random CRU state (GW_utils.tpp:210-218); draw it here too.
+    for (int i = 0; rc == GW_OK && i < c->n_cells; ++i) rc = gw_sample_initial_crus(c, i);
+    if (rc == GW_OK) {
+        int nclus = 0;
+        const int e = c->precision == GW_PRECISION_FP64 ? max_active_clusters_fp64(c->shape, c->ode64, &nclus)
+                                                        : max_active_clusters_fp32(c->shape, c->ode64, &nclus);
+        if (e != 0 || nclus < 1)
+            rc = fail(c, GW_ERR_UNSUPPORTED,
+                      "launch shape (cluster %d x %d threads, %zu B smem) cannot be resident (err %d, %d clusters)",
+                      c->shape.cluster, c->shape.threads, c->shape.smem, e, nclus);
+    }
+    if (rc != GW_OK) {
+        g_create_error = c->err;
+        delete c;
+        return rc;
+    }
+    c->stats.cluster_ctas = c->shape.cluster;
+    c->stats.cta_crus = c->tile_cap;
+    c->stats.threads_per_cta = c->shape.threads;
+    c->stats.n_clusters = c->n_clusters;
+    c->stats.ctas = c->shape.ctas;
+    *out = c;
+    return GW_OK;
+}
+
+int gw_destroy(gw_ctx *c) {
+    if (!c) return GW_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    delete c;
+    return GW_OK;
+}
+
+int gw_sample_initial_crus(gw_ctx *c, int cell) {
+    int rc = check_cell(c, cell);
+    if (rc) return rc;
+    cudaSetDevice(c->device);
+    KernelArgs a = base_args(c);
+    const int e = sample_initial_crus_dev(a, cell, c->ncru[cell], c->precision == GW_PRECISION_FP64, c->stream);
+    if (e != 0) return fail(c, GW_ERR_CUDA, "initial-state kernel: %s", cudaGetErrorString((cudaError_t)e));
+    CK(c, cudaStreamSynchronize(c->stream));
+    // JLCC = 0 and ClCh changed: refresh the JLCC / ClCh sums of the carry.
+    rc = pull_dyn(c);
+    if (rc) return rc;
+    std::vector<uint32_t> flags(c->ncru[cell]);
+    rc = plane_get(c, c->d_flags, 0, c->slot0[cell], c->ncru[cell], flags.data());
+    if (rc) return rc;
+    double cl = 0;
+    for (uint32_t f : flags) cl += __builtin_popcount((f >> 4) & 0xFu);
+    c->dyn_host[cell].sum_clch = cl;
+    c->dyn_host[cell].sum_jlcc = 0.0;
+    return push_dyn(c);
+}
+
+int gw_set_globals(gw_ctx *c, int cell, const gw_globals *g) {
+    int rc = check_cell(c, cell);
+    if (rc) return rc;
+    if (!g) return fail(c, GW_ERR_INVALID_ARGUMENT, "null globals");
+    cudaSetDevice(c->device);
+    if ((rc = pull_dyn(c))) return rc;
+    std::memcpy(c->dyn_host[cell].g, g, sizeof *g);
+    return push_dyn(c);
+}
+
+int gw_get_globals(gw_ctx *c, int cell, gw_globals *g) {
+    int rc = check_cell(c, cell);
+    if (rc) return rc;
+    if (!g) return fail(c, GW_ERR_INVALID_ARGUMENT, "null globals");
+    cudaSetDevice(c->device);
+    if ((rc = pull_dyn(c))) return rc;
+    std::memcpy(g, c->dyn_host[cell].g, sizeof *g);
+    return GW_OK;
+}
+
+int gw_set_crus(gw_ctx *c, int cell, const double *CaSS, const double *CaJSR, const int32_t *LCC,
+                const int32_t *LCCi, const int32_t *RyR, const int32_t *ClCh, const double *JLCC) {
+    int rc = check_cell(c, cell);
+    if (rc) return rc;
+    if (!CaSS || !CaJSR || !LCC || !LCCi || !RyR || !ClCh)
+        return fail(c, GW_ERR_INVALID_ARGUMENT, "null CRU array");
+    cudaSetDevice(c->device);
+    const int n = c->ncru[cell];
+    std::vector<uint32_t> lcc(n), flags(n), ryr(6 * (size_t)n);
+    double cl = 0, jl = 0;
+    for (int i = 0; i < n; ++i) {
+        uint32_t w = 0, f = 0;
+        for (int j = 0; j < 4; ++j) {
+            const int s = LCC[4 * i + j];
+            if (s < 1 || s > 12) return fail(c, GW_ERR_INVALID_ARGUMENT, "CRU %d subunit %d: LCC state %d not in 1..12", i, j, s);
+            const int li = LCCi[4 * i + j], ch = ClCh[4 * i + j];
+            if ((li != 0 && li != 1) || (ch != 0 && ch != 1))
+                return fail(c, GW_ERR_INVALID_ARGUMENT, "CRU %d subunit %d: LCC_inactivation/ClCh must be 0 or 1", i, j);
+            w |= (uint32_t)byte_of(s) << (8 * j);
+            f |= (uint32_t)li << j;
+            f |= (uint32_t)ch << (4 + j);
+            cl += ch;
+            for (int k = 0; k < 6; ++k) {
+                const int v = RyR[24 * i + 6 * j + k];
+                if (v < -128 || v > 127) return fail(c, GW_ERR_INVALID_ARGUMENT, "RyR count %d out of int8 range", v);
+                ryr[(size_t)k * n + i] |= (uint32_t)byte_of(v) << (8 * j);
+            }
+        }
+        lcc[i] = w;
+        flags[i] = f;
+    }
+    const int64_t s0 = c->slot0[cell];
+    if ((rc = plane_put(c, c->d_lcc, 0, s0, n, lcc.data()))) return rc;
+    if ((rc = plane_put(c, c->d_flags, 0, s0, n, flags.data()))) return rc;
+    for (int k = 0; k < 6; ++k)
+        if ((rc = plane_put(c, c->d_ryr, k, s0, n, ryr.data() + (size_t)k * n))) return rc;
+    std::vector<double> jv(4 * (size_t)n, 0.0);
+    if (JLCC) std::memcpy(jv.data(), JLCC, sizeof(double) * 4 * n);
+    for (double v : jv) jl += v;
+    if (c->precision == GW_PRECISION_FP64) {
+        std::vector<double> pl(n);
+        for (int j = 0; j < 4; ++j) {
+            for (int i = 0; i < n; ++i) pl[i] = CaSS[4 * i + j];
+            if ((rc = plane_put(c, c->d_cass, j, s0, n, pl.data()))) return rc;
+            for (int i = 0; i < n; ++i) pl[i] = jv[4 * i + j];
+            if ((rc = plane_put(c, c->d_jlcc, j, s0, n, pl.data()))) return rc;
+        }
+        if ((rc = plane_put(c, c->d_cajsr, 0, s0, n, CaJSR))) return rc;
+    } else {
+        std::vector<float> pl(n), lo(n);
+        for (int j = 0; j < 4; ++j) {
+            for (int i = 0; i < n; ++i) pl[i] = (float)CaSS[4 * i + j];
+            if ((rc = plane_put(c, c->d_cass, j, s0, n, pl.data()))) return rc;
+            for (int i = 0; i < n; ++i) pl[i] = (float)jv[4 * i + j];
+            if ((rc = plane_put(c, c->d_jlcc, j, s0, n, pl.data()))) return rc;
+        }
+        for (int i = 0; i < n; ++i) {
+            pl[i] = (float)CaJSR[i];
+            lo[i] = (float)(CaJSR[i] - (double)pl[i]);
+        }
+        if ((rc = plane_put(c, c->d_cajsr, 0, s0, n, pl.data()))) return rc;
+        if ((rc = plane_put(c, c->d_cajsr_lo, 0, s0, n, lo.data()))) return rc;
+    }
+    if ((rc = pull_dyn(c))) return rc;
+    c->dyn_host[cell].sum_clch = cl;
+    c->dyn_host[cell].sum_jlcc = jl;
+    return push_dyn(c);
+}
+
+int gw_get_crus(gw_ctx *c, int cell, double *CaSS, double *CaJSR, int32_t *LCC, int32_t *LCCi,
+                int32_t *RyR, int32_t *ClCh, double *JLCC) {
+    int rc = check_cell(c, cell);
+    if (rc) return rc;
+    cudaSetDevice(c->device);
+    CK(c, cudaStreamSynchronize(c->stream));
+    const int n = c->ncru[cell];
+    const int64_t s0 = c->slot0[cell];
+    std::vector<uint32_t> lcc(n), flags(n), ryr(6 * (size_t)n);
+    if ((rc = plane_get(c, c->d_lcc, 0, s0, n, lcc.data()))) return rc;
+    if ((rc = plane_get(c, c->d_flags, 0, s0, n, flags.data()))) return rc;
+    for (int k = 0; k < 6; ++k)
+        if ((rc = plane_get(c, c->d_ryr, k, s0, n, ryr.data() + (size_t)k * n))) return rc;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < 4; ++j) {
+            if (LCC) LCC[4 * i + j] = (int)((lcc[i] >> (8 * j)) & 0xFF);
+            if (LCCi) LCCi[4 * i + j] = (int)((flags[i] >> j) & 1);
+            if (ClCh) ClCh[4 * i + j] = (int)((flags[i] >> (4 + j)) & 1);
+            if (RyR)
+                for (int k = 0; k < 6; ++k) RyR[24 * i + 6 * j + k] = (int)(int8_t)((ryr[(size_t)k * n + i] >> (8 * j)) & 0xFF);
+        }
+    if (c->precision == GW_PRECISION_FP64) {
+        std::vector<double> pl(n);
+        for (int j = 0; j < 4; ++j) {
+            if (CaSS) {
+                if ((rc = plane_get(c, c->d_cass, j, s0, n, pl.data()))) return rc;
+                for (int i = 0; i < n; ++i) CaSS[4 * i + j] = pl[i];
+            }
+            if (JLCC) {
+                if ((rc = plane_get(c, c->d_jlcc, j, s0, n, pl.data()))) return rc;
+                for (int i = 0; i < n; ++i) JLCC[4 * i + j] = pl[i];
+            }
+        }
+        if (CaJSR && (rc = plane_get(c, c->d_cajsr, 0, s0, n, CaJSR))) return rc;
+    } else {
+        std::vector<float> pl(n), lo(n);
+        for (int j = 0; j < 4; ++j) {
+            if (CaSS) {
+                if ((rc = plane_get(c, c->d_cass, j, s0, n, pl.data()))) return rc;
+                for (int i = 0; i < n; ++i) CaSS[4 * i + j] = pl[i];
+            }
+            if (JLCC) {
+                if ((rc = plane_get(c, c->d_jlcc, j, s0, n, pl.data()))) return rc;
+                for (int i = 0; i < n; ++i) JLCC[4 * i + j] = pl[i];
+            }
+        }
+        if (CaJSR) {
+            if ((rc = plane_get(c, c->d_cajsr, 0, s0, n, pl.data()))) return rc;
+            if ((rc = plane_get(c, c->d_cajsr_lo, 0, s0, n, lo.data()))) return rc;
+            for (int i = 0; i < n; ++i) CaJSR[i] = (double)pl[i] + (double)lo[i];
+        }
+    }
+    return GW_OK;
+}
+
+int gw_set_flux_carry(gw_ctx *c, int cell, double sum_Jtr, double sum_Jxfer) {
+    int rc = check_cell(c, cell);
+    if (rc) return rc;
+    cudaSetDevice(c->device);
+    if ((rc = pull_dyn(c))) return rc;
+    c->dyn_host[cell].sum_jtr = sum_Jtr;
+    c->dyn_host[cell].sum_jxfer = sum_Jxfer;
+    return push_dyn(c);
+}
+
+int gw_get_flux_carry(gw_ctx *c, int cell, double *sum_Jtr, double *sum_Jxfer) {
+    int rc = check_cell(c, cell);
+    if (rc) return rc;
+    cudaSetDevice(c->device);
+    if ((rc = pull_dyn(c))) return rc;
+    if (sum_Jtr) *sum_Jtr = c->dyn_host[cell].sum_jtr;
+    if (sum_Jxfer) *sum_Jxfer = c->dyn_host[cell].sum_jxfer;
+    return GW_OK;
+}
+
+int gw_set_stimulus_pulse(gw_ctx *c, int cell, double start, double period, double duration,
+                          double amplitude) {
+    if (!c) return GW_ERR_INVALID_ARGUMENT;
+    if (cell >= c->n_cells) return fail(c, GW_ERR_INVALID_ARGUMENT, "cell %d out of range", cell);
+    if (!(duration >= 0.0) || !std::isfinite(start) || !std::isfinite(period) || !std::isfinite(amplitude))
+        return fail(c, GW_ERR_INVALID_ARGUMENT, "bad pulse train");
+    cudaSetDevice(c->device);
+    int rc = pull_dyn(c);
+    if (rc) return rc;
+    for (int i = 0; i < c->n_cells; ++i) {
+        if (cell >= 0 && i != cell) continue;
+        CellDyn &y = c->dyn_host[i];
+        y.stim_mode = STIM_PULSE;
+        y.stim_start = start;
+        y.stim_period = period;
+        y.stim_dur = duration;
+        y.stim_amp = amplitude;
+        y.stim_samples = nullptr;
+        y.stim_n = 0;
+    }
+    return push_dyn(c);
+}
+
+int gw_set_stimulus_samples(gw_ctx *c, int cell, const double *Istim, int64_t n) {
+    if (!c) return GW_ERR_INVALID_ARGUMENT;
+    if (cell >= c->n_cells) return fail(c, GW_ERR_INVALID_ARGUMENT, "cell %d out of range", cell);
+    if (n < 0 || (n > 0 && !Istim)) return fail(c, GW_ERR_INVALID_ARGUMENT, "bad stimulus samples");
+    cudaSetDevice(c->device);
+    DevBuf *b = new DevBuf;
+    c->stim_bufs.push_back(b);
+    CK(c, b->alloc(sizeof(double) * (size_t)std::max<int64_t>(n, 1)));
+    if (n > 0) CK(c, cudaMemcpy(b->p, Istim, sizeof(double) * n, cudaMemcpyHostToDevice));
+    int rc = pull_dyn(c);
+    if (rc) return rc;
+    for (int i = 0; i < c->n_cells; ++i) {
+        if (cell >= 0 && i != cell) continue;
+        CellDyn &y = c->dyn_host[i];
+        y.stim_mode = STIM_SAMPLES;
+        y.stim_samples = b->as<double>();
+        y.stim_n = n;
+    }
+    return push_dyn(c);
+}
+
+int gw_run(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_trace *tr) {
+    if (!c) return GW_ERR_INVALID_ARGUMENT;
+    if (!(dt > 0.0) || !std::isfinite(dt)) return fail(c, GW_ERR_INVALID_ARGUMENT, "dt must be > 0");
+    if (n_steps < 0) return fail(c, GW_ERR_INVALID_ARGUMENT, "n_steps must be >= 0");
+    if (record_every < 0) return fail(c, GW_ERR_INVALID_ARGUMENT, "record_every must be >= 0");
+    cudaSetDevice(c->device);
+    if (tr) tr->n_written = 0;
+    const bool recording = tr && record_every > 0 && tr->max_records > 0;
+    const int tr_cell = (recording && (tr->CaSS || tr->CaJSR || tr->LCC || tr->LCC_inactivation || tr->RyR || tr->ClCh))
+                            ? tr->cru_cell : -1;
+    if (tr_cell >= c->n_cells) return fail(c, GW_ERR_INVALID_ARGUMENT, "trace cell out of range");
+    {
+        // the RNG counter holds 32 bits of the step index
+        int rc = pull_dyn(c);
+        if (rc) return rc;
+        for (int i = 0; i < c->n_cells; ++i)
+            if (c->dyn_host[i].step + (uint64_t)n_steps > 0xFFFFFFFFull)
+                return fail(c, GW_ERR_INVALID_ARGUMENT, "more than 2^32 steps in one context");
+    }
+    const int chunk = c->steps_per_launch;
+    // Device trace buffers for the records of one launch.
+    const int rec_cap = recording ? (int)std::min<int64_t>(tr->max_records, chunk / record_every + 2) : 0;
+    DevBuf d_t, d_glob, d_tlcc, d_tflags, d_tryr, d_tcass, d_tcajsr;
+    int64_t stride = 0;
+    if (recording) {
+        CK(c, d_t.alloc(sizeof(double) * rec_cap));
+        CK(c, d_glob.alloc(sizeof(double) * kNumGlobals * (size_t)rec_cap * c->n_cells));
+        if (tr_cell >= 0) {
+            stride = ((int64_t)c->ncru[tr_cell] + 31) / 32 * 32;
+            CK(c, d_tlcc.alloc(4 * stride * rec_cap));
+            CK(c, d_tflags.alloc(4 * stride * rec_cap));
+            CK(c, d_tryr.alloc(4 * 6 * stride * rec_cap));
+            CK(c, d_tcass.alloc(c->rsize * 4 * stride * rec_cap));
+            CK(c, d_tcajsr.alloc(c->rsize * stride * rec_cap));
+        }
+    }
+    KernelArgs a = base_args(c);
+    a.dt = dt;
+    a.record_every = recording ? record_every : 0;
+    a.rec_cap = rec_cap;
+    a.tr_t = d_t.as<double>();
+    a.tr_glob = d_glob.as<double>();
+    a.tr_cell = tr_cell;
+    a.tr_cru_stride = stride;
+    a.tr_lcc = d_tlcc.as<uint32_t>();
+    a.tr_flags = d_tflags.as<uint32_t>();
+    a.tr_ryr = d_tryr.as<uint32_t>();
+    a.tr_cass = d_tcass.p;
+    a.tr_cajsr = d_tcajsr.p;
+    CK(c, cudaMemsetAsync(c->d_status.p, 0, sizeof(int) * c->n_cells, c->stream));
+    std::vector<double> h_t, h_glob;
+    std::vector<uint32_t> h_lcc, h_flags, h_ryr;
+    std::vector<unsigned char> h_cass, h_cajsr;
+    float total_ms = 0.f;
+    int64_t done = 0;
+    while (done < n_steps) {
+        const int n = (int)std::min<int64_t>(chunk, n_steps - done);
+        a.run_step0 = done;
+        a.n_steps = n;
+        // records of this launch: r in [r_lo, r_hi]
+        int64_t r_lo = 0, r_hi = -1;
+        if (recording) {
+            r_lo = (done + record_every - 1) / record_every;
+            r_hi = (done + n - 1) / record_every;
+            r_hi = std::min<int64_t>(r_hi, tr->max_records - 1);
+            a.rec_base = r_lo;
+        }
+        CK(c, cudaEventRecord(c->ev0, c->stream));
+        const int e = c->precision == GW_PRECISION_FP64 ? launch_engine_fp64(a, c->shape, c->stream, c->ode64)
+                                                        : launch_engine_fp32(a, c->shape, c->stream, c->ode64);
+        if (e != 0) return fail(c, GW_ERR_CUDA, "engine launch: %s", cudaGetErrorString((cudaError_t)e));
+        CK(c, cudaEventRecord(c->ev1, c->stream));
+        c->stats.launches++;
+        if (recording && r_hi >= r_lo) {
+            const int64_t nr = r_hi - r_lo + 1;
+            CK(c, cudaStreamSynchronize(c->stream));
+            h_t.resize(nr);
+            CK(c, cudaMemcpy(h_t.data(), d_t.p, sizeof(double) * nr, cudaMemcpyDeviceToHost));
+            if (tr->t)
+                for (int64_t r = 0; r < nr; ++r) tr->t[r_lo + r] = h_t[r];
+            if (tr->globals) {
+                h_glob.resize((size_t)kNumGlobals * rec_cap * c->n_cells);
+                CK(c, cudaMemcpy(h_glob.data(), d_glob.p, h_glob.size() * sizeof(double), cudaMemcpyDeviceToHost));
+                for (int cell = 0; cell < c->n_cells; ++cell)
+                    for (int64_t r = 0; r < nr; ++r)
+                        std::memcpy(tr->globals + ((int64_t)cell * tr->max_records + r_lo + r) * kNumGlobals,
+                                    h_glob.data() + ((int64_t)cell * rec_cap + r) * kNumGlobals,
+                                    sizeof(double) * kNumGlobals);
+            }
+            if (tr_cell >= 0) {
+                const int ncr = c->ncru[tr_cell];
+                h_lcc.resize(stride * nr);
+                h_flags.resize(stride * nr);
+                h_ryr.resize(6 * stride * nr);
+                h_cass.resize(c->rsize * 4 * stride * nr);
+                h_cajsr.resize(c->rsize * stride * nr);
+                CK(c, cudaMemcpy(h_lcc.data(), d_tlcc.p, 4 * stride * nr, cudaMemcpyDeviceToHost));
+                CK(c, cudaMemcpy(h_flags.data(), d_tflags.p, 4 * stride * nr, cudaMemcpyDeviceToHost));
+                CK(c, cudaMemcpy(h_ryr.data(), d_tryr.p, 4 * 6 * stride * nr, cudaMemcpyDeviceToHost));
+                CK(c, cudaMemcpy(h_cass.data(), d_tcass.p, c->rsize * 4 * stride * nr, cudaMemcpyDeviceToHost));
+                CK(c, cudaMemcpy(h_cajsr.data(), d_tcajsr.p, c->rsize * stride * nr, cudaMemcpyDeviceToHost));
+                for (int64_t r = 0; r < nr; ++r) {
+                    const int64_t R = r_lo + r;
+                    for (int i = 0; i < ncr; ++i) {
+                        const uint32_t w = h_lcc[r * stride + i], f = h_flags[r * stride + i];
+                        for (int j = 0; j < 4; ++j) {
+                            const int64_t o = (R * ncr + i) * 4 + j;
+                            if (tr->LCC) tr->LCC[o] = (int)((w >> (8 * j)) & 0xFF);
+                            if (tr->LCC_inactivation) tr->LCC_inactivation[o] = (int)((f >> j) & 1);
+                            if (tr->ClCh) tr->ClCh[o] = (int)((f >> (4 + j)) & 1);
+                            if (tr->RyR)
+                                for (int k = 0; k < 6; ++k)
+                                    tr->RyR[o * 6 + k] = (int)(int8_t)((h_ryr[(r * 6 + k) * stride + i] >> (8 * j)) & 0xFF);
+                            if (tr->CaSS) {
+                                const int64_t src = (r * 4 + j) * stride + i;
+                                tr->CaSS[o] = c->rsize == 8 ? reinterpret_cast<double *>(h_cass.data())[src]
+                                                            : (double)reinterpret_cast<float *>(h_cass.data())[src];
+                            }
+                        }
+                        if (tr->CaJSR) {
+                            const int64_t src = r * stride + i;
+                            tr->CaJSR[R * ncr + i] = c->rsize == 8 ? reinterpret_cast<double *>(h_cajsr.data())[src]
+                                                                   : (double)reinterpret_cast<float *>(h_cajsr.data())[src];
+                        }
+                    }
+                }
+            }
+            tr->n_written = std::max<int64_t>(tr->n_written, r_hi + 1);
+        }
+        CK(c, cudaEventSynchronize(c->ev1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        total_ms += ms;
+        done += n;
+    }
+    CK(c, cudaStreamSynchronize(c->stream));
+    CK(c, cudaGetLastError());
+    c->stats.kernel_ms += total_ms;
+    c->stats.steps += (uint64_t)n_steps;
+    unsigned long long ev = 0;
+    CK(c, cudaMemcpy(&ev, c->d_events.p, sizeof ev, cudaMemcpyDeviceToHost));
+    c->stats.events = ev;
+    std::vector<int> st(c->n_cells);
+    CK(c, cudaMemcpy(st.data(), c->d_status.p, sizeof(int) * c->n_cells, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < c->n_cells; ++i)
+        if (st[i] != 0) {
+            const char *what = st[i] == GW_ERR_EVENT_CAP ? "a CRU exceeded the per-step jump cap"
+                               : st[i] == GW_ERR_NERNST  ? "non-positive concentration in a Nernst potential"
+                               : st[i] == GW_ERR_NONFINITE ? "a global state variable became NaN/Inf"
+                                                           : "error";
+            return fail(c, st[i], "cell %d: %s", i, what);
+        }
+    return GW_OK;
+}
+
+int gw_get_time(gw_ctx *c, int cell, double *t, uint64_t *step) {
+    int rc = check_cell(c, cell);
+    if (rc) return rc;
+    cudaSetDevice(c->device);
+    if ((rc = pull_dyn(c))) return rc;
+    if (t) *t = c->dyn_host[cell].t;
+    if (step) *step = c->dyn_host[cell].step;
+    return GW_OK;
+}
+
+int gw_get_stats(gw_ctx *c, gw_stats *s) {
+    if (!c || !s) return GW_ERR_INVALID_ARGUMENT;
+    *s = c->stats;
+    return GW_OK;
+}
+
+int gw_last_error(gw_ctx *c, char *msg, size_t len) {
+    if (!msg || len == 0) return GW_ERR_INVALID_ARGUMENT;
+    const std::string &e = c ? c->err : g_create_error;
+    std::snprintf(msg, len, "%s", e.c_str());
+    return GW_OK;
+}
+
+int gw_simulate(const gw_params *p, int nCRU, double step_size, int64_t num_steps,
+                const double *Istim, int record_every, const double *init_CaSS,
+                const double *init_CaJSR, const int32_t *init_LCC,
+                const int32_t *init_LCC_inactivation, const int32_t *init_RyR,
+                const int32_t *init_ClCh, const gw_globals *init_globals, const char *prng,
+                uint64_t seed, int precision, gw_trace *trace) {
+    static const char *kEngines[] = {"mt19937",       "mt19937_64",    "xoshiro256+",
+                                     "xoshiro256++",  "xoshiro256**",  "xoroshiro128+",
+                                     "xoroshiro128++", "xoroshiro128**"};
+    bool ok = false;
+    for (const char *e : kEngines)
+        if (prng && std::strcmp(prng, e) == 0) ok = true;
+    if (!ok) return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "%s", prng ? prng : "(null)");
+    if (!p || nCRU <= 0 || num_steps < 0 || record_every <= 0 || !init_globals)
+        return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "bad arguments to gw_simulate");
+    gw_ensemble_desc d;
+    std::memset(&d, 0, sizeof d);
+    int32_t n = nCRU;
+    d.n_cells = 1;
+    d.ncru = &n;
+    d.params = p;
+    d.precision = precision;
+    d.seed = seed;
+    d.device = 0;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) d.device = dev;
+    gw_ctx *c = nullptr;
+    int rc = gw_create(&d, &c);
+    if (rc) return rc;
+    rc = gw_set_globals(c, 0, init_globals);
+    if (!rc) rc = gw_set_crus(c, 0, init_CaSS, init_CaJSR, init_LCC, init_LCC_inactivation, init_RyR, init_ClCh, nullptr);
+    if (!rc) rc = gw_set_stimulus_samples(c, 0, Istim, Istim ? num_steps : 0);
+    if (!rc) rc = gw_run(c, step_size, num_steps, record_every, trace);
+    if (rc) g_create_error = c->err;
+    gw_destroy(c);
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,26 @@
+// FP64 engine (reference semantics).  Compiled with -fmad=false so that products and sums round
+// as the reference's separate multiply and add do.
+#include "gw_engine.cuh"
+
+namespace gw {
+
+int launch_engine_fp64(const KernelArgs &a, const LaunchShape &s, void *stream, bool ode64) {
+    return dev::launch_engine<true>(a, s, stream, ode64);
+}
+size_t smem_bytes_fp64(int ssa_warps, int tile_cap, int max_cta_cell) {
+    return dev::smem_layout<double>(ssa_warps, tile_cap, max_cta_cell).total;
+}
+int max_active_clusters_fp64(const LaunchShape &s, bool ode64, int *out) {
+    return dev::max_active_clusters<true>(s, ode64, out);
+}
+int sample_initial_crus_dev(const KernelArgs &a, int cell, int ncru, int fp64, void *stream) {
+    const int threads = 256;
+    const int blocks = (ncru + threads - 1) / threads;
+    if (fp64)
+        dev::init_crus_kernel<true><<<blocks, threads, 0, (cudaStream_t)stream>>>(a, cell, ncru);
+    else
+        dev::init_crus_kernel<false><<<blocks, threads, 0, (cudaStream_t)stream>>>(a, cell, ncru);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace gw

@@ -1,0 +1,185 @@
+/*
+ * gw_gb300.h -- C ABI of the GB300 engine for the Greenstein-Winslow (2002) canine ventricular
+ * myocyte model: the per-CRU hybrid SSA and the FP64 global step, for one cell or an ensemble.
+ *
+ * The drop-in boundary is the reference's pybind11 module `GreensteinWinslow`
+ * (lukeoloughlin/GW-model, src/pyGW.cpp:160-344, src/pyGW.hpp), which src/model.py imports as
+ * build.GreensteinWinslow.  Each entry point below names the reference interface it replaces.
+ *
+ * Conventions
+ *  - Every call returns a gw_status (GW_OK == 0).  Nothing throws across this boundary.
+ *  - The caller owns every host pointer; the library owns device memory and copies in and out.
+ *  - A context is used by one host thread at a time.
+ *  - Arrays use the reference's layouts: CaSS [n][4] f64, CaJSR [n] f64, LCC / LCC_inactivation /
+ *    ClCh [n][4] int32, RyR [n][4][6] int32 (counts of the 5 RyRs per subunit in states 1..6).
+ *  - Random draws come from a counter-based stream (Philox4x32-10) keyed on
+ *    (seed, cell, CRU, step, draw #), so results do not depend on launch shape or thread count.
+ */
+#ifndef GW_GB300_H
+#define GW_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GW_ABI_VERSION 1
+
+/* Status codes. */
+typedef enum gw_status {
+    GW_OK = 0,
+    GW_ERR_INVALID_ARGUMENT = 1, /* bad size, pointer, option or PRNG name (Python: ValueError) */
+    GW_ERR_CUDA = 2,             /* a CUDA runtime call failed */
+    GW_ERR_NO_DEVICE = 3,        /* no usable sm_103 device */
+    GW_ERR_EVENT_CAP = 4,        /* a CRU exceeded the per-step jump cap */
+    GW_ERR_NONFINITE = 5,        /* a global state variable became NaN or Inf */
+    GW_ERR_NERNST = 6,           /* non-positive concentration in a Nernst potential (the reference
+                                    exits the process here, common.hpp:72-75) */
+    GW_ERR_UNSUPPORTED = 7,      /* the requested launch shape does not fit this device */
+    GW_ERR_OUT_OF_MEMORY = 8
+} gw_status;
+
+/* Arithmetic of the CRU state and the SSA.  The global ODE is FP64 in both. */
+typedef enum gw_precision {
+    GW_PRECISION_FP64 = 0, /* reference semantics, FP64 everywhere, 53-bit uniforms */
+    GW_PRECISION_FP32 = 1  /* FP32 CRU state and propensities, 24-bit uniforms */
+} gw_precision;
+
+/* Model parameters: GW::Parameters<double> (src/includes/GW_utils.hpp:38-160), same members in
+ * the same order, so a C++ caller may copy the reference struct member-wise. */
+typedef struct gw_params {
+    double T, CSA, Vcyto, VNSR, VJSR, VSS;
+    int NCaRU;
+    double Ko, Nao, Cao, Clo, Clcyto;
+    double f, g, f1, g1, a, b, gamma0, omega, PCaL, kfClCh, kbClCh, Pto2;
+    double k12, k21, k23, k32, k34, k43, k45, k54, k56, k65, k25, k52, rRyR;
+    double rxfer, rtr, riss, BSRT, KBSR, BSLT, KBSL, CSQNT, KCSQN, CMDNT, KCMDN;
+    double GNa, GKr, Kf, Kb, GKs;
+    double GKv43, alphaa0Kv43, aaKv43, betaa0Kv43, baKv43, alphai0Kv43, aiKv43, betai0Kv43, biKv43,
+        f1Kv43, f2Kv43, f3Kv43, f4Kv43, b1Kv43, b2Kv43, b3Kv43, b4Kv43;
+    double PKv14, alphaa0Kv14, aaKv14, betaa0Kv14, baKv14, alphai0Kv14, aiKv14, betai0Kv14, biKv14,
+        f1Kv14, f2Kv14, f3Kv14, f4Kv14, b1Kv14, b2Kv14, b3Kv14, b4Kv14;
+    double Csc, GK1, KmK1, GKp, kNaCa, KmNa, KmCa, ksat, eta, INaKmax, KmNai, KmKo, IpCamax,
+        KmpCa, GCab, GNab, kHTRPNp, kHTRPNm, kLTRPNp, kLTRPNm, HTRPNtot, LTRPNtot, Vmaxf, Vmaxr,
+        Kmf, Kmr, Hf, Hr;
+} gw_params;
+
+/* Global (whole-cell) state: GW::GlobalState<double> (GW_utils.hpp:229-252), same order. */
+typedef struct gw_globals {
+    double V, Nai, Ki, Cai, CaNSR, CaLTRPN, CaHTRPN, m, h, j, xKs;
+    double Kr[5];
+    double Kv43[10];
+    double Kv14[10];
+} gw_globals;
+
+/* Ensemble description for gw_create. */
+typedef struct gw_ensemble_desc {
+    int n_cells;
+    const int32_t *ncru;      /* [n_cells] CRUs simulated per cell (the reference's nCRU) */
+    const gw_params *params;  /* [n_cells] if params_per_cell, else [1] shared by all cells */
+    int params_per_cell;
+    int precision;            /* gw_precision */
+    uint64_t seed;
+    int device;               /* CUDA device ordinal */
+    int event_cap;            /* max jumps per CRU per step; 0 -> 65536 */
+    int cluster_ctas;         /* CTAs per thread-block cluster; 0 -> autotuned */
+    int cta_crus;             /* CRU capacity of one CTA; 0 -> autotuned */
+    int steps_per_launch;     /* global steps fused in one launch; 0 -> 1000 */
+    int ode_fp32_rhs;         /* GW_PRECISION_FP32 only: 1 evaluates the global right-hand side in
+                                 FP32 (state and Euler update stay FP64); 0 (default) keeps it FP64 */
+} gw_ensemble_desc;
+
+/* Optional recording for gw_run, mirroring record_state (pyGW.hpp:56-99): after step i of the
+ * run with i % record_every == 0, record r = i / record_every (for r < max_records). */
+typedef struct gw_trace {
+    int64_t max_records;
+    double *t;              /* [max_records] time after the step, or NULL */
+    double *globals;        /* [n_cells][max_records][36] gw_globals records, or NULL */
+    int cru_cell;           /* cell whose CRU arrays are recorded (below), if any */
+    double *CaSS;           /* [max_records][ncru][4], or NULL */
+    double *CaJSR;          /* [max_records][ncru] */
+    int32_t *LCC;           /* [max_records][ncru][4] */
+    int32_t *LCC_inactivation; /* [max_records][ncru][4] */
+    int32_t *RyR;           /* [max_records][ncru][4][6] */
+    int32_t *ClCh;          /* [max_records][ncru][4] */
+    int64_t n_written;      /* out: records written */
+} gw_trace;
+
+/* Run statistics. */
+typedef struct gw_stats {
+    uint64_t steps;          /* global steps taken by this context */
+    uint64_t launches;       /* engine kernel launches */
+    double kernel_ms;        /* device time of the engine kernels (CUDA events) */
+    uint64_t events;         /* SSA jumps (all CRUs, all cells) */
+    int cluster_ctas, cta_crus, threads_per_cta, n_clusters, ctas;
+} gw_stats;
+
+typedef struct gw_ctx gw_ctx;
+
+int gw_abi_version(void);
+
+/* Defaults of GW::Parameters (GW_utils.hpp:40-156), GW::GlobalState (GW_utils.hpp:231-247), and
+ * the Python-side GWGlobalState() (pyGW.cpp:31-76; CaLTRPN = 8.9282e-3). */
+void gw_params_default(gw_params *p);
+void gw_globals_default(gw_globals *g);
+void gw_globals_py_default(gw_globals *g);
+
+/* Replaces the GW_model constructor (GW.hpp:104-113) for every cell of an ensemble.  Cells start
+ * from GW::GlobalState defaults, CRU state from the reference's ctor constants, JLCC = 0 and the
+ * flux carry (sum Jtr, sum Jxfer) that the reference's ctor computes (GW.hpp:73-74). */
+int gw_create(const gw_ensemble_desc *desc, gw_ctx **out);
+int gw_destroy(gw_ctx *ctx);
+
+/* Replaces GW_model::set_initial_value (GW.tpp:6-10) for one cell.  JLCC may be NULL: the
+ * reference then keeps the ctor's JLCC, which is zero (GW.hpp:107-112). */
+int gw_set_globals(gw_ctx *ctx, int cell, const gw_globals *g);
+int gw_get_globals(gw_ctx *ctx, int cell, gw_globals *g);
+int gw_set_crus(gw_ctx *ctx, int cell, const double *CaSS, const double *CaJSR,
+                const int32_t *LCC, const int32_t *LCC_inactivation, const int32_t *RyR,
+                const int32_t *ClCh, const double *JLCC);
+int gw_get_crus(gw_ctx *ctx, int cell, double *CaSS, double *CaJSR, int32_t *LCC,
+                int32_t *LCC_inactivation, int32_t *RyR, int32_t *ClCh, double *JLCC);
+/* The flux sums the next step's global derivatives use (GW.tpp:188-198): sum of Jtr over CRUs
+ * and of Jxfer over CRUs and subunits, taken at the last update_fluxes of the previous step. */
+int gw_set_flux_carry(gw_ctx *ctx, int cell, double sum_Jtr, double sum_Jxfer);
+int gw_get_flux_carry(gw_ctx *ctx, int cell, double *sum_Jtr, double *sum_Jxfer);
+/* Draws the reference's random initial CRU state (GW_utils.tpp:5-64) on the device. */
+int gw_sample_initial_crus(gw_ctx *ctx, int cell);
+
+/* Stimulus of one cell (cell < 0: all cells).  The reference evaluates a Python callable per step
+ * (pyGW.hpp:114); here either a pulse train evaluated on the device at the accumulated time t
+ * (Istim = amplitude when t >= start and (t - start) mod period < duration; period <= 0 means a
+ * single pulse), or per-step samples Istim[i] for steps i = 0 .. n-1 of the next gw_run. */
+int gw_set_stimulus_pulse(gw_ctx *ctx, int cell, double start, double period, double duration,
+                          double amplitude);
+int gw_set_stimulus_samples(gw_ctx *ctx, int cell, const double *Istim, int64_t n);
+
+/* Replaces the time loop of run<PRNG> (pyGW.hpp:102-122) / GW_model::euler (GW.tpp:275-282):
+ * n_steps global steps of size dt for every cell; t accumulates by t += dt. */
+int gw_run(gw_ctx *ctx, double dt, int64_t n_steps, int record_every, gw_trace *trace);
+
+int gw_get_time(gw_ctx *ctx, int cell, double *t, uint64_t *step);
+int gw_get_stats(gw_ctx *ctx, gw_stats *stats);
+/* Message of the last failing call on ctx (ctx may be NULL for gw_create failures). */
+int gw_last_error(gw_ctx *ctx, char *msg, size_t len);
+
+/* One-shot drop-in for the pybind11 `run` (pyGW.cpp:134-157, 341-344): simulate one cell of nCRU
+ * CRUs from init_globals / init CRU arrays for num_steps steps of step_size with stimulus samples
+ * Istim[num_steps] (the caller evaluates its stimulus function at t_i = sum_{k<i} step_size), and
+ * record into trace every record_every steps.  prng must be one of the reference's engine names
+ * (mt19937, mt19937_64, xoshiro256+, xoshiro256++, xoshiro256**, xoroshiro128+, xoroshiro128++,
+ * xoroshiro128**); any other name returns GW_ERR_INVALID_ARGUMENT, as the reference raises
+ * std::invalid_argument.  The engine always draws from its counter-based stream keyed on seed. */
+int gw_simulate(const gw_params *p, int nCRU, double step_size, int64_t num_steps,
+                const double *Istim, int record_every, const double *init_CaSS,
+                const double *init_CaJSR, const int32_t *init_LCC,
+                const int32_t *init_LCC_inactivation, const int32_t *init_RyR,
+                const int32_t *init_ClCh, const gw_globals *init_globals, const char *prng,
+                uint64_t seed, int precision, gw_trace *trace);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
