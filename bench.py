@@ -1,0 +1,279 @@
+"""Benchmark: CRU-steps/s and simulated ms per wall-second of the Greenstein-Winslow hybrid SSA.
+
+Workload (one GPU): one full cell of 12,500 CRUs (NCaRU = 12,500, so each simulated CRU stands for
+one real CRU), reference default parameters, GW::GlobalState resting globals, the reference's random
+initial CRU distributions, dt = 1e-3 ms, 1 Hz pacing with a +100 pA/pF, 0.5 ms stimulus (the
+reference integrates dV = dt (Istim - sum I), so the usual -100 pA/pF inward stimulus is +100 here).
+CRU state FP32, global ODE FP64 with compensated flux reduction.  Synthetic seeded input.
+
+A bench step is `--span-ms` of simulated time of that paced cell (the timed steps continue the
+protocol, so they cover the AP, the Ca release and the diastolic interval in proportion).
+
+  value  : CRU-steps/s with the state resident on the device (CUDA events around the engine kernel)
+  e2e    : the same through the reference-facing C ABI (gw_simulate: host arrays in and out, the
+           per-step stimulus samples uploaded, final state and records copied back, every step)
+  roofline: the engine kernel against HBM (algorithmic bytes = the CRU state read and written once
+           per CRU-step) -- the kernel keeps the state on chip, so this bound is not binding; see
+           profiles/ for the FP32 / issue-bound counters
+  cpu_baseline: the oracle port of the reference's C++ on the host cores (OpenMP), bounded sample
+
+--impl reference times the reference's CPU implementation of the path (the oracle port; the
+reference's own C++ needs its sources, which exist only where it was built) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(REPO, "gw-model_gb300"), os.path.join(REPO, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+NCRU = 12500
+DT = 1e-3
+PERIOD = 1000.0
+STIM_AMP, STIM_DUR = 100.0, 0.5
+BYTES_PER_CRU_STEP = 2 * (4 * 4 + 4 * 4 + 4 * 4 + 4 + 4 + 4 * 4 + 4 * 4 + 4)  # FP32 state in + out
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--span-ms", type=float, default=20.0)
+    ap.add_argument("--cells", type=int, default=1, help="replicate cells per GPU (1 = plain path)")
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 3 + i and s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def cpu_baseline(seconds: float, ncru: int = NCRU):
+    """The oracle port (C restatement of the reference, OpenMP over CRUs) timed on the host cores on
+    a bounded sample of the paced cell: the first steps after the stimulus."""
+    import pyoracle as po
+
+    po.build()
+    threads = os.cpu_count() or 1
+    po.lib().orc_set_threads(threads)
+    p = po.default_params()
+    m = po.Model(p, ncru, seed=0)
+    m.sample_initial_crus()
+    m.set_globals(po.default_globals(py=False))
+    t0 = time.perf_counter()
+    steps = 0
+    t = 0.0
+    while True:
+        tb = t - PERIOD * float(int(t / PERIOD))
+        m.euler_step(DT, STIM_AMP if tb < STIM_DUR else 0.0)
+        t += DT
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    rate = ncru * steps / el
+    return {"value": rate, "unit": "CRU-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{ncru} CRUs x {steps} steps ({steps * DT:.3f} ms from the stimulus) in {el:.1f} s"}
+
+
+def run_reference(args):
+    from gwgb300 import dist as gd
+
+    rank, _, world = gd.env_rank()
+    if rank != 0:
+        return 0
+    K, W = args.steps, args.warmup
+    per = max(args.cpu_seconds / max(K + W, 1), 2.0)
+    for _ in range(W):
+        cpu_baseline(per)
+    vals = [cpu_baseline(per) for _ in range(K)]
+    v = statistics.median(x["value"] for x in vals)
+    line = {"impl": "reference", "metric": "CRU-steps/s", "value": v, "unit": "CRU-steps/s",
+            "n_gpus": args.gpus, "steps": K, "warmup": W, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"single cell, {NCRU} CRUs, 1 Hz pacing, dt 1e-3 ms"},
+            "cpu_baseline": {"value": v, "unit": "CRU-steps/s", "cores": vals[0]["cores"], "kind": "port",
+                             "sample": vals[0]["sample"]},
+            "e2e": {"value": v, "unit": "CRU-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import numpy as np
+
+    from gwgb300 import Ensemble
+    from gwgb300 import dist as gd
+
+    rank, local_rank, world = gd.env_rank()
+    d = gd.init()
+    span = int(round(args.span_ms / DT))
+    K, W = args.steps, max(args.warmup, 3)
+    cells = max(args.cells, 1)
+    e = Ensemble([NCRU] * cells, precision="fp32", seed=1000 + rank, device=local_rank)
+    for c in range(cells):
+        e.sample_initial_crus(c)
+    e.set_pulse(0.0, PERIOD, STIM_DUR, STIM_AMP)
+    for _ in range(W):
+        e.run(DT, span)
+    gd.barrier(d)
+    st0 = e.stats()
+    t0 = time.perf_counter()
+    with ClockSampler(local_rank) as clk:
+        for _ in range(K):
+            e.run(DT, span)
+    wall = time.perf_counter() - t0
+    st1 = e.stats()
+    kernel_s = (st1["kernel_ms"] - st0["kernel_ms"]) / 1e3
+    kernel_s = gd.max_over_ranks(d, kernel_s)
+    wall = gd.max_over_ranks(d, wall)
+    cru_steps = NCRU * cells * span * K * world
+    value = cru_steps / kernel_s
+    launches = int(st1["launches"] - st0["launches"])
+    pk, pk_kind = peaks()
+    per_launch_steps = span * K / max(launches, 1)
+    achieved_gbs = BYTES_PER_CRU_STEP * NCRU * cells * span * K / kernel_s / 1e9
+    line = {"metric": "CRU-steps/s", "value": value, "unit": "CRU-steps/s", "n_gpus": world,
+            "steps": K, "warmup": W, "ms_per_step": kernel_s / K * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{'single cell' if cells == 1 else f'{cells} replicate cells'}, "
+                                   f"{NCRU} CRUs each, 1 Hz pacing (+{STIM_AMP} pA/pF, {STIM_DUR} ms), "
+                                   f"dt 1e-3 ms, FP32 CRU state, FP64 global ODE",
+                       "ncru": NCRU, "cells_per_gpu": cells, "span_ms_per_step": args.span_ms,
+                       "parallelism": f"replicas x{world}", "l2": "state on chip; inputs < L2, no flush needed",
+                       "launch_shape": {k: st1[k] for k in ("cluster_ctas", "cta_crus", "threads_per_cta", "n_clusters")}},
+            "sim_ms_per_wall_s": cells * world * span * K * DT / kernel_s,
+            "events_per_cru_step": (st1["events"] - st0["events"]) / max(NCRU * cells * span * K, 1),
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                         "frac": achieved_gbs / pk["hbm_gbs"], "traffic": None,
+                         "peak_kind": pk_kind, "bytes_per_cru_step": BYTES_PER_CRU_STEP,
+                         "steps_per_launch": per_launch_steps},
+            "clocks": clk.summary(), "wall_s": wall}
+    e.close()
+    if rank == 0 and not args.no_extras:
+        line["e2e"] = e2e_measure(span, K)
+        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def e2e_measure(span, K):
+    """The reference-facing path: GreensteinWinslow.run-equivalent C call with host buffers."""
+    import ctypes as C
+
+    import numpy as np
+
+    from gwgb300 import _lib
+
+    L = _lib.load()
+    p = _lib.default_params()
+    g = _lib.default_globals(py=True)
+    import GreensteinWinslow as GW
+
+    rng = np.random.default_rng(0)
+    LCC, LCCi, RyR, ClCh = GW._initial_cru_arrays(NCRU, rng)
+    CaSS = np.full((NCRU, 4), 1.45370e-4)
+    CaJSR = np.full(NCRU, 0.908408)
+    t = np.arange(span) * DT
+    istim = np.where(t - PERIOD * np.floor(t / PERIOD) < STIM_DUR, STIM_AMP, 0.0)
+    rec_every = span
+    out = {k: np.zeros((1, NCRU, 4)) for k in ("CaSS",)}
+    tr = _lib.GwTrace()
+    rec_t = np.zeros(1)
+    recG = np.zeros(36)
+    rCaSS = np.zeros((1, NCRU, 4))
+    rCaJSR = np.zeros((1, NCRU))
+    rI = [np.zeros((1, NCRU, 4), np.int32) for _ in range(3)]
+    rRyR = np.zeros((1, NCRU, 4, 6), np.int32)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
+
+    def once():
+        tr.max_records = 1
+        tr.t, tr.globals, tr.cru_cell = dp(rec_t), dp(recG), 0
+        tr.CaSS, tr.CaJSR = dp(rCaSS), dp(rCaJSR)
+        tr.LCC, tr.LCC_inactivation, tr.ClCh, tr.RyR = ip(rI[0]), ip(rI[1]), ip(rI[2]), ip(rRyR)
+        rc = L.gw_simulate(C.byref(p), NCRU, DT, span, dp(istim), rec_every, dp(CaSS), dp(CaJSR), ip(LCC),
+                           ip(LCCi), ip(RyR), ip(ClCh), C.byref(g), b"xoshiro256++", 1, 1, C.byref(tr))
+        _lib.check(rc)
+
+    once()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        once()
+    el = time.perf_counter() - t0
+    h2d = CaSS.nbytes + CaJSR.nbytes + LCC.nbytes + LCCi.nbytes + RyR.nbytes + ClCh.nbytes + istim.nbytes
+    d2h = rec_t.nbytes + recG.nbytes + rCaSS.nbytes + rCaJSR.nbytes + sum(a.nbytes for a in rI) + rRyR.nbytes
+    return {"value": NCRU * span * K / el, "unit": "CRU-steps/s", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "path": "gw_simulate (C ABI, host arrays, fresh context per call)"}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

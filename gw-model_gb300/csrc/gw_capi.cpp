@@ -608,21 +608,27 @@ int gw_get_crus(gw_ctx *c, int cell, double *CaSS, double *CaJSR, int32_t *LCC, 
     return GW_OK;
 }
 
-int gw_set_flux_carry(gw_ctx *c, int cell, double sum_Jtr, double sum_Jxfer) {
+int gw_set_flux_carry(gw_ctx *c, int cell, double sum_JLCC, double sum_ClCh, double sum_Jtr,
+                      double sum_Jxfer) {
     int rc = check_cell(c, cell);
     if (rc) return rc;
     cudaSetDevice(c->device);
     if ((rc = pull_dyn(c))) return rc;
+    c->dyn_host[cell].sum_jlcc = sum_JLCC;
+    c->dyn_host[cell].sum_clch = sum_ClCh;
     c->dyn_host[cell].sum_jtr = sum_Jtr;
     c->dyn_host[cell].sum_jxfer = sum_Jxfer;
     return push_dyn(c);
 }
 
-int gw_get_flux_carry(gw_ctx *c, int cell, double *sum_Jtr, double *sum_Jxfer) {
+int gw_get_flux_carry(gw_ctx *c, int cell, double *sum_JLCC, double *sum_ClCh, double *sum_Jtr,
+                      double *sum_Jxfer) {
     int rc = check_cell(c, cell);
     if (rc) return rc;
     cudaSetDevice(c->device);
     if ((rc = pull_dyn(c))) return rc;
+    if (sum_JLCC) *sum_JLCC = c->dyn_host[cell].sum_jlcc;
+    if (sum_ClCh) *sum_ClCh = c->dyn_host[cell].sum_clch;
     if (sum_Jtr) *sum_Jtr = c->dyn_host[cell].sum_jtr;
     if (sum_Jxfer) *sum_Jxfer = c->dyn_host[cell].sum_jxfer;
     return GW_OK;
@@ -835,6 +841,17 @@ int gw_get_time(gw_ctx *c, int cell, double *t, uint64_t *step) {
     if (t) *t = c->dyn_host[cell].t;
     if (step) *step = c->dyn_host[cell].step;
     return GW_OK;
+}
+
+int gw_set_time(gw_ctx *c, int cell, double t, uint64_t step) {
+    int rc = check_cell(c, cell);
+    if (rc) return rc;
+    if (!std::isfinite(t) || step > 0xFFFFFFFFull) return fail(c, GW_ERR_INVALID_ARGUMENT, "bad time or step");
+    cudaSetDevice(c->device);
+    if ((rc = pull_dyn(c))) return rc;
+    c->dyn_host[cell].t = t;
+    c->dyn_host[cell].step = step;
+    return push_dyn(c);
 }
 
 int gw_get_stats(gw_ctx *c, gw_stats *s) {

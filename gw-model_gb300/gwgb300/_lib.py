@@ -83,13 +83,14 @@ _SIGS = {
                      _P(C.c_int32), _P(C.c_int32), _P(C.c_int32), _P(C.c_double)], C.c_int),
     "gw_get_crus": ([C.c_void_p, C.c_int, _P(C.c_double), _P(C.c_double), _P(C.c_int32),
                      _P(C.c_int32), _P(C.c_int32), _P(C.c_int32), _P(C.c_double)], C.c_int),
-    "gw_set_flux_carry": ([C.c_void_p, C.c_int, C.c_double, C.c_double], C.c_int),
-    "gw_get_flux_carry": ([C.c_void_p, C.c_int, _P(C.c_double), _P(C.c_double)], C.c_int),
+    "gw_set_flux_carry": ([C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double], C.c_int),
+    "gw_get_flux_carry": ([C.c_void_p, C.c_int] + [_P(C.c_double)] * 4, C.c_int),
     "gw_sample_initial_crus": ([C.c_void_p, C.c_int], C.c_int),
     "gw_set_stimulus_pulse": ([C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double], C.c_int),
     "gw_set_stimulus_samples": ([C.c_void_p, C.c_int, _P(C.c_double), C.c_int64], C.c_int),
     "gw_run": ([C.c_void_p, C.c_double, C.c_int64, C.c_int, _P(GwTrace)], C.c_int),
     "gw_get_time": ([C.c_void_p, C.c_int, _P(C.c_double), _P(C.c_uint64)], C.c_int),
+    "gw_set_time": ([C.c_void_p, C.c_int, C.c_double, C.c_uint64], C.c_int),
     "gw_get_stats": ([C.c_void_p, _P(GwStats)], C.c_int),
     "gw_last_error": ([C.c_void_p, C.c_char_p, C.c_size_t], C.c_int),
     "gw_simulate": ([_P(GwParams), C.c_int, C.c_double, C.c_int64, _P(C.c_double), C.c_int,

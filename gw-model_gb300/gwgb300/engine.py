@@ -170,18 +170,36 @@ class Ensemble:
     def sample_initial_crus(self, cell: int):
         check(self.L.gw_sample_initial_crus(self.h, cell), self.h)
 
-    def set_flux_carry(self, cell: int, sum_jtr: float, sum_jxfer: float):
-        check(self.L.gw_set_flux_carry(self.h, cell, sum_jtr, sum_jxfer), self.h)
+    def set_flux_carry(self, cell: int, sum_jlcc: float, sum_clch: float, sum_jtr: float,
+                       sum_jxfer: float):
+        check(self.L.gw_set_flux_carry(self.h, cell, sum_jlcc, sum_clch, sum_jtr, sum_jxfer), self.h)
 
     def get_flux_carry(self, cell: int):
-        a, b = C.c_double(), C.c_double()
-        check(self.L.gw_get_flux_carry(self.h, cell, C.byref(a), C.byref(b)), self.h)
-        return a.value, b.value
+        """(sum JLCC, sum ClCh, sum Jtr, sum Jxfer) that the next global step uses."""
+        v = [C.c_double() for _ in range(4)]
+        check(self.L.gw_get_flux_carry(self.h, cell, *[C.byref(x) for x in v]), self.h)
+        return tuple(x.value for x in v)
 
     def time(self, cell: int = 0):
         t, s = C.c_double(), C.c_uint64()
         check(self.L.gw_get_time(self.h, cell, C.byref(t), C.byref(s)), self.h)
         return t.value, int(s.value)
+
+    def set_time(self, cell: int, t: float, step: int):
+        check(self.L.gw_set_time(self.h, cell, t, int(step)), self.h)
+
+    def checkpoint(self, cell: int) -> dict:
+        """Everything needed to resume a cell bit for bit (globals, CRU arrays with JLCC, flux
+        carry, time and RNG step)."""
+        t, step = self.time(cell)
+        return {"globals": self.get_globals(cell), "crus": self.get_crus(cell),
+                "carry": self.get_flux_carry(cell), "t": t, "step": step}
+
+    def restore(self, cell: int, ck: dict):
+        self.set_globals(cell, ck["globals"])
+        self.set_crus(cell, ck["crus"], with_jlcc=True)
+        self.set_flux_carry(cell, *ck["carry"])
+        self.set_time(cell, ck["t"], ck["step"])
 
     # ---- stimulus ----
     def set_pulse(self, start: float = 0.0, period: float = 0.0, duration: float = 0.5,

@@ -141,10 +141,14 @@ int gw_set_crus(gw_ctx *ctx, int cell, const double *CaSS, const double *CaJSR,
                 const int32_t *ClCh, const double *JLCC);
 int gw_get_crus(gw_ctx *ctx, int cell, double *CaSS, double *CaJSR, int32_t *LCC,
                 int32_t *LCC_inactivation, int32_t *RyR, int32_t *ClCh, double *JLCC);
-/* The flux sums the next step's global derivatives use (GW.tpp:188-198): sum of Jtr over CRUs
- * and of Jxfer over CRUs and subunits, taken at the last update_fluxes of the previous step. */
-int gw_set_flux_carry(gw_ctx *ctx, int cell, double sum_Jtr, double sum_Jxfer);
-int gw_get_flux_carry(gw_ctx *ctx, int cell, double *sum_Jtr, double *sum_Jxfer);
+/* The flux sums the next step's global derivatives use (GW.tpp:188-198): sum of JLCC and of the
+ * open ClCh count over CRUs and subunits (ICaL, Ito2), sum of Jtr over CRUs and of Jxfer over CRUs
+ * and subunits, the last two taken at the last update_fluxes of the previous step.  gw_set_crus
+ * recomputes the first two from the arrays; gw_set_flux_carry overrides all four (resume). */
+int gw_set_flux_carry(gw_ctx *ctx, int cell, double sum_JLCC, double sum_ClCh, double sum_Jtr,
+                      double sum_Jxfer);
+int gw_get_flux_carry(gw_ctx *ctx, int cell, double *sum_JLCC, double *sum_ClCh, double *sum_Jtr,
+                      double *sum_Jxfer);
 /* Draws the reference's random initial CRU state (GW_utils.tpp:5-64) on the device. */
 int gw_sample_initial_crus(gw_ctx *ctx, int cell);
 
@@ -161,6 +165,10 @@ int gw_set_stimulus_samples(gw_ctx *ctx, int cell, const double *Istim, int64_t 
 int gw_run(gw_ctx *ctx, double dt, int64_t n_steps, int record_every, gw_trace *trace);
 
 int gw_get_time(gw_ctx *ctx, int cell, double *t, uint64_t *step);
+/* Restores a cell's accumulated time and global step index (the RNG counter).  With the globals,
+ * the CRU arrays including JLCC, and the flux carry, this resumes a run bit for bit; the reference
+ * has no resume (its engines are seeded from std::random_device, common.hpp:19-23). */
+int gw_set_time(gw_ctx *ctx, int cell, double t, uint64_t step);
 int gw_get_stats(gw_ctx *ctx, gw_stats *stats);
 /* Message of the last failing call on ctx (ctx may be NULL for gw_create failures). */
 int gw_last_error(gw_ctx *ctx, char *msg, size_t len);

@@ -1,0 +1,213 @@
+"""Parity of the CUDA engine (through the C ABI) with the oracle and with the golden fixtures
+recorded from the reference's own C++.
+
+Tolerances (RNG-injection harness: both sides consume the same counter-based uniforms):
+  FP64 engine: channel states bit-exact; CaSS, CaJSR and the globals within 1e-12 relative.
+  FP32 engine: one global step from a shared state, CaSS/CaJSR/globals within 1e-5 relative, with
+               channel-state differences counted (identical draws can fall on the other side of a
+               partial-sum boundary when the rates are rounded to FP32) and bounded.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+DT = 1e-3
+CHANNELS = ("LCC", "LCC_inactivation", "RyR", "ClCh")
+
+
+def engine_state(init):
+    from gwgb300 import engine
+
+    return engine.CRUState(init.CaSS, init.CaJSR, init.LCC, init.LCC_inactivation, init.RyR,
+                           init.ClCh, getattr(init, "JLCC", None))
+
+
+def rel(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300))) if a.size else 0.0
+
+
+def run_pair(po, n, steps, seed, prec="fp64", umode=None, params=None, istim=None, init_seed=None,
+             cell=0, **kw):
+    from gwgb300 import Ensemble, engine
+
+    umode = (po.U53 if prec == "fp64" else po.U24) if umode is None else umode
+    p = params or po.default_params()
+    init = po.initial_crus(p, n, seed=init_seed if init_seed is not None else seed + 1000)
+    g0 = po.default_globals(py=True)
+    if istim is None:
+        istim = po.pulse_train(steps, DT, 100.0, 0.5)
+    m = po.Model(p, n, seed=seed, cell=cell, umode=umode)
+    m.set_globals(g0)
+    m.set_crus(init)
+    for i in range(steps):
+        m.euler_step(DT, istim[i])
+    ncru = [n] * (cell + 1)
+    e = Ensemble(ncru, params=engine.params_from(p), precision=prec, seed=seed, **kw)
+    e.set_globals(cell, g0.to_array())
+    e.set_crus(cell, engine_state(init))
+    e.set_samples(istim, cell=cell)
+    e.run(DT, steps)
+    out = (e.get_globals(cell), e.get_crus(cell), e.stats())
+    e.close()
+    return m, out
+
+
+@pytest.mark.parametrize("case", ["rest", "ap", "params", "release", "stim35"])
+def test_fp64_matches_reference_fixture(oracle, case):
+    """FP64 engine vs the trajectory recorded from the reference's own C++."""
+    from gwgb300 import Ensemble, engine
+
+    z = np.load(os.path.join(GOLDEN, f"traj_{case}.npz"))
+    over = dict(zip(z["param_names"].tolist(), z["param_values"].tolist()))
+    if "NCaRU" in over:
+        over["NCaRU"] = int(over["NCaRU"])
+    p = oracle.default_params(**over)
+    n, steps, rec = int(z["ncru"]), int(z["steps"]), int(z["rec"])
+    istim = oracle.pulse_train(steps, DT, float(z["amp"]), float(z["dur"]), float(z["period"]))
+    e = Ensemble([n], params=engine.params_from(p), precision="fp64", seed=int(z["seed"]))
+    e.set_globals(0, z["g0"])
+    e.set_crus(0, engine.CRUState(*(z["init_" + k] for k in ("CaSS", "CaJSR", "LCC", "LCC_inactivation", "RyR", "ClCh"))))
+    e.set_samples(istim)
+    tr = e.run(DT, steps, record_every=rec)
+    # the engine records after steps i with i % rec == 0; the fixture after steps i with (i+1) % rec == 0
+    s = e.get_crus(0)
+    for k in CHANNELS:
+        np.testing.assert_array_equal(getattr(s, k), z["final_" + k], err_msg=k)
+    assert rel(s.CaSS, z["final_CaSS"]) <= 1e-12
+    assert rel(s.CaJSR, z["final_CaJSR"]) <= 1e-12
+    assert rel(e.get_globals(0), z["globals_final"]) <= 1e-12
+    jl = s.JLCC
+    assert rel(jl, z["JLCC"]) <= 1e-12 if np.any(z["JLCC"]) else np.all(jl == 0)
+    assert tr.globals.shape[1] == steps // rec
+    e.close()
+
+
+@pytest.mark.parametrize("n,steps,seed", [(96, 6000, 1), (33, 12000, 2), (200, 3000, 3)])
+def test_fp64_matches_oracle(oracle, n, steps, seed):
+    m, (g, s, st) = run_pair(oracle, n, steps, seed, "fp64")
+    sr = m.crus()
+    for k in CHANNELS:
+        np.testing.assert_array_equal(getattr(s, k), getattr(sr, k), err_msg=k)
+    assert rel(s.CaSS, sr.CaSS) <= 1e-12 and rel(s.CaJSR, sr.CaJSR) <= 1e-12
+    assert rel(g, m.globals().to_array()) <= 1e-12
+    assert st["events"] == m.events()
+
+
+def test_fp64_cell_index_keys_the_stream(oracle):
+    """Cell k of an ensemble draws the oracle's stream of cell k."""
+    m, (g, s, _) = run_pair(oracle, 40, 2000, 9, "fp64", cell=2)
+    for k in CHANNELS:
+        np.testing.assert_array_equal(getattr(s, k), getattr(m.crus(), k))
+    assert rel(g, m.globals().to_array()) <= 1e-12
+
+
+@pytest.mark.parametrize("shape", [dict(cluster_ctas=1), dict(cluster_ctas=4, cta_crus=64),
+                                   dict(cluster_ctas=8, cta_crus=32), dict(steps_per_launch=7)])
+def test_fp64_launch_shape_independent(oracle, shape):
+    """Different CTA tiles, cluster sizes and launch lengths give the oracle's trajectory."""
+    m, (g, s, _) = run_pair(oracle, 200, 1500, 4, "fp64", **shape)
+    for k in CHANNELS:
+        np.testing.assert_array_equal(getattr(s, k), getattr(m.crus(), k))
+    assert rel(g, m.globals().to_array()) <= 1e-12
+
+
+def _u24_state(oracle, n, seed, warm):
+    """A state taken from an FP64 oracle run `warm` steps into an AP (open channels, raised CaSS)."""
+    p = oracle.default_params()
+    init = oracle.initial_crus(p, n, seed=seed)
+    g0 = oracle.default_globals(py=True)
+    m = oracle.Model(p, n, seed=seed + 1)
+    m.set_globals(g0)
+    m.set_crus(init)
+    istim = oracle.pulse_train(warm, DT, 100.0, 0.5)
+    for i in range(warm):
+        m.euler_step(DT, istim[i])
+    s = m.crus()
+    # exactly representable in FP32 so both sides start from the same numbers
+    s.CaSS = s.CaSS.astype(np.float32).astype(np.float64)
+    s.CaJSR = s.CaJSR.astype(np.float32).astype(np.float64)
+    return p, m.globals(), s, m.fluxes()
+
+
+@pytest.mark.parametrize("warm", [10, 3000, 8000])
+def test_fp32_one_step_matches_oracle(oracle, warm):
+    from gwgb300 import Ensemble, engine
+
+    n = 4000
+    p, g, s, (JLCC, Jxfer, Jtr) = _u24_state(oracle, n, 21, warm)
+    JLCC = JLCC.astype(np.float32).astype(np.float64)
+    step = 777
+    m = oracle.Model(p, n, seed=5, umode=oracle.U24)
+    m.set_globals(g)
+    m.set_crus(s)
+    m.set_fluxes(JLCC, Jxfer, Jtr)
+    m.set_step(step)
+    m.euler_step(DT, 0.0)
+    e = Ensemble([n], params=engine.params_from(p), precision="fp32", seed=5)
+    e.set_globals(0, g.to_array())
+    e.set_crus(0, engine.CRUState(s.CaSS, s.CaJSR, s.LCC, s.LCC_inactivation, s.RyR, s.ClCh, JLCC),
+               with_jlcc=True)
+    e.set_flux_carry(0, float(JLCC.sum()), float(s.ClCh.sum()), float(Jtr.sum()), float(Jxfer.sum()))
+    e.set_time(0, 0.0, step)
+    e.run(DT, 1)
+    es, ms = e.get_crus(0), m.crus()
+    same = np.ones(n, bool)
+    for k in CHANNELS:
+        a, b = getattr(es, k).reshape(n, -1), getattr(ms, k).reshape(n, -1)
+        same &= np.all(a == b, axis=1)
+    flips = int(np.sum(~same))
+    assert flips <= max(2, n // 1000), flips
+    assert rel(es.CaSS[same], ms.CaSS[same]) <= 1e-5
+    assert rel(es.CaJSR[same], ms.CaJSR[same]) <= 1e-5
+    assert rel(e.get_globals(0), m.globals().to_array()) <= 1e-5
+    e.close()
+
+
+def test_determinism_and_resume(oracle):
+    """Same seed and config: bitwise-identical results; a checkpointed run resumed in a fresh
+    context continues bit for bit (counter-based draws)."""
+    from gwgb300 import Ensemble
+
+    def make():
+        e = Ensemble([300, 120], precision="fp32", seed=42)
+        e.sample_initial_crus(0)
+        e.sample_initial_crus(1)
+        e.set_pulse(0.0, 0.0, 0.5, 100.0)
+        return e
+
+    a, b = make(), make()
+    a.run(DT, 3000)
+    b.run(DT, 1200)
+    ck = [b.checkpoint(c) for c in range(2)]
+    b.close()
+    c = make()
+    for i in range(2):
+        c.restore(i, ck[i])
+    c.run(DT, 1800)
+    for cell in range(2):
+        assert np.array_equal(a.get_globals(cell), c.get_globals(cell))
+        sa, sc = a.get_crus(cell), c.get_crus(cell)
+        for k in CHANNELS + ("CaSS", "CaJSR", "JLCC"):
+            assert np.array_equal(getattr(sa, k), getattr(sc, k)), k
+    a.close()
+    c.close()
+
+
+def test_initial_state_sampler_matches_oracle(oracle):
+    from gwgb300 import Ensemble
+
+    for prec, um in (("fp64", oracle.U53), ("fp32", oracle.U24)):
+        e = Ensemble([500, 257], precision=prec, seed=77)
+        for cell in (0, 1):
+            ref = oracle.Model(oracle.default_params(), [500, 257][cell], seed=77, cell=cell, umode=um)
+            ref.sample_initial_crus()
+            r, s = ref.crus(), e.get_crus(cell)
+            for k in CHANNELS:
+                np.testing.assert_array_equal(getattr(s, k), getattr(r, k))
+        e.close()
