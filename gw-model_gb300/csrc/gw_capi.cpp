@@ -15,6 +15,7 @@
 
 #include "gw_gb300.h"
 #include "gw_internal.h"
+#include "gw_ode_program.h"
 
 using namespace gw;
 
@@ -22,6 +23,7 @@ namespace {
 
 constexpr double kFaraday = 96.5;   // common.hpp:9
 constexpr double kGasConst = 8.314; // common.hpp:10
+constexpr int kMaxSsaWarps = 12;    // + kOdeWarps ODE warps = 512 threads per CTA
 
 thread_local std::string g_create_error;
 
@@ -68,6 +70,8 @@ struct gw_ctx {
     DevBuf d_cs, d_dyn, d_slot0, d_work, d_lcc, d_flags, d_ryr, d_cass, d_jlcc, d_cajsr, d_cajsr_lo,
         d_events, d_status;
     std::vector<DevBuf *> stim_bufs;
+    DevBuf d_prog;
+    OdeProgram prog;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     gw_stats stats{};
@@ -169,7 +173,7 @@ int plan_shape(gw_ctx *c, int cluster_req, int tile_req) {
     if (C == 0 && tile == 0) {
         // Default: one CRU per SSA thread where possible, at most 16 CTAs per cell.
         C = 1;
-        while (C < kMaxClusterCtas && (max_n + C - 1) / C > 32 * 15) C *= 2;
+        while (C < kMaxClusterCtas && (max_n + C - 1) / C > 32 * kMaxSsaWarps) C *= 2;
         tile = (max_n + C - 1) / C;
     } else if (C == 0) {
         C = std::max(1, (max_n + tile - 1) / tile);
@@ -182,7 +186,7 @@ int plan_shape(gw_ctx *c, int cluster_req, int tile_req) {
     if (need > C)
         return fail(c, GW_ERR_UNSUPPORTED, "a cell of %d CRUs needs %d CTAs of %d CRUs but the cluster has %d",
                     max_n, need, tile, C);
-    c->ssa_warps = std::min(15, tile / 32);
+    c->ssa_warps = std::min(kMaxSsaWarps, tile / 32);
     c->tile_cap = tile;
     // Pack cells (first-fit decreasing on CTA count) into clusters of C CTAs.
     std::vector<int> order(c->n_cells);
@@ -224,7 +228,7 @@ int plan_shape(gw_ctx *c, int cluster_req, int tile_req) {
         }
     }
     c->shape.cluster = C;
-    c->shape.threads = (c->ssa_warps + 1) * 32;
+    c->shape.threads = (c->ssa_warps + kOdeWarps) * 32;
     c->shape.ctas = c->n_clusters * C;
     c->shape.smem = c->precision == GW_PRECISION_FP64
                         ? smem_bytes_fp64(c->ssa_warps, c->tile_cap, c->max_cta_cell)
@@ -239,6 +243,7 @@ int plan_shape(gw_ctx *c, int cluster_req, int tile_req) {
 KernelArgs base_args(gw_ctx *c) {
     KernelArgs a;
     std::memset(&a, 0, sizeof a);
+    a.prog = c->d_prog.as<OdeProgram>();
     a.work = c->d_work.as<CtaWork>();
     a.cs = c->d_cs.as<CellStatic>();
     a.dyn = c->d_dyn.as<CellDyn>();
@@ -376,9 +381,19 @@ int gw_create(const gw_ensemble_desc *d, gw_ctx **out) {
     c->n_slots = s;
     c->cs.resize(c->n_cells);
     c->dyn_host.assign(c->n_cells, CellDyn{});
+    bool pow_fast = true;
+    for (int i = 0; i < c->n_cells; ++i) {
+        const gw_params &p = d->params[d->params_per_cell ? i : 0];
+        pow_fast = pow_fast && p.Hf == 0.75 && p.Hr == 0.75;
+    }
     for (int i = 0; i < c->n_cells; ++i) {
         const gw_params &p = d->params[d->params_per_cell ? i : 0];
         make_static(p, c->ncru[i], c->cs[i]);
+        if (!ode_program_build(c->cs[i], pow_fast, i == 0 ? &c->prog : nullptr, c->cs[i].ode_consts)) {
+            g_create_error = "global-step program does not fit its tables";
+            delete c;
+            return GW_ERR_UNSUPPORTED;
+        }
         CellDyn &y = c->dyn_host[i];
         std::memset(&y, 0, sizeof y);
         gw_globals g;
@@ -391,6 +406,8 @@ int gw_create(const gw_ensemble_desc *d, gw_ctx **out) {
         CK(c, cudaEventCreate(&c->ev0));
         CK(c, cudaEventCreate(&c->ev1));
         CK(c, c->d_cs.alloc(sizeof(CellStatic) * c->n_cells));
+        CK(c, c->d_prog.alloc(sizeof(OdeProgram)));
+        CK(c, cudaMemcpy(c->d_prog.p, &c->prog, sizeof(OdeProgram), cudaMemcpyHostToDevice));
         CK(c, c->d_dyn.alloc(sizeof(CellDyn) * c->n_cells));
         CK(c, c->d_slot0.alloc(sizeof(int64_t) * c->n_cells));
         CK(c, c->d_work.alloc(sizeof(CtaWork) * c->work.size()));
@@ -864,6 +881,20 @@ int gw_last_error(gw_ctx *c, char *msg, size_t len) {
     if (!msg || len == 0) return GW_ERR_INVALID_ARGUMENT;
     const std::string &e = c ? c->err : g_create_error;
     std::snprintf(msg, len, "%s", e.c_str());
+    return GW_OK;
+}
+
+int gw_global_step_host(const gw_params *p, int nCRU, double *g, const double *sums, double Istim,
+                        double dt, double *sv) {
+    if (!p || nCRU <= 0 || !g || !sums) return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "bad arguments");
+    CellStatic cs;
+    make_static(*p, nCRU, cs);
+    static thread_local OdeProgram prog;
+    static thread_local double consts[kOdeMaxConsts];
+    const bool fast = p->Hf == 0.75 && p->Hr == 0.75;
+    if (!ode_program_build(cs, fast, &prog, consts)) return fail(nullptr, GW_ERR_UNSUPPORTED, "ODE program too large");
+    double tmp[kSvCount];
+    ode_program_step_host(prog, consts, g, sums, Istim, dt, sv ? sv : tmp);
     return GW_OK;
 }
 

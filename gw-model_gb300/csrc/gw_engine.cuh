@@ -1,10 +1,19 @@
 // gw_engine.cuh -- the cluster-resident multi-step engine kernel and its launcher.
 // Included by gw_kernel_fp64.cu and gw_kernel_fp32.cu, which instantiate one precision each.
+//
+// CTA = [ssa_warps SSA warps | kOdeWarps ODE warps].  The ODE warps of a cell's leader CTA run the
+// global step as the lane program of gw_ode_program.h; elsewhere they only take part in the
+// cluster barrier.  Per global step s, every thread does   wait(s) ... arrive(s+1):
+//   SSA warps : SSA of step s with the values sv[s&1], push per-warp flux partials to the leader.
+//   ODE warps : reduce the partials of step s-1, increments and Euler update (globals s -> s+1),
+//               transcendental phases of the new state, push sv[(s+1)&1], arrive; the phases
+//               that the SSA does not need (general Jup exponents) run after the arrive.
 #pragma once
 
 #include <type_traits>
 
 #include "gw_kernel.cuh"
+#include "gw_ode_program.h"
 
 namespace gw {
 namespace dev {
@@ -17,22 +26,20 @@ struct Partial {
 };
 
 struct OdeShared {
-    double g[kNumGlobals];
-    double sv[kSvCount];
-    double expm;
-    double t;
-    double sums[4];  // JLCC, ClCh, Jtr, Jxfer
+    double g[kNumGlobals];  // the cell's globals (FP64 state)
+    double t;               // accumulated time
+    double sums[4];         // JLCC, ClCh, Jtr, Jxfer sums of the last reduced step (FP64)
     int status;
     int pad;
 };
 
 struct SmemLayout {
-    size_t cc, sv, ode, part, tile, total;
+    size_t cc, sv, ode, prog, x, part, tile, total;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-template <typename R>
+template <typename R, typename T>
 __host__ __device__ inline SmemLayout smem_layout(int ssa_warps, int tile_cap, int max_cta_cell) {
     SmemLayout L;
     size_t o = 0;
@@ -42,6 +49,10 @@ __host__ __device__ inline SmemLayout smem_layout(int ssa_warps, int tile_cap, i
     o += align16(2 * kSvCount * sizeof(R));
     L.ode = o;
     o += align16(sizeof(OdeShared));
+    L.prog = o;
+    o += align16(sizeof(OdeProgram));
+    L.x = o;
+    o += align16(kOdeMaxSlots * sizeof(T));
     L.part = o;
     o += align16((size_t)2 * max_cta_cell * ssa_warps * sizeof(Partial));
     L.tile = o;
@@ -65,6 +76,15 @@ __device__ __forceinline__ bool finite_bits(double x) {
     return ((__double_as_longlong(x) >> 52) & 0x7FF) != 0x7FF;
 }
 
+__device__ __forceinline__ void cluster_arrive() {
+    asm volatile("barrier.cluster.arrive.release;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() {
+    asm volatile("barrier.cluster.wait.acquire;" ::: "memory");
+}
+// barrier of the ODE warps (named barrier 1, kOdeLanes threads)
+__device__ __forceinline__ void ode_bar() { asm volatile("bar.sync 1, %0;" ::"n"(kOdeLanes) : "memory"); }
+
 // Stimulus of step ri at time t (pulse train or per-step samples).  Uses explicit round-to-nearest
 // operations so the host's evaluation of the same pulse train gives the same values.
 __device__ __forceinline__ double stimulus(const CellDyn &d, double t, int64_t ri) {
@@ -80,76 +100,116 @@ __device__ __forceinline__ double stimulus(const CellDyn &d, double t, int64_t r
     return 0.0;
 }
 
+__device__ __forceinline__ int v_regime(double V) { return V >= -40.0 ? 0 : (V == -47.13 ? 2 : 1); }
+
+__device__ __forceinline__ double t_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float t_sqrt(float x) { return sqrtf(x); }
+
+// One phase of the lane program by the kOdeLanes ODE threads (t = 0 .. kOdeLanes-1).
+template <typename T>
+__device__ __forceinline__ void ode_phase(const OdeProgram &P, int q, int regime, T *X, double *g, int t,
+                                          int *bad) {
+    const int b0 = P.phase_begin[q], n = P.phase_begin[q + 1] - b0;
+    const int lane = t & 31;
+    for (int base = 0; base < n; base += kOdeLanes) {
+        const int j = base + t;
+        const OdeOp *op = nullptr;
+        int kind = OK_NOP, width = 1;
+        T v = (T)0;
+        if (j < n) {
+            op = &P.ops[b0 + j];
+            if (regime > 0 && P.alt_idx[b0 + j] != 255) op = &P.alt[regime - 1][P.alt_idx[b0 + j]];
+            kind = op->kind;
+            width = op->width;
+            const uint16_t *a = op->a;
+            switch (kind) {
+            case OK_LOG: v = t_log(X[a[0]] + X[a[1]] * X[a[2]]); break;
+            case OK_SQRT: v = X[a[0]] * X[a[1]] * t_sqrt(X[a[2]] * X[a[3]]); break;
+            case OK_EXP: v = X[a[0]] * t_exp(X[a[1]] * X[a[2]] + X[a[3]]); break;
+            case OK_AFF: v = X[a[0]] * X[a[1]] + X[a[2]] * X[a[3]] + X[a[4]] * X[a[5]] + X[a[6]]; break;
+            case OK_REC:
+                v = (T)1 / (X[a[0]] + X[a[1]] * X[a[2]] + X[a[3]] * X[a[4]] + X[a[5]] * X[a[6]] * X[a[7]]);
+                break;
+            case OK_PROD: v = X[a[0]] * X[a[1]] * X[a[2]] * X[a[3]] * X[a[4]] * X[a[5]] * X[a[6]]; break;
+            case OK_SUM:
+                v = X[a[2]] * X[a[3]] * X[a[4]] + X[a[5]] * X[a[6]] * X[a[7]] + X[a[8]] * X[a[9]] * X[a[10]] +
+                    X[a[11]] * X[a[12]] * X[a[13]];
+                break;
+            default: break;
+            }
+        }
+        // SUM rows of `width` lanes: tree over offsets 1, 2, 4 (all lanes take part)
+        const unsigned any_sum = __ballot_sync(0xffffffffu, kind == OK_SUM);
+        if (any_sum) {
+#pragma unroll
+            for (int off = 1; off < 8; off <<= 1) {
+                const T o = __shfl_down_sync(0xffffffffu, v, off);
+                if (kind == OK_SUM && (lane % width) + off < width && (lane % (2 * off)) == 0) v += o;
+            }
+        }
+        if (j < n && kind != OK_NOP) {
+            if (kind == OK_UPD) {
+                const double ng = g[op->out] + (double)X[op->a[0]];
+                g[op->out] = ng;
+                X[XS_G + op->out] = (T)ng;
+                if (!finite_bits(ng)) *bad = 1;
+            } else if (kind == OK_SUM) {
+                if (lane % width == 0) X[op->out] = X[op->a[0]] * X[op->a[1]] * v;
+            } else {
+                X[op->out] = v;
+            }
+        }
+    }
+}
+
+// Sums {JLCC, ClCh, Jtr, Jxfer} of the cell's per-warp partials of one slot; ODE warp w reduces
+// quantity w.  Writes the FP64 sums to out[] (shared) from lane 0 of each warp.
 template <bool FP64>
-__device__ __forceinline__ void push_sv(const OdeShared &os, void *svbuf, int slot,
-                                        const CtaWork &w, int lane) {
+__device__ __forceinline__ void reduce_partials(const Partial *slot, int n, int warp, int lane, double *out) {
+    if (warp >= 4) return;
+    double r;
+    if (FP64) {
+        const int src = warp == 0 ? 0 : (warp == 1 ? 3 : (warp == 2 ? 2 : 1));  // JLCC, ClCh, Jtr, Jxfer
+        double acc = 0;
+        for (int i = lane; i < n; i += 32) acc += slot[i].v[src];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        r = acc;
+    } else {
+        // float fields: 0,1 JLCC; 2,3 Jxfer; 4,5 Jtr; 6 ClCh
+        const int src = warp == 0 ? 0 : (warp == 1 ? 6 : (warp == 2 ? 4 : 2));
+        float hi = 0, lo = 0;
+        for (int i = lane; i < n; i += 32) {
+            const float *f = reinterpret_cast<const float *>(slot[i].v);
+            df_add(hi, lo, f[src], warp == 1 ? 0.f : f[src + 1]);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float a0 = __shfl_xor_sync(0xffffffffu, hi, o), a1 = __shfl_xor_sync(0xffffffffu, lo, o);
+            df_add(hi, lo, a0, a1);
+        }
+        r = (double)hi + (double)lo;
+    }
+    if (lane == 0) out[warp] = r;
+}
+
+template <bool FP64, typename T>
+__device__ __forceinline__ void push_sv(const OdeProgram &P, const T *X, const double *g, void *svbuf, int slot,
+                                        const CtaWork &w, int t) {
     using R = typename std::conditional<FP64, double, float>::type;
     R *sv = reinterpret_cast<R *>(svbuf) + slot * kSvCount;
-    for (int i = lane; i < kSvCount; i += 32) {
-        R v = (R)os.sv[i];
-        if (!FP64) {
-            if (i == SV_CAI_LO) v = (R)(os.sv[SV_CAI] - (double)(float)os.sv[SV_CAI]);
-            if (i == SV_CANSR_LO) v = (R)(os.sv[SV_CANSR] - (double)(float)os.sv[SV_CANSR]);
-        }
+    for (int i = t; i < kSvCount; i += kOdeLanes) {
+        R v;
+        if (i == SV_CAI) v = (R)g[3];
+        else if (i == SV_CANSR) v = (R)g[4];
+        else if (i == SV_CAI_LO) v = FP64 ? (R)0 : (R)(g[3] - (double)(float)g[3]);
+        else if (i == SV_CANSR_LO) v = FP64 ? (R)0 : (R)(g[4] - (double)(float)g[4]);
+        else v = (R)X[P.sv_src[i]];
         for (int r = 0; r < w.n_cta_cell; ++r) st_remote(map_rank(sv + i, (uint32_t)(w.first + r)), v);
     }
 }
 
-// Lane-parallel reduction of the cell's per-warp partials of one slot; lane 0 returns the sums
-// {JLCC, ClCh, Jtr, Jxfer} in FP64.
-template <bool FP64>
-__device__ __forceinline__ void reduce_partials(const Partial *slot, int n, int lane, double *out) {
-    if (FP64) {
-        double a = 0, b = 0, c = 0, d = 0;
-        for (int i = lane; i < n; i += 32) {
-            a += slot[i].v[0];
-            b += slot[i].v[1];
-            c += slot[i].v[2];
-            d += slot[i].v[3];
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            a += __shfl_xor_sync(0xffffffffu, a, o);
-            b += __shfl_xor_sync(0xffffffffu, b, o);
-            c += __shfl_xor_sync(0xffffffffu, c, o);
-            d += __shfl_xor_sync(0xffffffffu, d, o);
-        }
-        if (lane == 0) {
-            out[0] = a;  // JLCC
-            out[1] = d;  // ClCh
-            out[2] = c;  // Jtr
-            out[3] = b;  // Jxfer
-        }
-    } else {
-        float jh = 0, jl = 0, xh = 0, xl = 0, th = 0, tl = 0;
-        int cl = 0;
-        for (int i = lane; i < n; i += 32) {
-            const float *f = reinterpret_cast<const float *>(slot[i].v);
-            df_add(jh, jl, f[0], f[1]);
-            df_add(xh, xl, f[2], f[3]);
-            df_add(th, tl, f[4], f[5]);
-            cl += (int)f[6];
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float a0 = __shfl_xor_sync(0xffffffffu, jh, o), a1 = __shfl_xor_sync(0xffffffffu, jl, o);
-            const float b0 = __shfl_xor_sync(0xffffffffu, xh, o), b1 = __shfl_xor_sync(0xffffffffu, xl, o);
-            const float c0 = __shfl_xor_sync(0xffffffffu, th, o), c1 = __shfl_xor_sync(0xffffffffu, tl, o);
-            cl += __shfl_xor_sync(0xffffffffu, cl, o);
-            df_add(jh, jl, a0, a1);
-            df_add(xh, xl, b0, b1);
-            df_add(th, tl, c0, c1);
-        }
-        if (lane == 0) {
-            out[0] = (double)jh + (double)jl;
-            out[1] = (double)cl;
-            out[2] = (double)th + (double)tl;
-            out[3] = (double)xh + (double)xl;
-        }
-    }
-}
-
-constexpr int kMaxThreads = 512;  // SSA warps + ODE warp per CTA (128 registers per thread)
+constexpr int kMaxThreads = 512;  // SSA warps + ODE warps per CTA (128 registers per thread)
 
 template <bool FP64, bool ODE64>
 __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs a) {
@@ -159,13 +219,17 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
     extern __shared__ __align__(16) unsigned char smem[];
     const int nw = a.ssa_warps;
     const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
+    const bool ode_thread = warp >= nw;
+    const int ot = (int)threadIdx.x - nw * 32;  // ODE thread index 0 .. kOdeLanes-1
     const CtaWork w = a.work[blockIdx.x];
     const bool active = w.cell >= 0;
     const bool leader = active && w.rank_in_cell == 0;
-    const SmemLayout L = smem_layout<R>(nw, a.tile_cap, a.max_cta_cell);
+    const SmemLayout L = smem_layout<R, T>(nw, a.tile_cap, a.max_cta_cell);
     SsaConsts<R> &cc = *reinterpret_cast<SsaConsts<R> *>(smem + L.cc);
     R *svbuf = reinterpret_cast<R *>(smem + L.sv);
     OdeShared &os = *reinterpret_cast<OdeShared *>(smem + L.ode);
+    OdeProgram &P = *reinterpret_cast<OdeProgram *>(smem + L.prog);
+    T *X = reinterpret_cast<T *>(smem + L.x);
     Partial *part = reinterpret_cast<Partial *>(smem + L.part);
     const int cap = a.tile_cap;
     uint32_t *t_lcc = reinterpret_cast<uint32_t *>(smem + L.tile);
@@ -177,6 +241,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
     float *t_cajsr_lo = reinterpret_cast<float *>(t_cajsr + cap);
     const int cell = w.cell;
     const int pslot = a.max_cta_cell * nw;  // partial entries per parity slot
+    const int npart = w.n_cta_cell * nw;
     R *g_cass = reinterpret_cast<R *>(a.cass);
     R *g_jlcc = reinterpret_cast<R *>(a.jlcc);
     R *g_cajsr = reinterpret_cast<R *>(a.cajsr);
@@ -185,7 +250,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
     if (active) {
         if (threadIdx.x == 0) load_ssa_consts<R>(cc, a.cs[cell]);
         step0 = a.dyn[cell].step;
-        if (warp < nw) {
+        if (!ode_thread) {
             const int64_t base = a.slot0[cell] + w.cru_begin;
             for (int m = (int)threadIdx.x; m < w.cru_count; m += nw * 32) {
                 const int64_t gs = base + m;
@@ -203,23 +268,53 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
             }
         }
     }
-    if (leader && warp == nw) {
-        if (lane == 0) {
-            const CellDyn &d = a.dyn[cell];
-            for (int i = 0; i < kNumGlobals; ++i) os.g[i] = d.g[i];
+    int bad = 0;  // ODE threads: non-finite global seen
+    if (leader && ode_thread) {
+        // program, constants and state of the cell
+        {
+            const int4 *src = reinterpret_cast<const int4 *>(a.prog);
+            int4 *dst = reinterpret_cast<int4 *>(&P);
+            for (int i = ot; i < (int)(sizeof(OdeProgram) / 16); i += kOdeLanes) dst[i] = src[i];
+        }
+        const CellStatic &C = a.cs[cell];
+        const CellDyn &d = a.dyn[cell];
+        for (int i = ot; i < kOdeMaxSlots; i += kOdeLanes) X[i] = (T)0;
+        ode_bar();
+        if (ot == 0) {
+            X[XS_ONE] = (T)1;
+            X[XS_MONE] = (T)-1;
             os.t = d.t;
             os.sums[0] = d.sum_jlcc;
             os.sums[1] = d.sum_clch;
             os.sums[2] = d.sum_jtr;
             os.sums[3] = d.sum_jxfer;
             os.status = 0;
-            os.expm = step_values(a.cs[cell], os.g, os.sv);
+            X[XS_DT] = (T)a.dt;
+            X[XS_ISTIM] = (T)stimulus(d, d.t, a.run_step0);
         }
-        __syncwarp();
-        push_sv<FP64>(os, svbuf, 0, w, lane);
+        for (int i = ot; i < kNumGlobals; i += kOdeLanes) {
+            os.g[i] = d.g[i];
+            X[XS_G + i] = (T)d.g[i];
+        }
+        for (int i = ot; i < kOdeConstCap; i += kOdeLanes) X[XS_FIRST_FREE + i] = (T)C.ode_consts[i];
+        ode_bar();
+        // transcendental phases of the initial state, push sv[0]
+        const int reg = v_regime(os.g[0]);
+        for (int q = P.upd_phase + 1; q <= P.push_phase; ++q) {
+            ode_phase<T>(P, q, reg, X, os.g, ot, &bad);
+            ode_bar();
+        }
+        push_sv<FP64, T>(P, X, os.g, svbuf, 0, w, ot);
     }
     __syncthreads();
-    cluster_sync();
+    cluster_arrive();
+    if (leader && ode_thread) {
+        const int reg = v_regime(os.g[0]);
+        for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
+            ode_phase<T>(P, q, reg, X, os.g, ot, &bad);
+            ode_bar();
+        }
+    }
 
     const R dt = (R)a.dt;
     unsigned long long my_events = 0;
@@ -230,7 +325,8 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
         const bool rec = a.record_every > 0 && (ri % a.record_every) == 0;
         const int64_t r_idx = rec ? ri / a.record_every - a.rec_base : -1;
         const bool rec_ok = rec && r_idx >= 0 && r_idx < a.rec_cap;
-        if (warp < nw) {
+        cluster_wait();
+        if (!ode_thread) {
             if (active) {
                 const R *sv = svbuf + par * kSvCount;
                 float jh = 0, jl = 0, xh = 0, xl = 0, th = 0, tl = 0;
@@ -328,59 +424,64 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
                     st_remote(map_rank(&dst->v[lane], (uint32_t)w.first), v);
                 }
             }
+            cluster_arrive();
         } else if (leader) {
-            // The cell's global step s -> s+1 with the fluxes of step s-1, concurrently with the
-            // SSA warps' step s.
-            double sums[4];
-            if (s > 0) reduce_partials<FP64>(part + (par ^ 1) * pslot, w.n_cta_cell * nw, lane, sums);
-            if (lane == 0) {
-                if (s == 0) {
-                    sums[0] = os.sums[0];
-                    sums[1] = os.sums[1];
-                    sums[2] = os.sums[2];
-                    sums[3] = os.sums[3];
-                }
-                const CellStatic &C = a.cs[cell];
-                const double Istim = stimulus(a.dyn[cell], os.t, ri);
-                int st = ode_step<T>(C, os.g, sums, Istim, a.dt, os.expm);
-                os.t += a.dt;
-                bool fin = true;
-                for (int i = 0; i < kNumGlobals; ++i) fin = fin && finite_bits(os.g[i]);
-                if (!fin && st == 0) st = GW_ERR_NONFINITE;
-                if (st != 0 && os.status == 0) os.status = st;
-                if (rec_ok) {
-                    double *dst = a.tr_glob + ((int64_t)cell * a.rec_cap + r_idx) * kNumGlobals;
-                    for (int i = 0; i < kNumGlobals; ++i) dst[i] = os.g[i];
-                    if (cell == 0 || (a.tr_cell >= 0 && cell == a.tr_cell)) a.tr_t[r_idx] = os.t;
-                }
-                os.expm = step_values(C, os.g, os.sv);
+            // fluxes of step s-1 (or the carry), then the global step s -> s+1
+            if (s > 0) reduce_partials<FP64>(part + (par ^ 1) * pslot, npart, ot >> 5, lane, os.sums);
+            ode_bar();
+            if (ot < 4) X[XS_SUMS + ot] = (T)os.sums[ot];
+            if (ot == 0 && (!(os.g[1] > 0.0) || !(os.g[2] > 0.0)) && os.status == 0) os.status = GW_ERR_NERNST;
+            ode_bar();
+            const int reg_n = v_regime(os.g[0]);
+            for (int q = 0; q <= P.upd_phase; ++q) {
+                ode_phase<T>(P, q, reg_n, X, os.g, ot, &bad);
+                ode_bar();
             }
-            __syncwarp();
-            push_sv<FP64>(os, svbuf, par ^ 1, w, lane);
+            if (ot == 0) {
+                os.t += a.dt;
+                X[XS_ISTIM] = (T)stimulus(a.dyn[cell], os.t, ri + 1);
+            }
+            if (rec_ok) {
+                double *dst = a.tr_glob + ((int64_t)cell * a.rec_cap + r_idx) * kNumGlobals;
+                for (int i = ot; i < kNumGlobals; i += kOdeLanes) dst[i] = os.g[i];
+                if (ot == 0 && (cell == 0 || (a.tr_cell >= 0 && cell == a.tr_cell))) a.tr_t[r_idx] = os.t;
+            }
+            const int reg = v_regime(os.g[0]);
+            for (int q = P.upd_phase + 1; q <= P.push_phase; ++q) {
+                ode_phase<T>(P, q, reg, X, os.g, ot, &bad);
+                ode_bar();
+            }
+            push_sv<FP64, T>(P, X, os.g, svbuf, par ^ 1, w, ot);
+            cluster_arrive();
+            for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
+                ode_phase<T>(P, q, reg, X, os.g, ot, &bad);
+                ode_bar();
+            }
+        } else {
+            cluster_arrive();
         }
-        cluster_sync();
     }
+    cluster_wait();
 
     // Epilogue: carry of the last step's fluxes, globals and counters back to the cell block.
-    if (leader && warp == nw) {
-        double sums[4];
-        if (a.n_steps > 0)
-            reduce_partials<FP64>(part + ((a.n_steps - 1) & 1) * pslot, w.n_cta_cell * nw, lane, sums);
-        if (lane == 0) {
-            CellDyn &d = a.dyn[cell];
-            if (a.n_steps > 0) {
-                d.sum_jlcc = sums[0];
-                d.sum_clch = sums[1];
-                d.sum_jtr = sums[2];
-                d.sum_jxfer = sums[3];
-            }
-            for (int i = 0; i < kNumGlobals; ++i) d.g[i] = os.g[i];
+    if (leader && ode_thread) {
+        if (a.n_steps > 0) reduce_partials<FP64>(part + ((a.n_steps - 1) & 1) * pslot, npart, ot >> 5, lane, os.sums);
+        const unsigned anybad = __ballot_sync(0xffffffffu, bad != 0);
+        if (lane == 0 && anybad) atomicCAS(&os.status, 0, (int)GW_ERR_NONFINITE);
+        ode_bar();
+        CellDyn &d = a.dyn[cell];
+        for (int i = ot; i < kNumGlobals; i += kOdeLanes) d.g[i] = os.g[i];
+        if (ot == 0) {
+            d.sum_jlcc = os.sums[0];
+            d.sum_clch = os.sums[1];
+            d.sum_jtr = os.sums[2];
+            d.sum_jxfer = os.sums[3];
             d.t = os.t;
             d.step = step0 + (uint64_t)a.n_steps;
             if (os.status != 0) atomicCAS(&a.status[cell], 0, os.status);
         }
     }
-    if (active && warp < nw) {
+    if (active && !ode_thread) {
         const int64_t base = a.slot0[cell] + w.cru_begin;
         for (int m = (int)threadIdx.x; m < w.cru_count; m += nw * 32) {
             const int64_t gs = base + m;
@@ -421,10 +522,9 @@ __global__ void init_crus_kernel(const KernelArgs a, int cell, int ncru) {
     auto pick = [&](const double *w, int n) {
         const double u = FP64 ? s.u53(k) : (double)s.u24(k);
         ++k;
-        const double uu = u * 1.0;
         double cum = w[0];
         int idx = 0;
-        while (cum < uu && idx < n - 1) {
+        while (cum < u && idx < n - 1) {
             ++idx;
             cum += w[idx];
         }
@@ -463,59 +563,63 @@ __global__ void init_crus_kernel(const KernelArgs a, int cell, int ncru) {
     if (!FP64) a.cajsr_lo[gs] = (float)(0.908408 - (double)(float)0.908408);
 }
 
-template <bool FP64>
-inline int launch_engine(const KernelArgs &a, const LaunchShape &s, void *stream, bool ode64) {
+template <bool FP64, bool ODE64>
+inline cudaError_t set_attrs(size_t smem) {
+    auto k = engine_kernel<FP64, ODE64>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return e;
+}
+
+inline cudaLaunchConfig_t launch_cfg(const LaunchShape &s, void *stream, cudaLaunchAttribute *attr) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)s.ctas, 1, 1);
     cfg.blockDim = dim3((unsigned)s.threads, 1, 1);
     cfg.dynamicSmemBytes = s.smem;
     cfg.stream = (cudaStream_t)stream;
-    cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = (unsigned)s.cluster;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    return cfg;
+}
+
+template <bool FP64>
+inline int launch_engine(const KernelArgs &a, const LaunchShape &s, void *stream, bool ode64) {
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = launch_cfg(s, stream, attr);
     cudaError_t e;
-    if (ode64) {
-        auto k = engine_kernel<FP64, true>;
-        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
-        cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        e = cudaLaunchKernelEx(&cfg, k, a);
+    if constexpr (FP64) {
+        (void)ode64;
+        e = set_attrs<true, true>(s.smem);
+        if (e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, engine_kernel<true, true>, a);
+    } else if (ode64) {
+        e = set_attrs<false, true>(s.smem);
+        if (e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, engine_kernel<false, true>, a);
     } else {
-        auto k = engine_kernel<FP64, false>;
-        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
-        cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        e = cudaLaunchKernelEx(&cfg, k, a);
+        e = set_attrs<false, false>(s.smem);
+        if (e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, engine_kernel<false, false>, a);
     }
     return (int)e;
 }
 
 template <bool FP64>
 inline int max_active_clusters(const LaunchShape &s, bool ode64, int *out) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)s.ctas, 1, 1);
-    cfg.blockDim = dim3((unsigned)s.threads, 1, 1);
-    cfg.dynamicSmemBytes = s.smem;
     cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = (unsigned)s.cluster;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cudaLaunchConfig_t cfg = launch_cfg(s, nullptr, attr);
     cudaError_t e;
-    if (ode64) {
-        auto k = engine_kernel<FP64, true>;
-        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
-        cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        e = cudaOccupancyMaxActiveClusters(out, k, &cfg);
+    if constexpr (FP64) {
+        (void)ode64;
+        e = set_attrs<true, true>(s.smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(out, engine_kernel<true, true>, &cfg);
+    } else if (ode64) {
+        e = set_attrs<false, true>(s.smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(out, engine_kernel<false, true>, &cfg);
     } else {
-        auto k = engine_kernel<FP64, false>;
-        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
-        cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        e = cudaOccupancyMaxActiveClusters(out, k, &cfg);
+        e = set_attrs<false, false>(s.smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(out, engine_kernel<false, false>, &cfg);
     }
     return (int)e;
 }

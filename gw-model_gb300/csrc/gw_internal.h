@@ -39,6 +39,8 @@ enum SvIndex {
 
 // Per-cell constant block: the parameters and the reference's Constants (GW_utils.tpp:67-116),
 // computed on the host in FP64 exactly as the reference does.
+constexpr int kOdeConstCap = 256;  // per-cell constants of the global-step lane program
+
 struct CellStatic {
     gw_params p;
     double RT_F, F_RT, CRU_factor, CSA_FVcyto, VSS_Vcyto, Vcyto_VNSR, VJSR_VNSR;
@@ -46,6 +48,7 @@ struct CellStatic {
         omega_b3, omega_b4;
     double BSR_const, BSL_const, VSS_VJSR, CSQN_const, JLCC_const, Cao_scaled, Nao3, INaCa_const,
         sigma, INaK_const, sqrtKo, PKv14_Csc, Ito2_const, IK1_const, ICaL_const, CMDN_const;
+    double ode_consts[kOdeConstCap];  // constants of the lane program (gw_ode_program.h)
 };
 
 enum StimMode { STIM_NONE = 0, STIM_PULSE = 1, STIM_SAMPLES = 2 };
@@ -77,7 +80,10 @@ struct CtaWork {
     int pad0, pad1;
 };
 
+struct OdeProgram;
+
 struct KernelArgs {
+    const OdeProgram *prog;
     const CtaWork *work;
     const CellStatic *cs;
     CellDyn *dyn;
@@ -107,7 +113,7 @@ struct KernelArgs {
     int n_cells;
     unsigned long long *events;
     int *status;
-    int ssa_warps;      // SSA warps per CTA (the ODE warp is the last warp)
+    int ssa_warps;      // SSA warps per CTA (the ODE warps follow them)
     int tile_cap;       // CRU capacity of one CTA
     int max_cta_cell;   // max CTAs of one cell (partial slot stride)
     int pad;
@@ -115,7 +121,7 @@ struct KernelArgs {
 
 struct LaunchShape {
     int cluster;      // CTAs per cluster
-    int threads;      // threads per CTA (SSA warps + 1 ODE warp) * 32
+    int threads;      // threads per CTA (SSA warps + ODE warps) * 32
     int ctas;         // grid size (multiple of cluster)
     size_t smem;      // dynamic shared memory per CTA
 };

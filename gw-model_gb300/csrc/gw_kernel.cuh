@@ -586,267 +586,12 @@ __device__ __forceinline__ void ssa_cru(Cru<R> &s, const SsaConsts<R> &c, const 
 }
 
 // ------------------------------------------------------------------------------------------
-// Global step (GW_model::euler_step, GW.tpp:237-272) for one cell, evaluated by one thread.
-// T is the arithmetic of the right-hand side: double (reference semantics) or float (optional
-// mixed mode); the state and its Euler update are always FP64.  With T = double the expressions
-// follow the reference's order term by term.
+// Precision-generic math used by the global-step lane program.
 // ------------------------------------------------------------------------------------------
-enum { GI_V = 0, GI_Nai, GI_Ki, GI_Cai, GI_CaNSR, GI_CaLTRPN, GI_CaHTRPN, GI_m, GI_h, GI_j, GI_xKs,
-       GI_Kr = 11, GI_Kv43 = 16, GI_Kv14 = 26 };
-
 __device__ __forceinline__ double t_exp(double x) { return exp(x); }
 __device__ __forceinline__ float t_exp(float x) { return expf(x); }
 __device__ __forceinline__ double t_log(double x) { return log(x); }
 __device__ __forceinline__ float t_log(float x) { return logf(x); }
-__device__ __forceinline__ double t_pow(double x, double y) { return pow(x, y); }
-__device__ __forceinline__ float t_pow(float x, float y) { return powf(x, y); }
-
-// Generator entries of one 10-state Kv channel (update_QKv, GW.tpp:65-123) and its derivative
-// (update_Kv_derivatives, GW.tpp:136-160).
-template <typename T>
-__device__ __forceinline__ void kv_derivs(const double *xs_, T aa, T ai, T ba, T bi, T f1, T f2,
-                                          T f3, T f4, T b1, T b2, T b3, T b4, T dt, T *d) {
-    const T q01 = 4 * aa, q05 = bi, q00 = -(q01 + q05);
-    const T q10 = ba, q12 = 3 * aa, q16 = f1 * bi, q11 = -(q10 + q12 + q16);
-    const T q21 = 2 * ba, q23 = 2 * aa, q27 = f2 * bi, q22 = -(q21 + q23 + q27);
-    const T q32 = 3 * ba, q34 = aa, q38 = f3 * bi, q33 = -(q32 + q34 + q38);
-    const T q43 = 4 * ba, q49 = f4 * bi, q44 = -(q43 + q49);
-    const T q56 = 4 * aa * b1, q50 = ai, q55 = -(q56 + q50);
-    const T q65 = ba / f1, q67 = 3 * aa * b2 / b1, q61 = ai / b1, q66 = -(q65 + q67 + q61);
-    const T q76 = 2 * ba * f1 / f2, q78 = 2 * aa * b3 / b2, q72 = ai / b2, q77 = -(q76 + q78 + q72);
-    const T q87 = 3 * ba * f2 / f3, q89 = aa * b4 / b3, q83 = ai / b3, q88 = -(q87 + q89 + q83);
-    const T q98 = 4 * ba * f3 / f4, q94 = ai / b4, q99 = -(q98 + q94);
-    const T x0 = (T)xs_[0], x1 = (T)xs_[1], x2 = (T)xs_[2], x3 = (T)xs_[3], x4 = (T)xs_[4];
-    const T x5 = (T)xs_[5], x6 = (T)xs_[6], x7 = (T)xs_[7], x8 = (T)xs_[8], x9 = (T)xs_[9];
-    d[0] = dt * (q10 * x1 + q50 * x5 + q00 * x0);
-    d[1] = dt * (q01 * x0 + q21 * x2 + q61 * x6 + q11 * x1);
-    d[2] = dt * (q12 * x1 + q32 * x3 + q72 * x7 + q22 * x2);
-    d[3] = dt * (q23 * x2 + q43 * x4 + q83 * x8 + q33 * x3);
-    d[4] = dt * (q34 * x3 + q94 * x9 + q44 * x4);
-    d[5] = dt * (q65 * x6 + q05 * x0 + q55 * x5);
-    d[6] = dt * (q56 * x5 + q76 * x7 + q16 * x1 + q66 * x6);
-    d[7] = dt * (q67 * x6 + q87 * x8 + q27 * x2 + q77 * x7);
-    d[8] = dt * (q78 * x7 + q98 * x9 + q38 * x3 + q88 * x8);
-    d[9] = dt * (q89 * x8 + q49 * x4 + q99 * x9);
-}
-
-// One global step of one cell.  g: the 36 globals (updated in place).  sums: JLCC, ClCh, Jtr,
-// Jxfer sums of the previous step's SSA.  expm = exp(-V F/RT) of the current V.  Returns 0 or a
-// gw_status code (GW_ERR_NERNST where the reference would exit).
-template <typename T>
-__device__ __noinline__ int ode_step(const CellStatic &C, double *g, const double *sums, double Istim_,
-                        double dt_, double expm_) {
-    const gw_params &p = C.p;
-    const T V = (T)g[GI_V], Nai = (T)g[GI_Nai], Ki = (T)g[GI_Ki], Cai = (T)g[GI_Cai];
-    const T CaNSR = (T)g[GI_CaNSR], CaLTRPN = (T)g[GI_CaLTRPN], CaHTRPN = (T)g[GI_CaHTRPN];
-    const T m = (T)g[GI_m], h = (T)g[GI_h], j = (T)g[GI_j], xKs = (T)g[GI_xKs];
-    const T dt = (T)dt_, Istim = (T)Istim_;
-    const T RT_F = (T)C.RT_F, F_RT = (T)C.F_RT;
-    const T VF_RT = V * F_RT;
-    const T expm = (T)expm_;
-    int status = 0;
-    if (!(Nai > (T)0) || !(Ki > (T)0)) status = GW_ERR_NERNST;
-    // update_V_and_concentration_derivatives (GW.tpp:171-212)
-    const T ENa = t_log((T)p.Nao / Nai) * RT_F / (T)1.0;
-    const T EK = t_log((T)p.Ko / Ki) * RT_F / (T)1.0;
-    const T ECa = t_log((T)p.Ko / Ki) * RT_F / (T)2.0;
-    const T INa = (T)p.GNa * (m * m * m) * h * j * (V - ENa);
-    const T INab = (T)p.GNab * (V - ENa);
-    T INaCa;
-    {
-        const T e1 = t_exp((T)p.eta * VF_RT);
-        const T e2 = e1 * expm;
-        INaCa = (T)C.INaCa_const * (e1 * (Nai * Nai * Nai) * (T)p.Cao - e2 * (T)C.Nao3 * Cai) /
-                ((T)1.0 + (T)p.ksat * e2);
-    }
-    T INaK;
-    {
-        const T fNaK = (T)1.0 / ((T)1.0 + (T)0.1245 * t_exp((T)-0.1 * VF_RT) +
-                                 (T)0.0365 * (T)C.sigma * expm);
-        INaK = (T)C.INaK_const * fNaK / ((T)1.0 + t_pow((T)p.KmNai / Nai, (T)1.5));
-    }
-    T IKr;
-    {
-        const T RKr = (T)1.0 / ((T)1.0 + (T)1.4945 * t_exp((T)0.0446 * V));
-        IKr = (T)p.GKr * (T)C.sqrtKo * RKr * (T)g[GI_Kr + 3] * (V - EK) * (T)0.5;
-    }
-    T IKs;
-    {
-        const T EKs = t_log(((T)p.Ko + (T)0.01833 * (T)p.Nao) / (Ki + (T)0.01833 * Nai)) * RT_F;
-        IKs = (T)p.GKs * (xKs * xKs) * (V - EKs);
-    }
-    T Ito1;
-    {
-        const T mm = ((T)C.PKv14_Csc) * ((T)kFaraday * VF_RT) * (T)g[GI_Kv14 + 4] / ((T)1 - expm);
-        const T IKv14 = mm * ((Ki - (T)p.Ko * expm) + (T)0.02 * (Nai - (T)p.Nao * expm)) * (T)1.0e9;
-        const T IKv43 = (T)p.GKv43 * (T)g[GI_Kv43 + 4] * (V - EK);
-        Ito1 = IKv14 + IKv43;
-    }
-    const T Ito2 = (T)sums[1] * (T)C.Ito2_const * VF_RT * ((T)p.Clcyto * expm - (T)p.Clo) /
-                   (expm - (T)1.0);
-    T IK1;
-    {
-        const T K1inf = (T)1.0 / ((T)2.0 + t_exp((T)1.5 * (V - EK) * F_RT));
-        IK1 = (T)p.GK1 * K1inf * (T)C.IK1_const * (V - EK);
-    }
-    T IKp;
-    {
-        const T Kp = (T)1. / ((T)1. + t_exp(((T)7.488 - V) / (T)5.98));
-        IKp = (T)p.GKp * Kp * (V - EK);
-    }
-    const T ICaL = (T)sums[0] * (T)C.ICaL_const;
-    const T ICab = (T)p.GCab * (V - ECa);
-    const T IpCa = (T)p.IpCamax * (Cai / ((T)p.KmpCa + Cai));
-    T Jup;
-    {
-        const T f = t_pow(Cai / (T)p.Kmf, (T)p.Hf);
-        const T r = t_pow(CaNSR / (T)p.Kmr, (T)p.Hr);
-        Jup = ((T)p.Vmaxf * f - (T)p.Vmaxr * r) / ((T)1.0 + f + r);
-    }
-    const T Jtr_tot = (T)sums[2] * (T)C.CRU_factor;
-    const T Jxfer_tot = (T)sums[3] * (T)C.CRU_factor;
-    T beta_cyto;
-    {
-        const T x = (T)p.KCMDN + Cai;
-        beta_cyto = (T)1.0 / ((T)1.0 + (T)C.CMDN_const / (x * x));
-    }
-    T dLTRPN = (T)p.kLTRPNp * Cai * ((T)p.LTRPNtot - CaLTRPN) - (T)p.kLTRPNm * CaLTRPN;
-    T dHTRPN = (T)p.kHTRPNp * Cai * ((T)p.HTRPNtot - CaHTRPN) - (T)p.kHTRPNm * CaHTRPN;
-    const T CSA_FVcyto = (T)C.CSA_FVcyto;
-    const T dNai = -dt * CSA_FVcyto * (INa + INab + (T)3 * INaCa + (T)3 * INaK);
-    const T dKi = -dt * CSA_FVcyto * (IKr + IKs + Ito1 + IK1 + IKp - (T)2 * INaK);
-    const T dCai = dt * beta_cyto *
-                   ((T)-0.5 * CSA_FVcyto * (ICab + IpCa - (T)2 * INaCa) +
-                    (T)C.VSS_Vcyto * Jxfer_tot - Jup - (dLTRPN + dHTRPN));
-    const T dCaNSR = dt * ((T)C.Vcyto_VNSR * Jup - (T)C.VJSR_VNSR * Jtr_tot);
-    dLTRPN *= dt;
-    dHTRPN *= dt;
-    const T dV = dt * (Istim - (INa + ICaL + IKr + IKs + Ito1 + IK1 + IKp + Ito2 + INaK + INaCa +
-                                IpCa + ICab + INab));
-    // update_gate_derivatives (GW.tpp:163-168)
-    T dm, dh, dj, dxKs;
-    {
-        const T am = (V == (T)-47.13) ? (T)3.2
-                                      : (T)0.32 * (V + (T)47.13) /
-                                            ((T)1.0 - t_exp((T)-0.1 * (V + (T)47.13)));
-        const T bm = (T)0.08 * t_exp(-V / (T)11.0);
-        const T ah = (V >= (T)-40.0) ? (T)0.0 : (T)0.135 * t_exp(-(V + (T)80.0) / (T)6.8);
-        const T bh = (V >= (T)-40.0)
-                         ? (T)1.0 / ((T)0.13 * ((T)1.0 + t_exp(-(V + (T)10.66) / (T)11.1)))
-                         : (T)3.56 * t_exp((T)0.079 * V) + (T)3.1e5 * t_exp((T)0.35 * V);
-        const T aj = (V >= (T)-40.0)
-                         ? (T)0.0
-                         : ((T)-127140.0 * t_exp((T)0.2444 * V) -
-                            (T)3.474e-5 * t_exp((T)-0.04391 * V)) *
-                               (V + (T)37.78) / ((T)1.0 + t_exp((T)0.311 * (V + (T)79.23)));
-        const T bj = (V >= (T)-40.0)
-                         ? (T)0.3 * t_exp((T)-2.535e-7 * V) /
-                               ((T)1.0 + t_exp((T)-0.1 * (V + (T)32.0)))
-                         : (T)0.1212 * t_exp((T)-0.01052 * V) /
-                               ((T)1.0 + t_exp((T)-0.1378 * (V + (T)40.14)));
-        const T xinf = (T)1.0 / ((T)1.0 + t_exp(-(V - (T)24.7) / (T)13.6));
-        const T tinv = (T)0.0000719 * (V - (T)10.0) / ((T)1.0 - t_exp((T)-0.148 * (V - (T)10.0))) +
-                       (T)0.000131 * (V - (T)10.0) / (t_exp((T)0.0687 * (V - (T)10.0)) - (T)1.0);
-        dm = dt * (am * ((T)1.0 - m) - bm * m);
-        dh = dt * (ah * ((T)1.0 - h) - bh * h);
-        dj = dt * (aj * ((T)1.0 - j) - bj * j);
-        dxKs = dt * (xinf - xKs) * tinv;
-    }
-    // update_QKr + update_Kr_derivatives (GW.tpp:26-44, 127-133)
-    T dKr[5];
-    {
-        const T Q01 = (T)0.0069 * t_exp((T)0.0272 * V);
-        const T Q00 = -Q01;
-        const T Q10 = (T)0.0227 * t_exp((T)-0.0431 * V);
-        const T Q12 = (T)p.Kf, Q21 = (T)p.Kb;
-        const T Q11 = -(Q10 + Q12);
-        const T Q23 = (T)0.0218 * t_exp((T)0.0262 * V);
-        const T Q24 = (T)1.29e-5 * t_exp((T)2.71e-6 * V);
-        const T Q22 = -(Q21 + Q23 + Q24);
-        const T Q32 = (T)0.0009 * t_exp((T)-0.0269 * V);
-        const T Q34 = (T)0.0622 * t_exp((T)0.0120 * V);
-        const T Q33 = -(Q32 + Q34);
-        const T Q43 = (T)0.0059 * t_exp((T)-0.0443 * V);
-        const T Q42 = Q32 * Q43 * Q24 / (Q23 * Q34);
-        const T Q44 = -(Q42 + Q43);
-        T k[5];
-#pragma unroll
-        for (int i = 0; i < 5; ++i) k[i] = (T)g[GI_Kr + i];
-        dKr[0] = dt * (Q10 * k[1] + Q00 * k[0]);
-        dKr[1] = dt * (Q01 * k[0] + Q21 * k[2] + Q11 * k[1]);
-        dKr[2] = dt * (Q12 * k[1] + Q32 * k[3] + Q42 * k[4] + Q22 * k[2]);
-        dKr[3] = dt * (Q23 * k[2] + Q43 * k[4] + Q33 * k[3]);
-        dKr[4] = dt * (Q24 * k[2] + Q34 * k[3] + Q44 * k[4]);
-    }
-    T dKv14[10], dKv43[10];
-    {
-        const T aa14 = (T)p.alphaa0Kv14 * t_exp((T)p.aaKv14 * V);
-        const T aa43 = (T)p.alphaa0Kv43 * t_exp((T)p.aaKv43 * V);
-        const T ai14 = (T)p.alphai0Kv14 * t_exp(-(T)p.aiKv14 * V);
-        const T ai43 = (T)p.alphai0Kv43 * t_exp(-(T)p.aiKv43 * V);
-        const T ba14 = (T)p.betaa0Kv14 * t_exp(-(T)p.baKv14 * V);
-        const T ba43 = (T)p.betaa0Kv43 * t_exp(-(T)p.baKv43 * V);
-        const T bi14 = (T)p.betai0Kv14 * t_exp((T)p.biKv14 * V);
-        const T bi43 = (T)p.betai0Kv43 * t_exp((T)p.biKv43 * V);
-        kv_derivs<T>(g + GI_Kv14, aa14, ai14, ba14, bi14, (T)p.f1Kv14, (T)p.f2Kv14, (T)p.f3Kv14,
-                     (T)p.f4Kv14, (T)p.b1Kv14, (T)p.b2Kv14, (T)p.b3Kv14, (T)p.b4Kv14, dt, dKv14);
-        kv_derivs<T>(g + GI_Kv43, aa43, ai43, ba43, bi43, (T)p.f1Kv43, (T)p.f2Kv43, (T)p.f3Kv43,
-                     (T)p.f4Kv43, (T)p.b1Kv43, (T)p.b2Kv43, (T)p.b3Kv43, (T)p.b4Kv43, dt, dKv43);
-    }
-    // Euler update (GW.tpp:252-271), accumulated in FP64.
-    g[GI_V] += (double)dV;
-    g[GI_Nai] += (double)dNai;
-    g[GI_Ki] += (double)dKi;
-    g[GI_Cai] += (double)dCai;
-    g[GI_CaNSR] += (double)dCaNSR;
-    g[GI_CaLTRPN] += (double)dLTRPN;
-    g[GI_CaHTRPN] += (double)dHTRPN;
-    g[GI_m] += (double)dm;
-    g[GI_h] += (double)dh;
-    g[GI_j] += (double)dj;
-    g[GI_xKs] += (double)dxKs;
-#pragma unroll
-    for (int i = 0; i < 5; ++i) g[GI_Kr + i] += (double)dKr[i];
-#pragma unroll
-    for (int i = 0; i < 10; ++i) {
-        g[GI_Kv14 + i] += (double)dKv14[i];
-        g[GI_Kv43 + i] += (double)dKv43[i];
-    }
-    return status;
-}
-
-// Per-step SSA values at voltage V (GW_model::SSA, GW.tpp:216-221; alphaLCC..tauLCC,
-// GW_utils.hpp:365-375) with the LCC rate products of update_LCC_rates.  Fills sv[0..33] and
-// returns exp(-V F/RT), which the next global step uses as expmVF_RT.
-static __device__ __noinline__ double step_values(const CellStatic &C, const double *g, double *sv) {
-    const double V = g[GI_V];
-    const double expm = exp(-(V * C.F_RT));
-    const double al = 2.0 * exp(0.012 * (V - 35.0));
-    const double be = 0.0882 * exp(-0.05 * (V - 35.0));
-    const double yinf = 0.4 / (1.0 + exp((V + 12.5) / 5.0)) + 0.6;
-    const double tau = 340.0 / (1.0 + exp((V + 30.0) / 12.0)) + 60.0;
-    const gw_params &p = C.p;
-    sv[SV_ZERO] = 0.0;
-    sv[SV_A4] = 4 * al; sv[SV_A3] = 3 * al; sv[SV_A2] = 2 * al; sv[SV_A1] = al;
-    sv[SV_B1] = be; sv[SV_B2] = 2 * be; sv[SV_B3] = 3 * be; sv[SV_B4] = 4 * be;
-    sv[SV_A4a] = 4 * al * C.a; sv[SV_A3a] = 3 * al * C.a; sv[SV_A2a] = 2 * al * C.a;
-    sv[SV_A1a] = al * C.a;
-    sv[SV_B1bi] = be * C.binv; sv[SV_B2bi] = 2 * be * C.binv; sv[SV_B3bi] = 3 * be * C.binv;
-    sv[SV_B4bi] = 4 * be * C.binv;
-    sv[SV_F] = p.f; sv[SV_G] = p.g; sv[SV_OM] = C.omega; sv[SV_OMB1] = C.omega_b;
-    sv[SV_OMB2] = C.omega_b2; sv[SV_OMB3] = C.omega_b3; sv[SV_OMB4] = C.omega_b4;
-    sv[SV_F1] = p.f1; sv[SV_G1] = p.g1;
-    sv[SV_INACT0] = yinf / tau;
-    sv[SV_INACT1] = (1.0 - yinf) / tau;
-    const double jexp = (1.0 / expm) * (1.0 / expm);
-    sv[SV_JEXP] = jexp;
-    sv[SV_JMUL] = C.JLCC_const * V * C.F_RT / (jexp - 1);
-    sv[SV_CAI] = g[GI_Cai];
-    sv[SV_CANSR] = g[GI_CaNSR];
-    sv[SV_CAI_LO] = 0.0;
-    sv[SV_CANSR_LO] = 0.0;
-    return expm;
-}
 
 }  // namespace dev
 }  // namespace gw

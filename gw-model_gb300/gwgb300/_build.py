@@ -25,6 +25,7 @@ UNITS = [
     ("gw_kernel_fp64.cu", ["-fmad=false"]),
     ("gw_kernel_fp32.cu", []),
     ("gw_capi.cpp", ["-x", "cu"]),
+    ("gw_ode_program.cpp", []),
 ]
 
 

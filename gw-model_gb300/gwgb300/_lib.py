@@ -93,6 +93,8 @@ _SIGS = {
     "gw_set_time": ([C.c_void_p, C.c_int, C.c_double, C.c_uint64], C.c_int),
     "gw_get_stats": ([C.c_void_p, _P(GwStats)], C.c_int),
     "gw_last_error": ([C.c_void_p, C.c_char_p, C.c_size_t], C.c_int),
+    "gw_global_step_host": ([_P(GwParams), C.c_int, _P(C.c_double), _P(C.c_double), C.c_double, C.c_double,
+                             _P(C.c_double)], C.c_int),
     "gw_simulate": ([_P(GwParams), C.c_int, C.c_double, C.c_int64, _P(C.c_double), C.c_int,
                      _P(C.c_double), _P(C.c_double), _P(C.c_int32), _P(C.c_int32), _P(C.c_int32),
                      _P(C.c_int32), _P(GwGlobals), C.c_char_p, C.c_uint64, C.c_int, _P(GwTrace)],

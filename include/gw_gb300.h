@@ -173,6 +173,14 @@ int gw_get_stats(gw_ctx *ctx, gw_stats *stats);
 /* Message of the last failing call on ctx (ctx may be NULL for gw_create failures). */
 int gw_last_error(gw_ctx *ctx, char *msg, size_t len);
 
+/* The global update of GW_model::euler_step (GW.tpp:237-272: currents, concentrations, gates, IKr
+ * and Kv Markov chains, explicit Euler) for one cell, evaluated on the host in the engine's FP64
+ * operation order (the lane program its ODE warps run).  g: the 36 globals, updated in place;
+ * sums: {sum JLCC, sum ClCh, sum Jtr, sum Jxfer} of the previous step; sv (may be NULL) receives
+ * the engine's 40 per-step SSA values at the updated state.  Needs no device. */
+int gw_global_step_host(const gw_params *p, int nCRU, double *g, const double *sums, double Istim,
+                        double dt, double *sv);
+
 /* One-shot drop-in for the pybind11 `run` (pyGW.cpp:134-157, 341-344): simulate one cell of nCRU
  * CRUs from init_globals / init CRU arrays for num_steps steps of step_size with stimulus samples
  * Istim[num_steps] (the caller evaluates its stimulus function at t_i = sum_{k<i} step_size), and
