@@ -135,13 +135,18 @@ __device__ __forceinline__ void st_remote(uint32_t addr, float v) {
 // ------------------------------------------------------------------------------------------
 // Per-cell SSA constants (shared memory, in the CRU arithmetic type).
 // ------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t lcc_table(int s);
+__device__ __forceinline__ int lcc_next(int s, int tr);
+
 template <typename R>
 struct SsaConsts {
     R k12, k21, k23, k32, k34, k43, k45, k54, k56, k65, k25, k52;
     R rRyR, rxfer, rtr, riss, KBSR, KBSL, KCSQN, kfClCh, kbClCh;
     R BSR_const, BSL_const, VSS_VJSR, CSQN_const, Cao_scaled;
     R gam[5];  // gamma0 * a^k, k = 0..4 (Constants gamma0 .. gamma0a4)
-    R pad;
+    R k2325, k45k34, k32k43, k4543, k5654;  // combined rate constants (FP32 subunit total)
+    uint32_t lcct[16];  // LCC rate table by state (lcc_word), in shared memory: no divergent branch
+    uint32_t lccn[16];  // next LCC state by state: transition t in bits 4t..4t+3
 };
 
 template <typename R>
@@ -157,7 +162,15 @@ __device__ void load_ssa_consts(SsaConsts<R> &c, const CellStatic &s) {
     c.CSQN_const = (R)s.CSQN_const; c.Cao_scaled = (R)s.Cao_scaled;
     c.gam[0] = (R)s.gamma0; c.gam[1] = (R)s.gamma0a; c.gam[2] = (R)s.gamma0a2;
     c.gam[3] = (R)s.gamma0a3; c.gam[4] = (R)s.gamma0a4;
-    c.pad = (R)0;
+    c.k2325 = (R)(p.k23 + p.k25);
+    c.k45k34 = (R)(p.k45 * p.k34);
+    c.k32k43 = (R)(p.k32 * p.k43);
+    c.k4543 = (R)(p.k45 + p.k43);
+    c.k5654 = (R)(p.k56 + p.k54);
+    for (int st = 0; st < 16; ++st) {
+        c.lcct[st] = lcc_table(st);
+        c.lccn[st] = (uint32_t)lcc_next(st, 0) | ((uint32_t)lcc_next(st, 1) << 4) | ((uint32_t)lcc_next(st, 2) << 8);
+    }
 }
 
 // LCC transition table: for state s (1..12) the sv[] index of each of its 3 outgoing rates
@@ -247,7 +260,7 @@ template <typename R>
 __device__ __forceinline__ R subunit_rates(const Cru<R> &s, int j, R x, const SsaConsts<R> &c,
                                            const R *sv, Rates<R> &r) {
     const int st = byte_u(s.lcc, j);
-    const uint32_t w = lcc_table(st);
+    const uint32_t w = c.lcct[st & 15];
     r.lcc[0] = sv[w & 0xFFu];
     r.lcc[1] = sv[(w >> 8) & 0xFFu];
     r.lcc[2] = sv[(w >> 16) & 0xFFu];
@@ -299,6 +312,32 @@ __device__ __forceinline__ R subunit_rates(const Cru<R> &s, int j, R x, const Ss
     for (int k = 0; k < 12; ++k) sub = sub + r.ryr[k];
     sub = sub + r.clch;
     return sub;
+}
+
+// FP32 total outgoing rate of subunit j: the same rates as subunit_rates, regrouped (used only to
+// draw the jump time and the subunit; the transition itself is drawn from the full rate list).
+template <typename R>
+__device__ __forceinline__ R subunit_total_fast(const Cru<R> &s, int j, R x, const SsaConsts<R> &c,
+                                                const R *sv) {
+    const int st = byte_u(s.lcc, j);
+    const uint32_t w = c.lcct[st & 15];
+    R lcc = sv[w & 0xFFu] + sv[(w >> 8) & 0xFFu] + sv[(w >> 16) & 0xFFu];
+    if ((w >> 24) < 3u) lcc += c.gam[(st - 1) & 7] * x;
+    const R inact = ((s.flags >> j) & 1u) == 0u ? sv[SV_INACT0] : sv[SV_INACT1];
+    const R R0 = (R)byte_s(s.ryr[0], j), R1 = (R)byte_s(s.ryr[1], j), R2 = (R)byte_s(s.ryr[2], j);
+    const R R3 = (R)byte_s(s.ryr[3], j), R4 = (R)byte_s(s.ryr[4], j), R5 = (R)byte_s(s.ryr[5], j);
+    const R x2 = x * x;
+    R ryr = x2 * (R0 * c.k12 + R1 * c.k2325) + R1 * c.k21;
+    if (x > (R)3.685e-2)
+        ryr += (R2 + R3) * __fdividef((float)(c.k45k34 * x2 + c.k32k43), (float)(c.k34 * x2 + c.k43));
+    else
+        ryr += x2 * R2 * c.k34 + R3 * c.k4543 + R2 * c.k32;
+    if (x > (R)1.15e-4)
+        ryr += (R4 + R5) * __fdividef((float)(c.k65 * (c.k52 + c.k54 * x2)), (float)(c.k56 * x2 + c.k65));
+    else
+        ryr += x2 * R4 * c.k5654 + R4 * c.k52 + R5 * c.k65;
+    const R clch = ((s.flags >> (4 + j)) & 1u) == 0u ? c.kfClCh * x : c.kbClCh;
+    return lcc + inact + ryr + clch;
 }
 
 // sample_weights (common.hpp:49-59) with the draw already scaled: u = U * total.  In FP32 mode a
@@ -414,8 +453,12 @@ __device__ __forceinline__ void ssa_cru(Cru<R> &s, const SsaConsts<R> &c, const 
         R sub[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            Rates<R> r;
-            sub[j] = subunit_rates<R>(s, j, s.cass[j], c, sv, r);
+            if (EXACT) {
+                Rates<R> r;
+                sub[j] = subunit_rates<R>(s, j, s.cass[j], c, sv, r);
+            } else {
+                sub[j] = subunit_total_fast<R>(s, j, s.cass[j], c, sv);
+            }
         }
         const R total = sub[0] + sub[1] + sub[2] + sub[3];
         const R u0 = rng.uniform<R>(k);
@@ -423,7 +466,7 @@ __device__ __forceinline__ void ssa_cru(Cru<R> &s, const SsaConsts<R> &c, const 
         if (EXACT)
             jump = -log(u0) / total;
         else
-            jump = -logf((float)u0) / (float)total;
+            jump = __fdividef(-logf((float)u0), (float)total);
         const bool last = !(t + jump < dt);
         const R h = last ? (dt - t) : jump;
 
@@ -468,8 +511,7 @@ __device__ __forceinline__ void ssa_cru(Cru<R> &s, const SsaConsts<R> &c, const 
             aj = scan_weights<R, 4, !EXACT>(sub, us);
             Rates<R> r;
             const R sr = subunit_rates<R>(s, aj, pick4(s.cass, aj), c, sv, r);
-            (void)sr;
-            const R subr = pick4(sub, aj);
+            const R subr = EXACT ? pick4(sub, aj) : sr;
             const R sum_lcc = r.lcc[0] + r.lcc[1] + r.lcc[2];
             R sum_ryr;
             if (EXACT) {
@@ -543,7 +585,7 @@ __device__ __forceinline__ void ssa_cru(Cru<R> &s, const SsaConsts<R> &c, const 
                 if (act == 1) {
                     const int from = byte_u(s.lcc, j);
                     if (from >= 1 && from <= 12) {
-                        const int to = lcc_next(from, atr);
+                        const int to = (int)((c.lccn[from] >> (4 * atr)) & 0xFu);
                         s.lcc = byte_set(s.lcc, j, to);
                         const bool inact1 = ((s.flags >> j) & 1u) != 0u;
                         if ((from == 5 && to == 6) || (from == 11 && to == 12))
