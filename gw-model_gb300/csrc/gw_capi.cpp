@@ -210,29 +210,37 @@ int plan_shape(gw_ctx *c, int cluster_req, int tile_req) {
     }
     c->n_clusters = (int)used.size();
     c->work.assign((size_t)c->n_clusters * C, CtaWork{-1, 0, 0, 0, 0, 0, 0, 0});
+    // A cell's CRUs are split in proportion to the CTAs' SSA warps: the leader CTA has
+    // ssa_warps, the others ssa_warps + kOdeWarps.
+    const int64_t wl = c->ssa_warps, wo = c->ssa_warps + kOdeWarps;
+    int max_count = 0;
     for (int q = 0; q < c->n_clusters; ++q) {
         int rank = 0;
         for (int cell : members[q]) {
-            const int n = c->ncru[cell];
-            const int k = std::max(1, (n + tile - 1) / tile);
+            const int64_t n = c->ncru[cell];
+            const int k = std::max(1, (int)((n + tile - 1) / tile));
+            const int64_t W = wl + (k - 1) * wo;
+            auto cum = [&](int r) -> int64_t { return r == 0 ? 0 : wl + (r - 1) * wo; };
             for (int r = 0; r < k; ++r) {
                 CtaWork &w = c->work[(size_t)q * C + rank + r];
                 w.cell = cell;
-                w.cru_begin = (int)((int64_t)n * r / k);
-                w.cru_count = (int)((int64_t)n * (r + 1) / k) - w.cru_begin;
+                w.cru_begin = (int)(n * cum(r) / W);
+                w.cru_count = (int)(n * cum(r + 1) / W) - w.cru_begin;
                 w.rank_in_cell = r;
                 w.first = rank;
                 w.n_cta_cell = k;
+                max_count = std::max(max_count, w.cru_count);
             }
             rank += k;
         }
     }
+    c->tile_cap = std::max(32, (max_count + 31) / 32 * 32);
     c->shape.cluster = C;
     c->shape.threads = (c->ssa_warps + kOdeWarps) * 32;
     c->shape.ctas = c->n_clusters * C;
     c->shape.smem = c->precision == GW_PRECISION_FP64
-                        ? smem_bytes_fp64(c->ssa_warps, c->tile_cap, c->max_cta_cell)
-                        : smem_bytes_fp32(c->ssa_warps, c->tile_cap, c->max_cta_cell);
+                        ? smem_bytes_fp64(c->tile_cap, c->max_cta_cell)
+                        : smem_bytes_fp32(c->tile_cap, c->max_cta_cell);
     int dev_smem = 0;
     cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
     if ((int)c->shape.smem > dev_smem)

@@ -1,13 +1,18 @@
 // gw_engine.cuh -- the cluster-resident multi-step engine kernel and its launcher.
 // Included by gw_kernel_fp64.cu and gw_kernel_fp32.cu, which instantiate one precision each.
 //
-// CTA = [ssa_warps SSA warps | kOdeWarps ODE warps].  The ODE warps of a cell's leader CTA run the
-// global step as the lane program of gw_ode_program.h; elsewhere they only take part in the
-// cluster barrier.  Per global step s, every thread does   wait(s) ... arrive(s+1):
-//   SSA warps : SSA of step s with the values sv[s&1], push per-warp flux partials to the leader.
-//   ODE warps : reduce the partials of step s-1, increments and Euler update (globals s -> s+1),
-//               transcendental phases of the new state, push sv[(s+1)&1], arrive; the phases
-//               that the SSA does not need (general Jup exponents) run after the arrive.
+// CTA = ssa_warps + kOdeWarps warps.  In a cell's leader CTA the last kOdeWarps warps run the
+// global step as the lane program of gw_ode_program.h; in the other CTAs of the cell every warp
+// runs SSA.  Per global step s, every thread does   wait(s) ... arrive(s+1):
+//   SSA warps : claim 32-CRU chunks of the CTA's tile from a per-step shared counter, run the SSA
+//               of step s on them with the values sv[s&1] and store one flux partial per chunk;
+//               the warp that completes the last chunk sums the chunk partials in chunk order
+//               (so the result does not depend on which warp took which chunk) and pushes the
+//               CTA's partial into the leader's shared memory (DSMEM).
+//   ODE warps : reduce the CTA partials of step s-1, increments and Euler update (globals
+//               s -> s+1), transcendental phases of the new state, push sv[(s+1)&1], arrive; the
+//               stimulus of step s+1 and the phases that the SSA does not need (general Jup
+//               exponents) run after the arrive.
 #pragma once
 
 #include <type_traits>
@@ -18,7 +23,7 @@
 namespace gw {
 namespace dev {
 
-// Per-warp flux partial, 32 bytes in both precisions:
+// Flux partial of a chunk or a CTA, 32 bytes in both precisions:
 //   FP32: {JLCC hi, lo, Jxfer hi, lo, Jtr hi, lo, ClCh count, 0} (float pairs, TwoSum-compensated)
 //   FP64: {JLCC, Jxfer, Jtr, ClCh count}
 struct Partial {
@@ -34,13 +39,13 @@ struct OdeShared {
 };
 
 struct SmemLayout {
-    size_t cc, sv, ode, prog, x, part, tile, total;
+    size_t cc, sv, ode, prog, x, part, chunk, ctr, tile, total;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 template <typename R, typename T>
-__host__ __device__ inline SmemLayout smem_layout(int ssa_warps, int tile_cap, int max_cta_cell) {
+__host__ __device__ inline SmemLayout smem_layout(int tile_cap, int max_cta_cell) {
     SmemLayout L;
     size_t o = 0;
     L.cc = o;
@@ -53,8 +58,12 @@ __host__ __device__ inline SmemLayout smem_layout(int ssa_warps, int tile_cap, i
     o += align16(sizeof(OdeProgram));
     L.x = o;
     o += align16(kOdeMaxSlots * sizeof(T));
-    L.part = o;
-    o += align16((size_t)2 * max_cta_cell * ssa_warps * sizeof(Partial));
+    L.part = o;  // [parity][rank in cell]: CTA partials (written by remote CTAs)
+    o += align16((size_t)2 * max_cta_cell * sizeof(Partial));
+    L.chunk = o;  // [chunk]: chunk partials of this CTA
+    o += align16((size_t)((tile_cap + 31) / 32) * sizeof(Partial));
+    L.ctr = o;   // chunk claim counters [parity], chunk completion counters [parity]
+    o += 16;
     L.tile = o;
     // lcc, flags, ryr[6] (u32), cass[4], jlcc[4], cajsr (R), cajsr_lo (f32)
     o += align16((size_t)tile_cap * (8 * sizeof(uint32_t) + 9 * sizeof(R) + sizeof(float)));
@@ -162,7 +171,7 @@ __device__ __forceinline__ void ode_phase(const OdeProgram &P, int q, int regime
     }
 }
 
-// Sums {JLCC, ClCh, Jtr, Jxfer} of the cell's per-warp partials of one slot; ODE warp w reduces
+// Sums {JLCC, ClCh, Jtr, Jxfer} of the cell's CTA partials of one slot; ODE warp w reduces
 // quantity w.  Writes the FP64 sums to out[] (shared) from lane 0 of each warp.
 template <bool FP64>
 __device__ __forceinline__ void reduce_partials(const Partial *slot, int n, int warp, int lane, double *out) {
@@ -211,26 +220,95 @@ __device__ __forceinline__ void push_sv(const OdeProgram &P, const T *X, const d
 
 constexpr int kMaxThreads = 512;  // SSA warps + ODE warps per CTA (128 registers per thread)
 
+// Warp sums of one chunk's (or one CTA's) flux contributions into a Partial (all lanes hold it).
+template <bool FP64>
+struct FluxAcc {
+    float jh = 0, jl = 0, xh = 0, xl = 0, th = 0, tl = 0;  // FP32: (hi, lo) pairs
+    double dj = 0, dx = 0, dtr = 0;                       // FP64
+    int acl = 0;
+    __device__ __forceinline__ void add(float j, float x, float t, int cl) {
+        df_add(jh, jl, j, 0.f);
+        df_add(xh, xl, x, 0.f);
+        df_add(th, tl, t, 0.f);
+        acl += cl;
+    }
+    __device__ __forceinline__ void add(double j, double x, double t, int cl) {
+        dj += j;
+        dx += x;
+        dtr += t;
+        acl += cl;
+    }
+    __device__ __forceinline__ void add_partial(const Partial &p) {
+        if (FP64) {
+            dj += p.v[0];
+            dx += p.v[1];
+            dtr += p.v[2];
+            acl += (int)p.v[3];
+        } else {
+            const float *f = reinterpret_cast<const float *>(p.v);
+            df_add(jh, jl, f[0], f[1]);
+            df_add(xh, xl, f[2], f[3]);
+            df_add(th, tl, f[4], f[5]);
+            acl += (int)f[6];
+        }
+    }
+    __device__ __forceinline__ Partial warp_total() {
+        Partial pv;
+        if (FP64) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                dj += __shfl_xor_sync(0xffffffffu, dj, o);
+                dx += __shfl_xor_sync(0xffffffffu, dx, o);
+                dtr += __shfl_xor_sync(0xffffffffu, dtr, o);
+                acl += __shfl_xor_sync(0xffffffffu, acl, o);
+            }
+            pv.v[0] = dj;
+            pv.v[1] = dx;
+            pv.v[2] = dtr;
+            pv.v[3] = (double)acl;
+        } else {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float a0 = __shfl_xor_sync(0xffffffffu, jh, o), a1 = __shfl_xor_sync(0xffffffffu, jl, o);
+                const float b0 = __shfl_xor_sync(0xffffffffu, xh, o), b1 = __shfl_xor_sync(0xffffffffu, xl, o);
+                const float c0 = __shfl_xor_sync(0xffffffffu, th, o), c1 = __shfl_xor_sync(0xffffffffu, tl, o);
+                acl += __shfl_xor_sync(0xffffffffu, acl, o);
+                df_add(jh, jl, a0, a1);
+                df_add(xh, xl, b0, b1);
+                df_add(th, tl, c0, c1);
+            }
+            float *f = reinterpret_cast<float *>(pv.v);
+            f[0] = jh; f[1] = jl; f[2] = xh; f[3] = xl; f[4] = th; f[5] = tl;
+            f[6] = (float)acl;
+            f[7] = 0.f;
+        }
+        return pv;
+    }
+};
+
 template <bool FP64, bool ODE64>
 __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs a) {
     using R = typename std::conditional<FP64, double, float>::type;
     using T = typename std::conditional<ODE64, double, float>::type;
     constexpr bool EXACT = FP64;
     extern __shared__ __align__(16) unsigned char smem[];
-    const int nw = a.ssa_warps;
+    const int nw = a.ssa_warps;  // SSA warps of a leader CTA; the other CTAs have nw + kOdeWarps
     const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
-    const bool ode_thread = warp >= nw;
     const int ot = (int)threadIdx.x - nw * 32;  // ODE thread index 0 .. kOdeLanes-1
     const CtaWork w = a.work[blockIdx.x];
     const bool active = w.cell >= 0;
     const bool leader = active && w.rank_in_cell == 0;
-    const SmemLayout L = smem_layout<R, T>(nw, a.tile_cap, a.max_cta_cell);
+    const bool ode_thread = leader && warp >= nw;
+    const int n_ssa = (leader ? nw : nw + kOdeWarps) * 32;  // SSA threads of this CTA
+    const SmemLayout L = smem_layout<R, T>(a.tile_cap, a.max_cta_cell);
     SsaConsts<R> &cc = *reinterpret_cast<SsaConsts<R> *>(smem + L.cc);
     R *svbuf = reinterpret_cast<R *>(smem + L.sv);
     OdeShared &os = *reinterpret_cast<OdeShared *>(smem + L.ode);
     OdeProgram &P = *reinterpret_cast<OdeProgram *>(smem + L.prog);
     T *X = reinterpret_cast<T *>(smem + L.x);
     Partial *part = reinterpret_cast<Partial *>(smem + L.part);
+    Partial *chunkp = reinterpret_cast<Partial *>(smem + L.chunk);
+    int *ctr = reinterpret_cast<int *>(smem + L.ctr);
     const int cap = a.tile_cap;
     uint32_t *t_lcc = reinterpret_cast<uint32_t *>(smem + L.tile);
     uint32_t *t_flags = t_lcc + cap;
@@ -240,19 +318,22 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
     R *t_cajsr = t_jlcc + 4 * cap;
     float *t_cajsr_lo = reinterpret_cast<float *>(t_cajsr + cap);
     const int cell = w.cell;
-    const int pslot = a.max_cta_cell * nw;  // partial entries per parity slot
-    const int npart = w.n_cta_cell * nw;
+    const int pslot = a.max_cta_cell;  // partial entries per parity slot
+    const int n_chunks = (w.cru_count + 31) >> 5;
     R *g_cass = reinterpret_cast<R *>(a.cass);
     R *g_jlcc = reinterpret_cast<R *>(a.jlcc);
     R *g_cajsr = reinterpret_cast<R *>(a.cajsr);
 
     uint64_t step0 = 0;
     if (active) {
-        if (threadIdx.x == 0) load_ssa_consts<R>(cc, a.cs[cell]);
+        if (threadIdx.x == 0) {
+            load_ssa_consts<R>(cc, a.cs[cell]);
+            ctr[0] = ctr[1] = ctr[2] = ctr[3] = 0;
+        }
         step0 = a.dyn[cell].step;
         if (!ode_thread) {
             const int64_t base = a.slot0[cell] + w.cru_begin;
-            for (int m = (int)threadIdx.x; m < w.cru_count; m += nw * 32) {
+            for (int m = (int)threadIdx.x; m < w.cru_count; m += n_ssa) {
                 const int64_t gs = base + m;
                 t_lcc[m] = a.lcc[gs];
                 t_flags[m] = a.flags[gs];
@@ -328,106 +409,99 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
         cluster_wait();
         if (!ode_thread) {
             if (active) {
+                // The counters of parity par^1 were last used in step s-1, which every warp of
+                // this CTA has left; they are next used in step s+1, after the cluster barrier.
+                if (threadIdx.x == 0) {
+                    ctr[par ^ 1] = 0;
+                    ctr[2 + (par ^ 1)] = 0;
+                }
                 const R *sv = svbuf + par * kSvCount;
-                float jh = 0, jl = 0, xh = 0, xl = 0, th = 0, tl = 0;
-                double dj = 0, dx = 0, dtr = 0;
-                int acl = 0;
-                for (int m = (int)threadIdx.x; m < w.cru_count; m += nw * 32) {
-                    Cru<R> c;
-                    c.lcc = t_lcc[m];
-                    c.flags = t_flags[m];
+                if (n_chunks == 0 && threadIdx.x == 0) {
+                    Partial *dst = part + par * pslot + w.rank_in_cell;
 #pragma unroll
-                    for (int k = 0; k < 6; ++k) c.ryr[k] = t_ryr[k * cap + m];
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        c.cass[j] = t_cass[j * cap + m];
-                        c.jlcc[j] = t_jlcc[j * cap + m];
-                    }
-                    c.cajsr = t_cajsr[m];
-                    c.cajsr_lo = FP64 ? 0.f : t_cajsr_lo[m];
-                    Stream rng;
-                    rng.open(a.seed, (uint32_t)cell, (uint32_t)(w.cru_begin + m), step0 + s, 0);
-                    R jx, jt;
-                    int ev = 0, err = 0;
-                    ssa_cru<R, EXACT>(c, cc, sv, rng, dt, a.event_cap, jx, jt, ev, err);
-                    t_lcc[m] = c.lcc;
-                    t_flags[m] = c.flags;
-#pragma unroll
-                    for (int k = 0; k < 6; ++k) t_ryr[k * cap + m] = c.ryr[k];
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        t_cass[j * cap + m] = c.cass[j];
-                        t_jlcc[j * cap + m] = c.jlcc[j];
-                    }
-                    t_cajsr[m] = c.cajsr;
-                    if (!FP64) t_cajsr_lo[m] = c.cajsr_lo;
-                    my_events += (unsigned long long)ev;
-                    my_err |= err;
-                    const R jsum = c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3];
-                    if (FP64) {
-                        dj += (double)jsum;
-                        dx += (double)jx;
-                        dtr += (double)jt;
-                    } else {
-                        df_add(jh, jl, (float)jsum, 0.f);
-                        df_add(xh, xl, (float)jx, 0.f);
-                        df_add(th, tl, (float)jt, 0.f);
-                    }
-                    acl += __popc((c.flags >> 4) & 0xFu);
-                    if (rec_ok && cell == a.tr_cell) {
-                        const int64_t cm = w.cru_begin + m;
-                        const int64_t st = a.tr_cru_stride;
-                        a.tr_lcc[r_idx * st + cm] = c.lcc;
-                        a.tr_flags[r_idx * st + cm] = c.flags;
-#pragma unroll
-                        for (int k = 0; k < 6; ++k) a.tr_ryr[(r_idx * 6 + k) * st + cm] = c.ryr[k];
-#pragma unroll
-                        for (int j = 0; j < 4; ++j)
-                            reinterpret_cast<R *>(a.tr_cass)[(r_idx * 4 + j) * st + cm] = c.cass[j];
-                        reinterpret_cast<R *>(a.tr_cajsr)[r_idx * st + cm] = c.cajsr;
-                    }
+                    for (int v = 0; v < 4; ++v) st_remote(map_rank(&dst->v[v], (uint32_t)w.first), 0.0);
                 }
-                // warp reduction and push of the partial to the leader CTA
-                Partial pv;
-                if (FP64) {
-                    double dcl = (double)acl;
+                for (;;) {
+                    int ch = 0;
+                    if (lane == 0) ch = atomicAdd(&ctr[par], 1);
+                    ch = __shfl_sync(0xffffffffu, ch, 0);
+                    if (ch >= n_chunks) break;
+                    const int m = ch * 32 + lane;
+                    FluxAcc<FP64> acc;
+                    if (m < w.cru_count) {
+                        Cru<R> c;
+                        c.lcc = t_lcc[m];
+                        c.flags = t_flags[m];
 #pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) {
-                        dj += __shfl_xor_sync(0xffffffffu, dj, o);
-                        dx += __shfl_xor_sync(0xffffffffu, dx, o);
-                        dtr += __shfl_xor_sync(0xffffffffu, dtr, o);
-                        dcl += __shfl_xor_sync(0xffffffffu, dcl, o);
-                    }
-                    pv.v[0] = dj;
-                    pv.v[1] = dx;
-                    pv.v[2] = dtr;
-                    pv.v[3] = dcl;
-                } else {
+                        for (int k = 0; k < 6; ++k) c.ryr[k] = t_ryr[k * cap + m];
 #pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) {
-                        const float a0 = __shfl_xor_sync(0xffffffffu, jh, o), a1 = __shfl_xor_sync(0xffffffffu, jl, o);
-                        const float b0 = __shfl_xor_sync(0xffffffffu, xh, o), b1 = __shfl_xor_sync(0xffffffffu, xl, o);
-                        const float c0 = __shfl_xor_sync(0xffffffffu, th, o), c1 = __shfl_xor_sync(0xffffffffu, tl, o);
-                        acl += __shfl_xor_sync(0xffffffffu, acl, o);
-                        df_add(jh, jl, a0, a1);
-                        df_add(xh, xl, b0, b1);
-                        df_add(th, tl, c0, c1);
+                        for (int j = 0; j < 4; ++j) {
+                            c.cass[j] = t_cass[j * cap + m];
+                            c.jlcc[j] = t_jlcc[j * cap + m];
+                        }
+                        c.cajsr = t_cajsr[m];
+                        c.cajsr_lo = FP64 ? 0.f : t_cajsr_lo[m];
+                        Stream rng;
+                        rng.open(a.seed, (uint32_t)cell, (uint32_t)(w.cru_begin + m), step0 + s, 0);
+                        R jx, jt;
+                        int ev = 0, err = 0;
+                        ssa_cru<R, EXACT>(c, cc, sv, rng, dt, a.event_cap, jx, jt, ev, err);
+                        t_lcc[m] = c.lcc;
+                        t_flags[m] = c.flags;
+#pragma unroll
+                        for (int k = 0; k < 6; ++k) t_ryr[k * cap + m] = c.ryr[k];
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            t_cass[j * cap + m] = c.cass[j];
+                            t_jlcc[j * cap + m] = c.jlcc[j];
+                        }
+                        t_cajsr[m] = c.cajsr;
+                        if (!FP64) t_cajsr_lo[m] = c.cajsr_lo;
+                        my_events += (unsigned long long)ev;
+                        my_err |= err;
+                        acc.add(c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3], jx, jt,
+                                __popc((c.flags >> 4) & 0xFu));
+                        if (rec_ok && cell == a.tr_cell) {
+                            const int64_t cm = w.cru_begin + m;
+                            const int64_t st = a.tr_cru_stride;
+                            a.tr_lcc[r_idx * st + cm] = c.lcc;
+                            a.tr_flags[r_idx * st + cm] = c.flags;
+#pragma unroll
+                            for (int k = 0; k < 6; ++k) a.tr_ryr[(r_idx * 6 + k) * st + cm] = c.ryr[k];
+#pragma unroll
+                            for (int j = 0; j < 4; ++j)
+                                reinterpret_cast<R *>(a.tr_cass)[(r_idx * 4 + j) * st + cm] = c.cass[j];
+                            reinterpret_cast<R *>(a.tr_cajsr)[r_idx * st + cm] = c.cajsr;
+                        }
                     }
-                    float *f = reinterpret_cast<float *>(pv.v);
-                    f[0] = jh; f[1] = jl; f[2] = xh; f[3] = xl; f[4] = th; f[5] = tl;
-                    f[6] = (float)acl;
-                    f[7] = 0.f;
-                }
-                if (lane < 4) {
-                    Partial *dst = part + par * pslot + w.rank_in_cell * nw + warp;
-                    const double v = lane == 0 ? pv.v[0] : lane == 1 ? pv.v[1] : lane == 2 ? pv.v[2] : pv.v[3];
-                    st_remote(map_rank(&dst->v[lane], (uint32_t)w.first), v);
+                    const Partial pv = acc.warp_total();
+                    int done = 0;
+                    if (lane == 0) {
+                        chunkp[ch] = pv;
+                        __threadfence_block();
+                        done = atomicAdd(&ctr[2 + par], 1);
+                        __threadfence_block();
+                    }
+                    done = __shfl_sync(0xffffffffu, done, 0);
+                    if (done == n_chunks - 1) {
+                        // Last chunk of the CTA: sum the chunk partials in chunk order, push.
+                        __syncwarp();
+                        FluxAcc<FP64> tot;
+                        for (int q = lane; q < n_chunks; q += 32) tot.add_partial(chunkp[q]);
+                        const Partial pc = tot.warp_total();
+                        if (lane == 0) {
+                            Partial *dst = part + par * pslot + w.rank_in_cell;
+#pragma unroll
+                            for (int v = 0; v < 4; ++v) st_remote(map_rank(&dst->v[v], (uint32_t)w.first), pc.v[v]);
+                        }
+                    }
                 }
             }
             cluster_arrive();
-        } else if (leader) {
-            // fluxes of step s-1 (or the carry), then the global step s -> s+1
-            if (s > 0) reduce_partials<FP64>(part + (par ^ 1) * pslot, npart, ot >> 5, lane, os.sums);
+        } else {
+            // leader CTA's ODE warps: fluxes of step s-1 (or the carry), then the global step
+            // s -> s+1
+            if (s > 0) reduce_partials<FP64>(part + (par ^ 1) * pslot, w.n_cta_cell, ot >> 5, lane, os.sums);
             ode_bar();
             if (ot < 4) X[XS_SUMS + ot] = (T)os.sums[ot];
             if (ot == 0 && (!(os.g[1] > 0.0) || !(os.g[2] > 0.0)) && os.status == 0) os.status = GW_ERR_NERNST;
@@ -437,10 +511,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
                 ode_phase<T>(P, q, reg_n, X, os.g, ot, &bad);
                 ode_bar();
             }
-            if (ot == 0) {
-                os.t += a.dt;
-                X[XS_ISTIM] = (T)stimulus(a.dyn[cell], os.t, ri + 1);
-            }
+            if (ot == 0) os.t += a.dt;
             if (rec_ok) {
                 double *dst = a.tr_glob + ((int64_t)cell * a.rec_cap + r_idx) * kNumGlobals;
                 for (int i = ot; i < kNumGlobals; i += kOdeLanes) dst[i] = os.g[i];
@@ -453,19 +524,20 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
             }
             push_sv<FP64, T>(P, X, os.g, svbuf, par ^ 1, w, ot);
             cluster_arrive();
+            // off the critical path: the stimulus of step s+1 (read by the first phase of the
+            // next step, after its ode_bar) and the phases the SSA does not need
+            if (ot == 0) X[XS_ISTIM] = (T)stimulus(a.dyn[cell], os.t, ri + 1);
             for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
                 ode_phase<T>(P, q, reg, X, os.g, ot, &bad);
                 ode_bar();
             }
-        } else {
-            cluster_arrive();
         }
     }
     cluster_wait();
 
     // Epilogue: carry of the last step's fluxes, globals and counters back to the cell block.
     if (leader && ode_thread) {
-        if (a.n_steps > 0) reduce_partials<FP64>(part + ((a.n_steps - 1) & 1) * pslot, npart, ot >> 5, lane, os.sums);
+        if (a.n_steps > 0) reduce_partials<FP64>(part + ((a.n_steps - 1) & 1) * pslot, w.n_cta_cell, ot >> 5, lane, os.sums);
         const unsigned anybad = __ballot_sync(0xffffffffu, bad != 0);
         if (lane == 0 && anybad) atomicCAS(&os.status, 0, (int)GW_ERR_NONFINITE);
         ode_bar();
@@ -483,7 +555,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
     }
     if (active && !ode_thread) {
         const int64_t base = a.slot0[cell] + w.cru_begin;
-        for (int m = (int)threadIdx.x; m < w.cru_count; m += nw * 32) {
+        for (int m = (int)threadIdx.x; m < w.cru_count; m += n_ssa) {
             const int64_t gs = base + m;
             a.lcc[gs] = t_lcc[m];
             a.flags[gs] = t_flags[m];

@@ -113,7 +113,8 @@ struct KernelArgs {
     int n_cells;
     unsigned long long *events;
     int *status;
-    int ssa_warps;      // SSA warps per CTA (the ODE warps follow them)
+    int ssa_warps;      // SSA warps of a leader CTA (its kOdeWarps ODE warps follow them); the
+                        // other CTAs of a cell run SSA on all ssa_warps + kOdeWarps warps
     int tile_cap;       // CRU capacity of one CTA
     int max_cta_cell;   // max CTAs of one cell (partial slot stride)
     int pad;
@@ -129,8 +130,8 @@ struct LaunchShape {
 // Implemented per precision in gw_kernel_fp64.cu / gw_kernel_fp32.cu.
 int launch_engine_fp64(const KernelArgs &a, const LaunchShape &s, void *stream, bool ode64);
 int launch_engine_fp32(const KernelArgs &a, const LaunchShape &s, void *stream, bool ode64);
-size_t smem_bytes_fp64(int ssa_warps, int tile_cap, int max_cta_cell);
-size_t smem_bytes_fp32(int ssa_warps, int tile_cap, int max_cta_cell);
+size_t smem_bytes_fp64(int tile_cap, int max_cta_cell);
+size_t smem_bytes_fp32(int tile_cap, int max_cta_cell);
 int max_active_clusters_fp64(const LaunchShape &s, bool ode64, int *out);
 int max_active_clusters_fp32(const LaunchShape &s, bool ode64, int *out);
 int sample_initial_crus_dev(const KernelArgs &a, int cell, int ncru, int fp64, void *stream);

@@ -7,8 +7,8 @@ namespace gw {
 int launch_engine_fp64(const KernelArgs &a, const LaunchShape &s, void *stream, bool ode64) {
     return dev::launch_engine<true>(a, s, stream, ode64);
 }
-size_t smem_bytes_fp64(int ssa_warps, int tile_cap, int max_cta_cell) {
-    return dev::smem_layout<double, double>(ssa_warps, tile_cap, max_cta_cell).total;
+size_t smem_bytes_fp64(int tile_cap, int max_cta_cell) {
+    return dev::smem_layout<double, double>(tile_cap, max_cta_cell).total;
 }
 int max_active_clusters_fp64(const LaunchShape &s, bool ode64, int *out) {
     return dev::max_active_clusters<true>(s, ode64, out);
