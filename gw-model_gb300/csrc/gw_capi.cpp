@@ -10,6 +10,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -302,6 +303,77 @@ int plane_put(gw_ctx *c, DevBuf &b, int plane, int64_t s0, int64_t n, const T *i
     CK(c, cudaMemcpy(b.as<T>() + plane * c->n_slots + s0, in, sizeof(T) * n, cudaMemcpyHostToDevice));
     return GW_OK;
 }
+
+// ---- gw_run_noalloc: record staging in a static device array ----------------------------------
+// One array per device, in the module image.  Nothing in it has to start at zero: every record
+// slot the trace unpack reads was written by the engine launch just before it.
+constexpr size_t kNoallocScratchBytes = GW_NOALLOC_SCRATCH_BYTES;
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_ptr[kNoallocMaxDevices];  // device address per device, set once
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[GW_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+// Device address of the scratch on the current device (c->device), looked up once per device.
+int noalloc_scratch(gw_ctx *c, unsigned char **out) {
+    if (c->device < 0 || c->device >= kNoallocMaxDevices)
+        return fail(c, GW_ERR_UNSUPPORTED, "gw_run_noalloc supports devices 0..%d", kNoallocMaxDevices - 1);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[c->device]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(c, GW_ERR_CUDA, "cudaGetSymbolAddress(no-allocation scratch): %s", cudaGetErrorString(e));
+        g_noalloc_ptr[c->device] = static_cast<unsigned char *>(p);
+    }
+    *out = g_noalloc_ptr[c->device];
+    return GW_OK;
+}
+
+// Engine record planes -> the reference's record layouts (gw_trace), one thread per (record, CRU).
+__global__ void unpack_trace_kernel(int nr, int ncr, int64_t stride, bool fp64, const uint32_t *lcc,
+                                    const uint32_t *flags, const uint32_t *ryr, const void *cass,
+                                    const void *cajsr, int32_t *o_lcc, int32_t *o_lcci, int32_t *o_clch,
+                                    int32_t *o_ryr, double *o_cass, double *o_cajsr) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)nr * ncr) return;
+    const int64_t r = idx / ncr, i = idx % ncr;
+    const uint32_t w = lcc[r * stride + i], f = flags[r * stride + i];
+    for (int j = 0; j < 4; ++j) {
+        const int64_t o = idx * 4 + j;
+        if (o_lcc) o_lcc[o] = (int32_t)((w >> (8 * j)) & 0xFFu);
+        if (o_lcci) o_lcci[o] = (int32_t)((f >> j) & 1u);
+        if (o_clch) o_clch[o] = (int32_t)((f >> (4 + j)) & 1u);
+        if (o_ryr)
+            for (int k = 0; k < 6; ++k)
+                o_ryr[o * 6 + k] = (int32_t)(int8_t)((ryr[(r * 6 + k) * stride + i] >> (8 * j)) & 0xFFu);
+        if (o_cass) {
+            const int64_t src = (r * 4 + j) * stride + i;
+            o_cass[o] = fp64 ? static_cast<const double *>(cass)[src] : (double)static_cast<const float *>(cass)[src];
+        }
+    }
+    if (o_cajsr) {
+        const int64_t src = r * stride + i;
+        o_cajsr[idx] = fp64 ? static_cast<const double *>(cajsr)[src] : (double)static_cast<const float *>(cajsr)[src];
+    }
+}
+
+// Bump allocator over the scratch (256-byte aligned regions).
+struct ScratchCursor {
+    unsigned char *base;
+    size_t used;
+    template <typename T>
+    T *take(size_t bytes) {
+        if (bytes == 0) return nullptr;
+        T *p = reinterpret_cast<T *>(base + used);
+        used += (bytes + 255) & ~(size_t)255;
+        return p;
+    }
+};
 
 }  // namespace
 
@@ -855,6 +927,168 @@ int gw_run(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_trace *tr
                                                            : "error";
             return fail(c, st[i], "cell %d: %s", i, what);
         }
+    return GW_OK;
+}
+
+int gw_run_noalloc(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_trace *tr) {
+    if (!c) return GW_ERR_INVALID_ARGUMENT;
+    if (!(dt > 0.0) || !std::isfinite(dt)) return fail(c, GW_ERR_INVALID_ARGUMENT, "dt must be > 0");
+    if (n_steps < 0) return fail(c, GW_ERR_INVALID_ARGUMENT, "n_steps must be >= 0");
+    if (record_every < 0) return fail(c, GW_ERR_INVALID_ARGUMENT, "record_every must be >= 0");
+    CK(c, cudaSetDevice(c->device));
+    if (tr) tr->n_written = 0;
+    const bool recording = tr && record_every > 0 && tr->max_records > 0;
+    const bool cru_fields = recording && (tr->CaSS || tr->CaJSR || tr->LCC || tr->LCC_inactivation || tr->RyR || tr->ClCh);
+    const int tr_cell = cru_fields ? tr->cru_cell : -1;
+    if (tr_cell >= c->n_cells) return fail(c, GW_ERR_INVALID_ARGUMENT, "trace cell out of range");
+    {
+        int rc = pull_dyn(c);
+        if (rc) return rc;
+        for (int i = 0; i < c->n_cells; ++i)
+            if (c->dyn_host[i].step + (uint64_t)n_steps > 0xFFFFFFFFull)
+                return fail(c, GW_ERR_INVALID_ARGUMENT, "more than 2^32 steps in one context");
+    }
+    unsigned char *scratch = nullptr;
+    {
+        int rc = noalloc_scratch(c, &scratch);
+        if (rc) return rc;
+    }
+    // Scratch bytes of one record (engine planes + reference layouts), 256-byte padding included.
+    const int ncr = tr_cell >= 0 ? c->ncru[tr_cell] : 0;
+    const int64_t stride = tr_cell >= 0 ? ((int64_t)ncr + 31) / 32 * 32 : 0;
+    auto pad = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    auto bytes_for = [&](int64_t nrec) -> size_t {
+        if (!recording) return 0;
+        size_t b = pad(sizeof(double) * nrec) + pad(sizeof(double) * kNumGlobals * nrec * c->n_cells);
+        if (tr_cell >= 0) {
+            b += 2 * pad(4 * stride * nrec) + pad(4 * 6 * stride * nrec) + pad(c->rsize * 4 * stride * nrec) +
+                 pad(c->rsize * stride * nrec);
+            const size_t n4 = (size_t)nrec * ncr * 4;
+            if (tr->LCC) b += pad(4 * n4);
+            if (tr->LCC_inactivation) b += pad(4 * n4);
+            if (tr->ClCh) b += pad(4 * n4);
+            if (tr->RyR) b += pad(4 * 6 * n4);
+            if (tr->CaSS) b += pad(8 * n4);
+            if (tr->CaJSR) b += pad(8 * (size_t)nrec * ncr);
+        }
+        return b;
+    };
+    // Steps per launch: the engine's launch length, shortened so that its records fit the scratch.
+    int64_t chunk = c->steps_per_launch;
+    int64_t rec_cap = 0;
+    if (recording) {
+        if (bytes_for(3) > kNoallocScratchBytes)
+            return fail(c, GW_ERR_INVALID_ARGUMENT,
+                        "a trace record of this context needs about %zu bytes of staging and gw_run_noalloc stages at "
+                        "least 3 records in its %zu-byte scratch; record fewer CRU fields or use gw_run",
+                        bytes_for(1), kNoallocScratchBytes);
+        while (bytes_for(chunk / record_every + 2) > kNoallocScratchBytes) chunk = std::max<int64_t>(1, chunk / 2);
+        rec_cap = std::min<int64_t>(tr->max_records, chunk / record_every + 2);
+    }
+    ScratchCursor sc{scratch, 0};
+    KernelArgs a = base_args(c);
+    a.dt = dt;
+    a.record_every = recording ? record_every : 0;
+    a.rec_cap = (int)rec_cap;
+    a.tr_cell = tr_cell;
+    a.tr_cru_stride = stride;
+    int32_t *u_lcc = nullptr, *u_lcci = nullptr, *u_clch = nullptr, *u_ryr = nullptr;
+    double *u_cass = nullptr, *u_cajsr = nullptr;
+    if (recording) {
+        a.tr_t = sc.take<double>(sizeof(double) * rec_cap);
+        a.tr_glob = sc.take<double>(sizeof(double) * kNumGlobals * rec_cap * c->n_cells);
+        if (tr_cell >= 0) {
+            a.tr_lcc = sc.take<uint32_t>(4 * stride * rec_cap);
+            a.tr_flags = sc.take<uint32_t>(4 * stride * rec_cap);
+            a.tr_ryr = sc.take<uint32_t>(4 * 6 * stride * rec_cap);
+            a.tr_cass = sc.take<unsigned char>(c->rsize * 4 * stride * rec_cap);
+            a.tr_cajsr = sc.take<unsigned char>(c->rsize * stride * rec_cap);
+            const size_t n4 = (size_t)rec_cap * ncr * 4;
+            if (tr->LCC) u_lcc = sc.take<int32_t>(4 * n4);
+            if (tr->LCC_inactivation) u_lcci = sc.take<int32_t>(4 * n4);
+            if (tr->ClCh) u_clch = sc.take<int32_t>(4 * n4);
+            if (tr->RyR) u_ryr = sc.take<int32_t>(4 * 6 * n4);
+            if (tr->CaSS) u_cass = sc.take<double>(8 * n4);
+            if (tr->CaJSR) u_cajsr = sc.take<double>(8 * (size_t)rec_cap * ncr);
+        }
+    }
+    if (sc.used > kNoallocScratchBytes) return fail(c, GW_ERR_INVALID_ARGUMENT, "trace staging exceeds the scratch");
+    CK(c, cudaMemsetAsync(c->d_status.p, 0, sizeof(int) * c->n_cells, c->stream));
+    float total_ms = 0.f;
+    int64_t done = 0;
+    while (done < n_steps) {
+        const int n = (int)std::min<int64_t>(chunk, n_steps - done);
+        a.run_step0 = done;
+        a.n_steps = n;
+        int64_t r_lo = 0, r_hi = -1;
+        if (recording) {
+            r_lo = (done + record_every - 1) / record_every;
+            r_hi = std::min<int64_t>((done + n - 1) / record_every, tr->max_records - 1);
+            a.rec_base = r_lo;
+        }
+        CK(c, cudaEventRecord(c->ev0, c->stream));
+        const int e = c->precision == GW_PRECISION_FP64 ? launch_engine_fp64(a, c->shape, c->stream, c->ode64)
+                                                        : launch_engine_fp32(a, c->shape, c->stream, c->ode64);
+        if (e != 0) return fail(c, GW_ERR_CUDA, "engine launch: %s", cudaGetErrorString((cudaError_t)e));
+        CK(c, cudaEventRecord(c->ev1, c->stream));
+        c->stats.launches++;
+        if (recording && r_hi >= r_lo) {
+            const int64_t nr = r_hi - r_lo + 1;
+            if (tr->t)
+                CK(c, cudaMemcpyAsync(tr->t + r_lo, a.tr_t, sizeof(double) * nr, cudaMemcpyDeviceToHost, c->stream));
+            if (tr->globals)
+                CK(c, cudaMemcpy2DAsync(tr->globals + r_lo * kNumGlobals, sizeof(double) * kNumGlobals * tr->max_records,
+                                        a.tr_glob, sizeof(double) * kNumGlobals * rec_cap,
+                                        sizeof(double) * kNumGlobals * nr, c->n_cells, cudaMemcpyDeviceToHost, c->stream));
+            if (tr_cell >= 0 && ncr > 0) {
+                const int64_t total = nr * ncr;
+                const int threads = 256;
+                const unsigned blocks = (unsigned)((total + threads - 1) / threads);
+                unpack_trace_kernel<<<blocks, threads, 0, c->stream>>>(
+                    (int)nr, ncr, stride, c->rsize == 8, a.tr_lcc, a.tr_flags, a.tr_ryr, a.tr_cass, a.tr_cajsr, u_lcc,
+                    u_lcci, u_clch, u_ryr, u_cass, u_cajsr);
+                CK(c, cudaGetLastError());
+                const size_t n4 = (size_t)nr * ncr * 4;
+                const int64_t o4 = r_lo * ncr * 4;
+                if (tr->LCC) CK(c, cudaMemcpyAsync(tr->LCC + o4, u_lcc, 4 * n4, cudaMemcpyDeviceToHost, c->stream));
+                if (tr->LCC_inactivation)
+                    CK(c, cudaMemcpyAsync(tr->LCC_inactivation + o4, u_lcci, 4 * n4, cudaMemcpyDeviceToHost, c->stream));
+                if (tr->ClCh) CK(c, cudaMemcpyAsync(tr->ClCh + o4, u_clch, 4 * n4, cudaMemcpyDeviceToHost, c->stream));
+                if (tr->RyR) CK(c, cudaMemcpyAsync(tr->RyR + o4 * 6, u_ryr, 4 * 6 * n4, cudaMemcpyDeviceToHost, c->stream));
+                if (tr->CaSS) CK(c, cudaMemcpyAsync(tr->CaSS + o4, u_cass, 8 * n4, cudaMemcpyDeviceToHost, c->stream));
+                if (tr->CaJSR)
+                    CK(c, cudaMemcpyAsync(tr->CaJSR + r_lo * ncr, u_cajsr, 8 * (size_t)nr * ncr, cudaMemcpyDeviceToHost, c->stream));
+            }
+            // the next launch reuses the staging area
+            CK(c, cudaStreamSynchronize(c->stream));
+            tr->n_written = std::max<int64_t>(tr->n_written, r_hi + 1);
+        }
+        CK(c, cudaEventSynchronize(c->ev1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        total_ms += ms;
+        done += n;
+    }
+    CK(c, cudaStreamSynchronize(c->stream));
+    CK(c, cudaGetLastError());
+    c->stats.kernel_ms += total_ms;
+    c->stats.steps += (uint64_t)n_steps;
+    unsigned long long ev = 0;
+    CK(c, cudaMemcpy(&ev, c->d_events.p, sizeof ev, cudaMemcpyDeviceToHost));
+    c->stats.events = ev;
+    int st[64];
+    for (int i0 = 0; i0 < c->n_cells; i0 += 64) {
+        const int nb = std::min(64, c->n_cells - i0);
+        CK(c, cudaMemcpy(st, c->d_status.as<int>() + i0, sizeof(int) * nb, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < nb; ++i)
+            if (st[i] != 0) {
+                const char *what = st[i] == GW_ERR_EVENT_CAP ? "a CRU exceeded the per-step jump cap"
+                                   : st[i] == GW_ERR_NERNST  ? "non-positive concentration in a Nernst potential"
+                                   : st[i] == GW_ERR_NONFINITE ? "a global state variable became NaN/Inf"
+                                                               : "error";
+                return fail(c, st[i], "cell %d: %s", i0 + i, what);
+            }
+    }
     return GW_OK;
 }
 

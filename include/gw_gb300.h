@@ -164,6 +164,31 @@ int gw_set_stimulus_samples(gw_ctx *ctx, int cell, const double *Istim, int64_t 
  * n_steps global steps of size dt for every cell; t accumulates by t += dt. */
 int gw_run(gw_ctx *ctx, double dt, int64_t n_steps, int record_every, gw_trace *trace);
 
+/* gw_run without allocation.  No counterpart in the reference (its run<PRNG> allocates its record
+ * vectors per call, pyGW.hpp:102-122).
+ *
+ * Same steps, records and results as gw_run, but neither device nor host memory is allocated:
+ * gw_run stages the records of each launch in device buffers it cudaMallocs and cudaFrees per call
+ * (cudaFree synchronizes the whole device) and converts them in host vectors.  This variant stages
+ * them in one static device array of GW_NOALLOC_SCRATCH_BYTES per device, converts them to the
+ * gw_trace layouts on the device and copies them straight into the caller's arrays.  It is for
+ * callers that cannot allocate: a driver that steps cells from several host threads or streams,
+ * where every cudaFree would stall the other streams, and processes whose device memory is held by
+ * another allocator's pool (a cudaMalloc outside that pool fails although the pool has room).
+ *
+ * Limit: the records of one launch must fit the scratch.  Launches are shortened until they do;
+ * if even 3 records do not fit, the call returns GW_ERR_INVALID_ARGUMENT with the size needed
+ * (record fewer CRU fields, or use gw_run).  Without a trace it uses no scratch at all.
+ * Set-up: the first call on a device looks the array up (cudaGetSymbolAddress, which may load the
+ * module); make that first call before any stream capture begins.
+ * Nothing in the scratch has to start at zero: each record slot is written by the engine before
+ * it is read.  The per-cell status words are zeroed by the call itself, as gw_run does.
+ * Concurrency: the scratch is shared by every context on the device.  Calls that overlap in time
+ * on one device (other threads, other contexts) race on it; serialize them.  The call has
+ * synchronized its stream when it returns, so consecutive calls from one thread are safe. */
+#define GW_NOALLOC_SCRATCH_BYTES ((size_t)16 << 20)
+int gw_run_noalloc(gw_ctx *ctx, double dt, int64_t n_steps, int record_every, gw_trace *trace);
+
 int gw_get_time(gw_ctx *ctx, int cell, double *t, uint64_t *step);
 /* Restores a cell's accumulated time and global step index (the RNG counter).  With the globals,
  * the CRU arrays including JLCC, and the flux carry, this resumes a run bit for bit; the reference
