@@ -1,24 +1,28 @@
-"""Benchmark: CRU-steps/s and simulated ms per wall-second of the Greenstein-Winslow hybrid SSA.
+"""Benchmark: CRU-steps/s and simulated ms per wall-second of the Greenstein-Winslow hybrid SSA,
+batched GPU vs plain GPU vs the reference's CPU path.
 
-Workload (one GPU): one full cell of 12,500 CRUs (NCaRU = 12,500, so each simulated CRU stands for
-one real CRU), reference default parameters, GW::GlobalState resting globals, the reference's random
-initial CRU distributions, dt = 1e-3 ms, 1 Hz pacing with a +100 pA/pF, 0.5 ms stimulus (the
-reference integrates dV = dt (Istim - sum I), so the usual -100 pA/pF inward stimulus is +100 here).
-CRU state FP32, global ODE FP64 with compensated flux reduction.  Synthetic seeded input.
+Workload of the JSON line's `value` (one GPU): one full cell of 12,500 CRUs (NCaRU = 12,500, so
+each simulated CRU stands for one real CRU), reference default parameters, GW::GlobalState resting
+globals, the reference's random initial CRU distributions, dt = 1e-3 ms, 1 Hz pacing with a
++100 pA/pF, 0.5 ms stimulus (the reference integrates dV = dt (Istim - sum I), so the usual
+-100 pA/pF inward stimulus is +100 here).  CRU state FP32, global ODE FP64 with compensated flux
+reduction.  Synthetic seeded input.  A bench step is `--span-ms` of simulated time of that paced
+cell; the timed steps continue the protocol.
 
-A bench step is `--span-ms` of simulated time of that paced cell (the timed steps continue the
-protocol, so they cover the AP, the Ca release and the diastolic interval in proportion).
+  value        CRU-steps/s, state resident on the device, CUDA events around the engine kernel
+  e2e          the same through the reference-facing C ABI (gw_simulate: host arrays in and out,
+               the per-step stimulus samples uploaded, a fresh context per call)
+  paths        plain GPU (the same cell, one kernel launch per global step) and batched GPU (256
+               cells of 2,000-12,500 CRUs, log-normal per-cell parameters and 400-1000 ms cycle
+               lengths in one launch), each as CRU-steps/s and simulated ms per wall-second
+  roofline     the engine kernel against HBM, algorithmic bytes = the 72-byte FP32 CRU state read
+               and written once per CRU-step; the kernel keeps the state on chip between steps, so
+               the bound that binds is the per-step dependency chain (see profiles/)
+  cpu_baseline the oracle port of the reference's C++ (OpenMP over CRUs) on the host cores,
+               bounded sample
 
-  value  : CRU-steps/s with the state resident on the device (CUDA events around the engine kernel)
-  e2e    : the same through the reference-facing C ABI (gw_simulate: host arrays in and out, the
-           per-step stimulus samples uploaded, final state and records copied back, every step)
-  roofline: the engine kernel against HBM (algorithmic bytes = the CRU state read and written once
-           per CRU-step) -- the kernel keeps the state on chip, so this bound is not binding; see
-           profiles/ for the FP32 / issue-bound counters
-  cpu_baseline: the oracle port of the reference's C++ on the host cores (OpenMP), bounded sample
-
---impl reference times the reference's CPU implementation of the path (the oracle port; the
-reference's own C++ needs its sources, which exist only where it was built) on the host cores.
+--impl reference times the reference's CPU implementation of the path (the oracle port) on the
+host cores with all threads.
 """
 from __future__ import annotations
 
@@ -40,7 +44,10 @@ NCRU = 12500
 DT = 1e-3
 PERIOD = 1000.0
 STIM_AMP, STIM_DUR = 100.0, 0.5
-BYTES_PER_CRU_STEP = 2 * (4 * 4 + 4 * 4 + 4 * 4 + 4 + 4 + 4 * 4 + 4 * 4 + 4)  # FP32 state in + out
+METRIC = "CRU-steps/s and sim-ms/wall-s: batched vs plain GPU vs CPU, at KS/FP64 tol"
+# FP32 CRU state per CRU: LCC states 4 B, gate + ClCh bits 4 B, RyR counts 24 B, CaSS 16 B,
+# JLCC 16 B, CaJSR 4 B, CaJSR compensation 4 B = 72 B, read and written once per CRU-step.
+BYTES_PER_CRU_STEP = 2 * 72
 
 
 def parse():
@@ -138,6 +145,16 @@ def cpu_baseline(seconds: float, ncru: int = NCRU):
             "sample": f"{ncru} CRUs x {steps} steps ({steps * DT:.3f} ms from the stimulus) in {el:.1f} s"}
 
 
+def workload_config(args, world=1):
+    cells = max(args.cells, 1)
+    return {"workload": f"{'single cell' if cells == 1 else f'{cells} replicate cells'} of {NCRU} CRUs, "
+                        f"1 Hz pacing (+{STIM_AMP:g} pA/pF, {STIM_DUR:g} ms), dt 1e-3 ms, "
+                        f"FP32 CRU state, FP64 global ODE",
+            "ncru": NCRU, "cells_per_gpu": cells, "span_ms_per_step": args.span_ms,
+            "parallelism": f"replicas x{world}",
+            "l2": "CRU state (0.9 MB per cell) stays in shared memory across steps; no L2 flush"}
+
+
 def run_reference(args):
     from gwgb300 import dist as gd
 
@@ -150,10 +167,10 @@ def run_reference(args):
         cpu_baseline(per)
     vals = [cpu_baseline(per) for _ in range(K)]
     v = statistics.median(x["value"] for x in vals)
-    line = {"impl": "reference", "metric": "CRU-steps/s", "value": v, "unit": "CRU-steps/s",
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "CRU-steps/s",
             "n_gpus": args.gpus, "steps": K, "warmup": W, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"single cell, {NCRU} CRUs, 1 Hz pacing, dt 1e-3 ms"},
+            "config": workload_config(args, world),
             "cpu_baseline": {"value": v, "unit": "CRU-steps/s", "cores": vals[0]["cores"], "kind": "port",
                              "sample": vals[0]["sample"]},
             "e2e": {"value": v, "unit": "CRU-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -198,15 +215,11 @@ def main():
     pk, pk_kind = peaks()
     per_launch_steps = span * K / max(launches, 1)
     achieved_gbs = BYTES_PER_CRU_STEP * NCRU * cells * span * K / kernel_s / 1e9
-    line = {"metric": "CRU-steps/s", "value": value, "unit": "CRU-steps/s", "n_gpus": world,
+    line = {"metric": METRIC, "value": value, "unit": "CRU-steps/s", "n_gpus": world,
             "steps": K, "warmup": W, "ms_per_step": kernel_s / K * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"{'single cell' if cells == 1 else f'{cells} replicate cells'}, "
-                                   f"{NCRU} CRUs each, 1 Hz pacing (+{STIM_AMP} pA/pF, {STIM_DUR} ms), "
-                                   f"dt 1e-3 ms, FP32 CRU state, FP64 global ODE",
-                       "ncru": NCRU, "cells_per_gpu": cells, "span_ms_per_step": args.span_ms,
-                       "parallelism": f"replicas x{world}", "l2": "state on chip; inputs < L2, no flush needed",
-                       "launch_shape": {k: st1[k] for k in ("cluster_ctas", "cta_crus", "threads_per_cta", "n_clusters")}},
+            "config": workload_config(args, world),
+            "launch_shape": {k: st1[k] for k in ("cluster_ctas", "cta_crus", "threads_per_cta", "n_clusters")},
             "sim_ms_per_wall_s": cells * world * span * K * DT / kernel_s,
             "events_per_cru_step": (st1["events"] - st0["events"]) / max(NCRU * cells * span * K, 1),
             "gpu_launches": launches,
@@ -218,10 +231,82 @@ def main():
     e.close()
     if rank == 0 and not args.no_extras:
         line["e2e"] = e2e_measure(span, K)
+        line["paths"] = {"plain_gpu": plain_measure(local_rank), "batched_gpu": batched_measure(local_rank)}
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+        line["paths"]["cpu"] = {"cru_steps_per_s": line["cpu_baseline"]["value"],
+                                "sim_ms_per_wall_s": line["cpu_baseline"]["value"] / NCRU * DT,
+                                "cores": line["cpu_baseline"]["cores"]}
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+def plain_measure(device, steps=3000):
+    """The same paced cell with one engine launch (and one host synchronisation) per global step."""
+    from gwgb300 import Ensemble
+
+    e = Ensemble([NCRU], precision="fp32", seed=7, device=device, steps_per_launch=1)
+    e.sample_initial_crus(0)
+    e.set_pulse(0.0, PERIOD, STIM_DUR, STIM_AMP)
+    e.run(DT, 300)
+    st0 = e.stats()
+    t0 = time.perf_counter()
+    e.run(DT, steps)
+    wall = time.perf_counter() - t0
+    st1 = e.stats()
+    e.close()
+    kern = (st1["kernel_ms"] - st0["kernel_ms"]) / 1e3
+    return {"cru_steps_per_s": NCRU * steps / wall, "sim_ms_per_wall_s": steps * DT / wall,
+            "kernel_cru_steps_per_s": NCRU * steps / kern, "launches": int(st1["launches"] - st0["launches"]),
+            "workload": f"1 cell x {NCRU} CRUs, 1 launch per global step, {steps} steps, wall clock"}
+
+
+def batched_config(seed=3, n_cells=256):
+    """256 cells, CRU counts uniform in 2,000..12,500, per-cell PCaL, GKr, GKs, Vmaxf = Vmaxr and
+    rRyR scaled by log-normal(sigma 0.1) factors, cycle lengths uniform in 400..1000 ms."""
+    import numpy as np
+
+    from gwgb300 import _lib
+
+    rng = np.random.default_rng(seed)
+    ncru = rng.integers(2000, 12501, size=n_cells)
+    params = []
+    for _ in range(n_cells):
+        p = _lib.default_params()
+        f = rng.lognormal(0.0, 0.1, size=5)
+        p.PCaL *= f[0]
+        p.GKr *= f[1]
+        p.GKs *= f[2]
+        p.Vmaxf *= f[3]
+        p.Vmaxr *= f[3]
+        p.rRyR *= f[4]
+        params.append(p)
+    cl = rng.uniform(400.0, 1000.0, size=n_cells)
+    return ncru, params, cl
+
+
+def batched_measure(device, steps=2000, cluster_ctas=8):
+    from gwgb300 import Ensemble
+
+    ncru, params, cl = batched_config()
+    e = Ensemble(list(ncru), params, precision="fp32", seed=11, device=device, cluster_ctas=cluster_ctas)
+    for c in range(len(ncru)):
+        e.sample_initial_crus(c)
+        e.set_pulse(0.0, float(cl[c]), STIM_DUR, STIM_AMP, cell=c)
+    e.run(DT, 500)
+    st0 = e.stats()
+    t0 = time.perf_counter()
+    e.run(DT, steps)
+    wall = time.perf_counter() - t0
+    st1 = e.stats()
+    e.close()
+    kern = (st1["kernel_ms"] - st0["kernel_ms"]) / 1e3
+    total = int(ncru.sum()) * steps
+    return {"cru_steps_per_s": total / kern, "sim_ms_per_wall_s": len(ncru) * steps * DT / kern,
+            "wall_cru_steps_per_s": total / wall, "cells": len(ncru), "crus": int(ncru.sum()),
+            "launch_shape": {k: st1[k] for k in ("cluster_ctas", "cta_crus", "threads_per_cta", "n_clusters")},
+            "workload": f"{len(ncru)} cells, 2,000-12,500 CRUs, log-normal(0.1) PCaL/GKr/GKs/Vmax/rRyR, "
+                        f"CL 400-1000 ms, {steps} steps"}
 
 
 def e2e_measure(span, K):
