@@ -48,6 +48,9 @@ METRIC = "CRU-steps/s and sim-ms/wall-s: batched vs plain GPU vs CPU, at KS/FP64
 # FP32 CRU state per CRU: LCC states 4 B, gate + ClCh bits 4 B, RyR counts 24 B, CaSS 16 B,
 # JLCC 16 B, CaJSR 4 B, CaJSR compensation 4 B = 72 B, read and written once per CRU-step.
 BYTES_PER_CRU_STEP = 2 * 72
+# DRAM bytes (read + write) of one 1000-step launch of this workload, from the ncu capture in
+# profiles/engine_kernel_cell12500.txt (the bench's launches have exactly that shape).
+TRAFFIC_PER_LAUNCH = 1.320192e6
 
 
 def parse():
@@ -224,7 +227,9 @@ def main():
             "events_per_cru_step": (st1["events"] - st0["events"]) / max(NCRU * cells * span * K, 1),
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                         "frac": achieved_gbs / pk["hbm_gbs"], "traffic": None,
+                         "frac": achieved_gbs / pk["hbm_gbs"],
+                         "traffic": TRAFFIC_PER_LAUNCH if per_launch_steps == 1000 and cells == 1 else None,
+                         "traffic_unit": "bytes per launch (ncu dram read + write)",
                          "peak_kind": pk_kind, "bytes_per_cru_step": BYTES_PER_CRU_STEP,
                          "steps_per_launch": per_launch_steps},
             "clocks": clk.summary(), "wall_s": wall}
