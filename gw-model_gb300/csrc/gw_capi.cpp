@@ -1092,6 +1092,23 @@ int gw_run_noalloc(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_t
     return GW_OK;
 }
 
+int gw_math_check(const double *x, int64_t n, double *exp_out, double *log_out) {
+    if (!x || !exp_out || !log_out || n < 0 || n > (int64_t)1 << 26)
+        return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "bad arguments to gw_math_check");
+    if (n == 0) return GW_OK;
+    DevBuf dx, de, dl;
+    gw_ctx *c = nullptr;
+    CK(c, dx.alloc(sizeof(double) * n));
+    CK(c, de.alloc(sizeof(double) * n));
+    CK(c, dl.alloc(sizeof(double) * n));
+    CK(c, cudaMemcpy(dx.p, x, sizeof(double) * n, cudaMemcpyHostToDevice));
+    const int e = math_check_dev(dx.as<double>(), (int)n, de.as<double>(), dl.as<double>());
+    if (e != 0) return fail(nullptr, GW_ERR_CUDA, "math check launch: %s", cudaGetErrorString((cudaError_t)e));
+    CK(c, cudaMemcpy(exp_out, de.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    CK(c, cudaMemcpy(log_out, dl.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    return GW_OK;
+}
+
 int gw_get_time(gw_ctx *c, int cell, double *t, uint64_t *step) {
     int rc = check_cell(c, cell);
     if (rc) return rc;

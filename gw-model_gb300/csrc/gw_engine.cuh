@@ -4,11 +4,12 @@
 // CTA = ssa_warps + kOdeWarps warps.  In a cell's leader CTA the last kOdeWarps warps run the
 // global step as the lane program of gw_ode_program.h; in the other CTAs of the cell every warp
 // runs SSA.  Per global step s, every thread does   wait(s) ... arrive(s+1):
-//   SSA warps : claim 32-CRU chunks of the CTA's tile from a per-step shared counter, run the SSA
-//               of step s on them with the values sv[s&1] and store one flux partial per chunk;
-//               the warp that completes the last chunk sums the chunk partials in chunk order
-//               (so the result does not depend on which warp took which chunk) and pushes the
-//               CTA's partial into the leader's shared memory (DSMEM).
+//   SSA warps : each warp owns a contiguous range of the CTA's CRU tile and runs the SSA of step
+//               s on it with the values sv[s&1], one CRU per lane at a time; a lane whose CRU has
+//               finished its step takes the warp's next CRU, so lanes with pending SSA events do
+//               not hold the others back.  Each warp stores one flux partial; the warp that
+//               finishes last sums them in warp order and pushes the CTA's partial into the
+//               leader's shared memory (DSMEM).
 //   ODE warps : reduce the CTA partials of step s-1, increments and Euler update (globals
 //               s -> s+1), transcendental phases of the new state, push sv[(s+1)&1], arrive; the
 //               stimulus of step s+1 and the phases that the SSA does not need (general Jup
@@ -18,12 +19,13 @@
 #include <type_traits>
 
 #include "gw_kernel.cuh"
+#include "gw_math64.cuh"
 #include "gw_ode_program.h"
 
 namespace gw {
 namespace dev {
 
-// Flux partial of a chunk or a CTA, 32 bytes in both precisions:
+// Flux partial of a warp or a CTA, 32 bytes in both precisions:
 //   FP32: {JLCC hi, lo, Jxfer hi, lo, Jtr hi, lo, ClCh count, 0} (float pairs, TwoSum-compensated)
 //   FP64: {JLCC, Jxfer, Jtr, ClCh count}
 struct Partial {
@@ -39,7 +41,7 @@ struct OdeShared {
 };
 
 struct SmemLayout {
-    size_t cc, sv, ode, prog, x, part, chunk, ctr, tile, total;
+    size_t cc, sv, ode, prog, x, math, svs, rtab, part, chunk, ctr, tile, total;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -58,11 +60,17 @@ __host__ __device__ inline SmemLayout smem_layout(int tile_cap, int max_cta_cell
     o += align16(sizeof(OdeProgram));
     L.x = o;
     o += align16(kOdeMaxSlots * sizeof(T));
+    L.math = o;  // exp / log tables of the FP64 global step
+    o += align16(sizeof(math64::Tables));
+    L.svs = o;   // staging of the per-step SSA values before the push
+    o += align16(kSvCount * sizeof(R));
+    L.rtab = o;  // per-warp subunit rate tables (FP32 SSA)
+    o += align16((size_t)16 * kRateTab * sizeof(float2));
     L.part = o;  // [parity][rank in cell]: CTA partials (written by remote CTAs)
     o += align16((size_t)2 * max_cta_cell * sizeof(Partial));
-    L.chunk = o;  // [chunk]: chunk partials of this CTA
-    o += align16((size_t)((tile_cap + 31) / 32) * sizeof(Partial));
-    L.ctr = o;   // chunk claim counters [parity], chunk completion counters [parity]
+    L.chunk = o;  // [warp]: warp partials of this CTA
+    o += align16((size_t)16 * sizeof(Partial));
+    L.ctr = o;   // warp completion counters [2 + parity]
     o += 16;
     L.tile = o;
     // lcc, flags, ryr[6] (u32), cass[4], jlcc[4], cajsr (R), cajsr_lo (f32)
@@ -109,72 +117,97 @@ __device__ __forceinline__ double stimulus(const CellDyn &d, double t, int64_t r
     return 0.0;
 }
 
-__device__ __forceinline__ int v_regime(double V) { return V >= -40.0 ? 0 : (V == -47.13 ? 2 : 1); }
+// Branch of the gate rates (common.hpp:176-218): 0 for V >= -40, 2 for V == -47.13, 1 otherwise
+// (NaN included), from integer compares on the bit pattern (no FP64 issue slots).
+__device__ __forceinline__ int v_regime(double V) {
+    const long long b = __double_as_longlong(V);
+    if (b >= 0) return (unsigned long long)b > 0x7FF0000000000000ull ? 1 : 0;  // +NaN: 1
+    const unsigned long long u = (unsigned long long)b;
+    if (u <= 0xC044000000000000ull) return 0;  // -40 <= V <= -0
+    return u == 0xC04790A3D70A3D71ull ? 2 : 1;  // V == -47.13
+}
+
+// !(x > 0) for a concentration, from the bit pattern (non-positive or NaN).
+__device__ __forceinline__ bool not_positive(double x) {
+    const long long b = __double_as_longlong(x);
+    return b <= 0 || (unsigned long long)b > 0x7FF0000000000000ull;
+}
+
+__device__ __forceinline__ double o_exp(double x, const math64::Tables &M) { return math64::exp(x, M); }
+__device__ __forceinline__ float o_exp(float x, const math64::Tables &) { return expf(x); }
+__device__ __forceinline__ double o_log(double x, const math64::Tables &M) { return math64::log(x, M); }
+__device__ __forceinline__ float o_log(float x, const math64::Tables &) { return logf(x); }
 
 __device__ __forceinline__ double t_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float t_sqrt(float x) { return sqrtf(x); }
 
-// One phase of the lane program by the kOdeLanes ODE threads (t = 0 .. kOdeLanes-1).
+// One phase of the lane program by the kOdeLanes ODE threads (t = 0 .. kOdeLanes-1): thread t runs
+// op t of the phase.  Every warp holds one op kind per phase (P.wkind), so the switch does not
+// diverge; lanes without an op skip the arithmetic.
 template <typename T>
 __device__ __forceinline__ void ode_phase(const OdeProgram &P, int q, int regime, T *X, double *g, int t,
-                                          int *bad) {
-    const int b0 = P.phase_begin[q], n = P.phase_begin[q + 1] - b0;
+                                          int *bad, const math64::Tables &M) {
+    const int wk = P.wkind[q][t >> 5];
+    if (wk == OK_NOP) return;
     const int lane = t & 31;
-    for (int base = 0; base < n; base += kOdeLanes) {
-        const int j = base + t;
-        const OdeOp *op = nullptr;
-        int kind = OK_NOP, width = 1;
-        T v = (T)0;
-        if (j < n) {
-            op = &P.ops[b0 + j];
-            if (regime > 0 && P.alt_idx[b0 + j] != 255) op = &P.alt[regime - 1][P.alt_idx[b0 + j]];
-            kind = op->kind;
-            width = op->width;
-            const uint16_t *a = op->a;
-            switch (kind) {
-            case OK_LOG: v = t_log(X[a[0]] + X[a[1]] * X[a[2]]); break;
-            case OK_SQRT: v = X[a[0]] * X[a[1]] * t_sqrt(X[a[2]] * X[a[3]]); break;
-            case OK_EXP: v = X[a[0]] * t_exp(X[a[1]] * X[a[2]] + X[a[3]]); break;
-            case OK_AFF: v = X[a[0]] * X[a[1]] + X[a[2]] * X[a[3]] + X[a[4]] * X[a[5]] + X[a[6]]; break;
-            case OK_REC:
-                v = (T)1 / (X[a[0]] + X[a[1]] * X[a[2]] + X[a[3]] * X[a[4]] + X[a[5]] * X[a[6]] * X[a[7]]);
-                break;
-            case OK_PROD: v = X[a[0]] * X[a[1]] * X[a[2]] * X[a[3]] * X[a[4]] * X[a[5]] * X[a[6]]; break;
-            case OK_SUM:
-                v = X[a[2]] * X[a[3]] * X[a[4]] + X[a[5]] * X[a[6]] * X[a[7]] + X[a[8]] * X[a[9]] * X[a[10]] +
-                    X[a[11]] * X[a[12]] * X[a[13]];
-                break;
-            default: break;
-            }
+    const int b0 = P.phase_begin[q];
+    const bool live = t < P.phase_begin[q + 1] - b0;
+    const OdeOp *op = &P.ops[b0 + (live ? t : 0)];
+    if (live && regime > 0) {
+        const int ai = P.alt_idx[b0 + t];
+        if (ai != 255) op = &P.alt[regime - 1][ai];
+    }
+    // the 32-byte op in two 16-byte loads: consecutive lanes read consecutive ops, so the loads do
+    // not conflict on shared-memory banks (field-by-field loads at a 32-byte stride would)
+    const uint4 w0 = reinterpret_cast<const uint4 *>(op)[0], w1 = reinterpret_cast<const uint4 *>(op)[1];
+    const int kind = live ? (int)(w0.x & 0xFFu) : (int)OK_NOP;
+    const int out = (int)(w0.x >> 16);
+    const uint32_t pw[7] = {w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#define GW_ARG(k) (X[(pw[(k) >> 1] >> (16 * ((k) & 1))) & 0xFFFFu])
+    T v = (T)0;
+    if (kind != OK_NOP) {
+        switch (wk) {
+        case OK_LOG: v = o_log(GW_ARG(0) + GW_ARG(1) * GW_ARG(2), M); break;
+        case OK_SQRT: v = GW_ARG(0) * GW_ARG(1) * t_sqrt(GW_ARG(2) * GW_ARG(3)); break;
+        case OK_EXP: v = GW_ARG(0) * o_exp(GW_ARG(1) * GW_ARG(2) + GW_ARG(3), M); break;
+        case OK_AFF: v = GW_ARG(0) * GW_ARG(1) + GW_ARG(2) * GW_ARG(3) + GW_ARG(4) * GW_ARG(5) + GW_ARG(6); break;
+        case OK_REC:
+            v = (T)1 / (GW_ARG(0) + GW_ARG(1) * GW_ARG(2) + GW_ARG(3) * GW_ARG(4) + GW_ARG(5) * GW_ARG(6) * GW_ARG(7));
+            break;
+        case OK_PROD: v = GW_ARG(0) * GW_ARG(1) * GW_ARG(2) * GW_ARG(3) * GW_ARG(4) * GW_ARG(5) * GW_ARG(6); break;
+        case OK_SUM:
+            v = GW_ARG(2) * GW_ARG(3) * GW_ARG(4) + GW_ARG(5) * GW_ARG(6) * GW_ARG(7) + GW_ARG(8) * GW_ARG(9) * GW_ARG(10) +
+                GW_ARG(11) * GW_ARG(12) * GW_ARG(13);
+            break;
+        case OK_UPD: {
+            const double ng = g[out] + (double)GW_ARG(0);
+            g[out] = ng;
+            X[XS_G + out] = (T)ng;
+            if (!finite_bits(ng)) *bad = 1;
+            return;
         }
-        // SUM rows of `width` lanes: tree over offsets 1, 2, 4 (all lanes take part)
-        const unsigned any_sum = __ballot_sync(0xffffffffu, kind == OK_SUM);
-        if (any_sum) {
-#pragma unroll
-            for (int off = 1; off < 8; off <<= 1) {
-                const T o = __shfl_down_sync(0xffffffffu, v, off);
-                if (kind == OK_SUM && (lane % width) + off < width && (lane % (2 * off)) == 0) v += o;
-            }
-        }
-        if (j < n && kind != OK_NOP) {
-            if (kind == OK_UPD) {
-                const double ng = g[op->out] + (double)X[op->a[0]];
-                g[op->out] = ng;
-                X[XS_G + op->out] = (T)ng;
-                if (!finite_bits(ng)) *bad = 1;
-            } else if (kind == OK_SUM) {
-                if (lane % width == 0) X[op->out] = X[op->a[0]] * X[op->a[1]] * v;
-            } else {
-                X[op->out] = v;
-            }
+        default: break;
         }
     }
+    if (wk == OK_SUM) {
+        // rows of `width` lanes (a power of two, rows aligned to it): tree over offsets 1, 2, 4
+        const int wm = kind == OK_SUM ? (int)((w0.x >> 8) & 0xFFu) - 1 : 0;
+#pragma unroll
+        for (int off = 1; off < 8; off <<= 1) {
+            const T o = __shfl_down_sync(0xffffffffu, v, off);
+            if (kind == OK_SUM && (lane & wm) + off <= wm && (lane & (2 * off - 1)) == 0) v += o;
+        }
+        if (kind == OK_SUM && (lane & wm) == 0) X[out] = GW_ARG(0) * GW_ARG(1) * v;
+        return;
+    }
+#undef GW_ARG
+    if (kind != OK_NOP) X[out] = v;
 }
 
 // Sums {JLCC, ClCh, Jtr, Jxfer} of the cell's CTA partials of one slot; ODE warp w reduces
 // quantity w.  Writes the FP64 sums to out[] (shared) from lane 0 of each warp.
-template <bool FP64>
-__device__ __forceinline__ void reduce_partials(const Partial *slot, int n, int warp, int lane, double *out) {
+template <bool FP64, typename T>
+__device__ __forceinline__ void reduce_partials(const Partial *slot, int n, int warp, int lane, double *out, T *X) {
     if (warp >= 4) return;
     double r;
     if (FP64) {
@@ -199,28 +232,40 @@ __device__ __forceinline__ void reduce_partials(const Partial *slot, int n, int 
         }
         r = (double)hi + (double)lo;
     }
-    if (lane == 0) out[warp] = r;
+    if (lane == 0) {
+        out[warp] = r;
+        X[XS_SUMS + warp] = (T)r;
+    }
 }
 
+// Per-step SSA values of the new state to every CTA of the cell: staged in the leader's shared
+// memory by threads 0..kSvCount-1, then pushed as (value, CTA) pairs by all kOdeLanes threads.
 template <bool FP64, typename T>
-__device__ __forceinline__ void push_sv(const OdeProgram &P, const T *X, const double *g, void *svbuf, int slot,
-                                        const CtaWork &w, int t) {
+__device__ __forceinline__ void push_sv(const OdeProgram &P, const T *X, const double *g, void *svbuf, void *stage,
+                                        int slot, const CtaWork &w, int t) {
     using R = typename std::conditional<FP64, double, float>::type;
-    R *sv = reinterpret_cast<R *>(svbuf) + slot * kSvCount;
-    for (int i = t; i < kSvCount; i += kOdeLanes) {
+    R *st = reinterpret_cast<R *>(stage);
+    if (t < kSvCount) {
         R v;
-        if (i == SV_CAI) v = (R)g[3];
-        else if (i == SV_CANSR) v = (R)g[4];
-        else if (i == SV_CAI_LO) v = FP64 ? (R)0 : (R)(g[3] - (double)(float)g[3]);
-        else if (i == SV_CANSR_LO) v = FP64 ? (R)0 : (R)(g[4] - (double)(float)g[4]);
-        else v = (R)X[P.sv_src[i]];
-        for (int r = 0; r < w.n_cta_cell; ++r) st_remote(map_rank(sv + i, (uint32_t)(w.first + r)), v);
+        if (t == SV_CAI) v = (R)g[3];
+        else if (t == SV_CANSR) v = (R)g[4];
+        else if (t == SV_CAI_LO) v = FP64 ? (R)0 : (R)(g[3] - (double)(float)g[3]);
+        else if (t == SV_CANSR_LO) v = FP64 ? (R)0 : (R)(g[4] - (double)(float)g[4]);
+        else v = (R)X[P.sv_src[t]];
+        st[t] = v;
+    }
+    ode_bar();
+    R *sv = reinterpret_cast<R *>(svbuf) + slot * kSvCount;
+    const int total = kSvCount * w.n_cta_cell;
+    for (int idx = t; idx < total; idx += kOdeLanes) {
+        const int r = idx / kSvCount, i = idx - r * kSvCount;
+        st_remote(map_rank(sv + i, (uint32_t)(w.first + r)), st[i]);
     }
 }
 
 constexpr int kMaxThreads = 512;  // SSA warps + ODE warps per CTA (128 registers per thread)
 
-// Warp sums of one chunk's (or one CTA's) flux contributions into a Partial (all lanes hold it).
+// Per-lane flux accumulators and their warp sum as a Partial (all lanes hold it).
 template <bool FP64>
 struct FluxAcc {
     float jh = 0, jl = 0, xh = 0, xl = 0, th = 0, tl = 0;  // FP32: (hi, lo) pairs
@@ -306,8 +351,11 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
     OdeShared &os = *reinterpret_cast<OdeShared *>(smem + L.ode);
     OdeProgram &P = *reinterpret_cast<OdeProgram *>(smem + L.prog);
     T *X = reinterpret_cast<T *>(smem + L.x);
+    math64::Tables &M = *reinterpret_cast<math64::Tables *>(smem + L.math);
+    void *svstage = smem + L.svs;
     Partial *part = reinterpret_cast<Partial *>(smem + L.part);
-    Partial *chunkp = reinterpret_cast<Partial *>(smem + L.chunk);
+    Partial *chunkp = reinterpret_cast<Partial *>(smem + L.chunk);  // warp partials
+    float2 *rtab = reinterpret_cast<float2 *>(smem + L.rtab) + warp * kRateTab;  // this warp's table
     int *ctr = reinterpret_cast<int *>(smem + L.ctr);
     const int cap = a.tile_cap;
     uint32_t *t_lcc = reinterpret_cast<uint32_t *>(smem + L.tile);
@@ -319,7 +367,6 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
     float *t_cajsr_lo = reinterpret_cast<float *>(t_cajsr + cap);
     const int cell = w.cell;
     const int pslot = a.max_cta_cell;  // partial entries per parity slot
-    const int n_chunks = (w.cru_count + 31) >> 5;
     R *g_cass = reinterpret_cast<R *>(a.cass);
     R *g_jlcc = reinterpret_cast<R *>(a.jlcc);
     R *g_cajsr = reinterpret_cast<R *>(a.cajsr);
@@ -360,6 +407,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
         const CellStatic &C = a.cs[cell];
         const CellDyn &d = a.dyn[cell];
         for (int i = ot; i < kOdeMaxSlots; i += kOdeLanes) X[i] = (T)0;
+        math64::load_tables(M, ot, kOdeLanes);
         ode_bar();
         if (ot == 0) {
             X[XS_ONE] = (T)1;
@@ -372,6 +420,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
             os.status = 0;
             X[XS_DT] = (T)a.dt;
             X[XS_ISTIM] = (T)stimulus(d, d.t, a.run_step0);
+            for (int i = 0; i < 4; ++i) X[XS_SUMS + i] = (T)os.sums[i];
         }
         for (int i = ot; i < kNumGlobals; i += kOdeLanes) {
             os.g[i] = d.g[i];
@@ -382,17 +431,17 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
         // transcendental phases of the initial state, push sv[0]
         const int reg = v_regime(os.g[0]);
         for (int q = P.upd_phase + 1; q <= P.push_phase; ++q) {
-            ode_phase<T>(P, q, reg, X, os.g, ot, &bad);
+            ode_phase<T>(P, q, reg, X, os.g, ot, &bad, M);
             ode_bar();
         }
-        push_sv<FP64, T>(P, X, os.g, svbuf, 0, w, ot);
+        push_sv<FP64, T>(P, X, os.g, svbuf, svstage, 0, w, ot);
     }
     __syncthreads();
     cluster_arrive();
     if (leader && ode_thread) {
         const int reg = v_regime(os.g[0]);
         for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
-            ode_phase<T>(P, q, reg, X, os.g, ot, &bad);
+            ode_phase<T>(P, q, reg, X, os.g, ot, &bad, M);
             ode_bar();
         }
     }
@@ -409,91 +458,110 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
         cluster_wait();
         if (!ode_thread) {
             if (active) {
-                // The counters of parity par^1 were last used in step s-1, which every warp of
-                // this CTA has left; they are next used in step s+1, after the cluster barrier.
-                if (threadIdx.x == 0) {
-                    ctr[par ^ 1] = 0;
-                    ctr[2 + (par ^ 1)] = 0;
-                }
+                // The counter of parity par^1 was last used in step s-1, which every warp of this
+                // CTA has left; it is next used in step s+1, after the cluster barrier.
+                if (threadIdx.x == 0) ctr[2 + (par ^ 1)] = 0;
                 const R *sv = svbuf + par * kSvCount;
-                if (n_chunks == 0 && threadIdx.x == 0) {
+                const int nsw = n_ssa >> 5;
+                if (!FP64) {
+                    build_rate_table<R>(rtab, cc, sv, lane);
+                    __syncwarp();
+                }
+                if (w.cru_count == 0 && threadIdx.x == 0) {
                     Partial *dst = part + par * pslot + w.rank_in_cell;
 #pragma unroll
                     for (int v = 0; v < 4; ++v) st_remote(map_rank(&dst->v[v], (uint32_t)w.first), 0.0);
                 }
+                // This warp's CRUs [cursor, end).  A lane whose CRU has finished its step takes the
+                // next one, so lanes with pending SSA events do not hold the others back.
+                int cursor = (int)((int64_t)w.cru_count * warp / nsw);
+                const int end = (int)((int64_t)w.cru_count * (warp + 1) / nsw);
+                FluxAcc<FP64> acc;
+                Cru<R> c;
+                SsaLane<R, EXACT> sl;
+                Stream rng;
+                int m = -1;  // CRU of this lane; -1 none yet, -2 none left
                 for (;;) {
-                    int ch = 0;
-                    if (lane == 0) ch = atomicAdd(&ctr[par], 1);
-                    ch = __shfl_sync(0xffffffffu, ch, 0);
-                    if (ch >= n_chunks) break;
-                    const int m = ch * 32 + lane;
-                    FluxAcc<FP64> acc;
-                    if (m < w.cru_count) {
-                        Cru<R> c;
-                        c.lcc = t_lcc[m];
-                        c.flags = t_flags[m];
+                    const unsigned need = __ballot_sync(0xffffffffu, m == -1);
+                    if (need) {
+                        const int nm = cursor + __popc(need & ((1u << lane) - 1u));
+                        cursor += __popc(need);
+                        if (m == -1) {
+                            if (nm < end) {
+                                m = nm;
+                                c.lcc = t_lcc[m];
+                                c.flags = t_flags[m];
 #pragma unroll
-                        for (int k = 0; k < 6; ++k) c.ryr[k] = t_ryr[k * cap + m];
+                                for (int k = 0; k < 6; ++k) c.ryr[k] = t_ryr[k * cap + m];
 #pragma unroll
-                        for (int j = 0; j < 4; ++j) {
-                            c.cass[j] = t_cass[j * cap + m];
-                            c.jlcc[j] = t_jlcc[j * cap + m];
-                        }
-                        c.cajsr = t_cajsr[m];
-                        c.cajsr_lo = FP64 ? 0.f : t_cajsr_lo[m];
-                        Stream rng;
-                        rng.open(a.seed, (uint32_t)cell, (uint32_t)(w.cru_begin + m), step0 + s, 0);
-                        R jx, jt;
-                        int ev = 0, err = 0;
-                        ssa_cru<R, EXACT>(c, cc, sv, rng, dt, a.event_cap, jx, jt, ev, err);
-                        t_lcc[m] = c.lcc;
-                        t_flags[m] = c.flags;
-#pragma unroll
-                        for (int k = 0; k < 6; ++k) t_ryr[k * cap + m] = c.ryr[k];
-#pragma unroll
-                        for (int j = 0; j < 4; ++j) {
-                            t_cass[j * cap + m] = c.cass[j];
-                            t_jlcc[j * cap + m] = c.jlcc[j];
-                        }
-                        t_cajsr[m] = c.cajsr;
-                        if (!FP64) t_cajsr_lo[m] = c.cajsr_lo;
-                        my_events += (unsigned long long)ev;
-                        my_err |= err;
-                        acc.add(c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3], jx, jt,
-                                __popc((c.flags >> 4) & 0xFu));
-                        if (rec_ok && cell == a.tr_cell) {
-                            const int64_t cm = w.cru_begin + m;
-                            const int64_t st = a.tr_cru_stride;
-                            a.tr_lcc[r_idx * st + cm] = c.lcc;
-                            a.tr_flags[r_idx * st + cm] = c.flags;
-#pragma unroll
-                            for (int k = 0; k < 6; ++k) a.tr_ryr[(r_idx * 6 + k) * st + cm] = c.ryr[k];
-#pragma unroll
-                            for (int j = 0; j < 4; ++j)
-                                reinterpret_cast<R *>(a.tr_cass)[(r_idx * 4 + j) * st + cm] = c.cass[j];
-                            reinterpret_cast<R *>(a.tr_cajsr)[r_idx * st + cm] = c.cajsr;
+                                for (int j = 0; j < 4; ++j) {
+                                    c.cass[j] = t_cass[j * cap + m];
+                                    c.jlcc[j] = t_jlcc[j * cap + m];
+                                }
+                                c.cajsr = t_cajsr[m];
+                                c.cajsr_lo = FP64 ? 0.f : t_cajsr_lo[m];
+                                rng.open(a.seed, (uint32_t)cell, (uint32_t)(w.cru_begin + m), step0 + s, 0);
+                                sl.begin(c, cc);
+                            } else {
+                                m = -2;
+                            }
                         }
                     }
-                    const Partial pv = acc.warp_total();
-                    int done = 0;
+                    if (!__any_sync(0xffffffffu, m >= 0)) break;
+                    if (m >= 0) {
+                        int err = 0;
+                        if (sl.iterate(c, cc, sv, rtab, rng, dt, a.event_cap, err)) {
+                            t_lcc[m] = c.lcc;
+                            t_flags[m] = c.flags;
+#pragma unroll
+                            for (int k = 0; k < 6; ++k) t_ryr[k * cap + m] = c.ryr[k];
+#pragma unroll
+                            for (int j = 0; j < 4; ++j) {
+                                t_cass[j * cap + m] = c.cass[j];
+                                t_jlcc[j * cap + m] = c.jlcc[j];
+                            }
+                            t_cajsr[m] = c.cajsr;
+                            if (!FP64) t_cajsr_lo[m] = c.cajsr_lo;
+                            my_events += (unsigned long long)sl.ev;
+                            my_err |= err;
+                            acc.add(c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3], sl.jxfer_sum, sl.jtr,
+                                    __popc((c.flags >> 4) & 0xFu));
+                            if (rec_ok && cell == a.tr_cell) {
+                                const int64_t cm = w.cru_begin + m;
+                                const int64_t st = a.tr_cru_stride;
+                                a.tr_lcc[r_idx * st + cm] = c.lcc;
+                                a.tr_flags[r_idx * st + cm] = c.flags;
+#pragma unroll
+                                for (int k = 0; k < 6; ++k) a.tr_ryr[(r_idx * 6 + k) * st + cm] = c.ryr[k];
+#pragma unroll
+                                for (int j = 0; j < 4; ++j)
+                                    reinterpret_cast<R *>(a.tr_cass)[(r_idx * 4 + j) * st + cm] = c.cass[j];
+                                reinterpret_cast<R *>(a.tr_cajsr)[r_idx * st + cm] = c.cajsr;
+                            }
+                            m = -1;
+                        }
+                    }
+                }
+                // Warp partial; the warp that finishes last sums the warp partials in warp order
+                // and pushes the CTA's partial to the leader.
+                const Partial pv = acc.warp_total();
+                int done = 0;
+                if (lane == 0) {
+                    chunkp[warp] = pv;
+                    __threadfence_block();
+                    done = atomicAdd(&ctr[2 + par], 1);
+                    __threadfence_block();
+                }
+                done = __shfl_sync(0xffffffffu, done, 0);
+                if (done == nsw - 1) {
+                    __syncwarp();
+                    FluxAcc<FP64> tot;
+                    if (lane < nsw) tot.add_partial(chunkp[lane]);
+                    const Partial pc = tot.warp_total();
                     if (lane == 0) {
-                        chunkp[ch] = pv;
-                        __threadfence_block();
-                        done = atomicAdd(&ctr[2 + par], 1);
-                        __threadfence_block();
-                    }
-                    done = __shfl_sync(0xffffffffu, done, 0);
-                    if (done == n_chunks - 1) {
-                        // Last chunk of the CTA: sum the chunk partials in chunk order, push.
-                        __syncwarp();
-                        FluxAcc<FP64> tot;
-                        for (int q = lane; q < n_chunks; q += 32) tot.add_partial(chunkp[q]);
-                        const Partial pc = tot.warp_total();
-                        if (lane == 0) {
-                            Partial *dst = part + par * pslot + w.rank_in_cell;
+                        Partial *dst = part + par * pslot + w.rank_in_cell;
 #pragma unroll
-                            for (int v = 0; v < 4; ++v) st_remote(map_rank(&dst->v[v], (uint32_t)w.first), pc.v[v]);
-                        }
+                        for (int v = 0; v < 4; ++v) st_remote(map_rank(&dst->v[v], (uint32_t)w.first), pc.v[v]);
                     }
                 }
             }
@@ -501,14 +569,13 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
         } else {
             // leader CTA's ODE warps: fluxes of step s-1 (or the carry), then the global step
             // s -> s+1
-            if (s > 0) reduce_partials<FP64>(part + (par ^ 1) * pslot, w.n_cta_cell, ot >> 5, lane, os.sums);
-            ode_bar();
-            if (ot < 4) X[XS_SUMS + ot] = (T)os.sums[ot];
-            if (ot == 0 && (!(os.g[1] > 0.0) || !(os.g[2] > 0.0)) && os.status == 0) os.status = GW_ERR_NERNST;
+            if (ot == 0 && (not_positive(os.g[1]) || not_positive(os.g[2])) && os.status == 0)
+                os.status = GW_ERR_NERNST;
+            if (s > 0) reduce_partials<FP64, T>(part + (par ^ 1) * pslot, w.n_cta_cell, ot >> 5, lane, os.sums, X);
             ode_bar();
             const int reg_n = v_regime(os.g[0]);
             for (int q = 0; q <= P.upd_phase; ++q) {
-                ode_phase<T>(P, q, reg_n, X, os.g, ot, &bad);
+                ode_phase<T>(P, q, reg_n, X, os.g, ot, &bad, M);
                 ode_bar();
             }
             if (ot == 0) os.t += a.dt;
@@ -519,16 +586,16 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
             }
             const int reg = v_regime(os.g[0]);
             for (int q = P.upd_phase + 1; q <= P.push_phase; ++q) {
-                ode_phase<T>(P, q, reg, X, os.g, ot, &bad);
+                ode_phase<T>(P, q, reg, X, os.g, ot, &bad, M);
                 ode_bar();
             }
-            push_sv<FP64, T>(P, X, os.g, svbuf, par ^ 1, w, ot);
+            push_sv<FP64, T>(P, X, os.g, svbuf, svstage, par ^ 1, w, ot);
             cluster_arrive();
             // off the critical path: the stimulus of step s+1 (read by the first phase of the
             // next step, after its ode_bar) and the phases the SSA does not need
             if (ot == 0) X[XS_ISTIM] = (T)stimulus(a.dyn[cell], os.t, ri + 1);
             for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
-                ode_phase<T>(P, q, reg, X, os.g, ot, &bad);
+                ode_phase<T>(P, q, reg, X, os.g, ot, &bad, M);
                 ode_bar();
             }
         }
@@ -537,7 +604,8 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
 
     // Epilogue: carry of the last step's fluxes, globals and counters back to the cell block.
     if (leader && ode_thread) {
-        if (a.n_steps > 0) reduce_partials<FP64>(part + ((a.n_steps - 1) & 1) * pslot, w.n_cta_cell, ot >> 5, lane, os.sums);
+        if (a.n_steps > 0)
+            reduce_partials<FP64, T>(part + ((a.n_steps - 1) & 1) * pslot, w.n_cta_cell, ot >> 5, lane, os.sums, X);
         const unsigned anybad = __ballot_sync(0xffffffffu, bad != 0);
         if (lane == 0 && anybad) atomicCAS(&os.status, 0, (int)GW_ERR_NONFINITE);
         ode_bar();

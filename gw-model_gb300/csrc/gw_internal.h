@@ -135,5 +135,7 @@ size_t smem_bytes_fp32(int tile_cap, int max_cta_cell);
 int max_active_clusters_fp64(const LaunchShape &s, bool ode64, int *out);
 int max_active_clusters_fp32(const LaunchShape &s, bool ode64, int *out);
 int sample_initial_crus_dev(const KernelArgs &a, int cell, int ncru, int fp64, void *stream);
+// The global step's FP64 exp and log on n device inputs (accuracy check).
+int math_check_dev(const double *x, int n, double *ex, double *lg);
 
 }  // namespace gw

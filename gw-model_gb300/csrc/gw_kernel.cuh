@@ -314,16 +314,44 @@ __device__ __forceinline__ R subunit_rates(const Cru<R> &s, int j, R x, const Ss
     return sub;
 }
 
-// FP32 total outgoing rate of subunit j: the same rates as subunit_rates, regrouped (used only to
-// draw the jump time and the subunit; the transition itself is drawn from the full rate list).
+// Table of the rates of subunit j other than the RyR rates, by the subunit's (LCC state, gate,
+// ClCh) index: total = base + slope * CaSS.  base = the LCC state's V-dependent outgoing rates
+// + the gate's rate + (ClCh open ? kbClCh : 0); slope = (Ca-dependent LCC inactivation: gamma0 a^k)
+// + (ClCh closed ? kfClCh : 0).  Rebuilt by each warp at the start of every global step (the
+// V-dependent rates change per step); entry = state | gate << 4 | clch << 5.
+constexpr int kRateTab = 64;
+
+template <typename R>
+__device__ __forceinline__ void build_rate_table(float2 *tab, const SsaConsts<R> &c, const R *sv, int lane) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int e = lane + 32 * h;
+        const int st = e & 15, gate = (e >> 4) & 1, clch = (e >> 5) & 1;
+        const uint32_t w = c.lcct[st];
+        R base = sv[w & 0xFFu] + sv[(w >> 8) & 0xFFu] + sv[(w >> 16) & 0xFFu];
+        base += gate ? sv[SV_INACT1] : sv[SV_INACT0];
+        if (clch) base += c.kbClCh;
+        R slope = ((w >> 24) < 3u && st >= 1) ? c.gam[(st - 1) & 7] : (R)0;
+        if (!clch) slope += c.kfClCh;
+        tab[e] = make_float2((float)base, (float)slope);
+    }
+}
+
+// Byte j of the result: subunit j's rate-table index (LCC state | gate << 4 | ClCh << 5).
+__device__ __forceinline__ uint32_t rate_index_word(uint32_t lcc, uint32_t flags) {
+    const uint32_t g = ((flags & 0xFu) * 0x00204081u) & 0x01010101u;         // gate bit j -> bit 8j
+    const uint32_t k = (((flags >> 4) & 0xFu) * 0x00204081u) & 0x01010101u;  // ClCh bit j -> bit 8j
+    return lcc | (g << 4) | (k << 5);
+}
+
+// FP32 total outgoing rate of subunit j (used only to draw the jump time and the subunit; the
+// transition itself is drawn from the full rate list of subunit_rates): the table part plus the
+// RyR rates regrouped.
 template <typename R>
 __device__ __forceinline__ R subunit_total_fast(const Cru<R> &s, int j, R x, const SsaConsts<R> &c,
-                                                const R *sv) {
-    const int st = byte_u(s.lcc, j);
-    const uint32_t w = c.lcct[st & 15];
-    R lcc = sv[w & 0xFFu] + sv[(w >> 8) & 0xFFu] + sv[(w >> 16) & 0xFFu];
-    if ((w >> 24) < 3u) lcc += c.gam[(st - 1) & 7] * x;
-    const R inact = ((s.flags >> j) & 1u) == 0u ? sv[SV_INACT0] : sv[SV_INACT1];
+                                                const float2 *tab, uint32_t iw) {
+    const float2 tv = tab[(iw >> (8 * j)) & 0x3Fu];
+    const R other = fmaf(tv.y, x, tv.x);
     const R R0 = (R)byte_s(s.ryr[0], j), R1 = (R)byte_s(s.ryr[1], j), R2 = (R)byte_s(s.ryr[2], j);
     const R R3 = (R)byte_s(s.ryr[3], j), R4 = (R)byte_s(s.ryr[4], j), R5 = (R)byte_s(s.ryr[5], j);
     const R x2 = x * x;
@@ -336,8 +364,7 @@ __device__ __forceinline__ R subunit_total_fast(const Cru<R> &s, int j, R x, con
         ryr += (R4 + R5) * __fdividef((float)(c.k65 * (c.k52 + c.k54 * x2)), (float)(c.k56 * x2 + c.k65));
     else
         ryr += x2 * R4 * c.k5654 + R4 * c.k52 + R5 * c.k65;
-    const R clch = ((s.flags >> (4 + j)) & 1u) == 0u ? c.kfClCh * x : c.kbClCh;
-    return lcc + inact + ryr + clch;
+    return other + ryr;
 }
 
 // sample_weights (common.hpp:49-59) with the draw already scaled: u = U * total.  In FP32 mode a
@@ -415,23 +442,37 @@ struct CruOut {
 // iteration (as the reference's stored rate arrays are) and applied after the Ca update, so the
 // code reorders independent work but not values: re-split draws use indices k+1..k+D and the
 // selection draws k+D+1.. exactly as the reference's sequential urand() calls would.
+//
+// SsaLane holds the loop state of one CRU's step so that a lane can run one iteration at a time
+// (the engine's SSA warps interleave CRUs: a lane whose CRU has finished its step takes the next
+// CRU while lanes with pending events continue).
 template <typename R, bool EXACT>
-__device__ __forceinline__ void ssa_cru(Cru<R> &s, const SsaConsts<R> &c, const R *sv, Stream &rng,
-                                        R dt, int cap, R &out_jxfer, R &out_jtr, int &events,
-                                        int &err) {
-    int ev = 0;
-    const R Cai = sv[SV_CAI], CaNSR = sv[SV_CANSR];
-    const R Cai_lo = EXACT ? (R)0 : sv[SV_CAI_LO], CaNSR_lo = EXACT ? (R)0 : sv[SV_CANSR_LO];
-    R jrel[4];
+struct SsaLane {
+    R t;          // time reached within the global step
+    uint32_t k;   // next draw index
+    int ev;       // events so far in this step
+    R jrel[4];    // Jrel, updated at the start of the step and at RyR transitions (SSA.tpp:10-33)
+    R jxfer_sum;  // sum over subunits of Jxfer of the last update_fluxes
+    R jtr;        // Jtr of the last update_fluxes
+
+    __device__ __forceinline__ void begin(const Cru<R> &s, const SsaConsts<R> &c) {
+        t = (R)0;
+        k = 0;
+        ev = 0;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const R open = (R)(byte_s(s.ryr[2], j) + byte_s(s.ryr[3], j));
-        jrel[j] = c.rRyR * open * (s.cajsr - s.cass[j]);
+        for (int j = 0; j < 4; ++j) {
+            const R open = (R)(byte_s(s.ryr[2], j) + byte_s(s.ryr[3], j));
+            jrel[j] = c.rRyR * open * (s.cajsr - s.cass[j]);
+        }
     }
-    R t = (R)0;
-    uint32_t k = 0;
-    R jxfer[4], jiss[4], jtr;
-    for (;;) {
+
+    // One iteration of the event loop; true when the CRU's step is complete (the jump passed the
+    // end of the step, or the event cap was exceeded, which sets err).
+    __device__ __forceinline__ bool iterate(Cru<R> &s, const SsaConsts<R> &c, const R *sv, const float2 *tab,
+                                            Stream &rng, R dt, int cap, int &err) {
+        const R Cai = sv[SV_CAI], CaNSR = sv[SV_CANSR];
+        const R Cai_lo = EXACT ? (R)0 : sv[SV_CAI_LO], CaNSR_lo = EXACT ? (R)0 : sv[SV_CANSR_LO];
+        R jxfer[4], jiss[4];
         // update_fluxes (SSA.tpp:37-45)
         if (EXACT) {
             jtr = c.rtr * (CaNSR - s.cajsr);
@@ -451,13 +492,14 @@ __device__ __forceinline__ void ssa_cru(Cru<R> &s, const SsaConsts<R> &c, const 
         }
         // update_rates (SSA.tpp:48-56): only the subunit totals are kept here.
         R sub[4];
+        const uint32_t iw = EXACT ? 0u : rate_index_word(s.lcc, s.flags);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             if (EXACT) {
                 Rates<R> r;
                 sub[j] = subunit_rates<R>(s, j, s.cass[j], c, sv, r);
             } else {
-                sub[j] = subunit_total_fast<R>(s, j, s.cass[j], c, sv);
+                sub[j] = subunit_total_fast<R>(s, j, s.cass[j], c, tab, iw);
             }
         }
         const R total = sub[0] + sub[1] + sub[2] + sub[3];
@@ -615,25 +657,29 @@ __device__ __forceinline__ void ssa_cru(Cru<R> &s, const SsaConsts<R> &c, const 
                 }
             }
         }
+        jxfer_sum = jxfer[0] + jxfer[1] + jxfer[2] + jxfer[3];
         k = kk;
-        if (last) break;
+        if (last) return true;
         if (++ev > cap) {
             err = 1;
-            break;
+            return true;
         }
+        return false;
     }
-    events += ev;
-    out_jxfer = jxfer[0] + jxfer[1] + jxfer[2] + jxfer[3];
-    out_jtr = jtr;
-}
+};
 
-// ------------------------------------------------------------------------------------------
-// Precision-generic math used by the global-step lane program.
-// ------------------------------------------------------------------------------------------
-__device__ __forceinline__ double t_exp(double x) { return exp(x); }
-__device__ __forceinline__ float t_exp(float x) { return expf(x); }
-__device__ __forceinline__ double t_log(double x) { return log(x); }
-__device__ __forceinline__ float t_log(float x) { return logf(x); }
+template <typename R, bool EXACT>
+__device__ __forceinline__ void ssa_cru(Cru<R> &s, const SsaConsts<R> &c, const R *sv, const float2 *tab, Stream &rng,
+                                        R dt, int cap, R &out_jxfer, R &out_jtr, int &events,
+                                        int &err) {
+    SsaLane<R, EXACT> L;
+    L.begin(s, c);
+    while (!L.iterate(s, c, sv, tab, rng, dt, cap, err)) {
+    }
+    events += L.ev;
+    out_jxfer = L.jxfer_sum;
+    out_jtr = L.jtr;
+}
 
 }  // namespace dev
 }  // namespace gw

@@ -23,4 +23,24 @@ int sample_initial_crus_dev(const KernelArgs &a, int cell, int ncru, int fp64, v
     return (int)cudaGetLastError();
 }
 
+namespace dev {
+// The global step's FP64 exp and log (gw_math64.cuh) on n inputs, for their accuracy check.
+__global__ void math_check_kernel(const double *x, int n, double *ex, double *lg) {
+    __shared__ math64::Tables T;
+    math64::load_tables(T, (int)threadIdx.x, (int)blockDim.x);
+    __syncthreads();
+    const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= n) return;
+    ex[i] = math64::exp(x[i], T);
+    lg[i] = math64::log(x[i], T);
+}
+}  // namespace dev
+
+int math_check_dev(const double *x, int n, double *ex, double *lg) {
+    if (n <= 0) return 0;
+    const int threads = 256;
+    dev::math_check_kernel<<<(n + threads - 1) / threads, threads>>>(x, n, ex, lg);
+    return (int)cudaGetLastError();
+}
+
 }  // namespace gw

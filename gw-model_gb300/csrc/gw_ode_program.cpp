@@ -14,6 +14,7 @@
 // gate rates (common.hpp:176-218): 0: V >= -40, 1: V < -40, 2: V == -47.13.
 #include "gw_ode_program.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -507,6 +508,34 @@ bool ode_program_build(const CellStatic &cs, bool pow_fast, OdeProgram *prog, do
         }
     }
     prog->phase_begin[prog->n_phases] = n;
+    // Each warp of a phase must hold one op kind (in every regime): the device switches on it once
+    // per warp.
+    for (int q = 0; q < prog->n_phases; ++q) {
+        const int b0 = prog->phase_begin[q], nq = prog->phase_begin[q + 1] - b0;
+        if (nq > kOdeLanes) {
+            fprintf(stderr, "ode program: phase %d has %d ops (max %d)\n", q, nq, kOdeLanes);
+            return false;
+        }
+        for (int w = 0; w < kOdeWarps; ++w) {
+            int kind = OK_NOP;
+            for (int l = 32 * w; l < std::min(32 * w + 32, nq); ++l) {
+                const OdeOp *cand[3] = {&prog->ops[b0 + l], nullptr, nullptr};
+                if (prog->alt_idx[b0 + l] != 255) {
+                    cand[1] = &prog->alt[0][prog->alt_idx[b0 + l]];
+                    cand[2] = &prog->alt[1][prog->alt_idx[b0 + l]];
+                }
+                for (const OdeOp *op : cand) {
+                    if (!op || op->kind == OK_NOP) continue;
+                    if (kind != OK_NOP && kind != op->kind) {
+                        fprintf(stderr, "ode program: phase %d warp %d mixes op kinds\n", q, w);
+                        return false;
+                    }
+                    kind = op->kind;
+                }
+            }
+            prog->wkind[q][w] = (uint8_t)kind;
+        }
+    }
     prog->n_slots = v[0].next;
     prog->const_begin = XS_FIRST_FREE;
     prog->n_consts = v[0].nconst;

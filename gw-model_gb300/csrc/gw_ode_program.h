@@ -61,13 +61,14 @@ enum OdeSlot : uint16_t {
 // Per-step SSA values pushed to the CTAs (sv[]) that come from the program, by sv index.
 struct OdeProgram {
     int n_phases;
-    int phase_begin[kOdeMaxPhases + 1];  // ops [phase_begin[p], phase_begin[p+1]) of phase p
+    int phase_begin[kOdeMaxPhases + 1];  // ops [phase_begin[p], phase_begin[p+1]) of phase p (<= 128)
     int upd_phase;                       // phase holding the OK_UPD ops
     int push_phase;                      // sv are pushed after this phase
     int n_slots;
     int const_begin, n_consts;           // per-cell constants occupy X[const_begin, +n_consts)
     int n_alt;
     uint16_t sv_src[kSvCount];           // X slot of each sv value (XS_ZERO if not produced)
+    uint8_t wkind[kOdeMaxPhases][kOdeWarps];  // the one op kind of each warp in each phase (NOP: idle)
     uint8_t alt_idx[kOdeMaxOps];         // 255, or index of the op's variant in alt[regime-1]
     OdeOp ops[kOdeMaxOps];               // regime 0: V >= -40
     OdeOp alt[2][kOdeMaxAlt];            // regime 1: V < -40;  regime 2: V == -47.13

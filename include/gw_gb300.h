@@ -189,6 +189,11 @@ int gw_run(gw_ctx *ctx, double dt, int64_t n_steps, int record_every, gw_trace *
 #define GW_NOALLOC_SCRATCH_BYTES ((size_t)16 << 20)
 int gw_run_noalloc(gw_ctx *ctx, double dt, int64_t n_steps, int record_every, gw_trace *trace);
 
+/* Diagnostic, no counterpart in the reference: evaluates on the current device the FP64 exp and
+ * log that the global step uses (table-driven, see gw_math64.cuh) for n inputs, so that their
+ * error against a reference libm can be checked. */
+int gw_math_check(const double *x, int64_t n, double *exp_out, double *log_out);
+
 int gw_get_time(gw_ctx *ctx, int cell, double *t, uint64_t *step);
 /* Restores a cell's accumulated time and global step index (the RNG counter).  With the globals,
  * the CRU arrays including JLCC, and the flux carry, this resumes a run bit for bit; the reference
