@@ -237,6 +237,7 @@ def main():
     if rank == 0 and not args.no_extras:
         line["e2e"] = e2e_measure(span, K)
         line["paths"] = {"plain_gpu": plain_measure(local_rank), "batched_gpu": batched_measure(local_rank)}
+        line["accuracy"] = accuracy_vs_fp64(local_rank)
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
         line["paths"]["cpu"] = {"cru_steps_per_s": line["cpu_baseline"]["value"],
                                 "sim_ms_per_wall_s": line["cpu_baseline"]["value"] / NCRU * DT,
@@ -312,6 +313,37 @@ def batched_measure(device, steps=2000, cluster_ctas=8):
             "launch_shape": {k: st1[k] for k in ("cluster_ctas", "cta_crus", "threads_per_cta", "n_clusters")},
             "workload": f"{len(ncru)} cells, 2,000-12,500 CRUs, log-normal(0.1) PCaL/GKr/GKs/Vmax/rRyR, "
                         f"CL 400-1000 ms, {steps} steps"}
+
+
+def accuracy_vs_fp64(device, cells=64, ncru=200, t_ms=200.0):
+    """Error of the FP32 engine (the measured path) against the FP64 engine (reference arithmetic,
+    checked bit-exact against the oracle): replicate-cell ensembles of one paced beat, two-sample
+    KS p-values and relative differences of the ensemble means of peak Cai, its time and V."""
+    import numpy as np
+    from scipy.stats import ks_2samp
+
+    from gwgb300 import Ensemble
+
+    every = 500
+    out = {}
+    for prec, seed in (("fp32", 31), ("fp64", 32)):
+        e = Ensemble([ncru] * cells, precision=prec, seed=seed, device=device)
+        for c in range(cells):
+            e.sample_initial_crus(c)
+        e.set_pulse(0.0, PERIOD, STIM_DUR, STIM_AMP)
+        tr = e.run(DT, int(t_ms / DT), record_every=every)
+        e.close()
+        V, Cai = tr.var("V"), tr.var("Cai")
+        i100 = int(100.0 / (every * DT)) - 1
+        out[prec] = {"peak_Cai": Cai.max(axis=1), "t_peak_Cai": Cai.argmax(axis=1) * every * DT,
+                     "V_100ms": V[:, i100], "Cai_150ms": Cai[:, int(150.0 / (every * DT)) - 1]}
+    res = {"reference": "FP64 engine (reference arithmetic)", "cells": cells, "ncru": ncru,
+           "window_ms": t_ms, "ks_pvalue": {}, "rel_diff_of_means": {}}
+    for k in out["fp32"]:
+        a, b = out["fp32"][k], out["fp64"][k]
+        res["ks_pvalue"][k] = float(ks_2samp(a, b).pvalue)
+        res["rel_diff_of_means"][k] = float(abs(a.mean() - b.mean()) / max(abs(b.mean()), 1e-30))
+    return res
 
 
 def e2e_measure(span, K):
