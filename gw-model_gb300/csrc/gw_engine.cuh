@@ -146,7 +146,7 @@ __device__ __forceinline__ float t_sqrt(float x) { return sqrtf(x); }
 // diverge; lanes without an op skip the arithmetic.
 template <typename T>
 __device__ __forceinline__ void ode_phase(const OdeProgram &P, int q, int regime, T *X, double *g, int t,
-                                          int *bad, const math64::Tables &M) {
+                                          int *status, const math64::Tables &M) {
     const int wk = P.wkind[q][t >> 5];
     if (wk == OK_NOP) return;
     const int lane = t & 31;
@@ -183,7 +183,7 @@ __device__ __forceinline__ void ode_phase(const OdeProgram &P, int q, int regime
             const double ng = g[out] + (double)GW_ARG(0);
             g[out] = ng;
             X[XS_G + out] = (T)ng;
-            if (!finite_bits(ng)) *bad = 1;
+            if (!finite_bits(ng)) atomicCAS(status, 0, (int)GW_ERR_NONFINITE);  // first error of the cell
             return;
         }
         default: break;
@@ -396,7 +396,6 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
             }
         }
     }
-    int bad = 0;  // ODE threads: non-finite global seen
     if (leader && ode_thread) {
         // program, constants and state of the cell
         {
@@ -431,7 +430,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
         // transcendental phases of the initial state, push sv[0]
         const int reg = v_regime(os.g[0]);
         for (int q = P.upd_phase + 1; q <= P.push_phase; ++q) {
-            ode_phase<T>(P, q, reg, X, os.g, ot, &bad, M);
+            ode_phase<T>(P, q, reg, X, os.g, ot, &os.status, M);
             ode_bar();
         }
         push_sv<FP64, T>(P, X, os.g, svbuf, svstage, 0, w, ot);
@@ -441,7 +440,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
     if (leader && ode_thread) {
         const int reg = v_regime(os.g[0]);
         for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
-            ode_phase<T>(P, q, reg, X, os.g, ot, &bad, M);
+            ode_phase<T>(P, q, reg, X, os.g, ot, &os.status, M);
             ode_bar();
         }
     }
@@ -575,7 +574,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
             ode_bar();
             const int reg_n = v_regime(os.g[0]);
             for (int q = 0; q <= P.upd_phase; ++q) {
-                ode_phase<T>(P, q, reg_n, X, os.g, ot, &bad, M);
+                ode_phase<T>(P, q, reg_n, X, os.g, ot, &os.status, M);
                 ode_bar();
             }
             if (ot == 0) os.t += a.dt;
@@ -586,7 +585,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
             }
             const int reg = v_regime(os.g[0]);
             for (int q = P.upd_phase + 1; q <= P.push_phase; ++q) {
-                ode_phase<T>(P, q, reg, X, os.g, ot, &bad, M);
+                ode_phase<T>(P, q, reg, X, os.g, ot, &os.status, M);
                 ode_bar();
             }
             push_sv<FP64, T>(P, X, os.g, svbuf, svstage, par ^ 1, w, ot);
@@ -595,7 +594,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
             // next step, after its ode_bar) and the phases the SSA does not need
             if (ot == 0) X[XS_ISTIM] = (T)stimulus(a.dyn[cell], os.t, ri + 1);
             for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
-                ode_phase<T>(P, q, reg, X, os.g, ot, &bad, M);
+                ode_phase<T>(P, q, reg, X, os.g, ot, &os.status, M);
                 ode_bar();
             }
         }
@@ -606,8 +605,6 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
     if (leader && ode_thread) {
         if (a.n_steps > 0)
             reduce_partials<FP64, T>(part + ((a.n_steps - 1) & 1) * pslot, w.n_cta_cell, ot >> 5, lane, os.sums, X);
-        const unsigned anybad = __ballot_sync(0xffffffffu, bad != 0);
-        if (lane == 0 && anybad) atomicCAS(&os.status, 0, (int)GW_ERR_NONFINITE);
         ode_bar();
         CellDyn &d = a.dyn[cell];
         for (int i = ot; i < kNumGlobals; i += kOdeLanes) d.g[i] = os.g[i];
