@@ -783,8 +783,14 @@ int gw_run(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_trace *tr
     cudaSetDevice(c->device);
     if (tr) tr->n_written = 0;
     const bool recording = tr && record_every > 0 && tr->max_records > 0;
-    const int tr_cell = (recording && (tr->CaSS || tr->CaJSR || tr->LCC || tr->LCC_inactivation || tr->RyR || tr->ClCh))
-                            ? tr->cru_cell : -1;
+    const bool planes = recording && (tr->CaSS || tr->CaJSR || tr->LCC || tr->LCC_inactivation || tr->RyR || tr->ClCh);
+    const bool codec = recording && (tr->LCC_i8 || tr->LCC_inactivation_u8 || tr->ClCh_u8 || tr->RyR_i16 ||
+                                     tr->CaSS_f32 || tr->CaJSR_f32);
+    const bool sums = recording && tr->cru_sums;
+    if (planes && codec)
+        return fail(c, GW_ERR_INVALID_ARGUMENT,
+                    "trace: request either the int32/double CRU arrays or the reduced-memory ones, not both");
+    const int tr_cell = (planes || codec) ? tr->cru_cell : -1;
     if (tr_cell >= c->n_cells) return fail(c, GW_ERR_INVALID_ARGUMENT, "trace cell out of range");
     {
         // the RNG counter holds 32 bits of the step index
@@ -797,19 +803,29 @@ int gw_run(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_trace *tr
     const int chunk = c->steps_per_launch;
     // Device trace buffers for the records of one launch.
     const int rec_cap = recording ? (int)std::min<int64_t>(tr->max_records, chunk / record_every + 2) : 0;
-    DevBuf d_t, d_glob, d_tlcc, d_tflags, d_tryr, d_tcass, d_tcajsr;
+    DevBuf d_t, d_glob, d_tlcc, d_tflags, d_tryr, d_tcass, d_tcajsr, d_gate, d_clch, d_ryrc, d_cassf, d_cajsrf, d_sums;
     int64_t stride = 0;
+    const int64_t ncr = tr_cell >= 0 ? c->ncru[tr_cell] : 0;
     if (recording) {
         CK(c, d_t.alloc(sizeof(double) * rec_cap));
         CK(c, d_glob.alloc(sizeof(double) * kNumGlobals * (size_t)rec_cap * c->n_cells));
-        if (tr_cell >= 0) {
-            stride = ((int64_t)c->ncru[tr_cell] + 31) / 32 * 32;
+        if (planes && tr_cell >= 0) {
+            stride = (ncr + 31) / 32 * 32;
             CK(c, d_tlcc.alloc(4 * stride * rec_cap));
             CK(c, d_tflags.alloc(4 * stride * rec_cap));
             CK(c, d_tryr.alloc(4 * 6 * stride * rec_cap));
             CK(c, d_tcass.alloc(c->rsize * 4 * stride * rec_cap));
             CK(c, d_tcajsr.alloc(c->rsize * stride * rec_cap));
         }
+        if (codec && tr_cell >= 0) {
+            CK(c, d_tlcc.alloc(4 * ncr * rec_cap));
+            CK(c, d_gate.alloc(4 * ncr * rec_cap));
+            CK(c, d_clch.alloc(4 * ncr * rec_cap));
+            CK(c, d_ryrc.alloc(8 * ncr * rec_cap));
+            CK(c, d_cassf.alloc(16 * ncr * rec_cap));
+            CK(c, d_cajsrf.alloc(4 * ncr * rec_cap));
+        }
+        if (sums) CK(c, d_sums.alloc(sizeof(unsigned long long) * kSumFields * (size_t)rec_cap * c->n_cells));
     }
     KernelArgs a = base_args(c);
     a.dt = dt;
@@ -824,7 +840,16 @@ int gw_run(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_trace *tr
     a.tr_ryr = d_tryr.as<uint32_t>();
     a.tr_cass = d_tcass.p;
     a.tr_cajsr = d_tcajsr.p;
+    a.tr_mode = codec ? 1 : 0;
+    a.tr_ncru = ncr;
+    a.tr_gate = d_gate.as<uint32_t>();
+    a.tr_clch = d_clch.as<uint32_t>();
+    a.tr_ryrc = d_ryrc.as<uint32_t>();
+    a.tr_cass_f = d_cassf.as<float>();
+    a.tr_cajsr_f = d_cajsrf.as<float>();
+    a.tr_sums = d_sums.as<unsigned long long>();
     CK(c, cudaMemsetAsync(c->d_status.p, 0, sizeof(int) * c->n_cells, c->stream));
+    std::vector<unsigned long long> h_sums;
     std::vector<double> h_t, h_glob;
     std::vector<uint32_t> h_lcc, h_flags, h_ryr;
     std::vector<unsigned char> h_cass, h_cajsr;
@@ -842,6 +867,7 @@ int gw_run(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_trace *tr
             r_hi = std::min<int64_t>(r_hi, tr->max_records - 1);
             a.rec_base = r_lo;
         }
+        if (sums) CK(c, cudaMemsetAsync(d_sums.p, 0, d_sums.n, c->stream));
         CK(c, cudaEventRecord(c->ev0, c->stream));
         const int e = c->precision == GW_PRECISION_FP64 ? launch_engine_fp64(a, c->shape, c->stream, c->ode64)
                                                         : launch_engine_fp32(a, c->shape, c->stream, c->ode64);
@@ -851,6 +877,29 @@ int gw_run(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_trace *tr
         if (recording && r_hi >= r_lo) {
             const int64_t nr = r_hi - r_lo + 1;
             CK(c, cudaStreamSynchronize(c->stream));
+            if (sums) {
+                h_sums.resize((size_t)kSumFields * rec_cap * c->n_cells);
+                CK(c, cudaMemcpy(h_sums.data(), d_sums.p, d_sums.n, cudaMemcpyDeviceToHost));
+                for (int cell = 0; cell < c->n_cells; ++cell)
+                    for (int64_t r = 0; r < nr; ++r)
+                        for (int f = 0; f < kSumFields; ++f) {
+                            const long long v = (long long)h_sums[((size_t)cell * rec_cap + r) * kSumFields + f];
+                            const bool ca = f == GW_SUM_CASS_CONDUCTING || f == GW_SUM_CASS || f == GW_SUM_CAJSR;
+                            tr->cru_sums[((int64_t)cell * tr->max_records + r_lo + r) * kSumFields + f] =
+                                ca ? std::ldexp((double)v, -40) : (double)v;
+                        }
+            }
+            if (codec && tr_cell >= 0) {
+                const size_t n4 = (size_t)nr * ncr * 4, o4 = (size_t)r_lo * ncr * 4;
+                if (tr->LCC_i8) CK(c, cudaMemcpy(tr->LCC_i8 + o4, d_tlcc.p, n4, cudaMemcpyDeviceToHost));
+                if (tr->LCC_inactivation_u8)
+                    CK(c, cudaMemcpy(tr->LCC_inactivation_u8 + o4, d_gate.p, n4, cudaMemcpyDeviceToHost));
+                if (tr->ClCh_u8) CK(c, cudaMemcpy(tr->ClCh_u8 + o4, d_clch.p, n4, cudaMemcpyDeviceToHost));
+                if (tr->RyR_i16) CK(c, cudaMemcpy(tr->RyR_i16 + o4, d_ryrc.p, 2 * n4, cudaMemcpyDeviceToHost));
+                if (tr->CaSS_f32) CK(c, cudaMemcpy(tr->CaSS_f32 + o4, d_cassf.p, 4 * n4, cudaMemcpyDeviceToHost));
+                if (tr->CaJSR_f32)
+                    CK(c, cudaMemcpy(tr->CaJSR_f32 + (size_t)r_lo * ncr, d_cajsrf.p, n4, cudaMemcpyDeviceToHost));
+            }
             h_t.resize(nr);
             CK(c, cudaMemcpy(h_t.data(), d_t.p, sizeof(double) * nr, cudaMemcpyDeviceToHost));
             if (tr->t)
@@ -864,8 +913,7 @@ int gw_run(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_trace *tr
                                     h_glob.data() + ((int64_t)cell * rec_cap + r) * kNumGlobals,
                                     sizeof(double) * kNumGlobals);
             }
-            if (tr_cell >= 0) {
-                const int ncr = c->ncru[tr_cell];
+            if (planes && tr_cell >= 0) {
                 h_lcc.resize(stride * nr);
                 h_flags.resize(stride * nr);
                 h_ryr.resize(6 * stride * nr);
@@ -938,6 +986,9 @@ int gw_run_noalloc(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_t
     CK(c, cudaSetDevice(c->device));
     if (tr) tr->n_written = 0;
     const bool recording = tr && record_every > 0 && tr->max_records > 0;
+    if (recording && (tr->cru_sums || tr->LCC_i8 || tr->LCC_inactivation_u8 || tr->ClCh_u8 || tr->RyR_i16 ||
+                      tr->CaSS_f32 || tr->CaJSR_f32))
+        return fail(c, GW_ERR_INVALID_ARGUMENT, "gw_run_noalloc records the int32/double trace arrays only");
     const bool cru_fields = recording && (tr->CaSS || tr->CaJSR || tr->LCC || tr->LCC_inactivation || tr->RyR || tr->ClCh);
     const int tr_cell = cru_fields ? tr->cru_cell : -1;
     if (tr_cell >= c->n_cells) return fail(c, GW_ERR_INVALID_ARGUMENT, "trace cell out of range");

@@ -263,6 +263,98 @@ __device__ __forceinline__ void push_sv(const OdeProgram &P, const T *X, const d
     }
 }
 
+// Ca in 2^-40 mM fixed point (exact, order-independent sums of the record-time CRU sums).
+__device__ __forceinline__ long long fix40(float x) { return __float2ll_rn(x * 0x1p40f); }
+__device__ __forceinline__ long long fix40(double x) { return __double2ll_rn(x * 0x1p40); }
+
+// The RyR states of subunit j as the int16 code of the reference's reduced-memory trace
+// (utils.py:8-22): a negative count in a lumped pair (3/4, 5/6) moves the pair's total into the
+// pair's first state; code = n1 + 6 n2 + 36 n3 + 216 n4 + 1296 n5.
+__device__ __forceinline__ uint32_t ryr_code16(const uint32_t (&ry)[6], int j) {
+    const int r0 = byte_s(ry[0], j), r1 = byte_s(ry[1], j), r2 = byte_s(ry[2], j);
+    const int r3 = byte_s(ry[3], j), r4 = byte_s(ry[4], j), r5 = byte_s(ry[5], j);
+    const bool n34 = r2 < 0 || r3 < 0, n56 = r4 < 0 || r5 < 0;
+    const int q2 = n34 ? r2 + r3 : r2, q3 = n34 ? 0 : r3, q4 = n56 ? r4 + r5 : r4;
+    return (uint32_t)(uint16_t)(int16_t)(r0 + 6 * r1 + 36 * q2 + 216 * q3 + 1296 * q4);
+}
+
+// Record step, by one warp over its CRUs [beg, end) of the tile after the step's SSA: the trace
+// cell's CRU records (planes or the reduced-memory codec) and every cell's CRU sums (warp sums
+// added to the record's int64 counters; integer adds, so the totals do not depend on order).
+template <typename R>
+__device__ __forceinline__ void record_pass(const KernelArgs &a, const CtaWork &w, int cell, int64_t r_idx, int beg,
+                                            int end, int lane, int cap, const uint32_t *t_lcc, const uint32_t *t_flags,
+                                            const uint32_t *t_ryr, const R *t_cass, const R *t_cajsr,
+                                            const float *t_cajsr_lo) {
+    constexpr bool FP64 = sizeof(R) == 8;
+    const bool crus = cell == a.tr_cell;
+    const bool sums = a.tr_sums != nullptr;
+    long long v[kSumFields] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int m = beg + lane; m < end; m += 32) {
+        const uint32_t lcc = t_lcc[m], fl = t_flags[m];
+        uint32_t ry[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) ry[k] = t_ryr[k * cap + m];
+        R cs[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) cs[j] = t_cass[j * cap + m];
+        const R jsr = t_cajsr[m];
+        if (sums) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int st = byte_u(lcc, j);
+                const bool open = st == 6 || st == 12;
+                const bool cond = open && ((fl >> j) & 1u);
+                const long long f = fix40(cs[j]);
+                v[0] += open;
+                v[1] += cond;
+                v[2] += cond ? f : 0;
+                v[3] += byte_s(ry[2], j) + byte_s(ry[3], j);
+                v[5] += f;
+            }
+            v[4] += __popc((fl >> 4) & 0xFu);
+            v[6] += fix40(jsr) + (FP64 ? 0ll : fix40(t_cajsr_lo[m]));
+            v[7] += 1;
+        }
+        if (crus) {
+            const int64_t cm = w.cru_begin + m;
+            if (a.tr_mode == 0) {
+                const int64_t st = a.tr_cru_stride;
+                a.tr_lcc[r_idx * st + cm] = lcc;
+                a.tr_flags[r_idx * st + cm] = fl;
+#pragma unroll
+                for (int k = 0; k < 6; ++k) a.tr_ryr[(r_idx * 6 + k) * st + cm] = ry[k];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) reinterpret_cast<R *>(a.tr_cass)[(r_idx * 4 + j) * st + cm] = cs[j];
+                reinterpret_cast<R *>(a.tr_cajsr)[r_idx * st + cm] = jsr;
+            } else {
+                const int64_t o = r_idx * a.tr_ncru + cm;
+                a.tr_lcc[o] = lcc;
+                a.tr_gate[o] = ((fl & 0xFu) * 0x00204081u) & 0x01010101u;
+                a.tr_clch[o] = (((fl >> 4) & 0xFu) * 0x00204081u) & 0x01010101u;
+                a.tr_ryrc[2 * o] = ryr_code16(ry, 0) | (ryr_code16(ry, 1) << 16);
+                a.tr_ryrc[2 * o + 1] = ryr_code16(ry, 2) | (ryr_code16(ry, 3) << 16);
+                reinterpret_cast<float4 *>(a.tr_cass_f)[o] =
+                    make_float4((float)cs[0], (float)cs[1], (float)cs[2], (float)cs[3]);
+                a.tr_cajsr_f[o] = (float)jsr;  // FP32: the compensated value rounds to its leading part
+            }
+        }
+    }
+    if (sums) {
+#pragma unroll
+        for (int f = 0; f < kSumFields; ++f) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v[f] += __shfl_xor_sync(0xffffffffu, v[f], o);
+        }
+        if (lane == 0) {
+            unsigned long long *dst = a.tr_sums + ((int64_t)cell * a.rec_cap + r_idx) * kSumFields;
+#pragma unroll
+            for (int f = 0; f < kSumFields; ++f)
+                if (v[f] != 0) atomicAdd(dst + f, (unsigned long long)v[f]);
+        }
+    }
+}
+
 constexpr int kMaxThreads = 512;  // SSA warps + ODE warps per CTA (128 registers per thread)
 
 // Per-lane flux accumulators and their warp sum as a Partial (all lanes hold it).
@@ -473,8 +565,9 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
                 }
                 // This warp's CRUs [cursor, end).  A lane whose CRU has finished its step takes the
                 // next one, so lanes with pending SSA events do not hold the others back.
-                int cursor = (int)((int64_t)w.cru_count * warp / nsw);
+                const int beg = (int)((int64_t)w.cru_count * warp / nsw);
                 const int end = (int)((int64_t)w.cru_count * (warp + 1) / nsw);
+                int cursor = beg;
                 FluxAcc<FP64> acc;
                 Cru<R> c;
                 SsaLane<R, EXACT> sl;
@@ -525,22 +618,14 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
                             my_err |= err;
                             acc.add(c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3], sl.jxfer_sum, sl.jtr,
                                     __popc((c.flags >> 4) & 0xFu));
-                            if (rec_ok && cell == a.tr_cell) {
-                                const int64_t cm = w.cru_begin + m;
-                                const int64_t st = a.tr_cru_stride;
-                                a.tr_lcc[r_idx * st + cm] = c.lcc;
-                                a.tr_flags[r_idx * st + cm] = c.flags;
-#pragma unroll
-                                for (int k = 0; k < 6; ++k) a.tr_ryr[(r_idx * 6 + k) * st + cm] = c.ryr[k];
-#pragma unroll
-                                for (int j = 0; j < 4; ++j)
-                                    reinterpret_cast<R *>(a.tr_cass)[(r_idx * 4 + j) * st + cm] = c.cass[j];
-                                reinterpret_cast<R *>(a.tr_cajsr)[r_idx * st + cm] = c.cajsr;
-                            }
                             m = -1;
                         }
                     }
                 }
+                // Records of this step, from the warp's part of the tile (now at the end of the step)
+                if (rec_ok && (cell == a.tr_cell || a.tr_sums != nullptr))
+                    record_pass<R>(a, w, cell, r_idx, beg, end, lane, cap, t_lcc, t_flags, t_ryr, t_cass, t_cajsr,
+                                   t_cajsr_lo);
                 // Warp partial; the warp that finishes last sums the warp partials in warp order
                 // and pushes the CTA's partial to the leader.
                 const Partial pv = acc.warp_total();

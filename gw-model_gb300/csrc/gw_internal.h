@@ -18,6 +18,7 @@ namespace gw {
 constexpr int kNumGlobals = 36;
 constexpr int kMaxClusterCtas = 16;
 constexpr int kSvCount = 40;  // per-step SSA values pushed to every CTA each step
+constexpr int kSumFields = GW_CRU_SUMS;  // record-time CRU sums per cell (gw_trace.cru_sums)
 
 // Index of per-step SSA values (sv[]) computed by a cell's ODE warp from V and pushed to the
 // cell's CTAs: voltage-dependent LCC rates of update_LCC_rates (GW_utils.tpp:118-186) with the
@@ -106,8 +107,15 @@ struct KernelArgs {
     double *tr_glob;    // [n_cells][rec_cap][36]
     int tr_cell;        // cell whose CRU state is recorded (-1: none)
     int64_t tr_cru_stride;  // elements per record per plane (padded ncru of tr_cell)
-    uint32_t *tr_lcc, *tr_flags, *tr_ryr;  // [rec][plane][stride]
-    void *tr_cass, *tr_cajsr;              // Real
+    uint32_t *tr_lcc, *tr_flags, *tr_ryr;  // planes mode: [rec][plane][stride]; codec: tr_lcc [rec][ncru]
+    void *tr_cass, *tr_cajsr;              // planes mode, Real
+    int tr_mode;                           // 0: planes; 1: reduced-memory codec (AoS per CRU)
+    int tr_pad;
+    int64_t tr_ncru;                       // codec: CRUs of tr_cell (record stride)
+    uint32_t *tr_gate, *tr_clch;           // codec: [rec][ncru] 4 bools each
+    uint32_t *tr_ryrc;                     // codec: [rec][ncru][2] 4 int16 RyR codes
+    float *tr_cass_f, *tr_cajsr_f;         // codec: [rec][ncru][4], [rec][ncru]
+    unsigned long long *tr_sums;           // [n_cells][rec_cap][8] CRU sums (int64; Ca in 2^-40 mM)
     uint64_t seed;
     int event_cap;
     int n_cells;

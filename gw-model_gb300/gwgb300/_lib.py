@@ -59,7 +59,14 @@ class GwTrace(C.Structure):
                 ("CaSS", C.POINTER(C.c_double)), ("CaJSR", C.POINTER(C.c_double)),
                 ("LCC", C.POINTER(C.c_int32)), ("LCC_inactivation", C.POINTER(C.c_int32)),
                 ("RyR", C.POINTER(C.c_int32)), ("ClCh", C.POINTER(C.c_int32)),
-                ("n_written", C.c_int64)]
+                ("n_written", C.c_int64), ("cru_sums", C.POINTER(C.c_double)),
+                ("LCC_i8", C.POINTER(C.c_int8)), ("LCC_inactivation_u8", C.POINTER(C.c_uint8)),
+                ("ClCh_u8", C.POINTER(C.c_uint8)), ("RyR_i16", C.POINTER(C.c_int16)),
+                ("CaSS_f32", C.POINTER(C.c_float)), ("CaJSR_f32", C.POINTER(C.c_float))]
+
+
+CRU_SUMS = 8
+SUM_FIELDS = ["LCC_open", "LCC_conducting", "CaSS_conducting", "RyR_open", "ClCh_open", "CaSS", "CaJSR", "CRUs"]
 
 
 class GwStats(C.Structure):

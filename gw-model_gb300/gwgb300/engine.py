@@ -77,9 +77,14 @@ class Trace:
     t: np.ndarray
     globals: np.ndarray               # [n_cells, n_records, 36]
     crus: Optional[Dict[str, np.ndarray]] = None
+    cru_sums: Optional[np.ndarray] = None   # [n_cells, n_records, 8], fields _lib.SUM_FIELDS
+    codec: Optional[Dict[str, np.ndarray]] = None  # reduced-memory CRU records of cru_cell
 
     def var(self, name: str) -> np.ndarray:
         return self.globals[..., GLOBAL_NAMES.index(name)]
+
+    def sum(self, name: str) -> np.ndarray:
+        return self.cru_sums[..., _lib.SUM_FIELDS.index(name)]
 
 
 class Ensemble:
@@ -212,7 +217,10 @@ class Ensemble:
 
     # ---- stepping ----
     def run(self, dt: float, n_steps: int, record_every: int = 0, cru_cell: Optional[int] = None,
-            max_records: Optional[int] = None) -> Optional[Trace]:
+            max_records: Optional[int] = None, sums: bool = False, codec: bool = False) -> Optional[Trace]:
+        """Advance every cell by n_steps.  With record_every > 0, returns the globals of every cell
+        at each record; cru_cell adds that cell's CRU arrays (codec=True: in the reduced-memory
+        layout, written by the device); sums=True adds every cell's record-time CRU sums."""
         if record_every <= 0:
             check(self.L.gw_run(self.h, dt, int(n_steps), 0, None), self.h)
             return None
@@ -225,7 +233,24 @@ class Ensemble:
         tr.globals = _dp(G)
         tr.cru_cell = -1
         crus = None
-        if cru_cell is not None:
+        cod = None
+        cs = None
+        if sums:
+            cs = np.zeros((self.n_cells, max(nrec, 1), _lib.CRU_SUMS))
+            tr.cru_sums = _dp(cs)
+        if cru_cell is not None and codec:
+            n = int(self.ncru[cru_cell])
+            cod = {"LCC": np.zeros((nrec, n, 4), np.int8), "LCC_inactivation": np.zeros((nrec, n, 4), np.bool_),
+                   "ClCh": np.zeros((nrec, n, 4), np.bool_), "RyR": np.zeros((nrec, n, 4), np.int16),
+                   "CaSS": np.zeros((nrec, n, 4), np.float32), "CaJSR": np.zeros((nrec, n), np.float32)}
+            tr.cru_cell = cru_cell
+            tr.LCC_i8 = cod["LCC"].ctypes.data_as(C.POINTER(C.c_int8))
+            tr.LCC_inactivation_u8 = cod["LCC_inactivation"].ctypes.data_as(C.POINTER(C.c_uint8))
+            tr.ClCh_u8 = cod["ClCh"].ctypes.data_as(C.POINTER(C.c_uint8))
+            tr.RyR_i16 = cod["RyR"].ctypes.data_as(C.POINTER(C.c_int16))
+            tr.CaSS_f32 = cod["CaSS"].ctypes.data_as(C.POINTER(C.c_float))
+            tr.CaJSR_f32 = cod["CaJSR"].ctypes.data_as(C.POINTER(C.c_float))
+        elif cru_cell is not None:
             n = int(self.ncru[cru_cell])
             crus = {"CaSS": np.zeros((nrec, n, 4)), "CaJSR": np.zeros((nrec, n)),
                     "LCC": np.zeros((nrec, n, 4), np.int32),
@@ -239,7 +264,9 @@ class Ensemble:
         k = int(tr.n_written)
         if crus is not None:
             crus = {a: b[:k] for a, b in crus.items()}
-        return Trace(t=t[:k], globals=G[:, :k], crus=crus)
+        if cod is not None:
+            cod = {a: b[:k] for a, b in cod.items()}
+        return Trace(t=t[:k], globals=G[:, :k], crus=crus, cru_sums=None if cs is None else cs[:, :k], codec=cod)
 
     def stats(self) -> dict:
         s = GwStats()

@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define GW_ABI_VERSION 1
+#define GW_ABI_VERSION 2
 
 /* Status codes. */
 typedef enum gw_status {
@@ -105,7 +105,34 @@ typedef struct gw_trace {
     int32_t *RyR;           /* [max_records][ncru][4][6] */
     int32_t *ClCh;          /* [max_records][ncru][4] */
     int64_t n_written;      /* out: records written */
+    /* Per-record sums over each cell's CRUs, taken on the device at the record (no CRU arrays
+     * leave the device): [n_cells][max_records][GW_CRU_SUMS], or NULL.  Indices GW_SUM_*. */
+    double *cru_sums;
+    /* The trace cell's CRU records in the reference's reduced-memory layout
+     * (serialization.py:11-39): float32 Ca, int8 LCC states, bool gates and ClCh, and the RyR
+     * states of each subunit as the int16 code of utils.py:8-22.  Written by the device at the
+     * record step, copied as is; each NULL or [max_records][ncru][4] ([max_records][ncru] for
+     * CaJSR_f32).  Not with gw_run_noalloc. */
+    int8_t *LCC_i8;
+    uint8_t *LCC_inactivation_u8;
+    uint8_t *ClCh_u8;
+    int16_t *RyR_i16;
+    float *CaSS_f32;
+    float *CaJSR_f32;
 } gw_trace;
+
+/* Last axis of gw_trace.cru_sums.  Counts are exact; the Ca sums carry 2^-40 mM resolution. */
+#define GW_CRU_SUMS 8
+enum {
+    GW_SUM_LCC_OPEN = 0,         /* LCC subunits in an open state (6 or 12) */
+    GW_SUM_LCC_CONDUCTING = 1,   /* ... of which the voltage gate is not inactivated (= 1) */
+    GW_SUM_CASS_CONDUCTING = 2,  /* sum of CaSS over the conducting subunits [mM] */
+    GW_SUM_RYR_OPEN = 3,         /* RyRs in the open states 3 and 4 */
+    GW_SUM_CLCH_OPEN = 4,        /* open ClCh */
+    GW_SUM_CASS = 5,             /* sum of CaSS over all subunits [mM] */
+    GW_SUM_CAJSR = 6,            /* sum of CaJSR over CRUs [mM] */
+    GW_SUM_CRUS = 7              /* CRUs summed (= ncru) */
+};
 
 /* Run statistics. */
 typedef struct gw_stats {

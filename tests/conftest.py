@@ -1,5 +1,7 @@
+import importlib
 import os
 import sys
+import types
 
 import pytest
 
@@ -9,6 +11,8 @@ for p in (os.path.join(REPO, "gw-model_gb300"), os.path.join(REPO, "oracle"), RE
         sys.path.insert(0, p)
 
 GOLDEN = os.path.join(REPO, "tests", "golden")
+# the reference sources, present only where the reference was checked out next to this build
+REF = "/root/reference"
 
 
 def pytest_configure(config):
@@ -29,3 +33,35 @@ def enginelib():
     from gwgb300 import _lib
 
     return _lib.load(build_if_missing=True)
+
+
+@pytest.fixture(scope="session")
+def GW(enginelib):
+    import GreensteinWinslow
+
+    return GreensteinWinslow
+
+
+@pytest.fixture(scope="session")
+def ref_src(GW):
+    if not os.path.isdir(os.path.join(REF, "src")):
+        pytest.skip("reference Python layer not present")
+    build = types.ModuleType("build")
+    build.GreensteinWinslow = GW
+    saved = {k: sys.modules.get(k) for k in ("build", "build.GreensteinWinslow", "h5py")}
+    sys.modules["build"] = build
+    sys.modules["build.GreensteinWinslow"] = GW
+    h5 = types.ModuleType("h5py")
+    h5.File = object
+    sys.modules["h5py"] = h5
+    sys.path.insert(0, REF)
+    try:
+        src = importlib.import_module("src")
+        yield src
+    finally:
+        sys.path.remove(REF)
+        for k, v in saved.items():
+            if v is None:
+                sys.modules.pop(k, None)
+            else:
+                sys.modules[k] = v

@@ -45,7 +45,8 @@ int main(void) {
   P(gw_params) P(gw_globals) P(gw_ensemble_desc) P(gw_trace) P(gw_stats)
   O(gw_params, NCaRU) O(gw_params, Ko) O(gw_params, Hr) O(gw_globals, Kr) O(gw_globals, Kv43)
   O(gw_globals, Kv14) O(gw_ensemble_desc, seed) O(gw_ensemble_desc, ode_fp32_rhs)
-  O(gw_trace, cru_cell) O(gw_trace, n_written) O(gw_stats, kernel_ms) O(gw_stats, ctas)
+  O(gw_trace, cru_cell) O(gw_trace, n_written) O(gw_trace, cru_sums) O(gw_trace, CaJSR_f32)
+  O(gw_stats, kernel_ms) O(gw_stats, ctas)
   return 0;
 }
 """
@@ -88,7 +89,7 @@ def test_global_defaults(enginelib, oracle):
 
 
 def test_abi_version(enginelib):
-    assert enginelib.gw_abi_version() == 1
+    assert enginelib.gw_abi_version() == 2
 
 
 def test_invalid_arguments_without_device(enginelib):

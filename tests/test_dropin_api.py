@@ -1,22 +1,8 @@
 """The drop-in module GreensteinWinslow mirrors the reference's pybind11 surface (src/pyGW.cpp):
 class names, fields, defaults, shapes, repr strings and errors.  Where the reference sources are
 present, its own Python layer (src/model.py, src/parameters.py) is imported against this module."""
-import importlib
-import os
-import sys
-import types
-
 import numpy as np
 import pytest
-
-REF = "/root/reference"
-
-
-@pytest.fixture(scope="module")
-def GW(enginelib):
-    import GreensteinWinslow
-
-    return GreensteinWinslow
 
 
 def test_parameters(GW, oracle):
@@ -66,31 +52,6 @@ def test_variables(GW):
 def test_run_rejects_unknown_prng(GW):
     with pytest.raises(ValueError):
         GW.run(GW.GWParameters(), 4, 1e-3, 10, lambda t: 0.0, 1, GW.GWCRUState(4), PRNG="pcg64")
-
-
-@pytest.fixture(scope="module")
-def ref_src(GW):
-    if not os.path.isdir(os.path.join(REF, "src")):
-        pytest.skip("reference Python layer not present")
-    build = types.ModuleType("build")
-    build.GreensteinWinslow = GW
-    saved = {k: sys.modules.get(k) for k in ("build", "build.GreensteinWinslow", "h5py")}
-    sys.modules["build"] = build
-    sys.modules["build.GreensteinWinslow"] = GW
-    h5 = types.ModuleType("h5py")
-    h5.File = object
-    sys.modules["h5py"] = h5
-    sys.path.insert(0, REF)
-    try:
-        src = importlib.import_module("src")
-        yield src
-    finally:
-        sys.path.remove(REF)
-        for k, v in saved.items():
-            if v is None:
-                sys.modules.pop(k, None)
-            else:
-                sys.modules[k] = v
 
 
 def test_reference_python_layer_imports(ref_src, GW):
