@@ -72,9 +72,8 @@ __host__ __device__ inline SmemLayout smem_layout(int tile_cap, int max_cta_cell
     o += align16((size_t)16 * sizeof(Partial));
     L.ctr = o;   // warp completion counters [2 + parity]
     o += 16;
-    L.tile = o;
-    // lcc, flags, ryr[6] (u32), cass[4], jlcc[4], cajsr (R), cajsr_lo (f32)
-    o += align16((size_t)tile_cap * (8 * sizeof(uint32_t) + 9 * sizeof(R) + sizeof(float)));
+    L.tile = o;  // TileRec<R> per CRU
+    o += align16((size_t)tile_cap * sizeof(TileRec<R>));
     L.total = o;
     return L;
 }
@@ -283,22 +282,18 @@ __device__ __forceinline__ uint32_t ryr_code16(const uint32_t (&ry)[6], int j) {
 // added to the record's int64 counters; integer adds, so the totals do not depend on order).
 template <typename R>
 __device__ __forceinline__ void record_pass(const KernelArgs &a, const CtaWork &w, int cell, int64_t r_idx, int beg,
-                                            int end, int lane, int cap, const uint32_t *t_lcc, const uint32_t *t_flags,
-                                            const uint32_t *t_ryr, const R *t_cass, const R *t_cajsr,
-                                            const float *t_cajsr_lo) {
+                                            int end, int lane, const TileRec<R> *tile) {
     constexpr bool FP64 = sizeof(R) == 8;
     const bool crus = cell == a.tr_cell;
     const bool sums = a.tr_sums != nullptr;
     long long v[kSumFields] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int m = beg + lane; m < end; m += 32) {
-        const uint32_t lcc = t_lcc[m], fl = t_flags[m];
-        uint32_t ry[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) ry[k] = t_ryr[k * cap + m];
-        R cs[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) cs[j] = t_cass[j * cap + m];
-        const R jsr = t_cajsr[m];
+        Cru<R> c;
+        tile_get(c, tile[m]);
+        const uint32_t lcc = c.lcc, fl = c.flags;
+        const uint32_t(&ry)[6] = c.ryr;
+        const R(&cs)[4] = c.cass;
+        const R jsr = c.cajsr;
         if (sums) {
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
@@ -313,7 +308,7 @@ __device__ __forceinline__ void record_pass(const KernelArgs &a, const CtaWork &
                 v[5] += f;
             }
             v[4] += __popc((fl >> 4) & 0xFu);
-            v[6] += fix40(jsr) + (FP64 ? 0ll : fix40(t_cajsr_lo[m]));
+            v[6] += fix40(jsr) + (FP64 ? 0ll : fix40(c.cajsr_lo));
             v[7] += 1;
         }
         if (crus) {
@@ -449,14 +444,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
     Partial *chunkp = reinterpret_cast<Partial *>(smem + L.chunk);  // warp partials
     float2 *rtab = reinterpret_cast<float2 *>(smem + L.rtab) + warp * kRateTab;  // this warp's table
     int *ctr = reinterpret_cast<int *>(smem + L.ctr);
-    const int cap = a.tile_cap;
-    uint32_t *t_lcc = reinterpret_cast<uint32_t *>(smem + L.tile);
-    uint32_t *t_flags = t_lcc + cap;
-    uint32_t *t_ryr = t_flags + cap;
-    R *t_cass = reinterpret_cast<R *>(t_ryr + 6 * cap);
-    R *t_jlcc = t_cass + 4 * cap;
-    R *t_cajsr = t_jlcc + 4 * cap;
-    float *t_cajsr_lo = reinterpret_cast<float *>(t_cajsr + cap);
+    TileRec<R> *tile = reinterpret_cast<TileRec<R> *>(smem + L.tile);
     const int cell = w.cell;
     const int pslot = a.max_cta_cell;  // partial entries per parity slot
     R *g_cass = reinterpret_cast<R *>(a.cass);
@@ -474,17 +462,19 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
             const int64_t base = a.slot0[cell] + w.cru_begin;
             for (int m = (int)threadIdx.x; m < w.cru_count; m += n_ssa) {
                 const int64_t gs = base + m;
-                t_lcc[m] = a.lcc[gs];
-                t_flags[m] = a.flags[gs];
+                Cru<R> c;
+                c.lcc = a.lcc[gs];
+                c.flags = a.flags[gs];
 #pragma unroll
-                for (int k = 0; k < 6; ++k) t_ryr[k * cap + m] = a.ryr[k * a.n_slots + gs];
+                for (int k = 0; k < 6; ++k) c.ryr[k] = a.ryr[k * a.n_slots + gs];
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
-                    t_cass[j * cap + m] = g_cass[j * a.n_slots + gs];
-                    t_jlcc[j * cap + m] = g_jlcc[j * a.n_slots + gs];
+                    c.cass[j] = g_cass[j * a.n_slots + gs];
+                    c.jlcc[j] = g_jlcc[j * a.n_slots + gs];
                 }
-                t_cajsr[m] = g_cajsr[gs];
-                if (!FP64) t_cajsr_lo[m] = a.cajsr_lo[gs];
+                c.cajsr = g_cajsr[gs];
+                c.cajsr_lo = FP64 ? 0.f : a.cajsr_lo[gs];
+                tile_put(tile[m], c);
             }
         }
     }
@@ -581,17 +571,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
                         if (m == -1) {
                             if (nm < end) {
                                 m = nm;
-                                c.lcc = t_lcc[m];
-                                c.flags = t_flags[m];
-#pragma unroll
-                                for (int k = 0; k < 6; ++k) c.ryr[k] = t_ryr[k * cap + m];
-#pragma unroll
-                                for (int j = 0; j < 4; ++j) {
-                                    c.cass[j] = t_cass[j * cap + m];
-                                    c.jlcc[j] = t_jlcc[j * cap + m];
-                                }
-                                c.cajsr = t_cajsr[m];
-                                c.cajsr_lo = FP64 ? 0.f : t_cajsr_lo[m];
+                                tile_get(c, tile[m]);
                                 rng.open(a.seed, (uint32_t)cell, (uint32_t)(w.cru_begin + m), step0 + s, 0);
                                 sl.begin(c, cc);
                             } else {
@@ -603,17 +583,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
                     if (m >= 0) {
                         int err = 0;
                         if (sl.iterate(c, cc, sv, rtab, rng, dt, a.event_cap, err)) {
-                            t_lcc[m] = c.lcc;
-                            t_flags[m] = c.flags;
-#pragma unroll
-                            for (int k = 0; k < 6; ++k) t_ryr[k * cap + m] = c.ryr[k];
-#pragma unroll
-                            for (int j = 0; j < 4; ++j) {
-                                t_cass[j * cap + m] = c.cass[j];
-                                t_jlcc[j * cap + m] = c.jlcc[j];
-                            }
-                            t_cajsr[m] = c.cajsr;
-                            if (!FP64) t_cajsr_lo[m] = c.cajsr_lo;
+                            tile_put(tile[m], c);
                             my_events += (unsigned long long)sl.ev;
                             my_err |= err;
                             acc.add(c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3], sl.jxfer_sum, sl.jtr,
@@ -624,8 +594,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
                 }
                 // Records of this step, from the warp's part of the tile (now at the end of the step)
                 if (rec_ok && (cell == a.tr_cell || a.tr_sums != nullptr))
-                    record_pass<R>(a, w, cell, r_idx, beg, end, lane, cap, t_lcc, t_flags, t_ryr, t_cass, t_cajsr,
-                                   t_cajsr_lo);
+                    record_pass<R>(a, w, cell, r_idx, beg, end, lane, tile);
                 // Warp partial; the warp that finishes last sums the warp partials in warp order
                 // and pushes the CTA's partial to the leader.
                 const Partial pv = acc.warp_total();
@@ -707,17 +676,19 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
         const int64_t base = a.slot0[cell] + w.cru_begin;
         for (int m = (int)threadIdx.x; m < w.cru_count; m += n_ssa) {
             const int64_t gs = base + m;
-            a.lcc[gs] = t_lcc[m];
-            a.flags[gs] = t_flags[m];
+            Cru<R> c;
+            tile_get(c, tile[m]);
+            a.lcc[gs] = c.lcc;
+            a.flags[gs] = c.flags;
 #pragma unroll
-            for (int k = 0; k < 6; ++k) a.ryr[k * a.n_slots + gs] = t_ryr[k * cap + m];
+            for (int k = 0; k < 6; ++k) a.ryr[k * a.n_slots + gs] = c.ryr[k];
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                g_cass[j * a.n_slots + gs] = t_cass[j * cap + m];
-                g_jlcc[j * a.n_slots + gs] = t_jlcc[j * cap + m];
+                g_cass[j * a.n_slots + gs] = c.cass[j];
+                g_jlcc[j * a.n_slots + gs] = c.jlcc[j];
             }
-            g_cajsr[gs] = t_cajsr[m];
-            if (!FP64) a.cajsr_lo[gs] = t_cajsr_lo[m];
+            g_cajsr[gs] = c.cajsr;
+            if (!FP64) a.cajsr_lo[gs] = c.cajsr_lo;
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {

@@ -229,6 +229,59 @@ struct Cru {
     float cajsr_lo;   // FP32: compensation term of CaJSR
 };
 
+// Shared-memory tile record of one CRU: the Cru fields in 16-byte words, so that a lane moves its
+// CRU with 5 (FP32) or 7 (FP64) 16-byte accesses instead of 18 scalar ones (the SSA warps' share
+// of the shared-memory pipe, which the global step's shuffles and loads also queue on).
+//   words 0-1: lcc, flags, ryr[0..5]
+//   FP32: 2 cass[0..3], 3 jlcc[0..3], 4 {cajsr, cajsr_lo, 0, 0}
+//   FP64: 2-3 cass (lo, hi word pairs), 4-5 jlcc, 6 {cajsr lo, hi, cajsr_lo, 0}
+template <typename R>
+struct alignas(16) TileRec {
+    uint4 w[sizeof(R) == 8 ? 7 : 5];
+};
+
+__device__ __forceinline__ void tile_get(Cru<float> &c, const TileRec<float> &t) {
+    const uint4 a = t.w[0], b = t.w[1], d = t.w[2], e = t.w[3], f = t.w[4];
+    c.lcc = a.x; c.flags = a.y; c.ryr[0] = a.z; c.ryr[1] = a.w;
+    c.ryr[2] = b.x; c.ryr[3] = b.y; c.ryr[4] = b.z; c.ryr[5] = b.w;
+    c.cass[0] = __uint_as_float(d.x); c.cass[1] = __uint_as_float(d.y);
+    c.cass[2] = __uint_as_float(d.z); c.cass[3] = __uint_as_float(d.w);
+    c.jlcc[0] = __uint_as_float(e.x); c.jlcc[1] = __uint_as_float(e.y);
+    c.jlcc[2] = __uint_as_float(e.z); c.jlcc[3] = __uint_as_float(e.w);
+    c.cajsr = __uint_as_float(f.x); c.cajsr_lo = __uint_as_float(f.y);
+}
+__device__ __forceinline__ void tile_put(TileRec<float> &t, const Cru<float> &c) {
+    t.w[0] = make_uint4(c.lcc, c.flags, c.ryr[0], c.ryr[1]);
+    t.w[1] = make_uint4(c.ryr[2], c.ryr[3], c.ryr[4], c.ryr[5]);
+    t.w[2] = make_uint4(__float_as_uint(c.cass[0]), __float_as_uint(c.cass[1]), __float_as_uint(c.cass[2]),
+                        __float_as_uint(c.cass[3]));
+    t.w[3] = make_uint4(__float_as_uint(c.jlcc[0]), __float_as_uint(c.jlcc[1]), __float_as_uint(c.jlcc[2]),
+                        __float_as_uint(c.jlcc[3]));
+    t.w[4] = make_uint4(__float_as_uint(c.cajsr), __float_as_uint(c.cajsr_lo), 0u, 0u);
+}
+__device__ __forceinline__ double dbl_of(uint32_t lo, uint32_t hi) { return __hiloint2double((int)hi, (int)lo); }
+__device__ __forceinline__ uint32_t lo_of(double x) { return (uint32_t)__double2loint(x); }
+__device__ __forceinline__ uint32_t hi_of(double x) { return (uint32_t)__double2hiint(x); }
+__device__ __forceinline__ void tile_get(Cru<double> &c, const TileRec<double> &t) {
+    const uint4 a = t.w[0], b = t.w[1], d0 = t.w[2], d1 = t.w[3], e0 = t.w[4], e1 = t.w[5], f = t.w[6];
+    c.lcc = a.x; c.flags = a.y; c.ryr[0] = a.z; c.ryr[1] = a.w;
+    c.ryr[2] = b.x; c.ryr[3] = b.y; c.ryr[4] = b.z; c.ryr[5] = b.w;
+    c.cass[0] = dbl_of(d0.x, d0.y); c.cass[1] = dbl_of(d0.z, d0.w);
+    c.cass[2] = dbl_of(d1.x, d1.y); c.cass[3] = dbl_of(d1.z, d1.w);
+    c.jlcc[0] = dbl_of(e0.x, e0.y); c.jlcc[1] = dbl_of(e0.z, e0.w);
+    c.jlcc[2] = dbl_of(e1.x, e1.y); c.jlcc[3] = dbl_of(e1.z, e1.w);
+    c.cajsr = dbl_of(f.x, f.y); c.cajsr_lo = __uint_as_float(f.z);
+}
+__device__ __forceinline__ void tile_put(TileRec<double> &t, const Cru<double> &c) {
+    t.w[0] = make_uint4(c.lcc, c.flags, c.ryr[0], c.ryr[1]);
+    t.w[1] = make_uint4(c.ryr[2], c.ryr[3], c.ryr[4], c.ryr[5]);
+    t.w[2] = make_uint4(lo_of(c.cass[0]), hi_of(c.cass[0]), lo_of(c.cass[1]), hi_of(c.cass[1]));
+    t.w[3] = make_uint4(lo_of(c.cass[2]), hi_of(c.cass[2]), lo_of(c.cass[3]), hi_of(c.cass[3]));
+    t.w[4] = make_uint4(lo_of(c.jlcc[0]), hi_of(c.jlcc[0]), lo_of(c.jlcc[1]), hi_of(c.jlcc[1]));
+    t.w[5] = make_uint4(lo_of(c.jlcc[2]), hi_of(c.jlcc[2]), lo_of(c.jlcc[3]), hi_of(c.jlcc[3]));
+    t.w[6] = make_uint4(lo_of(c.cajsr), hi_of(c.cajsr), __float_as_uint(c.cajsr_lo), 0u);
+}
+
 __device__ __forceinline__ int byte_s(uint32_t w, int j) { return (int)(int8_t)(w >> (8 * j)); }
 __device__ __forceinline__ int byte_u(uint32_t w, int j) { return (int)((w >> (8 * j)) & 0xFFu); }
 __device__ __forceinline__ uint32_t byte_set(uint32_t w, int j, int v) {
@@ -429,12 +482,6 @@ __device__ __forceinline__ void resplit_pair(uint32_t &a, uint32_t &b, int j, R 
     }
 }
 
-struct CruOut {
-    float jxfer, jtr;   // FP32 path
-    double jxfer_d, jtr_d;
-    int events;
-    int err;
-};
 
 // One CRU over one global step: SSA_single_CRU (SSA.tpp:286-310) with the reference's draw order.
 // The jump draw comes first; then update_CaSS's binomial re-splits (sample_RyR56/34), then the
