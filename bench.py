@@ -236,7 +236,8 @@ def main():
     e.close()
     if rank == 0 and not args.no_extras:
         line["e2e"] = e2e_measure(span, K)
-        line["paths"] = {"plain_gpu": plain_measure(local_rank), "batched_gpu": batched_measure(local_rank)}
+        line["paths"] = {"plain_gpu": plain_measure(local_rank), "batched_gpu": batched_measure(local_rank),
+                         "large_ensemble_gpu": large_measure(local_rank)}
         line["accuracy"] = accuracy_vs_fp64(local_rank)
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
         line["paths"]["cpu"] = {"cru_steps_per_s": line["cpu_baseline"]["value"],
@@ -291,7 +292,7 @@ def batched_config(seed=3, n_cells=256):
     return ncru, params, cl
 
 
-def batched_measure(device, steps=2000, cluster_ctas=8):
+def batched_measure(device, steps=2000, cluster_ctas="auto"):
     from gwgb300 import Ensemble
 
     ncru, params, cl = batched_config()
@@ -310,6 +311,7 @@ def batched_measure(device, steps=2000, cluster_ctas=8):
     total = int(ncru.sum()) * steps
     return {"cru_steps_per_s": total / kern, "sim_ms_per_wall_s": len(ncru) * steps * DT / kern,
             "wall_cru_steps_per_s": total / wall, "cells": len(ncru), "crus": int(ncru.sum()),
+            "autotuned": cluster_ctas == "auto",
             "launch_shape": {k: st1[k] for k in ("cluster_ctas", "cta_crus", "threads_per_cta", "n_clusters")},
             "workload": f"{len(ncru)} cells, 2,000-12,500 CRUs, log-normal(0.1) PCaL/GKr/GKs/Vmax/rRyR, "
                         f"CL 400-1000 ms, {steps} steps"}
@@ -344,6 +346,43 @@ def accuracy_vs_fp64(device, cells=64, ncru=200, t_ms=200.0):
         res["ks_pvalue"][k] = float(ks_2samp(a, b).pvalue)
         res["rel_diff_of_means"][k] = float(abs(a.mean() - b.mean()) / max(abs(b.mean()), 1e-30))
     return res
+
+
+def large_measure(device, cells=1024, ncru=12500, steps=1000):
+    """Large ensemble: 1,024 cells of 12,500 CRUs (12.8M CRUs), per-cell PCaL, GKr, GKs,
+    Vmaxf = Vmaxr and rRyR scaled by log-normal(sigma 0.15) factors, 2 Hz pacing (CL 500 ms)."""
+    import numpy as np
+
+    from gwgb300 import Ensemble, _lib
+
+    rng = np.random.default_rng(5)
+    params = []
+    for _ in range(cells):
+        p = _lib.default_params()
+        f = rng.lognormal(0.0, 0.15, size=5)
+        p.PCaL *= f[0]
+        p.GKr *= f[1]
+        p.GKs *= f[2]
+        p.Vmaxf *= f[3]
+        p.Vmaxr *= f[3]
+        p.rRyR *= f[4]
+        params.append(p)
+    e = Ensemble([ncru] * cells, params, precision="fp32", seed=17, device=device, cluster_ctas="auto",
+                 tune_steps=100)
+    for c in range(cells):
+        e.sample_initial_crus(c)
+    e.set_pulse(0.0, 500.0, STIM_DUR, STIM_AMP)
+    e.run(DT, 200)
+    st0 = e.stats()
+    e.run(DT, steps)
+    st1 = e.stats()
+    e.close()
+    kern = (st1["kernel_ms"] - st0["kernel_ms"]) / 1e3
+    total = cells * ncru * steps
+    return {"cru_steps_per_s": total / kern, "sim_ms_per_wall_s": cells * steps * DT / kern,
+            "algorithmic_GBps": total * BYTES_PER_CRU_STEP / kern / 1e9, "cells": cells, "crus": cells * ncru,
+            "launch_shape": {k: st1[k] for k in ("cluster_ctas", "cta_crus", "threads_per_cta", "n_clusters")},
+            "workload": f"{cells} cells x {ncru} CRUs, log-normal(0.15) PCaL/GKr/GKs/Vmax/rRyR, CL 500 ms, {steps} steps"}
 
 
 def e2e_measure(span, K):

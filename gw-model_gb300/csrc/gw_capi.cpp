@@ -540,6 +540,40 @@ int gw_destroy(gw_ctx *c) {
     return GW_OK;
 }
 
+int gw_autotune(const gw_ensemble_desc *d, int trial_steps, int *best_cluster_ctas, double *best_us_per_step) {
+    if (!d || !best_cluster_ctas || trial_steps <= 0)
+        return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "gw_autotune: null descriptor/output or trial_steps <= 0");
+    static const int kCandidates[] = {16, 8, 4, 2, 1};
+    const int warm = std::max(20, trial_steps / 4);
+    int best = 0;
+    double best_us = 0.0;
+    for (int C : kCandidates) {
+        gw_ensemble_desc t = *d;
+        t.cluster_ctas = C;
+        t.cta_crus = 0;
+        gw_ctx *c = nullptr;
+        int rc = gw_create(&t, &c);
+        if (rc == GW_ERR_UNSUPPORTED) continue;  // this cluster size does not fit the cells
+        if (rc) return rc;
+        rc = gw_set_stimulus_pulse(c, -1, 0.0, 1000.0, 0.5, 100.0);
+        if (!rc) rc = gw_run(c, 1e-3, warm, 0, nullptr);
+        const double ms0 = c->stats.kernel_ms;
+        if (!rc) rc = gw_run(c, 1e-3, trial_steps, 0, nullptr);
+        const double us = (c->stats.kernel_ms - ms0) * 1e3 / trial_steps;
+        if (rc) g_create_error = c->err;
+        gw_destroy(c);
+        if (rc) return rc;
+        if (best == 0 || us < best_us) {
+            best = C;
+            best_us = us;
+        }
+    }
+    if (best == 0) return fail(nullptr, GW_ERR_UNSUPPORTED, "gw_autotune: no cluster size fits these cells");
+    *best_cluster_ctas = best;
+    if (best_us_per_step) *best_us_per_step = best_us;
+    return GW_OK;
+}
+
 int gw_sample_initial_crus(gw_ctx *c, int cell) {
     int rc = check_cell(c, cell);
     if (rc) return rc;

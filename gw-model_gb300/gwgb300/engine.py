@@ -91,8 +91,10 @@ class Ensemble:
     """An ensemble of cells on one device (gw_create / gw_run)."""
 
     def __init__(self, ncru: Sequence[int], params=None, *, precision: str = "fp32", seed: int = 0,
-                 device: int = 0, event_cap: int = 0, cluster_ctas: int = 0, cta_crus: int = 0,
-                 steps_per_launch: int = 0, ode_fp32_rhs: bool = False):
+                 device: int = 0, event_cap: int = 0, cluster_ctas=0, cta_crus: int = 0,
+                 steps_per_launch: int = 0, ode_fp32_rhs: bool = False, tune_steps: int = 200):
+        """cluster_ctas: CTAs per cluster, 0 for the size rule, or "auto" to measure the fastest
+        shape for these cells first (gw_autotune, tune_steps trial steps per candidate)."""
         self.L = _lib.load()
         self.ncru = np.ascontiguousarray(ncru, dtype=np.int32)
         self.n_cells = int(self.ncru.size)
@@ -117,7 +119,13 @@ class Ensemble:
         d.seed = seed & 0xFFFFFFFFFFFFFFFF
         d.device = device
         d.event_cap = event_cap
-        d.cluster_ctas = cluster_ctas
+        self.tuned_us_per_step = None
+        if cluster_ctas == "auto":
+            best, us = C.c_int(), C.c_double()
+            check(self.L.gw_autotune(C.byref(d), int(tune_steps), C.byref(best), C.byref(us)))
+            cluster_ctas, cta_crus = best.value, 0
+            self.tuned_us_per_step = us.value
+        d.cluster_ctas = int(cluster_ctas)
         d.cta_crus = cta_crus
         d.steps_per_launch = steps_per_launch
         d.ode_fp32_rhs = 1 if ode_fp32_rhs else 0

@@ -84,8 +84,10 @@ typedef struct gw_ensemble_desc {
     uint64_t seed;
     int device;               /* CUDA device ordinal */
     int event_cap;            /* max jumps per CRU per step; 0 -> 65536 */
-    int cluster_ctas;         /* CTAs per thread-block cluster; 0 -> autotuned */
-    int cta_crus;             /* CRU capacity of one CTA; 0 -> autotuned */
+    int cluster_ctas;         /* CTAs per thread-block cluster; 0 -> the smallest power of two that
+                                 keeps a cell's CTAs at <= 384 CRUs, at most 16 (gw_autotune
+                                 measures the best choice instead) */
+    int cta_crus;             /* CRU capacity of one CTA; 0 -> derived from cluster_ctas */
     int steps_per_launch;     /* global steps fused in one launch; 0 -> 1000 */
     int ode_fp32_rhs;         /* GW_PRECISION_FP32 only: 1 evaluates the global right-hand side in
                                  FP32 (state and Euler update stay FP64); 0 (default) keeps it FP64 */
@@ -158,6 +160,14 @@ void gw_globals_py_default(gw_globals *g);
  * flux carry (sum Jtr, sum Jxfer) that the reference's ctor computes (GW.hpp:73-74). */
 int gw_create(const gw_ensemble_desc *desc, gw_ctx **out);
 int gw_destroy(gw_ctx *ctx);
+/* No counterpart in the reference (it has one CPU code path).  Measures the launch shape for an
+ * ensemble: for each cluster size in {16, 8, 4, 2, 1} that fits (shared memory per CTA), builds a
+ * throwaway context from *desc (its cluster_ctas and cta_crus are ignored), paces it at 1 Hz and
+ * times trial_steps global steps after a short warm-up; returns the fastest cluster size and its
+ * device time per global step.  Set desc->cluster_ctas to the result before gw_create.  The
+ * contexts it builds draw their own initial states; no caller state is touched. */
+int gw_autotune(const gw_ensemble_desc *desc, int trial_steps, int *best_cluster_ctas,
+                double *best_us_per_step);
 
 /* Replaces GW_model::set_initial_value (GW.tpp:6-10) for one cell.  JLCC may be NULL: the
  * reference then keeps the ctor's JLCC, which is zero (GW.hpp:107-112). */
