@@ -95,6 +95,9 @@ __device__ __forceinline__ bool finite_bits(double x) {
 __device__ __forceinline__ void cluster_arrive() {
     asm volatile("barrier.cluster.arrive.release;" ::: "memory");
 }
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+    asm volatile("barrier.cluster.arrive.relaxed;" ::: "memory");
+}
 __device__ __forceinline__ void cluster_wait() {
     asm volatile("barrier.cluster.wait.acquire;" ::: "memory");
 }
@@ -419,77 +422,80 @@ struct FluxAcc {
     }
 };
 
+// A CTA's view of its work item and of the shared-memory layout, rebuilt from the kernel
+// arguments by each of the kernel's parts.
 template <bool FP64, bool ODE64>
-__global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs a) {
+struct CtaView {
     using R = typename std::conditional<FP64, double, float>::type;
     using T = typename std::conditional<ODE64, double, float>::type;
-    constexpr bool EXACT = FP64;
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int nw = a.ssa_warps;  // SSA warps of a leader CTA; the other CTAs have nw + kOdeWarps
-    const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
-    const int ot = (int)threadIdx.x - nw * 32;  // ODE thread index 0 .. kOdeLanes-1
-    const CtaWork w = a.work[blockIdx.x];
-    const bool active = w.cell >= 0;
-    const bool leader = active && w.rank_in_cell == 0;
-    const bool ode_thread = leader && warp >= nw;
-    const int n_ssa = (leader ? nw : nw + kOdeWarps) * 32;  // SSA threads of this CTA
-    const SmemLayout L = smem_layout<R, T>(a.tile_cap, a.max_cta_cell);
-    SsaConsts<R> &cc = *reinterpret_cast<SsaConsts<R> *>(smem + L.cc);
-    R *svbuf = reinterpret_cast<R *>(smem + L.sv);
-    OdeShared &os = *reinterpret_cast<OdeShared *>(smem + L.ode);
-    OdeProgram &P = *reinterpret_cast<OdeProgram *>(smem + L.prog);
-    T *X = reinterpret_cast<T *>(smem + L.x);
-    math64::Tables &M = *reinterpret_cast<math64::Tables *>(smem + L.math);
-    void *svstage = smem + L.svs;
-    Partial *part = reinterpret_cast<Partial *>(smem + L.part);
-    Partial *chunkp = reinterpret_cast<Partial *>(smem + L.chunk);  // warp partials
-    float2 *rtab = reinterpret_cast<float2 *>(smem + L.rtab) + warp * kRateTab;  // this warp's table
-    int *ctr = reinterpret_cast<int *>(smem + L.ctr);
-    TileRec<R> *tile = reinterpret_cast<TileRec<R> *>(smem + L.tile);
-    const int cell = w.cell;
-    const int pslot = a.max_cta_cell;  // partial entries per parity slot
-    R *g_cass = reinterpret_cast<R *>(a.cass);
-    R *g_jlcc = reinterpret_cast<R *>(a.jlcc);
-    R *g_cajsr = reinterpret_cast<R *>(a.cajsr);
+    CtaWork w;
+    int nw, warp, lane, ot, n_ssa;
+    bool active, leader, ode_thread;
+    SsaConsts<R> *cc;
+    R *svbuf;
+    OdeShared *os;
+    OdeProgram *P;
+    T *X;
+    math64::Tables *M;
+    void *svstage;
+    Partial *part, *chunkp;
+    float2 *rtab;
+    int *ctr;
+    TileRec<R> *tile;
 
-    uint64_t step0 = 0;
-    if (active) {
-        if (threadIdx.x == 0) {
-            load_ssa_consts<R>(cc, a.cs[cell]);
-            ctr[0] = ctr[1] = ctr[2] = ctr[3] = 0;
-        }
-        step0 = a.dyn[cell].step;
-        if (!ode_thread) {
-            const int64_t base = a.slot0[cell] + w.cru_begin;
-            for (int m = (int)threadIdx.x; m < w.cru_count; m += n_ssa) {
-                const int64_t gs = base + m;
-                Cru<R> c;
-                c.lcc = a.lcc[gs];
-                c.flags = a.flags[gs];
-#pragma unroll
-                for (int k = 0; k < 6; ++k) c.ryr[k] = a.ryr[k * a.n_slots + gs];
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    c.cass[j] = g_cass[j * a.n_slots + gs];
-                    c.jlcc[j] = g_jlcc[j * a.n_slots + gs];
-                }
-                c.cajsr = g_cajsr[gs];
-                c.cajsr_lo = FP64 ? 0.f : a.cajsr_lo[gs];
-                tile_put(tile[m], c);
-            }
-        }
+    __device__ __forceinline__ explicit CtaView(const KernelArgs &a) {
+        extern __shared__ __align__(16) unsigned char smem[];
+        nw = a.ssa_warps;  // SSA warps of a leader CTA; the other CTAs have nw + kOdeWarps
+        warp = (int)(threadIdx.x >> 5);
+        lane = (int)(threadIdx.x & 31);
+        ot = (int)threadIdx.x - nw * 32;  // ODE thread index 0 .. kOdeLanes-1
+        w = a.work[blockIdx.x];
+        active = w.cell >= 0;
+        leader = active && w.rank_in_cell == 0;
+        ode_thread = leader && warp >= nw;
+        n_ssa = (leader ? nw : nw + kOdeWarps) * 32;  // SSA threads of this CTA
+        const SmemLayout L = smem_layout<R, T>(a.tile_cap, a.max_cta_cell);
+        cc = reinterpret_cast<SsaConsts<R> *>(smem + L.cc);
+        svbuf = reinterpret_cast<R *>(smem + L.sv);
+        os = reinterpret_cast<OdeShared *>(smem + L.ode);
+        P = reinterpret_cast<OdeProgram *>(smem + L.prog);
+        X = reinterpret_cast<T *>(smem + L.x);
+        M = reinterpret_cast<math64::Tables *>(smem + L.math);
+        svstage = smem + L.svs;
+        part = reinterpret_cast<Partial *>(smem + L.part);
+        chunkp = reinterpret_cast<Partial *>(smem + L.chunk);  // warp partials
+        rtab = reinterpret_cast<float2 *>(smem + L.rtab) + warp * kRateTab;  // this warp's table
+        ctr = reinterpret_cast<int *>(smem + L.ctr);
+        tile = reinterpret_cast<TileRec<R> *>(smem + L.tile);
     }
-    if (leader && ode_thread) {
+};
+
+// The leader CTA's ODE warps over a launch: the transcendental phases of the initial state and
+// the push of sv[0], then per global step s the reduction of the CTA partials of step s-1, the
+// global step s -> s+1 and the push of sv[(s+1)&1], and the carry back to the cell block at the
+// end.  A function of its own (not inlined into the kernel), so that its register allocation and
+// schedule do not depend on the SSA code.
+template <bool FP64, bool ODE64>
+__device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
+    using T = typename std::conditional<ODE64, double, float>::type;
+    const CtaView<FP64, ODE64> v(a);
+    const OdeProgram &P = *v.P;
+    OdeShared &os = *v.os;
+    T *X = v.X;
+    const math64::Tables &M = *v.M;
+    const int ot = v.ot, lane = v.lane, cell = v.w.cell;
+    const int pslot = a.max_cta_cell;
+    {
         // program, constants and state of the cell
-        {
-            const int4 *src = reinterpret_cast<const int4 *>(a.prog);
-            int4 *dst = reinterpret_cast<int4 *>(&P);
-            for (int i = ot; i < (int)(sizeof(OdeProgram) / 16); i += kOdeLanes) dst[i] = src[i];
-        }
+        const int4 *src = reinterpret_cast<const int4 *>(a.prog);
+        int4 *dst = reinterpret_cast<int4 *>(v.P);
+        for (int i = ot; i < (int)(sizeof(OdeProgram) / 16); i += kOdeLanes) dst[i] = src[i];
+    }
+    {
         const CellStatic &C = a.cs[cell];
         const CellDyn &d = a.dyn[cell];
         for (int i = ot; i < kOdeMaxSlots; i += kOdeLanes) X[i] = (T)0;
-        math64::load_tables(M, ot, kOdeLanes);
+        math64::load_tables(*v.M, ot, kOdeLanes);
         ode_bar();
         if (ot == 0) {
             X[XS_ONE] = (T)1;
@@ -510,27 +516,21 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
         }
         for (int i = ot; i < kOdeConstCap; i += kOdeLanes) X[XS_FIRST_FREE + i] = (T)C.ode_consts[i];
         ode_bar();
-        // transcendental phases of the initial state, push sv[0]
+    }
+    // transcendental phases of the initial state, push sv[0]
+    {
         const int reg = v_regime(os.g[0]);
         for (int q = P.upd_phase + 1; q <= P.push_phase; ++q) {
             ode_phase<T>(P, q, reg, X, os.g, ot, &os.status, M);
             ode_bar();
         }
-        push_sv<FP64, T>(P, X, os.g, svbuf, svstage, 0, w, ot);
-    }
-    __syncthreads();
-    cluster_arrive();
-    if (leader && ode_thread) {
-        const int reg = v_regime(os.g[0]);
+        push_sv<FP64, T>(P, X, os.g, v.svbuf, v.svstage, 0, v.w, ot);
+        cluster_arrive();
         for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
             ode_phase<T>(P, q, reg, X, os.g, ot, &os.status, M);
             ode_bar();
         }
     }
-
-    const R dt = (R)a.dt;
-    unsigned long long my_events = 0;
-    int my_err = 0;
     for (int s = 0; s < a.n_steps; ++s) {
         const int par = s & 1;
         const int64_t ri = a.run_step0 + s;
@@ -538,169 +538,244 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const KernelArgs
         const int64_t r_idx = rec ? ri / a.record_every - a.rec_base : -1;
         const bool rec_ok = rec && r_idx >= 0 && r_idx < a.rec_cap;
         cluster_wait();
-        if (!ode_thread) {
-            if (active) {
-                // The counter of parity par^1 was last used in step s-1, which every warp of this
-                // CTA has left; it is next used in step s+1, after the cluster barrier.
-                if (threadIdx.x == 0) ctr[2 + (par ^ 1)] = 0;
-                const R *sv = svbuf + par * kSvCount;
-                const int nsw = n_ssa >> 5;
-                if (!FP64) {
-                    build_rate_table<R>(rtab, cc, sv, lane);
-                    __syncwarp();
-                }
-                if (w.cru_count == 0 && threadIdx.x == 0) {
-                    Partial *dst = part + par * pslot + w.rank_in_cell;
-#pragma unroll
-                    for (int v = 0; v < 4; ++v) st_remote(map_rank(&dst->v[v], (uint32_t)w.first), 0.0);
-                }
-                // This warp's CRUs [cursor, end).  A lane whose CRU has finished its step takes the
-                // next one, so lanes with pending SSA events do not hold the others back.
-                const int beg = (int)((int64_t)w.cru_count * warp / nsw);
-                const int end = (int)((int64_t)w.cru_count * (warp + 1) / nsw);
-                int cursor = beg;
-                FluxAcc<FP64> acc;
-                Cru<R> c;
-                SsaLane<R, EXACT> sl;
-                Stream rng;
-                int m = -1;  // CRU of this lane; -1 none yet, -2 none left
-                for (;;) {
-                    const unsigned need = __ballot_sync(0xffffffffu, m == -1);
-                    if (need) {
-                        const int nm = cursor + __popc(need & ((1u << lane) - 1u));
-                        cursor += __popc(need);
-                        if (m == -1) {
-                            if (nm < end) {
-                                m = nm;
-                                tile_get(c, tile[m]);
-                                rng.open(a.seed, (uint32_t)cell, (uint32_t)(w.cru_begin + m), step0 + s, 0);
-                                sl.begin(c, cc);
-                            } else {
-                                m = -2;
-                            }
-                        }
-                    }
-                    if (!__any_sync(0xffffffffu, m >= 0)) break;
-                    if (m >= 0) {
-                        int err = 0;
-                        if (sl.iterate(c, cc, sv, rtab, rng, dt, a.event_cap, err)) {
-                            tile_put(tile[m], c);
-                            my_events += (unsigned long long)sl.ev;
-                            my_err |= err;
-                            acc.add(c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3], sl.jxfer_sum, sl.jtr,
-                                    __popc((c.flags >> 4) & 0xFu));
-                            m = -1;
-                        }
-                    }
-                }
-                // Records of this step, from the warp's part of the tile (now at the end of the step)
-                if (rec_ok && (cell == a.tr_cell || a.tr_sums != nullptr))
-                    record_pass<R>(a, w, cell, r_idx, beg, end, lane, tile);
-                // Warp partial; the warp that finishes last sums the warp partials in warp order
-                // and pushes the CTA's partial to the leader.
-                const Partial pv = acc.warp_total();
-                int done = 0;
-                if (lane == 0) {
-                    chunkp[warp] = pv;
-                    __threadfence_block();
-                    done = atomicAdd(&ctr[2 + par], 1);
-                    __threadfence_block();
-                }
-                done = __shfl_sync(0xffffffffu, done, 0);
-                if (done == nsw - 1) {
-                    __syncwarp();
-                    FluxAcc<FP64> tot;
-                    if (lane < nsw) tot.add_partial(chunkp[lane]);
-                    const Partial pc = tot.warp_total();
-                    if (lane == 0) {
-                        Partial *dst = part + par * pslot + w.rank_in_cell;
-#pragma unroll
-                        for (int v = 0; v < 4; ++v) st_remote(map_rank(&dst->v[v], (uint32_t)w.first), pc.v[v]);
-                    }
-                }
-            }
-            cluster_arrive();
-        } else {
-            // leader CTA's ODE warps: fluxes of step s-1 (or the carry), then the global step
-            // s -> s+1
-            if (ot == 0 && (not_positive(os.g[1]) || not_positive(os.g[2])) && os.status == 0)
-                os.status = GW_ERR_NERNST;
-            if (s > 0) reduce_partials<FP64, T>(part + (par ^ 1) * pslot, w.n_cta_cell, ot >> 5, lane, os.sums, X);
+        // fluxes of step s-1 (or the carry), then the global step s -> s+1
+        if (ot == 0 && (not_positive(os.g[1]) || not_positive(os.g[2])) && os.status == 0)
+            os.status = GW_ERR_NERNST;
+        if (s > 0) reduce_partials<FP64, T>(v.part + (par ^ 1) * pslot, v.w.n_cta_cell, ot >> 5, lane, os.sums, X);
+        ode_bar();
+        const int reg_n = v_regime(os.g[0]);
+        for (int q = 0; q <= P.upd_phase; ++q) {
+            ode_phase<T>(P, q, reg_n, X, os.g, ot, &os.status, M);
             ode_bar();
-            const int reg_n = v_regime(os.g[0]);
-            for (int q = 0; q <= P.upd_phase; ++q) {
-                ode_phase<T>(P, q, reg_n, X, os.g, ot, &os.status, M);
-                ode_bar();
-            }
-            if (ot == 0) os.t += a.dt;
-            if (rec_ok) {
-                double *dst = a.tr_glob + ((int64_t)cell * a.rec_cap + r_idx) * kNumGlobals;
-                for (int i = ot; i < kNumGlobals; i += kOdeLanes) dst[i] = os.g[i];
-                if (ot == 0 && (cell == 0 || (a.tr_cell >= 0 && cell == a.tr_cell))) a.tr_t[r_idx] = os.t;
-            }
-            const int reg = v_regime(os.g[0]);
-            for (int q = P.upd_phase + 1; q <= P.push_phase; ++q) {
-                ode_phase<T>(P, q, reg, X, os.g, ot, &os.status, M);
-                ode_bar();
-            }
-            push_sv<FP64, T>(P, X, os.g, svbuf, svstage, par ^ 1, w, ot);
-            cluster_arrive();
-            // off the critical path: the stimulus of step s+1 (read by the first phase of the
-            // next step, after its ode_bar) and the phases the SSA does not need
-            if (ot == 0) X[XS_ISTIM] = (T)stimulus(a.dyn[cell], os.t, ri + 1);
-            for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
-                ode_phase<T>(P, q, reg, X, os.g, ot, &os.status, M);
-                ode_bar();
-            }
+        }
+        if (ot == 0) os.t += a.dt;
+        if (rec_ok) {
+            double *dst = a.tr_glob + ((int64_t)cell * a.rec_cap + r_idx) * kNumGlobals;
+            for (int i = ot; i < kNumGlobals; i += kOdeLanes) dst[i] = os.g[i];
+            if (ot == 0 && (cell == 0 || (a.tr_cell >= 0 && cell == a.tr_cell))) a.tr_t[r_idx] = os.t;
+        }
+        const int reg = v_regime(os.g[0]);
+        for (int q = P.upd_phase + 1; q <= P.push_phase; ++q) {
+            ode_phase<T>(P, q, reg, X, os.g, ot, &os.status, M);
+            ode_bar();
+        }
+        push_sv<FP64, T>(P, X, os.g, v.svbuf, v.svstage, par ^ 1, v.w, ot);
+        cluster_arrive();
+        // off the critical path: the stimulus of step s+1 (read by the first phase of the next
+        // step, after its ode_bar) and the phases the SSA does not need
+        if (ot == 0) X[XS_ISTIM] = (T)stimulus(a.dyn[cell], os.t, ri + 1);
+        for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
+            ode_phase<T>(P, q, reg, X, os.g, ot, &os.status, M);
+            ode_bar();
         }
     }
     cluster_wait();
+    // carry of the last step's fluxes, globals and counters back to the cell block
+    if (a.n_steps > 0)
+        reduce_partials<FP64, T>(v.part + ((a.n_steps - 1) & 1) * pslot, v.w.n_cta_cell, ot >> 5, lane, os.sums, X);
+    ode_bar();
+    CellDyn &d = a.dyn[cell];
+    for (int i = ot; i < kNumGlobals; i += kOdeLanes) d.g[i] = os.g[i];
+    if (ot == 0) {
+        d.sum_jlcc = os.sums[0];
+        d.sum_clch = os.sums[1];
+        d.sum_jtr = os.sums[2];
+        d.sum_jxfer = os.sums[3];
+        d.t = os.t;
+        d.step = step0 + (uint64_t)a.n_steps;
+        if (os.status != 0) atomicCAS(&a.status[cell], 0, os.status);
+    }
+}
 
-    // Epilogue: carry of the last step's fluxes, globals and counters back to the cell block.
-    if (leader && ode_thread) {
-        if (a.n_steps > 0)
-            reduce_partials<FP64, T>(part + ((a.n_steps - 1) & 1) * pslot, w.n_cta_cell, ot >> 5, lane, os.sums, X);
-        ode_bar();
-        CellDyn &d = a.dyn[cell];
-        for (int i = ot; i < kNumGlobals; i += kOdeLanes) d.g[i] = os.g[i];
-        if (ot == 0) {
-            d.sum_jlcc = os.sums[0];
-            d.sum_clch = os.sums[1];
-            d.sum_jtr = os.sums[2];
-            d.sum_jxfer = os.sums[3];
-            d.t = os.t;
-            d.step = step0 + (uint64_t)a.n_steps;
-            if (os.status != 0) atomicCAS(&a.status[cell], 0, os.status);
-        }
-    }
-    if (active && !ode_thread) {
-        const int64_t base = a.slot0[cell] + w.cru_begin;
-        for (int m = (int)threadIdx.x; m < w.cru_count; m += n_ssa) {
-            const int64_t gs = base + m;
-            Cru<R> c;
-            tile_get(c, tile[m]);
-            a.lcc[gs] = c.lcc;
-            a.flags[gs] = c.flags;
-#pragma unroll
-            for (int k = 0; k < 6; ++k) a.ryr[k * a.n_slots + gs] = c.ryr[k];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                g_cass[j * a.n_slots + gs] = c.cass[j];
-                g_jlcc[j * a.n_slots + gs] = c.jlcc[j];
+// The SSA warps over a launch (every warp of a CTA that is not a leader's ODE warp, and every
+// warp of an idle CTA, which only keeps the cluster barriers): per global step the SSA of the
+// warp's CRUs, the record pass and the flux partials, and the tile back to the cell's planes at
+// the end.  Inlined into the kernel (out of line it spills).
+template <bool FP64, bool ODE64>
+__device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
+    using R = typename std::conditional<FP64, double, float>::type;
+    constexpr bool EXACT = FP64;
+    const CtaView<FP64, ODE64> v(a);
+    const CtaWork &w = v.w;
+    const int warp = v.warp, lane = v.lane, cell = w.cell, n_ssa = v.n_ssa;
+    const SsaConsts<R> &cc = *v.cc;
+    TileRec<R> *tile = v.tile;
+    int *ctr = v.ctr;
+    const int pslot = a.max_cta_cell;
+    const R dt = (R)a.dt;
+    unsigned long long my_events = 0;
+    int my_err = 0;
+    cluster_arrive();
+    for (int s = 0; s < a.n_steps; ++s) {
+        const int par = s & 1;
+        const int64_t ri = a.run_step0 + s;
+        const bool rec = a.record_every > 0 && (ri % a.record_every) == 0;
+        const int64_t r_idx = rec ? ri / a.record_every - a.rec_base : -1;
+        const bool rec_ok = rec && r_idx >= 0 && r_idx < a.rec_cap;
+        cluster_wait();
+        if (v.active) {
+            // The counter of parity par^1 was last used in step s-1, which every warp of this
+            // CTA has left; it is next used in step s+1, after the cluster barrier.
+            if (threadIdx.x == 0) ctr[2 + (par ^ 1)] = 0;
+            const R *sv = v.svbuf + par * kSvCount;
+            const int nsw = n_ssa >> 5;
+            if (!FP64) {
+                build_rate_table<R>(v.rtab, cc, sv, lane);
+                __syncwarp();
             }
-            g_cajsr[gs] = c.cajsr;
-            if (!FP64) a.cajsr_lo[gs] = c.cajsr_lo;
-        }
+            if (w.cru_count == 0 && threadIdx.x == 0) {
+                Partial *dst = v.part + par * pslot + w.rank_in_cell;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            my_events += __shfl_xor_sync(0xffffffffu, my_events, o);
-            my_err |= __shfl_xor_sync(0xffffffffu, my_err, o);
+                for (int q = 0; q < 4; ++q) st_remote(map_rank(&dst->v[q], (uint32_t)w.first), 0.0);
+            }
+            // This warp's CRUs [cursor, end).  A lane whose CRU has finished its step takes the
+            // next one, so lanes with pending SSA events do not hold the others back.
+            const int beg = (int)((int64_t)w.cru_count * warp / nsw);
+            const int end = (int)((int64_t)w.cru_count * (warp + 1) / nsw);
+            int cursor = beg;
+            FluxAcc<FP64> acc;
+            Cru<R> c;
+            SsaLane<R, EXACT> sl;
+            Stream rng;
+            int m = -1;  // CRU of this lane; -1 none yet, -2 none left
+            for (;;) {
+                const unsigned need = __ballot_sync(0xffffffffu, m == -1);
+                if (need) {
+                    const int nm = cursor + __popc(need & ((1u << lane) - 1u));
+                    cursor += __popc(need);
+                    if (m == -1) {
+                        if (nm < end) {
+                            m = nm;
+                            tile_get(c, tile[m]);
+                            rng.open(a.seed, (uint32_t)cell, (uint32_t)(w.cru_begin + m), step0 + s, 0);
+                            sl.begin(c, cc);
+                        } else {
+                            m = -2;
+                        }
+                    }
+                }
+                if (!__any_sync(0xffffffffu, m >= 0)) break;
+                if (m >= 0) {
+                    int err = 0;
+                    if (sl.iterate(c, cc, sv, v.rtab, rng, dt, a.event_cap, err)) {
+                        tile_put(tile[m], c);
+                        my_events += (unsigned long long)sl.ev;
+                        my_err |= err;
+                        acc.add(c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3], sl.jxfer_sum, sl.jtr,
+                                __popc((c.flags >> 4) & 0xFu));
+                        m = -1;
+                    }
+                }
+            }
+            // Records of this step, from the warp's part of the tile (now at the end of the step)
+            if (rec_ok && (cell == a.tr_cell || a.tr_sums != nullptr))
+                record_pass<R>(a, w, cell, r_idx, beg, end, lane, tile);
+            // Warp partial; the warp that finishes last sums the warp partials in warp order
+            // and pushes the CTA's partial to the leader.
+            const Partial pv = acc.warp_total();
+            int done = 0;
+            if (lane == 0) {
+                v.chunkp[warp] = pv;
+                __threadfence_block();
+                done = atomicAdd(&ctr[2 + par], 1);
+                __threadfence_block();
+            }
+            done = __shfl_sync(0xffffffffu, done, 0);
+            if (done == nsw - 1) {
+                __syncwarp();
+                FluxAcc<FP64> tot;
+                if (lane < nsw) tot.add_partial(v.chunkp[lane]);
+                const Partial pc = tot.warp_total();
+                if (lane == 0) {
+                    Partial *dst = v.part + par * pslot + w.rank_in_cell;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) st_remote(map_rank(&dst->v[q], (uint32_t)w.first), pc.v[q]);
+                }
+            }
         }
-        if (lane == 0) {
-            if (my_events) atomicAdd(a.events, my_events);
-            if (my_err) atomicCAS(&a.status[cell], 0, (int)GW_ERR_EVENT_CAP);
+        cluster_arrive();
+    }
+    cluster_wait();
+    if (!v.active) return;
+    // the tile back to the cell's planes
+    R *g_cass = reinterpret_cast<R *>(a.cass);
+    R *g_jlcc = reinterpret_cast<R *>(a.jlcc);
+    R *g_cajsr = reinterpret_cast<R *>(a.cajsr);
+    const int64_t base = a.slot0[cell] + w.cru_begin;
+    for (int m = (int)threadIdx.x; m < w.cru_count; m += n_ssa) {
+        const int64_t gs = base + m;
+        Cru<R> c;
+        tile_get(c, tile[m]);
+        a.lcc[gs] = c.lcc;
+        a.flags[gs] = c.flags;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) a.ryr[k * a.n_slots + gs] = c.ryr[k];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            g_cass[j * a.n_slots + gs] = c.cass[j];
+            g_jlcc[j * a.n_slots + gs] = c.jlcc[j];
+        }
+        g_cajsr[gs] = c.cajsr;
+        if (!FP64) a.cajsr_lo[gs] = c.cajsr_lo;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        my_events += __shfl_xor_sync(0xffffffffu, my_events, o);
+        my_err |= __shfl_xor_sync(0xffffffffu, my_err, o);
+    }
+    if (lane == 0) {
+        if (my_events) atomicAdd(a.events, my_events);
+        if (my_err) atomicCAS(&a.status[cell], 0, (int)GW_ERR_EVENT_CAP);
+    }
+}
+
+// The engine kernel: every CTA of a cluster first waits for the whole cluster to be resident (it
+// writes into the other CTAs' shared memory from its first global step on), loads its CRU tile
+// and the cell's SSA constants, then splits into the ODE warps of a leader CTA and the SSA warps.
+// Both parts keep the same sequence of cluster barriers: one arrive after the setup, then one
+// wait and one arrive per global step, and one final wait.
+template <bool FP64, bool ODE64>
+__global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const __grid_constant__ KernelArgs a) {
+    using R = typename std::conditional<FP64, double, float>::type;
+    cluster_arrive_relaxed();
+    cluster_wait();
+    const CtaView<FP64, ODE64> v(a);
+    uint64_t step0 = 0;
+    if (v.active) {
+        const int cell = v.w.cell;
+        if (threadIdx.x == 0) {
+            load_ssa_consts<R>(*v.cc, a.cs[cell]);
+            v.ctr[0] = v.ctr[1] = v.ctr[2] = v.ctr[3] = 0;
+        }
+        step0 = a.dyn[cell].step;
+        if (!v.ode_thread) {
+            R *g_cass = reinterpret_cast<R *>(a.cass);
+            R *g_jlcc = reinterpret_cast<R *>(a.jlcc);
+            R *g_cajsr = reinterpret_cast<R *>(a.cajsr);
+            const int64_t base = a.slot0[cell] + v.w.cru_begin;
+            for (int m = (int)threadIdx.x; m < v.w.cru_count; m += v.n_ssa) {
+                const int64_t gs = base + m;
+                Cru<R> c;
+                c.lcc = a.lcc[gs];
+                c.flags = a.flags[gs];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) c.ryr[k] = a.ryr[k * a.n_slots + gs];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    c.cass[j] = g_cass[j * a.n_slots + gs];
+                    c.jlcc[j] = g_jlcc[j * a.n_slots + gs];
+                }
+                c.cajsr = g_cajsr[gs];
+                c.cajsr_lo = FP64 ? 0.f : a.cajsr_lo[gs];
+                tile_put(v.tile[m], c);
+            }
         }
     }
+    __syncthreads();
+    if (v.ode_thread)
+        ode_warps<FP64, ODE64>(a, step0);
+    else
+        ssa_warps<FP64, ODE64>(a, step0);
 }
 
 // Random initial CRU state (GW_utils.tpp:5-64) from stream 1, one thread per CRU, in the same
