@@ -143,13 +143,26 @@ __device__ __forceinline__ float o_log(float x, const math64::Tables &) { return
 __device__ __forceinline__ double t_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float t_sqrt(float x) { return sqrtf(x); }
 
+// Shared-memory offsets of the global step's data, passed to ode_phase in place of pointers: the
+// function is out of line, and pointer arguments would turn every operand, program and table
+// read into a generic load; addresses formed from the shared-memory symbol inside the function
+// stay shared-memory loads.
+struct OdeOffsets {
+    uint32_t prog, x, ode, math;
+};
+
 // One phase of the lane program by the kOdeLanes ODE threads (t = 0 .. kOdeLanes-1): thread t runs
 // op t of the phase.  Every warp holds one op kind per phase (P.wkind), so the switch does not
 // diverge; lanes without an op skip the arithmetic.  Kept out of line: inlined into the engine
 // kernel's loop, its shuffle tree measured 4x slower (2.2k vs 0.5k cycles per SUM phase).
 template <typename T>
-__device__ __noinline__ void ode_phase(const OdeProgram &P, int q, int regime, T *X, double *g, int t,
-                                          int *status, const math64::Tables &M) {
+__device__ __noinline__ void ode_phase(const OdeOffsets o, int q, int regime, int t) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const OdeProgram &P = *reinterpret_cast<const OdeProgram *>(smem + o.prog);
+    T *X = reinterpret_cast<T *>(smem + o.x);
+    OdeShared &os = *reinterpret_cast<OdeShared *>(smem + o.ode);
+    double *g = os.g;
+    const math64::Tables &M = *reinterpret_cast<const math64::Tables *>(smem + o.math);
     const int wk = P.wkind[q][t >> 5];
     if (wk == OK_NOP) return;
     const int lane = t & 31;
@@ -186,7 +199,7 @@ __device__ __noinline__ void ode_phase(const OdeProgram &P, int q, int regime, T
             const double ng = g[out] + (double)GW_ARG(0);
             g[out] = ng;
             X[XS_G + out] = (T)ng;
-            if (!finite_bits(ng)) atomicCAS(status, 0, (int)GW_ERR_NONFINITE);  // first error of the cell
+            if (!finite_bits(ng)) atomicCAS(&os.status, 0, (int)GW_ERR_NONFINITE);  // first error of the cell
             return;
         }
         default: break;
@@ -242,27 +255,37 @@ __device__ __forceinline__ void reduce_partials(const Partial *slot, int n, int 
 }
 
 // Per-step SSA values of the new state to every CTA of the cell: staged in the leader's shared
-// memory by threads 0..kSvCount-1, then pushed as (value, CTA) pairs by all kOdeLanes threads.
+// memory by threads 0..kSvCount-1, then pushed in 16-byte words (CTA, word) by all kOdeLanes
+// threads.  Every staging lane takes the same conversions (FP64 -> FP32 and the FP32 remainder of
+// Cai and CaNSR): divergent FP64 conversions would run one branch after another.
 template <bool FP64, typename T>
 __device__ __forceinline__ void push_sv(const OdeProgram &P, const T *X, const double *g, void *svbuf, void *stage,
                                         int slot, const CtaWork &w, int t) {
     using R = typename std::conditional<FP64, double, float>::type;
     R *st = reinterpret_cast<R *>(stage);
     if (t < kSvCount) {
+        const bool lo_part = t == SV_CAI_LO || t == SV_CANSR_LO;
+        const int gi = (t == SV_CAI || t == SV_CAI_LO) ? 3 : ((t == SV_CANSR || t == SV_CANSR_LO) ? 4 : -1);
+        const double d = gi >= 0 ? g[gi] : (double)X[P.sv_src[t]];
         R v;
-        if (t == SV_CAI) v = (R)g[3];
-        else if (t == SV_CANSR) v = (R)g[4];
-        else if (t == SV_CAI_LO) v = FP64 ? (R)0 : (R)(g[3] - (double)(float)g[3]);
-        else if (t == SV_CANSR_LO) v = FP64 ? (R)0 : (R)(g[4] - (double)(float)g[4]);
-        else v = (R)X[P.sv_src[t]];
+        if (FP64) {
+            v = lo_part ? (R)0 : (R)d;
+        } else {
+            const float hi = (float)d;
+            const float lo = (float)(d - (double)hi);
+            v = (R)(lo_part ? lo : hi);
+        }
         st[t] = v;
     }
     ode_bar();
-    R *sv = reinterpret_cast<R *>(svbuf) + slot * kSvCount;
-    const int total = kSvCount * w.n_cta_cell;
+    constexpr int kWords = kSvCount * (int)sizeof(R) / 16;  // 16-byte words of one slot
+    static_assert(kSvCount * sizeof(R) % 16 == 0, "sv slot in 16-byte words");
+    const uint4 *src = reinterpret_cast<const uint4 *>(st);
+    uint4 *dst = reinterpret_cast<uint4 *>(reinterpret_cast<R *>(svbuf) + slot * kSvCount);
+    const int total = kWords * w.n_cta_cell;
     for (int idx = t; idx < total; idx += kOdeLanes) {
-        const int r = idx / kSvCount, i = idx - r * kSvCount;
-        st_remote(map_rank(sv + i, (uint32_t)(w.first + r)), st[i]);
+        const int r = idx / kWords, i = idx - r * kWords;
+        st_remote(map_rank(dst + i, (uint32_t)(w.first + r)), src[i]);
     }
 }
 
@@ -442,6 +465,7 @@ struct CtaView {
     float2 *rtab;
     int *ctr;
     TileRec<R> *tile;
+    OdeOffsets off;  // for ode_phase
 
     __device__ __forceinline__ explicit CtaView(const KernelArgs &a) {
         extern __shared__ __align__(16) unsigned char smem[];
@@ -467,6 +491,7 @@ struct CtaView {
         rtab = reinterpret_cast<float2 *>(smem + L.rtab) + warp * kRateTab;  // this warp's table
         ctr = reinterpret_cast<int *>(smem + L.ctr);
         tile = reinterpret_cast<TileRec<R> *>(smem + L.tile);
+        off = OdeOffsets{(uint32_t)L.prog, (uint32_t)L.x, (uint32_t)L.ode, (uint32_t)L.math};
     }
 };
 
@@ -521,13 +546,13 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
     {
         const int reg = v_regime(os.g[0]);
         for (int q = P.upd_phase + 1; q <= P.push_phase; ++q) {
-            ode_phase<T>(P, q, reg, X, os.g, ot, &os.status, M);
+            ode_phase<T>(v.off, q, reg, ot);
             ode_bar();
         }
         push_sv<FP64, T>(P, X, os.g, v.svbuf, v.svstage, 0, v.w, ot);
         cluster_arrive();
         for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
-            ode_phase<T>(P, q, reg, X, os.g, ot, &os.status, M);
+            ode_phase<T>(v.off, q, reg, ot);
             ode_bar();
         }
     }
@@ -545,7 +570,7 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
         ode_bar();
         const int reg_n = v_regime(os.g[0]);
         for (int q = 0; q <= P.upd_phase; ++q) {
-            ode_phase<T>(P, q, reg_n, X, os.g, ot, &os.status, M);
+            ode_phase<T>(v.off, q, reg_n, ot);
             ode_bar();
         }
         if (ot == 0) os.t += a.dt;
@@ -556,7 +581,7 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
         }
         const int reg = v_regime(os.g[0]);
         for (int q = P.upd_phase + 1; q <= P.push_phase; ++q) {
-            ode_phase<T>(P, q, reg, X, os.g, ot, &os.status, M);
+            ode_phase<T>(v.off, q, reg, ot);
             ode_bar();
         }
         push_sv<FP64, T>(P, X, os.g, v.svbuf, v.svstage, par ^ 1, v.w, ot);
@@ -565,7 +590,7 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
         // step, after its ode_bar) and the phases the SSA does not need
         if (ot == 0) X[XS_ISTIM] = (T)stimulus(a.dyn[cell], os.t, ri + 1);
         for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
-            ode_phase<T>(P, q, reg, X, os.g, ot, &os.status, M);
+            ode_phase<T>(v.off, q, reg, ot);
             ode_bar();
         }
     }

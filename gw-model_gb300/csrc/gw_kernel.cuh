@@ -131,12 +131,23 @@ __device__ __forceinline__ void st_remote(uint32_t addr, double v) {
 __device__ __forceinline__ void st_remote(uint32_t addr, float v) {
     asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
 }
+__device__ __forceinline__ void st_remote(uint32_t addr, uint4 v) {  // addr 16-byte aligned
+    asm volatile("st.shared::cluster.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x), "r"(v.y), "r"(v.z),
+                 "r"(v.w)
+                 : "memory");
+}
 
 // ------------------------------------------------------------------------------------------
 // Per-cell SSA constants (shared memory, in the CRU arithmetic type).
 // ------------------------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t lcc_table(int s);
 __device__ __forceinline__ int lcc_next(int s, int tr);
+
+// Constants of the FP32 lane's packed arithmetic (SsaConsts::pk).
+enum PackedConst {
+    PK_RISS, PK_M2, PK_RXFER, PK_RRYR, PK_BIAS, PK_K12, PK_K2325, PK_K21, PK_K34, PK_K4543, PK_K32, PK_K45K34,
+    PK_K32K43, PK_K43, PK_K5654, PK_K52, PK_K65, PK_K54, PK_K56, PK_KBSR, PK_KBSL, PK_BSR, PK_BSL, PK_COUNT
+};
 
 template <typename R>
 struct SsaConsts {
@@ -147,6 +158,7 @@ struct SsaConsts {
     R k2325, k45k34, k32k43, k4543, k5654;  // combined rate constants (FP32 subunit total)
     uint32_t lcct[16];  // LCC rate table by state (lcc_word), in shared memory: no divergent branch
     uint32_t lccn[16];  // next LCC state by state: transition t in bits 4t..4t+3
+    float2 pk[PK_COUNT];  // FP32 lane: constants duplicated into (value, value) pairs
 };
 
 template <typename R>
@@ -167,6 +179,12 @@ __device__ void load_ssa_consts(SsaConsts<R> &c, const CellStatic &s) {
     c.k32k43 = (R)(p.k32 * p.k43);
     c.k4543 = (R)(p.k45 + p.k43);
     c.k5654 = (R)(p.k56 + p.k54);
+    const float pv[PK_COUNT] = {(float)p.riss, -2.f, (float)p.rxfer, (float)p.rRyR, -8388736.f, (float)p.k12,
+                                (float)(p.k23 + p.k25), (float)p.k21, (float)p.k34, (float)(p.k45 + p.k43),
+                                (float)p.k32, (float)(p.k45 * p.k34), (float)(p.k32 * p.k43), (float)p.k43,
+                                (float)(p.k56 + p.k54), (float)p.k52, (float)p.k65, (float)p.k54, (float)p.k56,
+                                (float)p.KBSR, (float)p.KBSL, (float)s.BSR_const, (float)s.BSL_const};
+    for (int i = 0; i < PK_COUNT; ++i) c.pk[i] = make_float2(pv[i], pv[i]);
     for (int st = 0; st < 16; ++st) {
         c.lcct[st] = lcc_table(st);
         c.lccn[st] = (uint32_t)lcc_next(st, 0) | ((uint32_t)lcc_next(st, 1) << 4) | ((uint32_t)lcc_next(st, 2) << 8);
@@ -493,6 +511,118 @@ __device__ __forceinline__ void resplit_pair(uint32_t &a, uint32_t &b, int j, R 
 // SsaLane holds the loop state of one CRU's step so that a lane can run one iteration at a time
 // (the engine's SSA warps interleave CRUs: a lane whose CRU has finished its step takes the next
 // CRU while lanes with pending events continue).
+
+// Threshold crossing of update_CaSS (SSA.tpp:87-99) by subunit j from x to x_new: 1 when CaSS
+// falls through 1.15e-4 (re-split of RyR states 5/6), else 2 when it falls through 3.685e-2
+// (states 3/4), else 0.  A positive count of the pair adds its draws to D.
+template <typename R>
+__device__ __forceinline__ int crossing(const Cru<R> &s, int j, R x, R x_new, uint32_t &D) {
+    if (x > (R)1.15e-4 && x_new <= (R)1.15e-4) {
+        const int n = byte_s(s.ryr[4], j) + byte_s(s.ryr[5], j);
+        if (n > 0) D += (uint32_t)n;
+        return 1;
+    }
+    if (x > (R)0.03685 && x_new <= (R)0.03685) {
+        const int n = byte_s(s.ryr[2], j) + byte_s(s.ryr[3], j);
+        if (n > 0) D += (uint32_t)n;
+        return 2;
+    }
+    return 0;
+}
+
+// Event selection (sample_weights over subunits, sample_new_state) from the rates of the start of
+// the iteration with draws kk, kk+1, kk+2: act 1 LCC, 2 inactivation toggle, 3 RyR, 4 ClCh
+// toggle; aj the subunit, atr the transition.
+template <typename R, bool EXACT>
+__device__ __forceinline__ void select_event(const Cru<R> &s, const SsaConsts<R> &c, const R *sv, const R (&sub)[4],
+                                             R total, Stream &rng, uint32_t &kk, int &act, int &aj, int &atr) {
+    const R us = rng.uniform<R>(kk++) * total;
+    aj = scan_weights<R, 4, !EXACT>(sub, us);
+    Rates<R> r;
+    const R sr = subunit_rates<R>(s, aj, pick4(s.cass, aj), c, sv, r);
+    const R subr = EXACT ? pick4(sub, aj) : sr;
+    const R sum_lcc = r.lcc[0] + r.lcc[1] + r.lcc[2];
+    R sum_ryr;
+    if (EXACT) {
+        sum_ryr = subr - (sum_lcc + r.inact + r.clch);
+    } else {
+        sum_ryr = (R)0;
+#pragma unroll
+        for (int q = 0; q < 12; ++q) sum_ryr += r.ryr[q];
+    }
+    const R u = rng.uniform<R>(kk++) * subr;
+    if (u < sum_lcc) {
+        act = 1;
+        atr = scan_weights<R, 3, !EXACT>(r.lcc, rng.uniform<R>(kk++) * sum_lcc);
+    } else if (u < (sum_lcc + r.inact)) {
+        act = 2;
+    } else if (u < (sum_lcc + r.inact + sum_ryr)) {
+        act = 3;
+        atr = scan_weights<R, 12, !EXACT>(r.ryr, rng.uniform<R>(kk++) * sum_ryr);
+    } else {
+        act = 4;
+    }
+}
+
+// update_CaSS's second pass: binomial re-splits (sample_RyR56/34, SSA.tpp:59-84) of the subunits
+// that crossed a threshold, with draws k+1 .. k+D; s.cass still holds the values before the update.
+template <typename R>
+__device__ __forceinline__ void resplit_crossed(Cru<R> &s, const SsaConsts<R> &c, const int (&kind)[4], Stream &rng,
+                                                uint32_t k) {
+    uint32_t kr = k + 1u;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (kind[j] == 0) continue;
+        const R x = s.cass[j];
+        if (kind[j] == 1)
+            resplit_pair<R>(s.ryr[4], s.ryr[5], j, c.k65 / (c.k65 + c.k56 * (x * x)), rng, kr);
+        else
+            resplit_pair<R>(s.ryr[2], s.ryr[3], j, c.k43 / (c.k43 + c.k34 * (x * x)), rng, kr);
+    }
+}
+
+// The transition (sample_new_state, SSA.tpp:262-283) applied to the updated state, with the JLCC
+// and Jrel updates of sample_LCC and sample_RyR.
+template <typename R>
+__device__ __forceinline__ void apply_event(Cru<R> &s, const SsaConsts<R> &c, const R *sv, int act, int aj, int atr,
+                                            R (&jrel)[4]) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (j != aj) continue;
+        if (act == 1) {
+            const int from = byte_u(s.lcc, j);
+            if (from >= 1 && from <= 12) {
+                const int to = (int)((c.lccn[from] >> (4 * atr)) & 0xFu);
+                s.lcc = byte_set(s.lcc, j, to);
+                const bool inact1 = ((s.flags >> j) & 1u) != 0u;
+                if ((from == 5 && to == 6) || (from == 11 && to == 12))
+                    s.jlcc[j] = inact1 ? sv[SV_JMUL] * (c.Cao_scaled - sv[SV_JEXP] * s.cass[j]) : (R)0;
+                else if (from == 6 || from == 12)
+                    s.jlcc[j] = (R)0;
+            }
+        } else if (act == 2) {
+            s.flags ^= (1u << j);
+            const int st = byte_u(s.lcc, j);
+            if (((s.flags >> j) & 1u) == 0u)
+                s.jlcc[j] = (R)0;
+            else if (st == 6 || st == 12)
+                s.jlcc[j] = sv[SV_JMUL] * (c.Cao_scaled - sv[SV_JEXP] * s.cass[j]);
+        } else if (act == 3) {
+            int from, to;
+            ryr_move(atr, from, to);
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                if (q == from) s.ryr[q] = byte_add(s.ryr[q], j, -1);
+                if (q == to) s.ryr[q] = byte_add(s.ryr[q], j, +1);
+            }
+            const R open = (R)(byte_s(s.ryr[2], j) + byte_s(s.ryr[3], j));
+            jrel[j] = c.rRyR * open * (s.cajsr - s.cass[j]);
+        } else {
+            s.flags ^= (1u << (4 + j));
+        }
+    }
+}
+
 template <typename R, bool EXACT>
 struct SsaLane {
     R t;          // time reached within the global step
@@ -577,67 +707,18 @@ struct SsaLane {
             }
             const R d = h * (s.jlcc[j] + jrel[j] - jxfer[j] + jiss[j]) * beta;
             tmp[j] = x + d;
-            kind[j] = 0;
-            if (x > (R)1.15e-4 && tmp[j] <= (R)1.15e-4) {
-                kind[j] = 1;
-                const int n = byte_s(s.ryr[4], j) + byte_s(s.ryr[5], j);
-                if (n > 0) D += (uint32_t)n;
-            } else if (x > (R)0.03685 && tmp[j] <= (R)0.03685) {
-                kind[j] = 2;
-                const int n = byte_s(s.ryr[2], j) + byte_s(s.ryr[3], j);
-                if (n > 0) D += (uint32_t)n;
-            }
+            kind[j] = crossing<R>(s, j, x, tmp[j], D);
         }
 
-        // Event selection (sample_weights over subunits, sample_new_state) from the rates of the
-        // start of this iteration, with draws k+D+1, k+D+2, k+D+3.
+        // Event selection from the rates of the start of this iteration, draws k+D+1, k+D+2, k+D+3.
         uint32_t kk = k + 1u + D;
-        int act = 0;      // 0 none, 1 LCC, 2 inactivation toggle, 3 RyR, 4 ClCh toggle
-        int aj = 0, atr = 0;
+        int act = 0, aj = 0, atr = 0;
         if (!last) {
             t += jump;
-            const R us = rng.uniform<R>(kk++) * total;
-            aj = scan_weights<R, 4, !EXACT>(sub, us);
-            Rates<R> r;
-            const R sr = subunit_rates<R>(s, aj, pick4(s.cass, aj), c, sv, r);
-            const R subr = EXACT ? pick4(sub, aj) : sr;
-            const R sum_lcc = r.lcc[0] + r.lcc[1] + r.lcc[2];
-            R sum_ryr;
-            if (EXACT) {
-                sum_ryr = subr - (sum_lcc + r.inact + r.clch);
-            } else {
-                sum_ryr = (R)0;
-#pragma unroll
-                for (int q = 0; q < 12; ++q) sum_ryr += r.ryr[q];
-            }
-            const R u = rng.uniform<R>(kk++) * subr;
-            if (u < sum_lcc) {
-                act = 1;
-                atr = scan_weights<R, 3, !EXACT>(r.lcc, rng.uniform<R>(kk++) * sum_lcc);
-            } else if (u < (sum_lcc + r.inact)) {
-                act = 2;
-            } else if (u < (sum_lcc + r.inact + sum_ryr)) {
-                act = 3;
-                atr = scan_weights<R, 12, !EXACT>(r.ryr, rng.uniform<R>(kk++) * sum_ryr);
-            } else {
-                act = 4;
-            }
+            select_event<R, EXACT>(s, c, sv, sub, total, rng, kk, act, aj, atr);
         }
-
-        // update_CaSS second pass: binomial re-splits (sample_RyR56/34, SSA.tpp:59-84) with draws
-        // k+1 .. k+D, then commit.
-        if (D > 0 || kind[0] || kind[1] || kind[2] || kind[3]) {
-            uint32_t kr = k + 1u;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                if (kind[j] == 0) continue;
-                const R x = s.cass[j];
-                if (kind[j] == 1)
-                    resplit_pair<R>(s.ryr[4], s.ryr[5], j, c.k65 / (c.k65 + c.k56 * (x * x)), rng, kr);
-                else
-                    resplit_pair<R>(s.ryr[2], s.ryr[3], j, c.k43 / (c.k43 + c.k34 * (x * x)), rng, kr);
-            }
-        }
+        // update_CaSS second pass, then commit.
+        if (D > 0 || kind[0] || kind[1] || kind[2] || kind[3]) resplit_crossed<R>(s, c, kind, rng, k);
 #pragma unroll
         for (int j = 0; j < 4; ++j) s.cass[j] = tmp[j];
 
@@ -666,45 +747,179 @@ struct SsaLane {
             }
         }
 
-        // Apply the transition (sample_new_state, SSA.tpp:262-283) to the updated state.
-        if (act != 0) {
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                if (j != aj) continue;
-                if (act == 1) {
-                    const int from = byte_u(s.lcc, j);
-                    if (from >= 1 && from <= 12) {
-                        const int to = (int)((c.lccn[from] >> (4 * atr)) & 0xFu);
-                        s.lcc = byte_set(s.lcc, j, to);
-                        const bool inact1 = ((s.flags >> j) & 1u) != 0u;
-                        if ((from == 5 && to == 6) || (from == 11 && to == 12))
-                            s.jlcc[j] = inact1 ? sv[SV_JMUL] * (c.Cao_scaled - sv[SV_JEXP] * s.cass[j]) : (R)0;
-                        else if (from == 6 || from == 12)
-                            s.jlcc[j] = (R)0;
-                    }
-                } else if (act == 2) {
-                    s.flags ^= (1u << j);
-                    const int st = byte_u(s.lcc, j);
-                    if (((s.flags >> j) & 1u) == 0u)
-                        s.jlcc[j] = (R)0;
-                    else if (st == 6 || st == 12)
-                        s.jlcc[j] = sv[SV_JMUL] * (c.Cao_scaled - sv[SV_JEXP] * s.cass[j]);
-                } else if (act == 3) {
-                    int from, to;
-                    ryr_move(atr, from, to);
-#pragma unroll
-                    for (int q = 0; q < 6; ++q) {
-                        if (q == from) s.ryr[q] = byte_add(s.ryr[q], j, -1);
-                        if (q == to) s.ryr[q] = byte_add(s.ryr[q], j, +1);
-                    }
-                    const R open = (R)(byte_s(s.ryr[2], j) + byte_s(s.ryr[3], j));
-                    jrel[j] = c.rRyR * open * (s.cajsr - s.cass[j]);
-                } else {
-                    s.flags ^= (1u << (4 + j));
-                }
-            }
-        }
+        // Apply the transition to the updated state.
+        if (act != 0) apply_event<R>(s, c, sv, act, aj, atr, jrel);
         jxfer_sum = jxfer[0] + jxfer[1] + jxfer[2] + jxfer[3];
+        k = kk;
+        if (last) return true;
+        if (++ev > cap) {
+            err = 1;
+            return true;
+        }
+        return false;
+    }
+};
+
+// ------------------------------------------------------------------------------------------
+// FP32 lane on subunit pairs.  The iteration of the generic lane (same formulas, same draws) with
+// subunits (0,1) and (2,3) held as float2 pairs for the packed FP32x2 instructions of sm_100 and
+// later (FFMA2, FADD2, FMUL2: each half rounds as the scalar instruction).  RyR counts become
+// floats by a byte permute into the bit pattern of 2^23 + 128 + n and one packed subtraction.
+// Sums over the four subunits are taken as (0+2) + (1+3).
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+// Signed byte counts of subunits 2p and 2p+1 from a RyR plane word whose bytes carry a +0x80 bias
+// (w ^ 0x80808080): float(0x4B0000bb) = 2^23 + bb, less 2^23 + 128.
+__device__ __forceinline__ float2 counts2(uint32_t wb, int p, float2 bias) {
+    const float a = __uint_as_float(__byte_perm(wb, 0x4B000000u, (uint32_t)(2 * p) | 0x7540u));
+    const float b = __uint_as_float(__byte_perm(wb, 0x4B000000u, (uint32_t)(2 * p + 1) | 0x7540u));
+    return add2(make_float2(a, b), bias);
+}
+
+template <>
+struct SsaLane<float, false> {
+    float t;
+    uint32_t k;
+    int ev;
+    float jrel[4];
+    float jxfer_sum;
+    float jtr;
+
+    __device__ __forceinline__ void begin(const Cru<float> &s, const SsaConsts<float> &c) {
+        t = 0.f;
+        k = 0;
+        ev = 0;
+        const float2 *K = c.pk;
+        const uint32_t b2 = s.ryr[2] ^ 0x80808080u, b3 = s.ryr[3] ^ 0x80808080u;
+        const float2 cj = make_float2(s.cajsr, s.cajsr);
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            const float2 open = add2(counts2(b2, p, K[PK_BIAS]), counts2(b3, p, K[PK_BIAS]));
+            const float2 x = make_float2(s.cass[2 * p], s.cass[2 * p + 1]);
+            const float2 jr = mul2(mul2(K[PK_RRYR], open), add2(cj, neg2(x)));
+            jrel[2 * p] = jr.x;
+            jrel[2 * p + 1] = jr.y;
+        }
+    }
+
+    __device__ __forceinline__ bool iterate(Cru<float> &s, const SsaConsts<float> &c, const float *sv,
+                                            const float2 *tab, Stream &rng, float dt, int cap, int &err) {
+        const float2 *K = c.pk;
+        const float Cai = sv[SV_CAI], CaNSR = sv[SV_CANSR], Cai_lo = sv[SV_CAI_LO], CaNSR_lo = sv[SV_CANSR_LO];
+        const float2 C[2] = {make_float2(s.cass[0], s.cass[1]), make_float2(s.cass[2], s.cass[3])};
+        // update_fluxes (SSA.tpp:37-45)
+        jtr = c.rtr * ((CaNSR - s.cajsr) + (CaNSR_lo - s.cajsr_lo));
+        const float2 eo = add2(C[0], C[1]);  // (c0 + c2, c1 + c3)
+        const float2 oe = make_float2(eo.y, eo.x);
+        float2 jiss[2], jx[2];
+        const float2 ncai = make_float2(-Cai, -Cai), ncailo = make_float2(-Cai_lo, -Cai_lo);
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            jiss[p] = mul2(K[PK_RISS], fma2(K[PK_M2], C[p], oe));
+            jx[p] = mul2(K[PK_RXFER], add2(add2(C[p], ncai), ncailo));
+        }
+        // subunit totals (the FP32 regrouping of subunit_total_fast)
+        const uint32_t iw = rate_index_word(s.lcc, s.flags);
+        const uint32_t b0 = s.ryr[0] ^ 0x80808080u, b1 = s.ryr[1] ^ 0x80808080u, b2 = s.ryr[2] ^ 0x80808080u;
+        const uint32_t b3 = s.ryr[3] ^ 0x80808080u, b4 = s.ryr[4] ^ 0x80808080u, b5 = s.ryr[5] ^ 0x80808080u;
+        float2 S[2];
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            const float2 X = C[p];
+            const float2 X2 = mul2(X, X);
+            const float2 R0 = counts2(b0, p, K[PK_BIAS]), R1 = counts2(b1, p, K[PK_BIAS]);
+            float2 y = fma2(X2, fma2(R1, K[PK_K2325], mul2(R0, K[PK_K12])), mul2(R1, K[PK_K21]));
+            // RyR states 3/4: lumped above 3.685e-2
+            const bool h0 = X.x > 3.685e-2f, h1 = X.y > 3.685e-2f;
+            const float2 R2 = counts2(b2, p, K[PK_BIAS]), R3 = counts2(b3, p, K[PK_BIAS]);
+            float2 p34 = fma2(R2, K[PK_K32], fma2(R3, K[PK_K4543], mul2(mul2(X2, R2), K[PK_K34])));
+            if (h0 || h1) {
+                const float2 num = fma2(K[PK_K45K34], X2, K[PK_K32K43]), den = fma2(K[PK_K34], X2, K[PK_K43]);
+                const float2 hv = mul2(add2(R2, R3), make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y)));
+                if (h0) p34.x = hv.x;
+                if (h1) p34.y = hv.y;
+            }
+            y = add2(y, p34);
+            // RyR states 5/6: lumped above 1.15e-4
+            const bool g0 = X.x > 1.15e-4f, g1 = X.y > 1.15e-4f;
+            const float2 R4 = counts2(b4, p, K[PK_BIAS]), R5 = counts2(b5, p, K[PK_BIAS]);
+            float2 p56 = make_float2(0.f, 0.f);
+            if (!(g0 && g1)) p56 = fma2(R5, K[PK_K65], fma2(R4, K[PK_K52], mul2(mul2(X2, R4), K[PK_K5654])));
+            if (g0 || g1) {
+                const float2 num = mul2(K[PK_K65], fma2(K[PK_K54], X2, K[PK_K52])), den = fma2(K[PK_K56], X2, K[PK_K65]);
+                const float2 hv = mul2(add2(R4, R5), make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y)));
+                if (g0) p56.x = hv.x;
+                if (g1) p56.y = hv.y;
+            }
+            y = add2(y, p56);
+            // LCC, gate and ClCh rates from the warp's table: base + slope * CaSS
+            const float2 ta = tab[(iw >> (16 * p)) & 0x3Fu], tb = tab[(iw >> (16 * p + 8)) & 0x3Fu];
+            S[p] = add2(make_float2(fmaf(ta.y, X.x, ta.x), fmaf(tb.y, X.y, tb.x)), y);
+        }
+        const float sub[4] = {S[0].x, S[0].y, S[1].x, S[1].y};
+        const float2 st = add2(S[0], S[1]);
+        const float total = st.x + st.y;
+        const float u0 = rng.uniform<float>(k);
+        const float jump = __fdividef(-logf(u0), total);
+        const bool last = !(t + jump < dt);
+        const float h = last ? (dt - t) : jump;
+
+        // update_CaSS (SSA.tpp:87-99), first pass
+        float2 tmp[2];
+        const float2 H = make_float2(h, h);
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            const float2 A = add2(K[PK_KBSR], C[p]), B = add2(K[PK_KBSL], C[p]);
+            const float2 U = mul2(A, A), V = mul2(B, B);
+            const float2 UV = mul2(U, V);
+            const float2 den = fma2(K[PK_BSL], U, fma2(K[PK_BSR], V, UV));
+            const float2 beta = make_float2(__fdividef(UV.x, den.x), __fdividef(UV.y, den.y));
+            const float2 jl = make_float2(s.jlcc[2 * p], s.jlcc[2 * p + 1]);
+            const float2 jr = make_float2(jrel[2 * p], jrel[2 * p + 1]);
+            const float2 f = add2(add2(add2(jl, jr), neg2(jx[p])), jiss[p]);
+            tmp[p] = add2(C[p], mul2(mul2(H, f), beta));
+        }
+        int kind[4];
+        uint32_t D = 0;
+        kind[0] = crossing<float>(s, 0, C[0].x, tmp[0].x, D);
+        kind[1] = crossing<float>(s, 1, C[0].y, tmp[0].y, D);
+        kind[2] = crossing<float>(s, 2, C[1].x, tmp[1].x, D);
+        kind[3] = crossing<float>(s, 3, C[1].y, tmp[1].y, D);
+
+        uint32_t kk = k + 1u + D;
+        int act = 0, aj = 0, atr = 0;
+        if (!last) {
+            t += jump;
+            select_event<float, false>(s, c, sv, sub, total, rng, kk, act, aj, atr);
+        }
+        if (D > 0 || kind[0] || kind[1] || kind[2] || kind[3]) resplit_crossed<float>(s, c, kind, rng, k);
+        s.cass[0] = tmp[0].x;
+        s.cass[1] = tmp[0].y;
+        s.cass[2] = tmp[1].x;
+        s.cass[3] = tmp[1].y;
+
+        // update_CaJSR (SSA.hpp:68-71), Fast2Sum into (hi, lo) as in the generic lane
+        {
+            const float x = s.cajsr;
+            const float u = (c.KCSQN + x) * (c.KCSQN + x);
+            const float beta = __fdividef(u, u + c.CSQN_const);
+            const float2 jr = add2(make_float2(jrel[0], jrel[1]), make_float2(jrel[2], jrel[3]));
+            const float d = h * beta * (jtr - c.VSS_VJSR * (jr.x + jr.y));
+            const float hi = s.cajsr;
+            const float y = d + s.cajsr_lo;
+            const float sum = hi + y;
+            const float err_ = y - (sum - hi);
+            s.cajsr = sum;
+            s.cajsr_lo = err_;
+        }
+
+        if (act != 0) apply_event<float>(s, c, sv, act, aj, atr, jrel);
+        const float2 jxs = add2(jx[0], jx[1]);
+        jxfer_sum = jxs.x + jxs.y;
         k = kk;
         if (last) return true;
         if (++ev > cap) {
