@@ -9,11 +9,11 @@
 //               finished its step takes the warp's next CRU, so lanes with pending SSA events do
 //               not hold the others back.  Each warp stores one flux partial; the warp that
 //               finishes last sums them in warp order and pushes the CTA's partial into the
-//               leader's shared memory (DSMEM).
+//               leader's shared memory (DSMEM).  In a leader CTA the warp that finishes first
+//               also evaluates the stimulus of step s+1 for the ODE warps.
 //   ODE warps : reduce the CTA partials of step s-1, increments and Euler update (globals
 //               s -> s+1), transcendental phases of the new state, push sv[(s+1)&1], arrive; the
-//               stimulus of step s+1 and the phases that the SSA does not need (general Jup
-//               exponents) run after the arrive.
+//               phases that the SSA does not need (general Jup exponents) run after the arrive.
 #pragma once
 
 #include <type_traits>
@@ -36,6 +36,8 @@ struct OdeShared {
     double g[kNumGlobals];  // the cell's globals (FP64 state)
     double t;               // accumulated time
     double sums[4];         // JLCC, ClCh, Jtr, Jxfer sums of the last reduced step (FP64)
+    double tstim;           // time of the next stimulus evaluation (the same sums as t)
+    double stim[2];         // stimulus of step s in slot s & 1, from the leader's SSA warps
     int status;
     int pad;
 };
@@ -385,10 +387,12 @@ struct FluxAcc {
     float jh = 0, jl = 0, xh = 0, xl = 0, th = 0, tl = 0;  // FP32: (hi, lo) pairs
     double dj = 0, dx = 0, dtr = 0;                       // FP64
     int acl = 0;
+    // FP32: a lane's own CRUs (one to a few per step) add up in FP32; the lane sums are then
+    // combined with compensation (warp_total, add_partial).
     __device__ __forceinline__ void add(float j, float x, float t, int cl) {
-        df_add(jh, jl, j, 0.f);
-        df_add(xh, xl, x, 0.f);
-        df_add(th, tl, t, 0.f);
+        jh += j;
+        xh += x;
+        th += t;
         acl += cl;
     }
     __device__ __forceinline__ void add(double j, double x, double t, int cl) {
@@ -567,6 +571,7 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
         if (ot == 0 && (not_positive(os.g[1]) || not_positive(os.g[2])) && os.status == 0)
             os.status = GW_ERR_NERNST;
         if (s > 0) reduce_partials<FP64, T>(v.part + (par ^ 1) * pslot, v.w.n_cta_cell, ot >> 5, lane, os.sums, X);
+        if (s > 0 && ot == 0) X[XS_ISTIM] = (T)os.stim[par];
         ode_bar();
         const int reg_n = v_regime(os.g[0]);
         for (int q = 0; q <= P.upd_phase; ++q) {
@@ -586,9 +591,7 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
         }
         push_sv<FP64, T>(P, X, os.g, v.svbuf, v.svstage, par ^ 1, v.w, ot);
         cluster_arrive();
-        // off the critical path: the stimulus of step s+1 (read by the first phase of the next
-        // step, after its ode_bar) and the phases the SSA does not need
-        if (ot == 0) X[XS_ISTIM] = (T)stimulus(a.dyn[cell], os.t, ri + 1);
+        // off the critical path: the phases the SSA does not need
         for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
             ode_phase<T>(v.off, q, reg, ot);
             ode_bar();
@@ -706,6 +709,14 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
                 __threadfence_block();
             }
             done = __shfl_sync(0xffffffffu, done, 0);
+            if (v.leader && done == 0 && lane == 0) {
+                // The stimulus of step s+1 at t_{s+1} (the ODE warps' t after this step's update,
+                // formed by the same additions), by the warp of the leader CTA that finishes first:
+                // it has slack, the ODE warps read it after the barrier.
+                OdeShared &os = *v.os;
+                os.tstim += a.dt;
+                os.stim[par ^ 1] = stimulus(a.dyn[cell], os.tstim, ri + 1);
+            }
             if (done == nsw - 1) {
                 __syncwarp();
                 FluxAcc<FP64> tot;
@@ -771,6 +782,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const __grid_con
         if (threadIdx.x == 0) {
             load_ssa_consts<R>(*v.cc, a.cs[cell]);
             v.ctr[0] = v.ctr[1] = v.ctr[2] = v.ctr[3] = 0;
+            if (v.leader) v.os->tstim = a.dyn[cell].t;
         }
         step0 = a.dyn[cell].step;
         if (!v.ode_thread) {
