@@ -42,6 +42,9 @@ struct OdeShared {
     int pad;
 };
 
+constexpr int kMaxThreads = 512;  // SSA warps + ODE warps per CTA (128 registers per thread)
+constexpr int kMaxWarps = kMaxThreads / 32;
+
 struct SmemLayout {
     size_t cc, sv, ode, prog, x, math, svs, rtab, part, chunk, ctr, tile, total;
 };
@@ -67,11 +70,11 @@ __host__ __device__ inline SmemLayout smem_layout(int tile_cap, int max_cta_cell
     L.svs = o;   // staging of the per-step SSA values before the push
     o += align16(kSvCount * sizeof(R));
     L.rtab = o;  // per-warp subunit rate tables (FP32 SSA)
-    o += align16((size_t)16 * kRateTab * sizeof(float2));
+    o += align16((size_t)kMaxWarps * kRateTab * sizeof(float2));
     L.part = o;  // [parity][rank in cell]: CTA partials (written by remote CTAs)
     o += align16((size_t)2 * max_cta_cell * sizeof(Partial));
     L.chunk = o;  // [warp]: warp partials of this CTA
-    o += align16((size_t)16 * sizeof(Partial));
+    o += align16((size_t)kMaxWarps * sizeof(Partial));
     L.ctr = o;   // warp completion counters [2 + parity]
     o += 16;
     L.tile = o;  // TileRec<R> per CRU
@@ -379,7 +382,6 @@ __device__ __forceinline__ void record_pass(const KernelArgs &a, const CtaWork &
     }
 }
 
-constexpr int kMaxThreads = 512;  // SSA warps + ODE warps per CTA (128 registers per thread)
 
 // Per-lane flux accumulators and their warp sum as a Partial (all lanes hold it).
 template <bool FP64>
