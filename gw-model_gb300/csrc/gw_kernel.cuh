@@ -771,6 +771,16 @@ __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+// x / y as x * rcp.approx(y), the arithmetic of __fdividef without its guard for |y| > 2^126 (the
+// divisors here are rate sums and buffer terms far below that)
+__device__ __forceinline__ float rcp_approx(float y) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(y));
+    return r;
+}
+__device__ __forceinline__ float2 div2(float2 x, float2 y) {
+    return __fmul2_rn(x, make_float2(rcp_approx(y.x), rcp_approx(y.y)));
+}
 
 // Signed byte counts of subunits 2p and 2p+1 from a RyR plane word whose bytes carry a +0x80 bias
 // (w ^ 0x80808080): float(0x4B0000bb) = 2^23 + bb, less 2^23 + 128.
@@ -839,7 +849,7 @@ struct SsaLane<float, false> {
             float2 p34 = fma2(R2, K[PK_K32], fma2(R3, K[PK_K4543], mul2(mul2(X2, R2), K[PK_K34])));
             if (h0 || h1) {
                 const float2 num = fma2(K[PK_K45K34], X2, K[PK_K32K43]), den = fma2(K[PK_K34], X2, K[PK_K43]);
-                const float2 hv = mul2(add2(R2, R3), make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y)));
+                const float2 hv = mul2(add2(R2, R3), div2(num, den));
                 if (h0) p34.x = hv.x;
                 if (h1) p34.y = hv.y;
             }
@@ -851,7 +861,7 @@ struct SsaLane<float, false> {
             if (!(g0 && g1)) p56 = fma2(R5, K[PK_K65], fma2(R4, K[PK_K52], mul2(mul2(X2, R4), K[PK_K5654])));
             if (g0 || g1) {
                 const float2 num = mul2(K[PK_K65], fma2(K[PK_K54], X2, K[PK_K52])), den = fma2(K[PK_K56], X2, K[PK_K65]);
-                const float2 hv = mul2(add2(R4, R5), make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y)));
+                const float2 hv = mul2(add2(R4, R5), div2(num, den));
                 if (g0) p56.x = hv.x;
                 if (g1) p56.y = hv.y;
             }
@@ -864,7 +874,7 @@ struct SsaLane<float, false> {
         const float2 st = add2(S[0], S[1]);
         const float total = st.x + st.y;
         const float u0 = rng.uniform<float>(k);
-        const float jump = __fdividef(-logf(u0), total);
+        const float jump = -logf(u0) * rcp_approx(total);
         const bool last = !(t + jump < dt);
         const float h = last ? (dt - t) : jump;
 
@@ -877,18 +887,29 @@ struct SsaLane<float, false> {
             const float2 U = mul2(A, A), V = mul2(B, B);
             const float2 UV = mul2(U, V);
             const float2 den = fma2(K[PK_BSL], U, fma2(K[PK_BSR], V, UV));
-            const float2 beta = make_float2(__fdividef(UV.x, den.x), __fdividef(UV.y, den.y));
+            const float2 beta = div2(UV, den);
             const float2 jl = make_float2(s.jlcc[2 * p], s.jlcc[2 * p + 1]);
             const float2 jr = make_float2(jrel[2 * p], jrel[2 * p + 1]);
             const float2 f = add2(add2(add2(jl, jr), neg2(jx[p])), jiss[p]);
             tmp[p] = add2(C[p], mul2(mul2(H, f), beta));
         }
-        int kind[4];
+        // Threshold crossings are rare: an exact any-crossing test first, then the kinds and the
+        // re-split draw count only when one occurred (if-converted, the full test per subunit
+        // cost ~120 instructions per CRU-step).
+        bool crossed = false;
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            crossed |= (C[p].x > 1.15e-4f && tmp[p].x <= 1.15e-4f) || (C[p].x > 0.03685f && tmp[p].x <= 0.03685f);
+            crossed |= (C[p].y > 1.15e-4f && tmp[p].y <= 1.15e-4f) || (C[p].y > 0.03685f && tmp[p].y <= 0.03685f);
+        }
+        int kind[4] = {0, 0, 0, 0};
         uint32_t D = 0;
-        kind[0] = crossing<float>(s, 0, C[0].x, tmp[0].x, D);
-        kind[1] = crossing<float>(s, 1, C[0].y, tmp[0].y, D);
-        kind[2] = crossing<float>(s, 2, C[1].x, tmp[1].x, D);
-        kind[3] = crossing<float>(s, 3, C[1].y, tmp[1].y, D);
+        if (crossed) {
+            kind[0] = crossing<float>(s, 0, C[0].x, tmp[0].x, D);
+            kind[1] = crossing<float>(s, 1, C[0].y, tmp[0].y, D);
+            kind[2] = crossing<float>(s, 2, C[1].x, tmp[1].x, D);
+            kind[3] = crossing<float>(s, 3, C[1].y, tmp[1].y, D);
+        }
 
         uint32_t kk = k + 1u + D;
         int act = 0, aj = 0, atr = 0;
@@ -896,7 +917,7 @@ struct SsaLane<float, false> {
             t += jump;
             select_event<float, false>(s, c, sv, sub, total, rng, kk, act, aj, atr);
         }
-        if (D > 0 || kind[0] || kind[1] || kind[2] || kind[3]) resplit_crossed<float>(s, c, kind, rng, k);
+        if (crossed) resplit_crossed<float>(s, c, kind, rng, k);
         s.cass[0] = tmp[0].x;
         s.cass[1] = tmp[0].y;
         s.cass[2] = tmp[1].x;
@@ -906,7 +927,7 @@ struct SsaLane<float, false> {
         {
             const float x = s.cajsr;
             const float u = (c.KCSQN + x) * (c.KCSQN + x);
-            const float beta = __fdividef(u, u + c.CSQN_const);
+            const float beta = u * rcp_approx(u + c.CSQN_const);
             const float2 jr = add2(make_float2(jrel[0], jrel[1]), make_float2(jrel[2], jrel[3]));
             const float d = h * beta * (jtr - c.VSS_VJSR * (jr.x + jr.y));
             const float hi = s.cajsr;
