@@ -790,6 +790,48 @@ __device__ __forceinline__ float2 counts2(uint32_t wb, int p, float2 bias) {
     return add2(make_float2(a, b), bias);
 }
 
+// FP32 event selection: select_event's draws and decisions, with the subunit's RyR total taken
+// from the iteration's packed total computation (ryr_sub) and the 12 individual RyR rates formed
+// only when the RyR class is drawn (at rest most events are LCC and gate transitions).
+__device__ __forceinline__ void select_event_f32(const Cru<float> &s, const SsaConsts<float> &c, const float *sv,
+                                                 const float (&sub)[4], const float (&ryr_sub)[4], float total,
+                                                 Stream &rng, uint32_t &kk, int &act, int &aj, int &atr) {
+    const float us = rng.uniform<float>(kk++) * total;
+    aj = scan_weights<float, 4, true>(sub, us);
+    const float x = pick4(s.cass, aj);
+    // update_LCC_rates, update_LCC_inactivation_rates, update_ClCh_rates of subunit aj
+    const int st = byte_u(s.lcc, aj);
+    const uint32_t w = c.lcct[st & 15];
+    float lcc[3] = {sv[w & 0xFFu], sv[(w >> 8) & 0xFFu], sv[(w >> 16) & 0xFFu]};
+    const int kin = (int)(w >> 24);
+    if (kin < 3) {
+        const float gx = c.gam[st - 1] * x;
+        if (kin == 1) lcc[1] = gx; else lcc[2] = gx;
+    }
+    const float inact = ((s.flags >> aj) & 1u) == 0u ? sv[SV_INACT0] : sv[SV_INACT1];
+    const float clch = ((s.flags >> (4 + aj)) & 1u) == 0u ? c.kfClCh * x : c.kbClCh;
+    const float sum_lcc = lcc[0] + lcc[1] + lcc[2];
+    const float sum_ryr = pick4(ryr_sub, aj);
+    const float subr = ((sum_lcc + inact) + sum_ryr) + clch;
+    const float u = rng.uniform<float>(kk++) * subr;
+    if (u < sum_lcc) {
+        act = 1;
+        atr = scan_weights<float, 3, true>(lcc, rng.uniform<float>(kk++) * sum_lcc);
+    } else if (u < sum_lcc + inact) {
+        act = 2;
+    } else if (u < sum_lcc + inact + sum_ryr) {
+        act = 3;
+        Rates<float> r;
+        subunit_rates<float>(s, aj, x, c, sv, r);
+        float direct = 0.f;
+#pragma unroll
+        for (int q = 0; q < 12; ++q) direct += r.ryr[q];
+        atr = scan_weights<float, 12, true>(r.ryr, rng.uniform<float>(kk++) * direct);
+    } else {
+        act = 4;
+    }
+}
+
 template <>
 struct SsaLane<float, false> {
     float t;
@@ -836,7 +878,7 @@ struct SsaLane<float, false> {
         const uint32_t iw = rate_index_word(s.lcc, s.flags);
         const uint32_t b0 = s.ryr[0] ^ 0x80808080u, b1 = s.ryr[1] ^ 0x80808080u, b2 = s.ryr[2] ^ 0x80808080u;
         const uint32_t b3 = s.ryr[3] ^ 0x80808080u, b4 = s.ryr[4] ^ 0x80808080u, b5 = s.ryr[5] ^ 0x80808080u;
-        float2 S[2];
+        float2 S[2], Y[2];  // subunit totals, and their RyR parts
 #pragma unroll
         for (int p = 0; p < 2; ++p) {
             const float2 X = C[p];
@@ -868,6 +910,7 @@ struct SsaLane<float, false> {
             y = add2(y, p56);
             // LCC, gate and ClCh rates from the warp's table: base + slope * CaSS
             const float2 ta = tab[(iw >> (16 * p)) & 0x3Fu], tb = tab[(iw >> (16 * p + 8)) & 0x3Fu];
+            Y[p] = y;
             S[p] = add2(make_float2(fmaf(ta.y, X.x, ta.x), fmaf(tb.y, X.y, tb.x)), y);
         }
         const float sub[4] = {S[0].x, S[0].y, S[1].x, S[1].y};
@@ -915,7 +958,8 @@ struct SsaLane<float, false> {
         int act = 0, aj = 0, atr = 0;
         if (!last) {
             t += jump;
-            select_event<float, false>(s, c, sv, sub, total, rng, kk, act, aj, atr);
+            const float ryr_sub[4] = {Y[0].x, Y[0].y, Y[1].x, Y[1].y};
+            select_event_f32(s, c, sv, sub, ryr_sub, total, rng, kk, act, aj, atr);
         }
         if (crossed) resplit_crossed<float>(s, c, kind, rng, k);
         s.cass[0] = tmp[0].x;
