@@ -12,6 +12,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <memory>
 #include <vector>
 
 #include "gw_gb300.h"
@@ -540,36 +541,61 @@ int gw_destroy(gw_ctx *c) {
     return GW_OK;
 }
 
-int gw_autotune(const gw_ensemble_desc *d, int trial_steps, int *best_cluster_ctas, double *best_us_per_step) {
-    if (!d || !best_cluster_ctas || trial_steps <= 0)
+int gw_autotune(const gw_ensemble_desc *d, int trial_steps, int *best_cluster_ctas, int *best_cta_crus,
+                double *best_us_per_step) {
+    if (!d || !best_cluster_ctas || trial_steps <= 0 || d->n_cells <= 0 || !d->ncru)
         return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "gw_autotune: null descriptor/output or trial_steps <= 0");
     static const int kCandidates[] = {16, 8, 4, 2, 1};
     const int warm = std::max(20, trial_steps / 4);
-    int best = 0;
+    // The planner alone (no allocation): whether a cluster size and CTA capacity fit these cells.
+    std::unique_ptr<gw_ctx> probe(new gw_ctx);
+    probe->device = d->device;
+    probe->precision = d->precision;
+    probe->n_cells = d->n_cells;
+    probe->ncru.assign(d->ncru, d->ncru + d->n_cells);
+    auto fits = [&](int C, int tile) { return plan_shape(probe.get(), C, tile) == GW_OK; };
+    int best = 0, best_tile = 0;
     double best_us = 0.0;
     for (int C : kCandidates) {
-        gw_ensemble_desc t = *d;
-        t.cluster_ctas = C;
-        t.cta_crus = 0;
-        gw_ctx *c = nullptr;
-        int rc = gw_create(&t, &c);
-        if (rc == GW_ERR_UNSUPPORTED) continue;  // this cluster size does not fit the cells
-        if (rc) return rc;
-        rc = gw_set_stimulus_pulse(c, -1, 0.0, 1000.0, 0.5, 100.0);
-        if (!rc) rc = gw_run(c, 1e-3, warm, 0, nullptr);
-        const double ms0 = c->stats.kernel_ms;
-        if (!rc) rc = gw_run(c, 1e-3, trial_steps, 0, nullptr);
-        const double us = (c->stats.kernel_ms - ms0) * 1e3 / trial_steps;
-        if (rc) g_create_error = c->err;
-        gw_destroy(c);
-        if (rc) return rc;
-        if (best == 0 || us < best_us) {
-            best = C;
-            best_us = us;
+        if (!fits(C, 0)) continue;  // this cluster size does not fit the cells
+        // Two capacities per cluster size: the size rule's, and the largest that fits shared
+        // memory (fewer, fuller CTAs amortise the per-step barrier and global step over more CRUs,
+        // which pays off for cells of uneven size).
+        int big = 0;
+        for (int t = 4096; t > 0; t -= 64)
+            if (fits(C, t)) {
+                big = t;
+                break;
+            }
+        const int rule_tile = fits(C, 0) ? probe->tile_cap : 0;
+        const int tiles[2] = {0, big > rule_tile + 64 ? big : -1};
+        for (int tile : tiles) {
+            if (tile < 0) continue;
+            gw_ensemble_desc t = *d;
+            t.cluster_ctas = C;
+            t.cta_crus = tile;
+            gw_ctx *c = nullptr;
+            int rc = gw_create(&t, &c);
+            if (rc == GW_ERR_UNSUPPORTED) continue;
+            if (rc) return rc;
+            rc = gw_set_stimulus_pulse(c, -1, 0.0, 1000.0, 0.5, 100.0);
+            if (!rc) rc = gw_run(c, 1e-3, warm, 0, nullptr);
+            const double ms0 = c->stats.kernel_ms;
+            if (!rc) rc = gw_run(c, 1e-3, trial_steps, 0, nullptr);
+            const double us = (c->stats.kernel_ms - ms0) * 1e3 / trial_steps;
+            if (rc) g_create_error = c->err;
+            gw_destroy(c);
+            if (rc) return rc;
+            if (best == 0 || us < best_us) {
+                best = C;
+                best_tile = tile;
+                best_us = us;
+            }
         }
     }
     if (best == 0) return fail(nullptr, GW_ERR_UNSUPPORTED, "gw_autotune: no cluster size fits these cells");
     *best_cluster_ctas = best;
+    if (best_cta_crus) *best_cta_crus = best_tile;
     if (best_us_per_step) *best_us_per_step = best_us;
     return GW_OK;
 }

@@ -97,7 +97,7 @@ _SIGS = {
     "gw_set_stimulus_samples": ([C.c_void_p, C.c_int, _P(C.c_double), C.c_int64], C.c_int),
     "gw_run": ([C.c_void_p, C.c_double, C.c_int64, C.c_int, _P(GwTrace)], C.c_int),
     "gw_run_noalloc": ([C.c_void_p, C.c_double, C.c_int64, C.c_int, _P(GwTrace)], C.c_int),
-    "gw_autotune": ([_P(GwEnsembleDesc), C.c_int, _P(C.c_int), _P(C.c_double)], C.c_int),
+    "gw_autotune": ([_P(GwEnsembleDesc), C.c_int, _P(C.c_int), _P(C.c_int), _P(C.c_double)], C.c_int),
     "gw_math_check": ([_P(C.c_double), C.c_int64, _P(C.c_double), _P(C.c_double)], C.c_int),
     "gw_get_time": ([C.c_void_p, C.c_int, _P(C.c_double), _P(C.c_uint64)], C.c_int),
     "gw_set_time": ([C.c_void_p, C.c_int, C.c_double, C.c_uint64], C.c_int),

@@ -94,7 +94,8 @@ class Ensemble:
                  device: int = 0, event_cap: int = 0, cluster_ctas=0, cta_crus: int = 0,
                  steps_per_launch: int = 0, ode_fp32_rhs: bool = False, tune_steps: int = 200):
         """cluster_ctas: CTAs per cluster, 0 for the size rule, or "auto" to measure the fastest
-        shape for these cells first (gw_autotune, tune_steps trial steps per candidate)."""
+        shape (cluster size and CTA capacity) for these cells first (gw_autotune, tune_steps trial
+        steps per candidate)."""
         self.L = _lib.load()
         self.ncru = np.ascontiguousarray(ncru, dtype=np.int32)
         self.n_cells = int(self.ncru.size)
@@ -121,9 +122,9 @@ class Ensemble:
         d.event_cap = event_cap
         self.tuned_us_per_step = None
         if cluster_ctas == "auto":
-            best, us = C.c_int(), C.c_double()
-            check(self.L.gw_autotune(C.byref(d), int(tune_steps), C.byref(best), C.byref(us)))
-            cluster_ctas, cta_crus = best.value, 0
+            best, tile, us = C.c_int(), C.c_int(), C.c_double()
+            check(self.L.gw_autotune(C.byref(d), int(tune_steps), C.byref(best), C.byref(tile), C.byref(us)))
+            cluster_ctas, cta_crus = best.value, tile.value
             self.tuned_us_per_step = us.value
         d.cluster_ctas = int(cluster_ctas)
         d.cta_crus = cta_crus

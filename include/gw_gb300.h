@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define GW_ABI_VERSION 2
+#define GW_ABI_VERSION 3
 
 /* Status codes. */
 typedef enum gw_status {
@@ -161,12 +161,15 @@ void gw_globals_py_default(gw_globals *g);
 int gw_create(const gw_ensemble_desc *desc, gw_ctx **out);
 int gw_destroy(gw_ctx *ctx);
 /* No counterpart in the reference (it has one CPU code path).  Measures the launch shape for an
- * ensemble: for each cluster size in {16, 8, 4, 2, 1} that fits (shared memory per CTA), builds a
- * throwaway context from *desc (its cluster_ctas and cta_crus are ignored), paces it at 1 Hz and
- * times trial_steps global steps after a short warm-up; returns the fastest cluster size and its
- * device time per global step.  Set desc->cluster_ctas to the result before gw_create.  The
- * contexts it builds draw their own initial states; no caller state is touched. */
-int gw_autotune(const gw_ensemble_desc *desc, int trial_steps, int *best_cluster_ctas,
+ * ensemble: for each cluster size in {16, 8, 4, 2, 1} that fits, and for two CTA capacities each
+ * (the size rule's, cta_crus = 0, and the largest that fits shared memory: fewer, fuller CTAs
+ * amortise the per-step cluster barrier and global step over more CRUs, which pays off for cells
+ * of uneven size), builds a throwaway context from *desc (its cluster_ctas and cta_crus are
+ * ignored), paces it at 1 Hz and times trial_steps global steps after a short warm-up; returns the
+ * fastest cluster size, its CTA capacity (0 = size rule; best_cta_crus may be NULL) and its
+ * device time per global step.  Set desc->cluster_ctas and desc->cta_crus to the results before
+ * gw_create.  The contexts it builds draw their own initial states; no caller state is touched. */
+int gw_autotune(const gw_ensemble_desc *desc, int trial_steps, int *best_cluster_ctas, int *best_cta_crus,
                 double *best_us_per_step);
 
 /* Replaces GW_model::set_initial_value (GW.tpp:6-10) for one cell.  JLCC may be NULL: the

@@ -89,7 +89,7 @@ def test_global_defaults(enginelib, oracle):
 
 
 def test_abi_version(enginelib):
-    assert enginelib.gw_abi_version() == 2
+    assert enginelib.gw_abi_version() == 3
 
 
 def test_invalid_arguments_without_device(enginelib):
@@ -103,7 +103,7 @@ def test_invalid_arguments_without_device(enginelib):
     assert "n_cells" in _lib.last_error()
     assert enginelib.gw_run(None, 1e-3, 10, 0, None) == _lib.GW_ERR_INVALID_ARGUMENT
     assert enginelib.gw_run_noalloc(None, 1e-3, 10, 0, None) == _lib.GW_ERR_INVALID_ARGUMENT
-    assert enginelib.gw_autotune(None, 10, None, None) == _lib.GW_ERR_INVALID_ARGUMENT
+    assert enginelib.gw_autotune(None, 10, None, None, None) == _lib.GW_ERR_INVALID_ARGUMENT
 
 
 def test_unknown_prng_rejected_before_any_device_work(enginelib):

@@ -1,5 +1,6 @@
-"""gw_autotune: picks a cluster size that fits the cells, reports its time per step, and the
-ensemble built with it runs (through the C ABI and through Ensemble(cluster_ctas="auto"))."""
+"""gw_autotune: picks a cluster size and CTA capacity that fit the cells, reports its time per
+step, and the ensemble built with them runs (through the C ABI and through
+Ensemble(cluster_ctas="auto"))."""
 import ctypes as C
 
 import numpy as np
@@ -30,10 +31,12 @@ def test_autotune_picks_a_fitting_shape(ncru, allowed):
     L = _lib.load()
     keep = []
     d = _desc(ncru, keep)
-    best, us = C.c_int(), C.c_double()
-    assert L.gw_autotune(C.byref(d), 100, C.byref(best), C.byref(us)) == _lib.GW_OK, _lib.last_error()
+    best, tile, us = C.c_int(), C.c_int(-1), C.c_double()
+    assert L.gw_autotune(C.byref(d), 100, C.byref(best), C.byref(tile), C.byref(us)) == _lib.GW_OK, _lib.last_error()
     assert best.value in allowed and 0.0 < us.value < 1e4
+    assert tile.value == 0 or tile.value >= 64
     d.cluster_ctas = best.value
+    d.cta_crus = tile.value
     h = C.c_void_p()
     assert L.gw_create(C.byref(d), C.byref(h)) == _lib.GW_OK
     assert L.gw_run(h, 1e-3, 50, 0, None) == _lib.GW_OK
@@ -51,3 +54,15 @@ def test_ensemble_auto_shape():
     assert np.all(np.isfinite(tr.globals))
     assert e.stats()["cluster_ctas"] in (1, 2, 4, 8, 16)
     e.close()
+
+
+def test_autotune_tile_optional_and_uneven_cells():
+    """best_cta_crus may be NULL; for uneven cells the chosen capacity fits them all."""
+    from gwgb300 import _lib
+
+    L = _lib.load()
+    keep = []
+    d = _desc([4000, 1500, 2600, 900], keep)
+    best, us = C.c_int(), C.c_double()
+    assert L.gw_autotune(C.byref(d), 60, C.byref(best), None, C.byref(us)) == _lib.GW_OK, _lib.last_error()
+    assert best.value in (1, 2, 4, 8, 16) and us.value > 0.0
