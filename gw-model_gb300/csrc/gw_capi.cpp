@@ -545,7 +545,9 @@ int gw_autotune(const gw_ensemble_desc *d, int trial_steps, int *best_cluster_ct
                 double *best_us_per_step) {
     if (!d || !best_cluster_ctas || trial_steps <= 0 || d->n_cells <= 0 || !d->ncru)
         return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "gw_autotune: null descriptor/output or trial_steps <= 0");
-    static const int kCandidates[] = {16, 8, 4, 2, 1};
+    // Cluster sizes: powers of two, and 9, 6, 3, which pack two, three and six clusters into a
+    // GPC of 18-19 SMs (GB300: 152 SMs) where 8 and 4 leave SMs idle.
+    static const int kCandidates[] = {16, 9, 8, 6, 4, 3, 2, 1};
     const int warm = std::max(20, trial_steps / 4);
     // The planner alone (no allocation): whether a cluster size and CTA capacity fit these cells.
     std::unique_ptr<gw_ctx> probe(new gw_ctx);

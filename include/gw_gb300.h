@@ -161,7 +161,7 @@ void gw_globals_py_default(gw_globals *g);
 int gw_create(const gw_ensemble_desc *desc, gw_ctx **out);
 int gw_destroy(gw_ctx *ctx);
 /* No counterpart in the reference (it has one CPU code path).  Measures the launch shape for an
- * ensemble: for each cluster size in {16, 8, 4, 2, 1} that fits, and for two CTA capacities each
+ * ensemble: for each cluster size in {16, 9, 8, 6, 4, 3, 2, 1} that fits, and for two CTA capacities each
  * (the size rule's, cta_crus = 0, and the largest that fits shared memory: fewer, fuller CTAs
  * amortise the per-step cluster barrier and global step over more CRUs, which pays off for cells
  * of uneven size), builds a throwaway context from *desc (its cluster_ctas and cta_crus are

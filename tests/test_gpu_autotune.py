@@ -24,7 +24,7 @@ def _desc(ncru, keep):
     return d
 
 
-@pytest.mark.parametrize("ncru,allowed", [([12500], {8, 16}), ([300] * 6, {1, 2, 4, 8, 16})])
+@pytest.mark.parametrize("ncru,allowed", [([12500], {6, 8, 9, 16}), ([300] * 6, {1, 2, 3, 4, 6, 8, 9, 16})])
 def test_autotune_picks_a_fitting_shape(ncru, allowed):
     from gwgb300 import _lib
 
@@ -52,7 +52,7 @@ def test_ensemble_auto_shape():
         e.sample_initial_crus(c)
     tr = e.run(1e-3, 100, record_every=50)
     assert np.all(np.isfinite(tr.globals))
-    assert e.stats()["cluster_ctas"] in (1, 2, 4, 8, 16)
+    assert e.stats()["cluster_ctas"] in (1, 2, 3, 4, 6, 8, 9, 16)
     e.close()
 
 
@@ -65,4 +65,4 @@ def test_autotune_tile_optional_and_uneven_cells():
     d = _desc([4000, 1500, 2600, 900], keep)
     best, us = C.c_int(), C.c_double()
     assert L.gw_autotune(C.byref(d), 60, C.byref(best), None, C.byref(us)) == _lib.GW_OK, _lib.last_error()
-    assert best.value in (1, 2, 4, 8, 16) and us.value > 0.0
+    assert best.value in (1, 2, 3, 4, 6, 8, 9, 16) and us.value > 0.0
