@@ -389,8 +389,9 @@ struct FluxAcc {
     float jh = 0, jl = 0, xh = 0, xl = 0, th = 0, tl = 0;  // FP32: (hi, lo) pairs
     double dj = 0, dx = 0, dtr = 0;                       // FP64
     int acl = 0;
-    // FP32: a lane's own CRUs (one to a few per step) add up in FP32; the lane sums are then
-    // combined with compensation (warp_total, add_partial).
+    // FP32: a lane's own CRUs (one to a few per step) add up in FP32, the lane sums in a plain
+    // FP32 tree (warp_total); the warp partials of a CTA and the CTA partials of a cell are then
+    // combined with compensation (add_partial, warp_total_compensated, reduce_partials).
     __device__ __forceinline__ void add(float j, float x, float t, int cl) {
         jh += j;
         xh += x;
@@ -417,6 +418,27 @@ struct FluxAcc {
             acl += (int)f[6];
         }
     }
+    // The compensated warp sum of (hi, lo) pairs (FP32), for the CTA partial from the warp
+    // partials; FP64 as warp_total.
+    __device__ __forceinline__ Partial warp_total_compensated() {
+        if (FP64) return warp_total();
+        Partial pv;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float a0 = __shfl_xor_sync(0xffffffffu, jh, o), a1 = __shfl_xor_sync(0xffffffffu, jl, o);
+            const float b0 = __shfl_xor_sync(0xffffffffu, xh, o), b1 = __shfl_xor_sync(0xffffffffu, xl, o);
+            const float c0 = __shfl_xor_sync(0xffffffffu, th, o), c1 = __shfl_xor_sync(0xffffffffu, tl, o);
+            acl += __shfl_xor_sync(0xffffffffu, acl, o);
+            df_add(jh, jl, a0, a1);
+            df_add(xh, xl, b0, b1);
+            df_add(th, tl, c0, c1);
+        }
+        float *f = reinterpret_cast<float *>(pv.v);
+        f[0] = jh; f[1] = jl; f[2] = xh; f[3] = xl; f[4] = th; f[5] = tl;
+        f[6] = (float)acl;
+        f[7] = 0.f;
+        return pv;
+    }
     __device__ __forceinline__ Partial warp_total() {
         Partial pv;
         if (FP64) {
@@ -432,18 +454,20 @@ struct FluxAcc {
             pv.v[2] = dtr;
             pv.v[3] = (double)acl;
         } else {
+            // FP32: a plain tree over the 32 lane sums (each covers one to a few CRUs; the
+            // compensated sums start where most terms meet, across the warp partials of a CTA and
+            // the CTA partials of a cell), and one REDUX for the ClCh count.  The per-step tree ran
+            // on every lane of every warp: with compensation it was ~150 instructions per CRU-step
+            // of a 12,500-CRU cell.
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                const float a0 = __shfl_xor_sync(0xffffffffu, jh, o), a1 = __shfl_xor_sync(0xffffffffu, jl, o);
-                const float b0 = __shfl_xor_sync(0xffffffffu, xh, o), b1 = __shfl_xor_sync(0xffffffffu, xl, o);
-                const float c0 = __shfl_xor_sync(0xffffffffu, th, o), c1 = __shfl_xor_sync(0xffffffffu, tl, o);
-                acl += __shfl_xor_sync(0xffffffffu, acl, o);
-                df_add(jh, jl, a0, a1);
-                df_add(xh, xl, b0, b1);
-                df_add(th, tl, c0, c1);
+                jh += __shfl_xor_sync(0xffffffffu, jh, o);
+                xh += __shfl_xor_sync(0xffffffffu, xh, o);
+                th += __shfl_xor_sync(0xffffffffu, th, o);
             }
+            acl = (int)__reduce_add_sync(0xffffffffu, (unsigned)acl);
             float *f = reinterpret_cast<float *>(pv.v);
-            f[0] = jh; f[1] = jl; f[2] = xh; f[3] = xl; f[4] = th; f[5] = tl;
+            f[0] = jh; f[1] = 0.f; f[2] = xh; f[3] = 0.f; f[4] = th; f[5] = 0.f;
             f[6] = (float)acl;
             f[7] = 0.f;
         }
@@ -723,7 +747,7 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
                 __syncwarp();
                 FluxAcc<FP64> tot;
                 if (lane < nsw) tot.add_partial(v.chunkp[lane]);
-                const Partial pc = tot.warp_total();
+                const Partial pc = tot.warp_total_compensated();
                 if (lane == 0) {
                     Partial *dst = v.part + par * pslot + w.rank_in_cell;
 #pragma unroll
