@@ -69,8 +69,8 @@ __host__ __device__ inline SmemLayout smem_layout(int tile_cap, int max_cta_cell
     o += align16(sizeof(math64::Tables));
     L.svs = o;   // staging of the per-step SSA values before the push
     o += align16(kSvCount * sizeof(R));
-    L.rtab = o;  // per-warp subunit rate tables (FP32 SSA)
-    o += align16((size_t)kMaxWarps * kRateTab * sizeof(float2));
+    L.rtab = o;  // the CTA's subunit rate table (FP32 SSA)
+    o += align16((size_t)kRateTab * sizeof(float2));
     L.part = o;  // [parity][rank in cell]: CTA partials (written by remote CTAs)
     o += align16((size_t)2 * max_cta_cell * sizeof(Partial));
     L.chunk = o;  // [warp]: warp partials of this CTA
@@ -108,6 +108,8 @@ __device__ __forceinline__ void cluster_wait() {
 }
 // barrier of the ODE warps (named barrier 1, kOdeLanes threads)
 __device__ __forceinline__ void ode_bar() { asm volatile("bar.sync 1, %0;" ::"n"(kOdeLanes) : "memory"); }
+// barrier of a CTA's SSA warps (named barrier 2, n threads: the CTA's SSA threads 0 .. n-1)
+__device__ __forceinline__ void ssa_bar(int n) { asm volatile("bar.sync 2, %0;" ::"r"(n) : "memory"); }
 
 // Stimulus of step ri at time t (pulse train or per-step samples).  Uses explicit round-to-nearest
 // operations so the host's evaluation of the same pulse train gives the same values.
@@ -518,7 +520,7 @@ struct CtaView {
         svstage = smem + L.svs;
         part = reinterpret_cast<Partial *>(smem + L.part);
         chunkp = reinterpret_cast<Partial *>(smem + L.chunk);  // warp partials
-        rtab = reinterpret_cast<float2 *>(smem + L.rtab) + warp * kRateTab;  // this warp's table
+        rtab = reinterpret_cast<float2 *>(smem + L.rtab);
         ctr = reinterpret_cast<int *>(smem + L.ctr);
         tile = reinterpret_cast<TileRec<R> *>(smem + L.tile);
         off = OdeOffsets{(uint32_t)L.prog, (uint32_t)L.x, (uint32_t)L.ode, (uint32_t)L.math};
@@ -674,8 +676,10 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
             const R *sv = v.svbuf + par * kSvCount;
             const int nsw = n_ssa >> 5;
             if (!FP64) {
-                build_rate_table<R>(v.rtab, cc, sv, lane);
-                __syncwarp();
+                // The CTA's rate table for this step: entry e by SSA thread e, then the CTA's SSA
+                // warps meet at named barrier 2 (they leave the cluster barrier together).
+                for (int e = (int)threadIdx.x; e < kRateTab; e += n_ssa) build_rate_entry<R>(v.rtab, cc, sv, e);
+                ssa_bar(n_ssa);
             }
             if (w.cru_count == 0 && threadIdx.x == 0) {
                 Partial *dst = v.part + par * pslot + w.rank_in_cell;

@@ -388,24 +388,20 @@ __device__ __forceinline__ R subunit_rates(const Cru<R> &s, int j, R x, const Ss
 // Table of the rates of subunit j other than the RyR rates, by the subunit's (LCC state, gate,
 // ClCh) index: total = base + slope * CaSS.  base = the LCC state's V-dependent outgoing rates
 // + the gate's rate + (ClCh open ? kbClCh : 0); slope = (Ca-dependent LCC inactivation: gamma0 a^k)
-// + (ClCh closed ? kfClCh : 0).  Rebuilt by each warp at the start of every global step (the
+// + (ClCh closed ? kfClCh : 0).  Rebuilt by each CTA at the start of every global step (the
 // V-dependent rates change per step); entry = state | gate << 4 | clch << 5.
 constexpr int kRateTab = 64;
 
 template <typename R>
-__device__ __forceinline__ void build_rate_table(float2 *tab, const SsaConsts<R> &c, const R *sv, int lane) {
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int e = lane + 32 * h;
-        const int st = e & 15, gate = (e >> 4) & 1, clch = (e >> 5) & 1;
-        const uint32_t w = c.lcct[st];
-        R base = sv[w & 0xFFu] + sv[(w >> 8) & 0xFFu] + sv[(w >> 16) & 0xFFu];
-        base += gate ? sv[SV_INACT1] : sv[SV_INACT0];
-        if (clch) base += c.kbClCh;
-        R slope = ((w >> 24) < 3u && st >= 1) ? c.gam[(st - 1) & 7] : (R)0;
-        if (!clch) slope += c.kfClCh;
-        tab[e] = make_float2((float)base, (float)slope);
-    }
+__device__ __forceinline__ void build_rate_entry(float2 *tab, const SsaConsts<R> &c, const R *sv, int e) {
+    const int st = e & 15, gate = (e >> 4) & 1, clch = (e >> 5) & 1;
+    const uint32_t w = c.lcct[st];
+    R base = sv[w & 0xFFu] + sv[(w >> 8) & 0xFFu] + sv[(w >> 16) & 0xFFu];
+    base += gate ? sv[SV_INACT1] : sv[SV_INACT0];
+    if (clch) base += c.kbClCh;
+    R slope = ((w >> 24) < 3u && st >= 1) ? c.gam[(st - 1) & 7] : (R)0;
+    if (!clch) slope += c.kfClCh;
+    tab[e] = make_float2((float)base, (float)slope);
 }
 
 // Byte j of the result: subunit j's rate-table index (LCC state | gate << 4 | ClCh << 5).
