@@ -155,16 +155,31 @@ __device__ __forceinline__ float t_sqrt(float x) { return sqrtf(x); }
 // read into a generic load; addresses formed from the shared-memory symbol inside the function
 // stay shared-memory loads.
 struct OdeOffsets {
-    uint32_t prog, x, ode, math;
+    uint32_t prog, x, ode, math, stage;
 };
+
+// The FP32 pair (hi, lo) of an FP64 value for the SSA: hi = (float)d, lo = (float)(d - hi); for an
+// FP64 SSA the value itself and 0.
+__device__ __forceinline__ void stage_pair(float *st, int ihi, int ilo, double d) {
+    const float hi = (float)d;
+    st[ihi] = hi;
+    st[ilo] = (float)(d - (double)hi);
+}
+__device__ __forceinline__ void stage_pair(double *st, int ihi, int ilo, double d) {
+    st[ihi] = d;
+    st[ilo] = 0.0;
+}
 
 // One phase of the lane program by the kOdeLanes ODE threads (t = 0 .. kOdeLanes-1): thread t runs
 // op t of the phase.  Every warp holds one op kind per phase (P.wkind), so the switch does not
 // diverge; lanes without an op skip the arithmetic.  Kept out of line: inlined into the engine
 // kernel's loop, its shuffle tree measured 4x slower (2.2k vs 0.5k cycles per SUM phase).
-template <typename T>
+// An op whose output is a per-step SSA value also writes it, in the SSA's precision, to the push
+// staging row (P.sv_stage); the updates of Cai and CaNSR stage them with their FP32 remainders.
+template <typename T, typename R>
 __device__ __noinline__ void ode_phase(const OdeOffsets o, int q, int regime, int t) {
     extern __shared__ __align__(16) unsigned char smem[];
+    R *stage = reinterpret_cast<R *>(smem + o.stage);
     const OdeProgram &P = *reinterpret_cast<const OdeProgram *>(smem + o.prog);
     T *X = reinterpret_cast<T *>(smem + o.x);
     OdeShared &os = *reinterpret_cast<OdeShared *>(smem + o.ode);
@@ -206,6 +221,8 @@ __device__ __noinline__ void ode_phase(const OdeOffsets o, int q, int regime, in
             const double ng = g[out] + (double)GW_ARG(0);
             g[out] = ng;
             X[XS_G + out] = (T)ng;
+            if (out == 3) stage_pair(stage, SV_CAI, SV_CAI_LO, ng);
+            if (out == 4) stage_pair(stage, SV_CANSR, SV_CANSR_LO, ng);
             if (!finite_bits(ng)) atomicCAS(&os.status, 0, (int)GW_ERR_NONFINITE);  // first error of the cell
             return;
         }
@@ -220,11 +237,20 @@ __device__ __noinline__ void ode_phase(const OdeOffsets o, int q, int regime, in
             const T o = __shfl_down_sync(0xffffffffu, v, off);
             if (kind == OK_SUM && (lane & wm) + off <= wm && (lane & (2 * off - 1)) == 0) v += o;
         }
-        if (kind == OK_SUM && (lane & wm) == 0) X[out] = GW_ARG(0) * GW_ARG(1) * v;
+        if (kind == OK_SUM && (lane & wm) == 0) {
+            const T r = GW_ARG(0) * GW_ARG(1) * v;
+            X[out] = r;
+            const int sv = P.sv_stage[b0 + t];
+            if (sv) stage[sv - 1] = (R)r;
+        }
         return;
     }
 #undef GW_ARG
-    if (kind != OK_NOP) X[out] = v;
+    if (kind != OK_NOP) {
+        X[out] = v;
+        const int sv = P.sv_stage[b0 + t];
+        if (sv) stage[sv - 1] = (R)v;
+    }
 }
 
 // Sums {JLCC, ClCh, Jtr, Jxfer} of the cell's CTA partials of one slot; ODE warp w reduces
@@ -261,33 +287,15 @@ __device__ __forceinline__ void reduce_partials(const Partial *slot, int n, int 
     }
 }
 
-// Per-step SSA values of the new state to every CTA of the cell: staged in the leader's shared
-// memory by threads 0..kSvCount-1, then pushed in 16-byte words (CTA, word) by all kOdeLanes
-// threads.  Every staging lane takes the same conversions (FP64 -> FP32 and the FP32 remainder of
-// Cai and CaNSR): divergent FP64 conversions would run one branch after another.
-template <bool FP64, typename T>
-__device__ __forceinline__ void push_sv(const OdeProgram &P, const T *X, const double *g, void *svbuf, void *stage,
-                                        int slot, const CtaWork &w, int t) {
+// Per-step SSA values of the new state to every CTA of the cell: the staging row (written by the
+// ops that produce the values, see ode_phase, and visible after the phase's barrier) pushed in
+// 16-byte words (CTA, word) by all kOdeLanes threads.
+template <bool FP64>
+__device__ __forceinline__ void push_sv(void *svbuf, const void *stage, int slot, const CtaWork &w, int t) {
     using R = typename std::conditional<FP64, double, float>::type;
-    R *st = reinterpret_cast<R *>(stage);
-    if (t < kSvCount) {
-        const bool lo_part = t == SV_CAI_LO || t == SV_CANSR_LO;
-        const int gi = (t == SV_CAI || t == SV_CAI_LO) ? 3 : ((t == SV_CANSR || t == SV_CANSR_LO) ? 4 : -1);
-        const double d = gi >= 0 ? g[gi] : (double)X[P.sv_src[t]];
-        R v;
-        if (FP64) {
-            v = lo_part ? (R)0 : (R)d;
-        } else {
-            const float hi = (float)d;
-            const float lo = (float)(d - (double)hi);
-            v = (R)(lo_part ? lo : hi);
-        }
-        st[t] = v;
-    }
-    ode_bar();
     constexpr int kWords = kSvCount * (int)sizeof(R) / 16;  // 16-byte words of one slot
     static_assert(kSvCount * sizeof(R) % 16 == 0, "sv slot in 16-byte words");
-    const uint4 *src = reinterpret_cast<const uint4 *>(st);
+    const uint4 *src = reinterpret_cast<const uint4 *>(stage);
     uint4 *dst = reinterpret_cast<uint4 *>(reinterpret_cast<R *>(svbuf) + slot * kSvCount);
     const int total = kWords * w.n_cta_cell;
     for (int idx = t; idx < total; idx += kOdeLanes) {
@@ -523,7 +531,7 @@ struct CtaView {
         rtab = reinterpret_cast<float2 *>(smem + L.rtab);
         ctr = reinterpret_cast<int *>(smem + L.ctr);
         tile = reinterpret_cast<TileRec<R> *>(smem + L.tile);
-        off = OdeOffsets{(uint32_t)L.prog, (uint32_t)L.x, (uint32_t)L.ode, (uint32_t)L.math};
+        off = OdeOffsets{(uint32_t)L.prog, (uint32_t)L.x, (uint32_t)L.ode, (uint32_t)L.math, (uint32_t)L.svs};
     }
 };
 
@@ -535,6 +543,7 @@ struct CtaView {
 template <bool FP64, bool ODE64>
 __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
     using T = typename std::conditional<ODE64, double, float>::type;
+    using R = typename std::conditional<FP64, double, float>::type;
     const CtaView<FP64, ODE64> v(a);
     const OdeProgram &P = *v.P;
     OdeShared &os = *v.os;
@@ -573,18 +582,26 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
         }
         for (int i = ot; i < kOdeConstCap; i += kOdeLanes) X[XS_FIRST_FREE + i] = (T)C.ode_consts[i];
         ode_bar();
+        // staging row: the constant SSA values once per launch, Cai and CaNSR of the initial state
+        // (the other values are staged by the phases that compute them)
+        R *stage = reinterpret_cast<R *>(v.svstage);
+        if (ot < kSvCount && ot != SV_CAI && ot != SV_CANSR && ot != SV_CAI_LO && ot != SV_CANSR_LO &&
+            P.sv_src[ot] < XS_FIRST_FREE + kOdeMaxConsts)
+            stage[ot] = (R)X[P.sv_src[ot]];
+        if (ot == 0) stage_pair(stage, SV_CAI, SV_CAI_LO, os.g[3]);
+        if (ot == 1) stage_pair(stage, SV_CANSR, SV_CANSR_LO, os.g[4]);
     }
     // transcendental phases of the initial state, push sv[0]
     {
         const int reg = v_regime(os.g[0]);
         for (int q = P.upd_phase + 1; q <= P.push_phase; ++q) {
-            ode_phase<T>(v.off, q, reg, ot);
+            ode_phase<T, R>(v.off, q, reg, ot);
             ode_bar();
         }
-        push_sv<FP64, T>(P, X, os.g, v.svbuf, v.svstage, 0, v.w, ot);
+        push_sv<FP64>(v.svbuf, v.svstage, 0, v.w, ot);
         cluster_arrive();
         for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
-            ode_phase<T>(v.off, q, reg, ot);
+            ode_phase<T, R>(v.off, q, reg, ot);
             ode_bar();
         }
     }
@@ -603,7 +620,7 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
         ode_bar();
         const int reg_n = v_regime(os.g[0]);
         for (int q = 0; q <= P.upd_phase; ++q) {
-            ode_phase<T>(v.off, q, reg_n, ot);
+            ode_phase<T, R>(v.off, q, reg_n, ot);
             ode_bar();
         }
         if (ot == 0) os.t += a.dt;
@@ -614,14 +631,14 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
         }
         const int reg = v_regime(os.g[0]);
         for (int q = P.upd_phase + 1; q <= P.push_phase; ++q) {
-            ode_phase<T>(v.off, q, reg, ot);
+            ode_phase<T, R>(v.off, q, reg, ot);
             ode_bar();
         }
-        push_sv<FP64, T>(P, X, os.g, v.svbuf, v.svstage, par ^ 1, v.w, ot);
+        push_sv<FP64>(v.svbuf, v.svstage, par ^ 1, v.w, ot);
         cluster_arrive();
         // off the critical path: the phases the SSA does not need
         for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
-            ode_phase<T>(v.off, q, reg, ot);
+            ode_phase<T, R>(v.off, q, reg, ot);
             ode_bar();
         }
     }

@@ -540,6 +540,24 @@ bool ode_program_build(const CellStatic &cs, bool pow_fast, OdeProgram *prog, do
     prog->const_begin = XS_FIRST_FREE;
     prog->n_consts = v[0].nconst;
     for (int i = 0; i < kSvCount; ++i) prog->sv_src[i] = v[0].sv_src[i];
+    // The ops whose outputs are per-step SSA values stage them for the push themselves (Cai and
+    // CaNSR are staged by their updates, constant values once per launch).
+    for (int i = 0; i < kSvCount; ++i) {
+        if (i == SV_CAI || i == SV_CANSR || i == SV_CAI_LO || i == SV_CANSR_LO) continue;
+        const int src = prog->sv_src[i];
+        if (src < XS_FIRST_FREE + kOdeMaxConsts) continue;  // fixed or constant slot
+        for (int j = 0; j < n; ++j) {
+            const bool writes = prog->ops[j].kind != OK_NOP && prog->ops[j].out == src;
+            const bool alt_writes = prog->alt_idx[j] != 255 && (prog->alt[0][prog->alt_idx[j]].out == src ||
+                                                                prog->alt[1][prog->alt_idx[j]].out == src);
+            if (!writes && !alt_writes) continue;
+            if (prog->sv_stage[j] != 0 && prog->sv_stage[j] != i + 1) {
+                fprintf(stderr, "ode program: slot %d staged to two sv values\n", src);
+                return false;
+            }
+            prog->sv_stage[j] = (uint8_t)(i + 1);
+        }
+    }
     return true;
 }
 

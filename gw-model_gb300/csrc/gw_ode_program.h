@@ -59,7 +59,7 @@ enum OdeSlot : uint16_t {
 };
 
 // Per-step SSA values pushed to the CTAs (sv[]) that come from the program, by sv index.
-struct OdeProgram {
+struct alignas(16) OdeProgram {
     int n_phases;
     int phase_begin[kOdeMaxPhases + 1];  // ops [phase_begin[p], phase_begin[p+1]) of phase p (<= 128)
     int upd_phase;                       // phase holding the OK_UPD ops
@@ -70,9 +70,11 @@ struct OdeProgram {
     uint16_t sv_src[kSvCount];           // X slot of each sv value (XS_ZERO if not produced)
     uint8_t wkind[kOdeMaxPhases][kOdeWarps];  // the one op kind of each warp in each phase (NOP: idle)
     uint8_t alt_idx[kOdeMaxOps];         // 255, or index of the op's variant in alt[regime-1]
+    uint8_t sv_stage[kOdeMaxOps];        // 1 + the sv index an op's output is staged to for the push, or 0
     OdeOp ops[kOdeMaxOps];               // regime 0: V >= -40
     OdeOp alt[2][kOdeMaxAlt];            // regime 1: V < -40;  regime 2: V == -47.13
 };
+static_assert(sizeof(OdeProgram) % 16 == 0, "OdeProgram is copied in 16-byte words");
 
 // Builds the program shared by all cells (pow_fast: all cells have Hf == Hr == 0.75, so the
 // Jup powers are taken with square roots) and the per-cell constant values.
