@@ -108,9 +108,12 @@ def test_fp64_cell_index_keys_the_stream(oracle):
 
 
 @pytest.mark.parametrize("shape", [dict(cluster_ctas=1), dict(cluster_ctas=4, cta_crus=64),
-                                   dict(cluster_ctas=8, cta_crus=32), dict(steps_per_launch=7)])
+                                   dict(cluster_ctas=8, cta_crus=32), dict(steps_per_launch=7),
+                                   dict(cluster_ctas=3, cta_crus=96), dict(cluster_ctas=6, cta_crus=40),
+                                   dict(cluster_ctas=9, cta_crus=32)])
 def test_fp64_launch_shape_independent(oracle, shape):
-    """Different CTA tiles, cluster sizes and launch lengths give the oracle's trajectory."""
+    """Different CTA tiles, cluster sizes (including the 3, 6 and 9 the autotuner uses to fill a
+    GPC) and launch lengths give the oracle's trajectory."""
     m, (g, s, _) = run_pair(oracle, 200, 1500, 4, "fp64", **shape)
     for k in CHANNELS:
         np.testing.assert_array_equal(getattr(s, k), getattr(m.crus(), k))
