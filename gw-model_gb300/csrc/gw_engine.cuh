@@ -7,9 +7,9 @@
 //   SSA warps : each warp owns a contiguous range of the CTA's CRU tile and runs the SSA of step
 //               s on it with the values sv[s&1], one CRU per lane at a time; a lane whose CRU has
 //               finished its step takes the warp's next CRU, so lanes with pending SSA events do
-//               not hold the others back.  Each warp stores one flux partial; the warp that
-//               finishes last sums them in warp order and pushes the CTA's partial into the
-//               leader's shared memory (DSMEM).  In a leader CTA the warp that finishes first
+//               not hold the others back.  Each warp stores one flux partial; after a barrier
+//               of the CTA's SSA warps, warp 0 sums them in warp order and pushes the CTA's
+//               partial into the leader's shared memory (DSMEM).  In a leader CTA the warp that finishes first
 //               also evaluates the stimulus of step s+1 for the ODE warps.
 //   ODE warps : reduce the CTA partials of step s-1, increments and Euler update (globals
 //               s -> s+1), transcendental phases of the new state, push sv[(s+1)&1], arrive; the
@@ -745,15 +745,12 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
             // Records of this step, from the warp's part of the tile (now at the end of the step)
             if (rec_ok && (cell == a.tr_cell || a.tr_sums != nullptr))
                 record_pass<R>(a, w, cell, r_idx, beg, end, lane, tile);
-            // Warp partial; the warp that finishes last sums the warp partials in warp order
-            // and pushes the CTA's partial to the leader.
+            // Warp partial.
             const Partial pv = acc.warp_total();
             int done = 0;
             if (lane == 0) {
                 v.chunkp[warp] = pv;
-                __threadfence_block();
-                done = atomicAdd(&ctr[2 + par], 1);
-                __threadfence_block();
+                done = atomicAdd(&ctr[2 + par], 1);  // the order of finishing (first warp below)
             }
             done = __shfl_sync(0xffffffffu, done, 0);
             if (v.leader && done == 0 && lane == 0) {
@@ -764,8 +761,10 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
                 os.tstim += a.dt;
                 os.stim[par ^ 1] = stimulus(a.dyn[cell], os.tstim, ri + 1);
             }
-            if (done == nsw - 1) {
-                __syncwarp();
+            // The CTA partial: the warp partials, ordered by the SSA warps' barrier, summed in warp
+            // order by warp 0 and pushed to the leader.
+            ssa_bar(n_ssa);
+            if (warp == 0) {
                 FluxAcc<FP64> tot;
                 if (lane < nsw) tot.add_partial(v.chunkp[lane]);
                 const Partial pc = tot.warp_total_compensated();
