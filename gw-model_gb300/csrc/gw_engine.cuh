@@ -7,11 +7,10 @@
 //   SSA warps : each warp owns a contiguous range of the CTA's CRU tile and runs the SSA of step
 //               s on it with the values sv[s&1], one CRU per lane at a time; a lane whose CRU has
 //               finished its step takes the warp's next CRU, so lanes with pending SSA events do
-//               not hold the others back.  Each warp stores one flux partial; after a barrier
-//               of the CTA's SSA warps, warp 0 sums them in warp order and pushes the CTA's
-//               partial into the leader's shared memory (DSMEM).  In a leader CTA the warp that finishes first
-//               also evaluates the stimulus of step s+1 for the ODE warps.
-//   ODE warps : reduce the CTA partials of step s-1, increments and Euler update (globals
+//               not hold the others back.  Each warp pushes its flux partial into its slot in
+//               the leader's shared memory (DSMEM).  In a leader CTA the warp that finishes
+//               first also evaluates the stimulus of step s+1 for the ODE warps.
+//   ODE warps : reduce the warp partials of step s-1, increments and Euler update (globals
 //               s -> s+1), transcendental phases of the new state, push sv[(s+1)&1], arrive; the
 //               phases that the SSA does not need (general Jup exponents) run after the arrive.
 #pragma once
@@ -46,7 +45,7 @@ constexpr int kMaxThreads = 512;  // SSA warps + ODE warps per CTA (128 register
 constexpr int kMaxWarps = kMaxThreads / 32;
 
 struct SmemLayout {
-    size_t cc, sv, ode, prog, x, math, svs, rtab, part, chunk, ctr, tile, total;
+    size_t cc, sv, ode, prog, x, math, svs, rtab, part, ctr, tile, total;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -71,10 +70,8 @@ __host__ __device__ inline SmemLayout smem_layout(int tile_cap, int max_cta_cell
     o += align16(kSvCount * sizeof(R));
     L.rtab = o;  // the CTA's subunit rate table (FP32 SSA)
     o += align16((size_t)kRateTab * sizeof(float2));
-    L.part = o;  // [parity][rank in cell]: CTA partials (written by remote CTAs)
-    o += align16((size_t)2 * max_cta_cell * sizeof(Partial));
-    L.chunk = o;  // [warp]: warp partials of this CTA
-    o += align16((size_t)kMaxWarps * sizeof(Partial));
+    L.part = o;  // [parity][rank in cell][warp]: warp partials (written by the cell's CTAs)
+    o += align16((size_t)2 * max_cta_cell * kMaxWarps * sizeof(Partial));
     L.ctr = o;   // warp completion counters [2 + parity]
     o += 16;
     L.tile = o;  // TileRec<R> per CRU
@@ -400,8 +397,8 @@ struct FluxAcc {
     double dj = 0, dx = 0, dtr = 0;                       // FP64
     int acl = 0;
     // FP32: a lane's own CRUs (one to a few per step) add up in FP32, the lane sums in a plain
-    // FP32 tree (warp_total); the warp partials of a CTA and the CTA partials of a cell are then
-    // combined with compensation (add_partial, warp_total_compensated, reduce_partials).
+    // FP32 tree (warp_total); the cell's warp partials are then combined with compensation
+    // (reduce_partials).
     __device__ __forceinline__ void add(float j, float x, float t, int cl) {
         jh += j;
         xh += x;
@@ -413,41 +410,6 @@ struct FluxAcc {
         dx += x;
         dtr += t;
         acl += cl;
-    }
-    __device__ __forceinline__ void add_partial(const Partial &p) {
-        if (FP64) {
-            dj += p.v[0];
-            dx += p.v[1];
-            dtr += p.v[2];
-            acl += (int)p.v[3];
-        } else {
-            const float *f = reinterpret_cast<const float *>(p.v);
-            df_add(jh, jl, f[0], f[1]);
-            df_add(xh, xl, f[2], f[3]);
-            df_add(th, tl, f[4], f[5]);
-            acl += (int)f[6];
-        }
-    }
-    // The compensated warp sum of (hi, lo) pairs (FP32), for the CTA partial from the warp
-    // partials; FP64 as warp_total.
-    __device__ __forceinline__ Partial warp_total_compensated() {
-        if (FP64) return warp_total();
-        Partial pv;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float a0 = __shfl_xor_sync(0xffffffffu, jh, o), a1 = __shfl_xor_sync(0xffffffffu, jl, o);
-            const float b0 = __shfl_xor_sync(0xffffffffu, xh, o), b1 = __shfl_xor_sync(0xffffffffu, xl, o);
-            const float c0 = __shfl_xor_sync(0xffffffffu, th, o), c1 = __shfl_xor_sync(0xffffffffu, tl, o);
-            acl += __shfl_xor_sync(0xffffffffu, acl, o);
-            df_add(jh, jl, a0, a1);
-            df_add(xh, xl, b0, b1);
-            df_add(th, tl, c0, c1);
-        }
-        float *f = reinterpret_cast<float *>(pv.v);
-        f[0] = jh; f[1] = jl; f[2] = xh; f[3] = xl; f[4] = th; f[5] = tl;
-        f[6] = (float)acl;
-        f[7] = 0.f;
-        return pv;
     }
     __device__ __forceinline__ Partial warp_total() {
         Partial pv;
@@ -501,7 +463,7 @@ struct CtaView {
     T *X;
     math64::Tables *M;
     void *svstage;
-    Partial *part, *chunkp;
+    Partial *part;
     float2 *rtab;
     int *ctr;
     TileRec<R> *tile;
@@ -527,7 +489,6 @@ struct CtaView {
         M = reinterpret_cast<math64::Tables *>(smem + L.math);
         svstage = smem + L.svs;
         part = reinterpret_cast<Partial *>(smem + L.part);
-        chunkp = reinterpret_cast<Partial *>(smem + L.chunk);  // warp partials
         rtab = reinterpret_cast<float2 *>(smem + L.rtab);
         ctr = reinterpret_cast<int *>(smem + L.ctr);
         tile = reinterpret_cast<TileRec<R> *>(smem + L.tile);
@@ -550,7 +511,7 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
     T *X = v.X;
     const math64::Tables &M = *v.M;
     const int ot = v.ot, lane = v.lane, cell = v.w.cell;
-    const int pslot = a.max_cta_cell;
+    const int pslot = a.max_cta_cell * kMaxWarps;  // warp partials per parity slot
     {
         // program, constants and state of the cell
         const int4 *src = reinterpret_cast<const int4 *>(a.prog);
@@ -615,7 +576,7 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
         // fluxes of step s-1 (or the carry), then the global step s -> s+1
         if (ot == 0 && (not_positive(os.g[1]) || not_positive(os.g[2])) && os.status == 0)
             os.status = GW_ERR_NERNST;
-        if (s > 0) reduce_partials<FP64, T>(v.part + (par ^ 1) * pslot, v.w.n_cta_cell, ot >> 5, lane, os.sums, X);
+        if (s > 0) reduce_partials<FP64, T>(v.part + (par ^ 1) * pslot, v.w.n_cta_cell * kMaxWarps, ot >> 5, lane, os.sums, X);
         if (s > 0 && ot == 0) X[XS_ISTIM] = (T)os.stim[par];
         ode_bar();
         const int reg_n = v_regime(os.g[0]);
@@ -645,7 +606,7 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
     cluster_wait();
     // carry of the last step's fluxes, globals and counters back to the cell block
     if (a.n_steps > 0)
-        reduce_partials<FP64, T>(v.part + ((a.n_steps - 1) & 1) * pslot, v.w.n_cta_cell, ot >> 5, lane, os.sums, X);
+        reduce_partials<FP64, T>(v.part + ((a.n_steps - 1) & 1) * pslot, v.w.n_cta_cell * kMaxWarps, ot >> 5, lane, os.sums, X);
     ode_bar();
     CellDyn &d = a.dyn[cell];
     for (int i = ot; i < kNumGlobals; i += kOdeLanes) d.g[i] = os.g[i];
@@ -674,7 +635,7 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
     const SsaConsts<R> &cc = *v.cc;
     TileRec<R> *tile = v.tile;
     int *ctr = v.ctr;
-    const int pslot = a.max_cta_cell;
+    const int pslot = a.max_cta_cell * kMaxWarps;  // warp partials per parity slot
     const R dt = (R)a.dt;
     unsigned long long my_events = 0;
     int my_err = 0;
@@ -697,11 +658,6 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
                 // warps meet at named barrier 2 (they leave the cluster barrier together).
                 for (int e = (int)threadIdx.x; e < kRateTab; e += n_ssa) build_rate_entry<R>(v.rtab, cc, sv, e);
                 ssa_bar(n_ssa);
-            }
-            if (w.cru_count == 0 && threadIdx.x == 0) {
-                Partial *dst = v.part + par * pslot + w.rank_in_cell;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) st_remote(map_rank(&dst->v[q], (uint32_t)w.first), 0.0);
             }
             // This warp's CRUs [cursor, end).  A lane whose CRU has finished its step takes the
             // next one, so lanes with pending SSA events do not hold the others back.
@@ -745,11 +701,15 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
             // Records of this step, from the warp's part of the tile (now at the end of the step)
             if (rec_ok && (cell == a.tr_cell || a.tr_sums != nullptr))
                 record_pass<R>(a, w, cell, r_idx, beg, end, lane, tile);
-            // Warp partial.
+            // The warp partial, pushed straight into the leader's slot (rank, warp): the leader
+            // sums the cell's warp partials in slot order (no reduction on this side of the
+            // barrier).
             const Partial pv = acc.warp_total();
             int done = 0;
             if (lane == 0) {
-                v.chunkp[warp] = pv;
+                Partial *dst = v.part + par * pslot + w.rank_in_cell * kMaxWarps + warp;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) st_remote(map_rank(&dst->v[q], (uint32_t)w.first), pv.v[q]);
                 done = atomicAdd(&ctr[2 + par], 1);  // the order of finishing (first warp below)
             }
             done = __shfl_sync(0xffffffffu, done, 0);
@@ -760,19 +720,6 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
                 OdeShared &os = *v.os;
                 os.tstim += a.dt;
                 os.stim[par ^ 1] = stimulus(a.dyn[cell], os.tstim, ri + 1);
-            }
-            // The CTA partial: the warp partials, ordered by the SSA warps' barrier, summed in warp
-            // order by warp 0 and pushed to the leader.
-            ssa_bar(n_ssa);
-            if (warp == 0) {
-                FluxAcc<FP64> tot;
-                if (lane < nsw) tot.add_partial(v.chunkp[lane]);
-                const Partial pc = tot.warp_total_compensated();
-                if (lane == 0) {
-                    Partial *dst = v.part + par * pslot + w.rank_in_cell;
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) st_remote(map_rank(&dst->v[q], (uint32_t)w.first), pc.v[q]);
-                }
             }
         }
         cluster_arrive();
@@ -829,6 +776,13 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const __grid_con
             load_ssa_consts<R>(*v.cc, a.cs[cell]);
             v.ctr[0] = v.ctr[1] = v.ctr[2] = v.ctr[3] = 0;
             if (v.leader) v.os->tstim = a.dyn[cell].t;
+        }
+        // The leader's warp-partial slots start at zero (slots of warps a CTA does not have stay
+        // so); the cell's CTAs write them only after the first cluster barrier of the steps.
+        if (v.leader) {
+            double *pz = &v.part[0].v[0];
+            const int nz = 2 * a.max_cta_cell * kMaxWarps * 4;
+            for (int i = (int)threadIdx.x; i < nz; i += (int)blockDim.x) pz[i] = 0.0;
         }
         step0 = a.dyn[cell].step;
         if (!v.ode_thread) {
