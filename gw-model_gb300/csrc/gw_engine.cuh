@@ -211,34 +211,38 @@ __device__ __noinline__ void ode_phase(const OdeOffsets o, int q, int regime, in
             break;
         case OK_PROD: v = GW_ARG(0) * GW_ARG(1) * GW_ARG(2) * GW_ARG(3) * GW_ARG(4) * GW_ARG(5) * GW_ARG(6); break;
         case OK_SUM:
+        case OK_SUMU:
             v = GW_ARG(2) * GW_ARG(3) * GW_ARG(4) + GW_ARG(5) * GW_ARG(6) * GW_ARG(7) + GW_ARG(8) * GW_ARG(9) * GW_ARG(10) +
                 GW_ARG(11) * GW_ARG(12) * GW_ARG(13);
             break;
-        case OK_UPD: {
-            const double ng = g[out] + (double)GW_ARG(0);
-            g[out] = ng;
-            X[XS_G + out] = (T)ng;
-            if (out == 3) stage_pair(stage, SV_CAI, SV_CAI_LO, ng);
-            if (out == 4) stage_pair(stage, SV_CANSR, SV_CANSR_LO, ng);
-            if (!finite_bits(ng)) atomicCAS(&os.status, 0, (int)GW_ERR_NONFINITE);  // first error of the cell
-            return;
-        }
         default: break;
         }
     }
-    if (wk == OK_SUM) {
+    if (wk == OK_SUM || wk == OK_SUMU) {
         // rows of `width` lanes (a power of two, rows aligned to it): tree over offsets 1, 2, 4
-        const int wm = kind == OK_SUM ? (int)((w0.x >> 8) & 0xFFu) - 1 : 0;
+        const bool row = kind == OK_SUM || kind == OK_SUMU;
+        const int wm = row ? (int)((w0.x >> 8) & 0xFFu) - 1 : 0;
 #pragma unroll
         for (int off = 1; off < 8; off <<= 1) {
             const T o = __shfl_down_sync(0xffffffffu, v, off);
-            if (kind == OK_SUM && (lane & wm) + off <= wm && (lane & (2 * off - 1)) == 0) v += o;
+            if (row && (lane & wm) + off <= wm && (lane & (2 * off - 1)) == 0) v += o;
         }
-        if (kind == OK_SUM && (lane & wm) == 0) {
+        if (row && (lane & wm) == 0) {
             const T r = GW_ARG(0) * GW_ARG(1) * v;
-            X[out] = r;
-            const int sv = P.sv_stage[b0 + t];
-            if (sv) stage[sv - 1] = (R)r;
+            if (kind == OK_SUMU) {
+                // Euler update of global `out` (FP64 state); every row of the phase reads the old
+                // values at XS_G, the new one goes to XS_GN for the phases that follow
+                const double ng = g[out] + (double)r;
+                g[out] = ng;
+                X[XS_GN + out] = (T)ng;
+                if (out == 3) stage_pair(stage, SV_CAI, SV_CAI_LO, ng);
+                if (out == 4) stage_pair(stage, SV_CANSR, SV_CANSR_LO, ng);
+                if (!finite_bits(ng)) atomicCAS(&os.status, 0, (int)GW_ERR_NONFINITE);  // first error of the cell
+            } else {
+                X[out] = r;
+                const int sv = P.sv_stage[b0 + t];
+                if (sv) stage[sv - 1] = (R)r;
+            }
         }
         return;
     }
@@ -539,7 +543,7 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
         }
         for (int i = ot; i < kNumGlobals; i += kOdeLanes) {
             os.g[i] = d.g[i];
-            X[XS_G + i] = (T)d.g[i];
+            X[XS_G + i] = X[XS_GN + i] = (T)d.g[i];
         }
         for (int i = ot; i < kOdeConstCap; i += kOdeLanes) X[XS_FIRST_FREE + i] = (T)C.ode_consts[i];
         ode_bar();
@@ -595,6 +599,9 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
             ode_phase<T, R>(v.off, q, reg, ot);
             ode_bar();
         }
+        // the new globals become the old ones of the next step's increments (read after the
+        // next step's first barrier; no phase after this point reads XS_G)
+        if (ot < kNumGlobals) X[XS_G + ot] = X[XS_GN + ot];
         push_sv<FP64>(v.svbuf, v.svstage, par ^ 1, v.w, ot);
         cluster_arrive();
         // off the critical path: the phases the SSA does not need

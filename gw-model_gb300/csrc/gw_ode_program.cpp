@@ -4,8 +4,9 @@
 // (update_V_and_concentration_derivatives GW.tpp:171-212, update_QKr/QKv GW.tpp:26-44/65-123,
 // update_*_derivatives GW.tpp:127-168, the currents of common.hpp:70-218 and GW_utils.hpp:273-375,
 // and the per-step constants of GW_model::SSA GW.tpp:216-221), rearranged into
-//   phase E  SUM  : increments of the 36 globals (linear combinations of current / rate terms)
-//   phase F  UPD  : Euler update g += dg (FP64)
+//   phase E  SUMU : increments of the 36 globals (linear combinations of current / rate terms)
+//                   and the Euler update g += dg (FP64) by each row's first lane; the rows read
+//                   the old globals (X[XS_G]), the new ones go to X[XS_GN]
 //   phase A  LOG | EXP | SQRT : transcendental terms of the new globals
 //   phase B  AFF | REC | PROD | SQRT : reversal-potential differences, reciprocals, LCC rate table
 //   phase C  PROD | REC | SUM | EXP : current terms, inactivation rates, JLCC factors
@@ -61,7 +62,12 @@ struct Builder {
         return s;
     }
     uint16_t S() { return (uint16_t)next++; }
-    static uint16_t G(int i) { return (uint16_t)(XS_G + i); }
+    // Global i as read by the phase being built: the updated value (XS_GN) in the phases after
+    // the update, the old value (XS_G) in the increments.
+    bool post = true;
+    uint16_t G(int i) const { return (uint16_t)((post ? XS_GN : XS_G) + i); }
+    // increments emit OK_SUMU rows (out = global index) instead of OK_SUM
+    bool upd_rows = false;
 
     void phase(int n) {
         ph.assign(n, {});
@@ -96,7 +102,7 @@ struct Builder {
         while (v.size() % width != 0) v.push_back(OdeOp{OK_NOP, 1, 0, {}});
         for (int l = 0; l < width; ++l) {
             OdeOp op{};
-            op.kind = OK_SUM;
+            op.kind = upd_rows ? OK_SUMU : OK_SUM;
             op.width = (uint8_t)width;
             op.out = out;
             op.a[0] = s0;
@@ -149,8 +155,6 @@ void build(Builder &b) {
                    T_IKp = S(), T_ICab = S(), T_IpCa = S(), T_dL1 = S(), T_dL2 = S(), T_dH1 = S(), T_dH2 = S(),
                    T_am = S(), T_aj1 = S(), T_aj2 = S(), T_bj = S(), T_t1 = S(), T_t2 = S(), Q42 = S(),
                    JMUL = S(), beta = S(), rJup = S(), INACT0 = S(), INACT1 = S();
-    uint16_t dG[kNumGlobals];
-    for (auto &x : dG) x = S();
 
     const double RT_F = C.RT_F, F_RT = C.F_RT;
     // ---------------- phase A: LOG | EXP | SQRT ----------------
@@ -355,7 +359,9 @@ void build(Builder &b) {
     }
     // ---------------- phase C2: general Jup exponents ----------------
     if (!b.fast) b.emit(PH_C2, OK_REC, rJup, {ONE, ONE, pf, ONE, pr});
-    // ---------------- phase E: increments (SUM rows) ----------------
+    // ---------------- phase E: increments and update (OK_SUMU rows) ----------------
+    b.post = false;
+    b.upd_rows = true;
     {
         const int q = PH_E;
         using T = Builder::Term;
@@ -363,7 +369,7 @@ void build(Builder &b) {
         const double CSA = C.CSA_FVcyto;
         const uint16_t cGK1 = b.K(p.GK1 * C.IK1_const), cmGK1 = b.K(-p.GK1 * C.IK1_const);
         // dV (GW.tpp:211)
-        b.sum_row(q, dG[iV], DT, ONE,
+        b.sum_row(q, (uint16_t)(iV), DT, ONE,
                   {{ONE, XS_ISTIM, ONE}, {MONE, T_INa, ONE}, {b.K(-C.ICaL_const), SJLCC, ONE},
                    {MONE, T_IKr, ONE}, {MONE, T_IKs, ONE}, {MONE, T_Kv14a, ONE}, {ONE, T_Kv14b, ONE},
                    {MONE, T_Kv43, ONE}, {cmGK1, rK1, VmEK}, {MONE, T_IKp, ONE}, {MONE, P_Ito2a, SClCh},
@@ -371,46 +377,46 @@ void build(Builder &b) {
                    {ONE, T_NaCa2, ONE}, {MONE, T_IpCa, ONE}, {MONE, T_ICab, ONE}, {MONE, T_INab, ONE}});
         const uint16_t cmCSA = b.K(-CSA);
         // dNai, dKi (GW.tpp:201-202)
-        b.sum_row(q, dG[iNai], DT, cmCSA,
+        b.sum_row(q, (uint16_t)(iNai), DT, cmCSA,
                   {{ONE, T_INa, ONE}, {ONE, T_INab, ONE}, {b.K(3.0), T_NaCa1, ONE}, {b.K(-3.0), T_NaCa2, ONE},
                    {b.K(3.0 * C.INaK_const), P_NaK, ONE}});
-        b.sum_row(q, dG[iKi], DT, cmCSA,
+        b.sum_row(q, (uint16_t)(iKi), DT, cmCSA,
                   {{ONE, T_IKr, ONE}, {ONE, T_IKs, ONE}, {ONE, T_Kv14a, ONE}, {MONE, T_Kv14b, ONE},
                    {ONE, T_Kv43, ONE}, {cGK1, rK1, VmEK}, {ONE, T_IKp, ONE}, {b.K(-2.0 * C.INaK_const), P_NaK, ONE}});
         // dCai, dCaNSR (GW.tpp:203-204)
-        b.sum_row(q, dG[iCai], DT, beta,
+        b.sum_row(q, (uint16_t)(iCai), DT, beta,
                   {{b.K(-0.5 * CSA), T_ICab, ONE}, {b.K(-0.5 * CSA), T_IpCa, ONE}, {b.K(CSA), T_NaCa1, ONE},
                    {b.K(-CSA), T_NaCa2, ONE}, {b.K(C.VSS_Vcyto * C.CRU_factor), SJxfer, ONE},
                    {b.K(-p.Vmaxf), rJup, pf}, {b.K(p.Vmaxr), rJup, pr}, {MONE, T_dL1, ONE}, {ONE, T_dL2, ONE},
                    {MONE, T_dH1, ONE}, {ONE, T_dH2, ONE}});
-        b.sum_row(q, dG[iCaNSR], DT, ONE,
+        b.sum_row(q, (uint16_t)(iCaNSR), DT, ONE,
                   {{b.K(C.Vcyto_VNSR * p.Vmaxf), rJup, pf}, {b.K(-C.Vcyto_VNSR * p.Vmaxr), rJup, pr},
                    {b.K(-C.VJSR_VNSR * C.CRU_factor), SJtr, ONE}});
-        b.sum_row(q, dG[iCaL], DT, ONE, {{ONE, T_dL1, ONE}, {MONE, T_dL2, ONE}});
-        b.sum_row(q, dG[iCaH], DT, ONE, {{ONE, T_dH1, ONE}, {MONE, T_dH2, ONE}});
+        b.sum_row(q, (uint16_t)(iCaL), DT, ONE, {{ONE, T_dL1, ONE}, {MONE, T_dL2, ONE}});
+        b.sum_row(q, (uint16_t)(iCaH), DT, ONE, {{ONE, T_dH1, ONE}, {MONE, T_dH2, ONE}});
         // gates (GW.tpp:163-168)
-        b.sum_row(q, dG[im], DT, ONE, {{ONE, T_am, ONE}, {MONE, T_am, b.G(im)}, {MONE, E_bm, b.G(im)}});
+        b.sum_row(q, (uint16_t)(im), DT, ONE, {{ONE, T_am, ONE}, {MONE, T_am, b.G(im)}, {MONE, E_bm, b.G(im)}});
         const uint16_t cbh = b.K(-1.0 / 0.13);
         if (r0)
-            b.sum_row(q, dG[ih], DT, ONE, {{cbh, rbh, b.G(ih)}});
+            b.sum_row(q, (uint16_t)(ih), DT, ONE, {{cbh, rbh, b.G(ih)}});
         else
-            b.sum_row(q, dG[ih], DT, ONE,
+            b.sum_row(q, (uint16_t)(ih), DT, ONE,
                       {{ONE, E_ah, ONE}, {MONE, E_ah, b.G(ih)}, {MONE, E_bh1, b.G(ih)}, {MONE, E_bh2, b.G(ih)}});
-        b.sum_row(q, dG[ij], DT, ONE,
+        b.sum_row(q, (uint16_t)(ij), DT, ONE,
                   {{ONE, T_aj1, ONE}, {ONE, T_aj2, ONE}, {MONE, T_aj1, b.G(ij)}, {MONE, T_aj2, b.G(ij)},
                    {MONE, T_bj, b.G(ij)}});
-        b.sum_row(q, dG[ixKs], DT, ONE,
+        b.sum_row(q, (uint16_t)(ixKs), DT, ONE,
                   {{ONE, T_t1, rxinf}, {ONE, T_t2, rxinf}, {MONE, T_t1, b.G(ixKs)}, {MONE, T_t2, b.G(ixKs)}});
         // IKr Markov chain (update_QKr + update_Kr_derivatives)
         const uint16_t cKf = b.K(p.Kf), cKb = b.K(p.Kb), cmKf = b.K(-p.Kf), cmKb = b.K(-p.Kb);
         auto kr = [&](int i) { return b.G(iKr + i); };
-        b.sum_row(q, dG[iKr + 0], DT, ONE, {{ONE, Q10, kr(1)}, {MONE, Q01, kr(0)}});
-        b.sum_row(q, dG[iKr + 1], DT, ONE, {{ONE, Q01, kr(0)}, {cKb, kr(2), ONE}, {MONE, Q10, kr(1)}, {cmKf, kr(1), ONE}});
-        b.sum_row(q, dG[iKr + 2], DT, ONE,
+        b.sum_row(q, (uint16_t)(iKr + 0), DT, ONE, {{ONE, Q10, kr(1)}, {MONE, Q01, kr(0)}});
+        b.sum_row(q, (uint16_t)(iKr + 1), DT, ONE, {{ONE, Q01, kr(0)}, {cKb, kr(2), ONE}, {MONE, Q10, kr(1)}, {cmKf, kr(1), ONE}});
+        b.sum_row(q, (uint16_t)(iKr + 2), DT, ONE,
                   {{cKf, kr(1), ONE}, {ONE, Q32, kr(3)}, {ONE, Q42, kr(4)}, {cmKb, kr(2), ONE},
                    {MONE, Q23, kr(2)}, {MONE, Q24, kr(2)}});
-        b.sum_row(q, dG[iKr + 3], DT, ONE, {{ONE, Q23, kr(2)}, {ONE, Q43, kr(4)}, {MONE, Q32, kr(3)}, {MONE, Q34, kr(3)}});
-        b.sum_row(q, dG[iKr + 4], DT, ONE, {{ONE, Q24, kr(2)}, {ONE, Q34, kr(3)}, {MONE, Q42, kr(4)}, {MONE, Q43, kr(4)}});
+        b.sum_row(q, (uint16_t)(iKr + 3), DT, ONE, {{ONE, Q23, kr(2)}, {ONE, Q43, kr(4)}, {MONE, Q32, kr(3)}, {MONE, Q34, kr(3)}});
+        b.sum_row(q, (uint16_t)(iKr + 4), DT, ONE, {{ONE, Q24, kr(2)}, {ONE, Q34, kr(3)}, {MONE, Q42, kr(4)}, {MONE, Q43, kr(4)}});
         // Kv1.4 and Kv4.3 10-state chains (update_QKv + update_Kv_derivatives)
         for (int ch = 0; ch < 2; ++ch) {
             const int base = ch == 0 ? iKv14 : iKv43;
@@ -422,33 +428,31 @@ void build(Builder &b) {
             auto x = [&](int i) { return b.G(base + i); };
             auto K = [&](double v) { return b.K(v); };
             auto L = [&](double v) { return b.KL(v); };
-            b.sum_row(q, dG[base + 0], DT, ONE, {{ONE, ba, x(1)}, {ONE, ai, x(5)}, {L(-4), aa, x(0)}, {MONE, bi, x(0)}});
-            b.sum_row(q, dG[base + 1], DT, ONE,
+            b.sum_row(q, (uint16_t)(base + 0), DT, ONE, {{ONE, ba, x(1)}, {ONE, ai, x(5)}, {L(-4), aa, x(0)}, {MONE, bi, x(0)}});
+            b.sum_row(q, (uint16_t)(base + 1), DT, ONE,
                       {{L(4), aa, x(0)}, {L(2), ba, x(2)}, {K(1 / b1), ai, x(6)}, {MONE, ba, x(1)}, {L(-3), aa, x(1)},
                        {K(-f1), bi, x(1)}});
-            b.sum_row(q, dG[base + 2], DT, ONE,
+            b.sum_row(q, (uint16_t)(base + 2), DT, ONE,
                       {{L(3), aa, x(1)}, {L(3), ba, x(3)}, {K(1 / b2), ai, x(7)}, {L(-2), ba, x(2)}, {L(-2), aa, x(2)},
                        {K(-f2), bi, x(2)}});
-            b.sum_row(q, dG[base + 3], DT, ONE,
+            b.sum_row(q, (uint16_t)(base + 3), DT, ONE,
                       {{L(2), aa, x(2)}, {L(4), ba, x(4)}, {K(1 / b3), ai, x(8)}, {L(-3), ba, x(3)}, {MONE, aa, x(3)},
                        {K(-f3), bi, x(3)}});
-            b.sum_row(q, dG[base + 4], DT, ONE, {{ONE, aa, x(3)}, {K(1 / b4), ai, x(9)}, {L(-4), ba, x(4)}, {K(-f4), bi, x(4)}});
-            b.sum_row(q, dG[base + 5], DT, ONE, {{K(1 / f1), ba, x(6)}, {ONE, bi, x(0)}, {K(-4 * b1), aa, x(5)}, {MONE, ai, x(5)}});
-            b.sum_row(q, dG[base + 6], DT, ONE,
+            b.sum_row(q, (uint16_t)(base + 4), DT, ONE, {{ONE, aa, x(3)}, {K(1 / b4), ai, x(9)}, {L(-4), ba, x(4)}, {K(-f4), bi, x(4)}});
+            b.sum_row(q, (uint16_t)(base + 5), DT, ONE, {{K(1 / f1), ba, x(6)}, {ONE, bi, x(0)}, {K(-4 * b1), aa, x(5)}, {MONE, ai, x(5)}});
+            b.sum_row(q, (uint16_t)(base + 6), DT, ONE,
                       {{K(4 * b1), aa, x(5)}, {K(2 * f1 / f2), ba, x(7)}, {K(f1), bi, x(1)}, {K(-1 / f1), ba, x(6)},
                        {K(-3 * b2 / b1), aa, x(6)}, {K(-1 / b1), ai, x(6)}});
-            b.sum_row(q, dG[base + 7], DT, ONE,
+            b.sum_row(q, (uint16_t)(base + 7), DT, ONE,
                       {{K(3 * b2 / b1), aa, x(6)}, {K(3 * f2 / f3), ba, x(8)}, {K(f2), bi, x(2)}, {K(-2 * f1 / f2), ba, x(7)},
                        {K(-2 * b3 / b2), aa, x(7)}, {K(-1 / b2), ai, x(7)}});
-            b.sum_row(q, dG[base + 8], DT, ONE,
+            b.sum_row(q, (uint16_t)(base + 8), DT, ONE,
                       {{K(2 * b3 / b2), aa, x(7)}, {K(4 * f3 / f4), ba, x(9)}, {K(f3), bi, x(3)}, {K(-3 * f2 / f3), ba, x(8)},
                        {K(-b4 / b3), aa, x(8)}, {K(-1 / b3), ai, x(8)}});
-            b.sum_row(q, dG[base + 9], DT, ONE,
+            b.sum_row(q, (uint16_t)(base + 9), DT, ONE,
                       {{K(b4 / b3), aa, x(8)}, {K(f4), bi, x(4)}, {K(-4 * f3 / f4), ba, x(9)}, {K(-1 / b4), ai, x(9)}});
         }
     }
-    // ---------------- phase F: Euler update ----------------
-    for (int i = 0; i < kNumGlobals; ++i) b.emit(PH_F, OK_UPD, (uint16_t)i, {dG[i]});
     // per-step SSA values
     b.sv_src[SV_ZERO] = ZERO;
     b.sv_src[SV_A4] = A4; b.sv_src[SV_A3] = A3; b.sv_src[SV_A2] = A2; b.sv_src[SV_A1] = E_al;
@@ -491,7 +495,7 @@ bool ode_program_build(const CellStatic &cs, bool pow_fast, OdeProgram *prog, do
                 fprintf(stderr, "ode program: phase %d size differs in regime %d (%zu vs %zu)\n", q, k, v[k].ph[q].size(), v[0].ph[q].size());
                 return false;
             }
-        if (q == PH_F) prog->upd_phase = prog->n_phases;
+        if (q == PH_E) prog->upd_phase = prog->n_phases;
         if (q == PH_C) prog->push_phase = prog->n_phases;
         prog->phase_begin[prog->n_phases++] = n;
         for (size_t j = 0; j < v[0].ph[q].size(); ++j) {
@@ -570,7 +574,7 @@ void ode_program_step_host(const OdeProgram &P, const double *consts, double *g,
     X[XS_ONE] = 1.0;
     X[XS_MONE] = -1.0;
     for (int i = 0; i < P.n_consts; ++i) X[P.const_begin + i] = consts[i];
-    for (int i = 0; i < kNumGlobals; ++i) X[XS_G + i] = g[i];
+    for (int i = 0; i < kNumGlobals; ++i) X[XS_G + i] = X[XS_GN + i] = g[i];
     for (int i = 0; i < 4; ++i) X[XS_SUMS + i] = sums[i];
     X[XS_ISTIM] = Istim;
     X[XS_DT] = dt;
@@ -593,6 +597,7 @@ void ode_program_step_host(const OdeProgram &P, const double *consts, double *g,
             case OK_REC: v = 1.0 / (X[a[0]] + X[a[1]] * X[a[2]] + X[a[3]] * X[a[4]] + X[a[5]] * X[a[6]] * X[a[7]]); break;
             case OK_PROD: v = X[a[0]] * X[a[1]] * X[a[2]] * X[a[3]] * X[a[4]] * X[a[5]] * X[a[6]]; break;
             case OK_SUM:
+            case OK_SUMU:
                 v = X[a[2]] * X[a[3]] * X[a[4]] + X[a[5]] * X[a[6]] * X[a[7]] + X[a[8]] * X[a[9]] * X[a[10]] +
                     X[a[11]] * X[a[12]] * X[a[13]];
                 break;
@@ -603,14 +608,18 @@ void ode_program_step_host(const OdeProgram &P, const double *consts, double *g,
         // SUM rows: lane tree (offsets 1, 2, 4) as the device's shuffles, then the scale
         for (int off = 1; off < 8; off <<= 1)
             for (int j = 0; j < n; ++j)
-                if (ops[j]->kind == OK_SUM && (j % ops[j]->width) + off < ops[j]->width && (j % (2 * off)) == 0)
+                if ((ops[j]->kind == OK_SUM || ops[j]->kind == OK_SUMU) && (j % ops[j]->width) + off < ops[j]->width &&
+                    (j % (2 * off)) == 0)
                     val[j] += val[j + off];
         for (int j = 0; j < n; ++j) {
             const OdeOp *op = ops[j];
             if (op->kind == OK_NOP) continue;
-            if (op->kind == OK_UPD) {
-                g[op->out] += X[op->a[0]];
-                X[XS_G + op->out] = g[op->out];
+            if (op->kind == OK_SUMU) {
+                // every row reads the old globals (XS_G) before any update, as on the device
+                if (j % op->width == 0) {
+                    g[op->out] += X[op->a[0]] * X[op->a[1]] * val[j];
+                    X[XS_GN + op->out] = g[op->out];
+                }
             } else if (op->kind == OK_SUM) {
                 if (j % op->width == 0) X[op->out] = X[op->a[0]] * X[op->a[1]] * val[j];
             } else {
@@ -620,9 +629,10 @@ void ode_program_step_host(const OdeProgram &P, const double *consts, double *g,
     };
     // the transcendental phases of the current state (run before the loop on the device)
     for (int q = P.upd_phase + 1; q < P.n_phases; ++q) run_phase(q, regime());
-    // the step: increments, update, then the new state's phases
+    // the step: increments and update, then the new state's phases
     for (int q = 0; q < P.n_phases; ++q) run_phase(q, q <= P.upd_phase ? regime_of(g[0], true) : regime());
     for (int i = 0; i < kSvCount; ++i) sv[i] = X[P.sv_src[i]];
+    for (int i = 0; i < kNumGlobals; ++i) X[XS_G + i] = X[XS_GN + i];
 }
 
 }  // namespace gw

@@ -27,7 +27,8 @@ enum OdeKind : uint8_t {
     OK_PROD,  // out = X[a0]*X[a1]*X[a2]*X[a3]*X[a4]*X[a5]*X[a6]
     OK_SUM,   // row of `width` lanes: out = X[a0]*X[a1] * sum over lanes and t<4 of
               //                             X[a2+3t]*X[a3+3t]*X[a4+3t]
-    OK_UPD,   // g[out] += X[a0]   (FP64 state), then X[slot of g[out]] = g[out]
+    OK_SUMU,  // SUM row whose result is the increment of global `out`: g[out] += result (FP64
+              // state) by the row's first lane, the new value to X[XS_GN + out]
 };
 
 struct OdeOp {
@@ -51,8 +52,10 @@ enum OdeSlot : uint16_t {
     XS_ZERO = 0,
     XS_ONE = 1,
     XS_MONE = 2,
-    XS_G = 3,                      // 36 globals (gw_globals order)
-    XS_SUMS = XS_G + kNumGlobals,  // JLCC, ClCh, Jtr, Jxfer sums of the previous step
+    XS_G = 3,                        // 36 globals (gw_globals order), read by the increments
+    XS_GN = XS_G + kNumGlobals,      // the updated globals, read by the phases after the update
+                                     // (copied to XS_G after the push phase)
+    XS_SUMS = XS_GN + kNumGlobals,   // JLCC, ClCh, Jtr, Jxfer sums of the previous step
     XS_ISTIM = XS_SUMS + 4,
     XS_DT = XS_ISTIM + 1,
     XS_FIRST_FREE = XS_DT + 1,
@@ -62,7 +65,7 @@ enum OdeSlot : uint16_t {
 struct alignas(16) OdeProgram {
     int n_phases;
     int phase_begin[kOdeMaxPhases + 1];  // ops [phase_begin[p], phase_begin[p+1]) of phase p (<= 128)
-    int upd_phase;                       // phase holding the OK_UPD ops
+    int upd_phase;                       // phase of the increments and the update (OK_SUMU rows)
     int push_phase;                      // sv are pushed after this phase
     int n_slots;
     int const_begin, n_consts;           // per-cell constants occupy X[const_begin, +n_consts)
