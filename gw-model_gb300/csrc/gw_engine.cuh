@@ -172,7 +172,7 @@ __device__ __forceinline__ void stage_pair(double *st, int ihi, int ilo, double 
 // diverge; lanes without an op skip the arithmetic.  Kept out of line: inlined into the engine
 // kernel's loop, its shuffle tree measured 4x slower (2.2k vs 0.5k cycles per SUM phase).
 // An op whose output is a per-step SSA value also writes it, in the SSA's precision, to the push
-// staging row (P.sv_stage); the updates of Cai and CaNSR stage them with their FP32 remainders.
+// staging row (P.sv_stage); Cai and CaNSR are staged by the caller (ode_warps).
 template <typename T, typename R>
 __device__ __noinline__ void ode_phase(const OdeOffsets o, int q, int regime, int t) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -235,8 +235,6 @@ __device__ __noinline__ void ode_phase(const OdeOffsets o, int q, int regime, in
                 const double ng = g[out] + (double)r;
                 g[out] = ng;
                 X[XS_GN + out] = (T)ng;
-                if (out == 3) stage_pair(stage, SV_CAI, SV_CAI_LO, ng);
-                if (out == 4) stage_pair(stage, SV_CANSR, SV_CANSR_LO, ng);
                 if (!finite_bits(ng)) atomicCAS(&os.status, 0, (int)GW_ERR_NONFINITE);  // first error of the cell
             } else {
                 X[out] = r;
@@ -595,6 +593,10 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
             if (ot == 0 && (cell == 0 || (a.tr_cell >= 0 && cell == a.tr_cell))) a.tr_t[r_idx] = os.t;
         }
         const int reg = v_regime(os.g[0]);
+        // Cai and CaNSR of the new state with their FP32 remainders, staged for the push by two
+        // lanes of the last ODE warp, whose ops in the next phase finish early
+        if (ot == kOdeLanes - 1) stage_pair(reinterpret_cast<R *>(v.svstage), SV_CAI, SV_CAI_LO, os.g[3]);
+        if (ot == kOdeLanes - 2) stage_pair(reinterpret_cast<R *>(v.svstage), SV_CANSR, SV_CANSR_LO, os.g[4]);
         for (int q = P.upd_phase + 1; q <= P.push_phase; ++q) {
             ode_phase<T, R>(v.off, q, reg, ot);
             ode_bar();
