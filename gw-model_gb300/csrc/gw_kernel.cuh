@@ -98,6 +98,30 @@ struct Stream {
     }
     template <typename R>
     __device__ __forceinline__ R uniform(uint32_t k);
+    // U24 draws k, k+1, k+2 (an event selection's draws).  They lie in blocks k >> 1 and
+    // (k >> 1) + 1; both are computed without a branch, so that their rounds interleave (the first
+    // is often the block already held: recomputing it costs instructions but no latency), and the
+    // second is kept for the next draws.
+    __device__ __forceinline__ void u24x3(uint32_t k, float &a, float &b2, float &c) {
+        const uint32_t B = k >> 1;
+        uint32_t o1[4], o2[4];
+        philox10(B, cru, step, cellw, k0, k1, o1);
+        philox10(B + 1u, cru, step, cellw, k0, k1, o2);
+        const bool odd = (k & 1u) != 0u;
+        a = u24_of(odd ? o1[3] : o1[1]);
+        b2 = u24_of(odd ? o2[1] : o1[3]);
+        c = u24_of(odd ? o2[3] : o2[1]);
+        blk = B + 1u;
+        b[0] = o2[0];
+        b[1] = o2[1];
+        b[2] = o2[2];
+        b[3] = o2[3];
+    }
+    __device__ __forceinline__ static float u24_of(uint32_t hi) {
+        uint32_t m = hi >> 8;
+        if (m == 0u) m = 1u;
+        return (float)m * 0x1p-24f;
+    }
 };
 template <>
 __device__ __forceinline__ double Stream::uniform<double>(uint32_t k) {
@@ -577,45 +601,53 @@ __device__ __forceinline__ void resplit_crossed(Cru<R> &s, const SsaConsts<R> &c
     }
 }
 
+// Element i of a 4-element register array set to v (predicated moves, no local memory).
+template <typename T>
+__device__ __forceinline__ void set4(T (&a)[4], int i, T v) {
+    a[0] = i == 0 ? v : a[0];
+    a[1] = i == 1 ? v : a[1];
+    a[2] = i == 2 ? v : a[2];
+    a[3] = i == 3 ? v : a[3];
+}
+
 // The transition (sample_new_state, SSA.tpp:262-283) applied to the updated state, with the JLCC
-// and Jrel updates of sample_LCC and sample_RyR.
+// and Jrel updates of sample_LCC and sample_RyR.  Works on subunit aj directly: byte fields by a
+// shift of 8*aj, a RyR move as a per-byte modular addition (__vadd4) of +1 and -1 in byte aj of
+// the two state planes.  Counts are signed bytes and may go below zero (a lumped 3/4 or 5/6 rate
+// moves a RyR out of a state whose own count is 0, as in the reference), so the planes must not
+// carry or borrow between subunits.
 template <typename R>
 __device__ __forceinline__ void apply_event(Cru<R> &s, const SsaConsts<R> &c, const R *sv, int act, int aj, int atr,
                                             R (&jrel)[4]) {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        if (j != aj) continue;
-        if (act == 1) {
-            const int from = byte_u(s.lcc, j);
-            if (from >= 1 && from <= 12) {
-                const int to = (int)((c.lccn[from] >> (4 * atr)) & 0xFu);
-                s.lcc = byte_set(s.lcc, j, to);
-                const bool inact1 = ((s.flags >> j) & 1u) != 0u;
-                if ((from == 5 && to == 6) || (from == 11 && to == 12))
-                    s.jlcc[j] = inact1 ? sv[SV_JMUL] * (c.Cao_scaled - sv[SV_JEXP] * s.cass[j]) : (R)0;
-                else if (from == 6 || from == 12)
-                    s.jlcc[j] = (R)0;
-            }
-        } else if (act == 2) {
-            s.flags ^= (1u << j);
-            const int st = byte_u(s.lcc, j);
-            if (((s.flags >> j) & 1u) == 0u)
-                s.jlcc[j] = (R)0;
-            else if (st == 6 || st == 12)
-                s.jlcc[j] = sv[SV_JMUL] * (c.Cao_scaled - sv[SV_JEXP] * s.cass[j]);
-        } else if (act == 3) {
-            int from, to;
-            ryr_move(atr, from, to);
-#pragma unroll
-            for (int q = 0; q < 6; ++q) {
-                if (q == from) s.ryr[q] = byte_add(s.ryr[q], j, -1);
-                if (q == to) s.ryr[q] = byte_add(s.ryr[q], j, +1);
-            }
-            const R open = (R)(byte_s(s.ryr[2], j) + byte_s(s.ryr[3], j));
-            jrel[j] = c.rRyR * open * (s.cajsr - s.cass[j]);
-        } else {
-            s.flags ^= (1u << (4 + j));
+    const uint32_t sh = 8u * (uint32_t)aj;
+    if (act == 1) {
+        const int from = (int)((s.lcc >> sh) & 0xFFu);
+        if (from >= 1 && from <= 12) {
+            const int to = (int)((c.lccn[from] >> (4 * atr)) & 0xFu);
+            s.lcc = (s.lcc & ~(0xFFu << sh)) | ((uint32_t)to << sh);
+            const bool inact1 = ((s.flags >> aj) & 1u) != 0u;
+            if ((from == 5 && to == 6) || (from == 11 && to == 12))
+                set4(s.jlcc, aj, inact1 ? sv[SV_JMUL] * (c.Cao_scaled - sv[SV_JEXP] * pick4(s.cass, aj)) : (R)0);
+            else if (from == 6 || from == 12)
+                set4(s.jlcc, aj, (R)0);
         }
+    } else if (act == 2) {
+        s.flags ^= (1u << aj);
+        const int st = (int)((s.lcc >> sh) & 0xFFu);
+        if (((s.flags >> aj) & 1u) == 0u)
+            set4(s.jlcc, aj, (R)0);
+        else if (st == 6 || st == 12)
+            set4(s.jlcc, aj, sv[SV_JMUL] * (c.Cao_scaled - sv[SV_JEXP] * pick4(s.cass, aj)));
+    } else if (act == 3) {
+        int from, to;
+        ryr_move(atr, from, to);
+        const uint32_t up = 1u << sh, down = 0xFFu << sh;  // +1 and -1 (mod 256) in byte aj
+#pragma unroll
+        for (int q = 0; q < 6; ++q) s.ryr[q] = __vadd4(s.ryr[q], q == to ? up : (q == from ? down : 0u));
+        const R open = (R)(byte_s(s.ryr[2], aj) + byte_s(s.ryr[3], aj));
+        set4(jrel, aj, c.rRyR * open * (s.cajsr - pick4(s.cass, aj)));
+    } else {
+        s.flags ^= (1u << (4 + aj));
     }
 }
 
@@ -786,13 +818,56 @@ __device__ __forceinline__ float2 counts2(uint32_t wb, int p, float2 bias) {
     return add2(make_float2(a, b), bias);
 }
 
+// The 12 RyR rates of subunit j (update_RyR_rates, GW_utils.tpp:222-255) in FP32, with the two
+// divisions of the lumped regimes as reciprocal estimates (rcp_approx), as in the subunit totals.
+__device__ __forceinline__ void ryr_rates_f32(const Cru<float> &s, int j, float x, const SsaConsts<float> &c,
+                                              float (&r)[12]) {
+    const float R0 = (float)byte_s(s.ryr[0], j), R1 = (float)byte_s(s.ryr[1], j), R2 = (float)byte_s(s.ryr[2], j);
+    const float R3 = (float)byte_s(s.ryr[3], j), R4 = (float)byte_s(s.ryr[4], j), R5 = (float)byte_s(s.ryr[5], j);
+    const float R23 = (float)(byte_s(s.ryr[2], j) + byte_s(s.ryr[3], j));
+    const float R45 = (float)(byte_s(s.ryr[4], j) + byte_s(s.ryr[5], j));
+    const float x2 = x * x;
+    r[0] = R0 * c.k12 * x2;
+    r[1] = R1 * c.k23 * x2;
+    r[2] = R1 * c.k25 * x2;
+    r[6] = R1 * c.k21;
+    if (x > 3.685e-2f) {
+        const float tau34 = rcp_approx(c.k34 * x2 + c.k43);
+        r[3] = 0.f;
+        r[4] = R23 * c.k45 * c.k34 * x2 * tau34;
+        r[7] = R23 * c.k32 * c.k43 * tau34;
+        r[8] = 0.f;
+    } else {
+        r[3] = R2 * c.k34 * x2;
+        r[4] = R3 * c.k45;
+        r[7] = R2 * c.k32;
+        r[8] = R3 * c.k43;
+    }
+    if (x > 1.15e-4f) {
+        const float eq56 = c.k65 * rcp_approx(c.k56 * x2 + c.k65);
+        r[5] = 0.f;
+        r[9] = R45 * c.k52 * eq56;
+        r[10] = R45 * c.k54 * x2 * eq56;
+        r[11] = 0.f;
+    } else {
+        r[5] = R4 * c.k56 * x2;
+        r[9] = R4 * c.k52;
+        r[10] = R4 * c.k54 * x2;
+        r[11] = R5 * c.k65;
+    }
+}
+
 // FP32 event selection: select_event's draws and decisions, with the subunit's RyR total taken
 // from the iteration's packed total computation (ryr_sub) and the 12 individual RyR rates formed
-// only when the RyR class is drawn (at rest most events are LCC and gate transitions).
+// only when the RyR class is drawn (at rest most events are LCC and gate transitions).  The three
+// draws are formed up front (Stream::u24x3); a selection uses two or three of them, as
+// select_event's sequential draws would.
 __device__ __forceinline__ void select_event_f32(const Cru<float> &s, const SsaConsts<float> &c, const float *sv,
                                                  const float (&sub)[4], const float (&ryr_sub)[4], float total,
                                                  Stream &rng, uint32_t &kk, int &act, int &aj, int &atr) {
-    const float us = rng.uniform<float>(kk++) * total;
+    float ua, ub, uc;
+    rng.u24x3(kk, ua, ub, uc);
+    const float us = ua * total;
     aj = scan_weights<float, 4, true>(sub, us);
     const float x = pick4(s.cass, aj);
     // update_LCC_rates, update_LCC_inactivation_rates, update_ClCh_rates of subunit aj
@@ -809,20 +884,24 @@ __device__ __forceinline__ void select_event_f32(const Cru<float> &s, const SsaC
     const float sum_lcc = lcc[0] + lcc[1] + lcc[2];
     const float sum_ryr = pick4(ryr_sub, aj);
     const float subr = ((sum_lcc + inact) + sum_ryr) + clch;
-    const float u = rng.uniform<float>(kk++) * subr;
+    const float u = ub * subr;
+    kk += 2u;
     if (u < sum_lcc) {
         act = 1;
-        atr = scan_weights<float, 3, true>(lcc, rng.uniform<float>(kk++) * sum_lcc);
+        atr = scan_weights<float, 3, true>(lcc, uc * sum_lcc);
+        kk += 1u;
     } else if (u < sum_lcc + inact) {
         act = 2;
     } else if (u < sum_lcc + inact + sum_ryr) {
         act = 3;
-        Rates<float> r;
-        subunit_rates<float>(s, aj, x, c, sv, r);
-        float direct = 0.f;
-#pragma unroll
-        for (int q = 0; q < 12; ++q) direct += r.ryr[q];
-        atr = scan_weights<float, 12, true>(r.ryr, rng.uniform<float>(kk++) * direct);
+        float r[12];
+        ryr_rates_f32(s, aj, x, c, r);
+        // the rates' sum in three groups of four (independent chains), then the sequential scan
+        const float g0 = ((r[0] + r[1]) + r[2]) + r[3];
+        const float g1 = ((r[4] + r[5]) + r[6]) + r[7];
+        const float g2 = ((r[8] + r[9]) + r[10]) + r[11];
+        atr = scan_weights<float, 12, true>(r, uc * ((g0 + g1) + g2));
+        kk += 1u;
     } else {
         act = 4;
     }
