@@ -253,26 +253,46 @@ __device__ __noinline__ void ode_phase(const OdeOffsets o, int q, int regime, in
 }
 
 // Sums {JLCC, ClCh, Jtr, Jxfer} of the cell's CTA partials of one slot; ODE warp w reduces
-// quantity w.  Writes the FP64 sums to out[] (shared) from lane 0 of each warp.
+// quantity w.  Writes the FP64 sums to out[] (shared) from lane 0 of each warp.  A lane takes the
+// slots lane, lane + 32, ... (at most kSlotsPerLane): all its loads are issued first and summed in
+// a pairwise tree, so the lane's part costs one load latency and three dependent additions.
+constexpr int kSlotsPerLane = 16 * kMaxWarps / 32;  // up to 16 CTAs per cell
 template <bool FP64, typename T>
 __device__ __forceinline__ void reduce_partials(const Partial *slot, int n, int warp, int lane, double *out, T *X) {
     if (warp >= 4) return;
     double r;
     if (FP64) {
         const int src = warp == 0 ? 0 : (warp == 1 ? 3 : (warp == 2 ? 2 : 1));  // JLCC, ClCh, Jtr, Jxfer
-        double acc = 0;
-        for (int i = lane; i < n; i += 32) acc += slot[i].v[src];
+        double a[kSlotsPerLane];
+#pragma unroll
+        for (int k = 0; k < kSlotsPerLane; ++k) {
+            const int i = lane + 32 * k;
+            a[k] = i < n ? slot[i].v[src] : 0.0;
+        }
+#pragma unroll
+        for (int w = kSlotsPerLane / 2; w > 0; w >>= 1)
+#pragma unroll
+            for (int k = 0; k < w; ++k) a[k] += a[k + w];
+        double acc = a[0];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         r = acc;
     } else {
         // float fields: 0,1 JLCC; 2,3 Jxfer; 4,5 Jtr; 6 ClCh
         const int src = warp == 0 ? 0 : (warp == 1 ? 6 : (warp == 2 ? 4 : 2));
-        float hi = 0, lo = 0;
-        for (int i = lane; i < n; i += 32) {
-            const float *f = reinterpret_cast<const float *>(slot[i].v);
-            df_add(hi, lo, f[src], warp == 1 ? 0.f : f[src + 1]);
+        float h[kSlotsPerLane], l[kSlotsPerLane];
+#pragma unroll
+        for (int k = 0; k < kSlotsPerLane; ++k) {
+            const int i = lane + 32 * k;
+            const float *f = reinterpret_cast<const float *>(slot[i < n ? i : 0].v);
+            h[k] = i < n ? f[src] : 0.f;
+            l[k] = i < n && warp != 1 ? f[src + 1] : 0.f;
         }
+#pragma unroll
+        for (int w = kSlotsPerLane / 2; w > 0; w >>= 1)
+#pragma unroll
+            for (int k = 0; k < w; ++k) df_add(h[k], l[k], h[k + w], l[k + w]);
+        float hi = h[0], lo = l[0];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const float a0 = __shfl_xor_sync(0xffffffffu, hi, o), a1 = __shfl_xor_sync(0xffffffffu, lo, o);
