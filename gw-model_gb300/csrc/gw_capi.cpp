@@ -1034,6 +1034,7 @@ int gw_run(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_trace *tr
             const char *what = st[i] == GW_ERR_EVENT_CAP ? "a CRU exceeded the per-step jump cap"
                                : st[i] == GW_ERR_NERNST  ? "non-positive concentration in a Nernst potential"
                                : st[i] == GW_ERR_NONFINITE ? "a global state variable became NaN/Inf"
+                               : st[i] == GW_ERR_SYNC_TIMEOUT ? "a bounded wait in the engine kernel ran out"
                                                            : "error";
             return fail(c, st[i], "cell %d: %s", i, what);
         }
@@ -1198,6 +1199,7 @@ int gw_run_noalloc(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_t
                 const char *what = st[i] == GW_ERR_EVENT_CAP ? "a CRU exceeded the per-step jump cap"
                                    : st[i] == GW_ERR_NERNST  ? "non-positive concentration in a Nernst potential"
                                    : st[i] == GW_ERR_NONFINITE ? "a global state variable became NaN/Inf"
+                                   : st[i] == GW_ERR_SYNC_TIMEOUT ? "a bounded wait in the engine kernel ran out"
                                                                : "error";
                 return fail(c, st[i], "cell %d: %s", i0 + i, what);
             }

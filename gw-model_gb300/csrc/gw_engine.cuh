@@ -45,7 +45,7 @@ constexpr int kMaxThreads = 512;  // SSA warps + ODE warps per CTA (128 register
 constexpr int kMaxWarps = kMaxThreads / 32;
 
 struct SmemLayout {
-    size_t cc, sv, ode, prog, x, math, svs, rtab, part, ctr, tile, total;
+    size_t cc, sv, ode, prog, x, math, svs, rtab, part, ctr, mbar, tile, total;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -74,6 +74,8 @@ __host__ __device__ inline SmemLayout smem_layout(int tile_cap, int max_cta_cell
     o += align16((size_t)2 * max_cta_cell * kMaxWarps * sizeof(Partial));
     L.ctr = o;   // warp completion counters [2 + parity]
     o += 16;
+    L.mbar = o;  // mbarriers: the warp partials of steps of parity 0 and 1 (leader CTA), then the
+    o += 32;     // per-step SSA values of parity 0 and 1 (every CTA)
     L.tile = o;  // TileRec<R> per CRU
     o += align16((size_t)tile_cap * sizeof(TileRec<R>));
     L.total = o;
@@ -308,9 +310,11 @@ __device__ __forceinline__ void reduce_partials(const Partial *slot, int n, int 
 
 // Per-step SSA values of the new state to every CTA of the cell: the staging row (written by the
 // ops that produce the values, see ode_phase, and visible after the phase's barrier) pushed in
-// 16-byte words (CTA, word) by all kOdeLanes threads.
+// 16-byte words (CTA, word) by all kOdeLanes threads, as asynchronous stores that count themselves
+// off the receiving CTA's mbarrier of this slot (local shared address mbar_slot in every CTA).
 template <bool FP64>
-__device__ __forceinline__ void push_sv(void *svbuf, const void *stage, int slot, const CtaWork &w, int t) {
+__device__ __forceinline__ void push_sv(void *svbuf, const void *stage, int slot, uint32_t mbar_slot, const CtaWork &w,
+                                        int t) {
     using R = typename std::conditional<FP64, double, float>::type;
     constexpr int kWords = kSvCount * (int)sizeof(R) / 16;  // 16-byte words of one slot
     static_assert(kSvCount * sizeof(R) % 16 == 0, "sv slot in 16-byte words");
@@ -319,7 +323,8 @@ __device__ __forceinline__ void push_sv(void *svbuf, const void *stage, int slot
     const int total = kWords * w.n_cta_cell;
     for (int idx = t; idx < total; idx += kOdeLanes) {
         const int r = idx / kWords, i = idx - r * kWords;
-        st_remote(map_rank(dst + i, (uint32_t)(w.first + r)), src[i]);
+        const uint32_t rank = (uint32_t)(w.first + r);
+        st_async(map_rank(dst + i, rank), src[i], map_rank_addr(mbar_slot, rank));
     }
 }
 
@@ -488,6 +493,8 @@ struct CtaView {
     Partial *part;
     float2 *rtab;
     int *ctr;
+    uint32_t mbar;  // shared address of the partials' mbarrier of parity 0 (parity 1 at +8); the
+                    // SSA values' mbarriers of parity 0 and 1 at +16 and +24
     TileRec<R> *tile;
     OdeOffsets off;  // for ode_phase
 
@@ -513,6 +520,7 @@ struct CtaView {
         part = reinterpret_cast<Partial *>(smem + L.part);
         rtab = reinterpret_cast<float2 *>(smem + L.rtab);
         ctr = reinterpret_cast<int *>(smem + L.ctr);
+        mbar = smem_addr(smem + L.mbar);
         tile = reinterpret_cast<TileRec<R> *>(smem + L.tile);
         off = OdeOffsets{(uint32_t)L.prog, (uint32_t)L.x, (uint32_t)L.ode, (uint32_t)L.math, (uint32_t)L.svs};
     }
@@ -581,13 +589,20 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
             ode_phase<T, R>(v.off, q, reg, ot);
             ode_bar();
         }
-        push_sv<FP64>(v.svbuf, v.svstage, 0, v.w, ot);
-        cluster_arrive();
+        push_sv<FP64>(v.svbuf, v.svstage, 0, v.mbar + 16u, v.w, ot);
+        // nothing this thread wrote is read by another CTA through the barrier (the SSA values
+        // travel by st.async), and within the CTA a fence suffices: a relaxed arrive does not wait
+        // for the remote stores to land
+        __threadfence_block();
+        cluster_arrive_relaxed();
         for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
             ode_phase<T, R>(v.off, q, reg, ot);
             ode_bar();
         }
     }
+    // bytes of the cell's warp partials per step (every SSA warp of the cell pushes 32 B)
+    const uint32_t part_bytes =
+        (uint32_t)sizeof(Partial) * (uint32_t)(v.nw + (v.w.n_cta_cell - 1) * (v.nw + kOdeWarps));
     for (int s = 0; s < a.n_steps; ++s) {
         const int par = s & 1;
         const int64_t ri = a.run_step0 + s;
@@ -595,9 +610,16 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
         const int64_t r_idx = rec ? ri / a.record_every - a.rec_base : -1;
         const bool rec_ok = rec && r_idx >= 0 && r_idx < a.rec_cap;
         cluster_wait();
+        // the partials of step s will complete the next phase of mbarrier par (the previous one,
+        // step s-2's, completed before this thread's wait in step s-1)
+        if (ot == 0) mbar_arrive_expect_tx(v.mbar + 8u * (uint32_t)par, part_bytes);
         // fluxes of step s-1 (or the carry), then the global step s -> s+1
         if (ot == 0 && (not_positive(os.g[1]) || not_positive(os.g[2])) && os.status == 0)
             os.status = GW_ERR_NERNST;
+        // (after one wait has run out, the cell's results are void: no further waits)
+        if (s > 0 && os.status != GW_ERR_SYNC_TIMEOUT &&
+            !mbar_wait(v.mbar + 8u * (uint32_t)(par ^ 1), (uint32_t)((s - 1) >> 1) & 1u) && lane == 0)
+            atomicCAS(&os.status, 0, (int)GW_ERR_SYNC_TIMEOUT);
         if (s > 0) reduce_partials<FP64, T>(v.part + (par ^ 1) * pslot, v.w.n_cta_cell * kMaxWarps, ot >> 5, lane, os.sums, X);
         if (s > 0 && ot == 0) X[XS_ISTIM] = (T)os.stim[par];
         ode_bar();
@@ -624,8 +646,9 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
         // the new globals become the old ones of the next step's increments (read after the
         // next step's first barrier; no phase after this point reads XS_G)
         if (ot < kNumGlobals) X[XS_G + ot] = X[XS_GN + ot];
-        push_sv<FP64>(v.svbuf, v.svstage, par ^ 1, v.w, ot);
-        cluster_arrive();
+        push_sv<FP64>(v.svbuf, v.svstage, par ^ 1, v.mbar + 16u + 8u * (uint32_t)(par ^ 1), v.w, ot);
+        __threadfence_block();
+        cluster_arrive_relaxed();
         // off the critical path: the phases the SSA does not need
         for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
             ode_phase<T, R>(v.off, q, reg, ot);
@@ -634,6 +657,9 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
     }
     cluster_wait();
     // carry of the last step's fluxes, globals and counters back to the cell block
+    if (a.n_steps > 0 && os.status != GW_ERR_SYNC_TIMEOUT &&
+        !mbar_wait(v.mbar + 8u * (uint32_t)((a.n_steps - 1) & 1), (uint32_t)((a.n_steps - 1) >> 1) & 1u) && lane == 0)
+        atomicCAS(&os.status, 0, (int)GW_ERR_SYNC_TIMEOUT);
     if (a.n_steps > 0)
         reduce_partials<FP64, T>(v.part + ((a.n_steps - 1) & 1) * pslot, v.w.n_cta_cell * kMaxWarps, ot >> 5, lane, os.sums, X);
     ode_bar();
@@ -667,7 +693,7 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
     const int pslot = a.max_cta_cell * kMaxWarps;  // warp partials per parity slot
     const R dt = (R)a.dt;
     unsigned long long my_events = 0;
-    int my_err = 0;
+    int my_err = 0;  // bit 0: a CRU hit the event cap; bit 1: a wait for the SSA values ran out
     cluster_arrive();
     for (int s = 0; s < a.n_steps; ++s) {
         const int par = s & 1;
@@ -680,6 +706,13 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
             // The counter of parity par^1 was last used in step s-1, which every warp of this
             // CTA has left; it is next used in step s+1, after the cluster barrier.
             if (threadIdx.x == 0) ctr[2 + (par ^ 1)] = 0;
+            // The SSA values of step s arrive by st.async from the leader's ODE warps and complete
+            // this CTA's mbarrier of parity par (thread 0 declares the bytes; that mbarrier's
+            // previous phase, step s-2's, completed before this CTA's waits of step s-2).  After
+            // one wait has run out the results are void and no further waits are made.
+            const uint32_t svm = v.mbar + 16u + 8u * (uint32_t)par;
+            if (threadIdx.x == 0) mbar_arrive_expect_tx(svm, (uint32_t)(kSvCount * sizeof(R)));
+            if (!(my_err & 2) && !mbar_wait(svm, (uint32_t)(s >> 1) & 1u)) my_err |= 2;
             const R *sv = v.svbuf + par * kSvCount;
             const int nsw = n_ssa >> 5;
             if (!FP64) {
@@ -736,9 +769,13 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
             const Partial pv = acc.warp_total();
             int done = 0;
             if (lane == 0) {
+                // two 16-byte asynchronous stores that count themselves off the leader's mbarrier
+                // of this parity: the arrive below does not wait for them to land
                 Partial *dst = v.part + par * pslot + w.rank_in_cell * kMaxWarps + warp;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) st_remote(map_rank(&dst->v[q], (uint32_t)w.first), pv.v[q]);
+                const uint32_t rd = map_rank(dst, (uint32_t)w.first);
+                const uint32_t rm = map_rank_addr(v.mbar + 8u * (uint32_t)par, (uint32_t)w.first);
+                st_async(rd, make_uint4(lo_of(pv.v[0]), hi_of(pv.v[0]), lo_of(pv.v[1]), hi_of(pv.v[1])), rm);
+                st_async(rd + 16u, make_uint4(lo_of(pv.v[2]), hi_of(pv.v[2]), lo_of(pv.v[3]), hi_of(pv.v[3])), rm);
                 done = atomicAdd(&ctr[2 + par], 1);  // the order of finishing (first warp below)
             }
             done = __shfl_sync(0xffffffffu, done, 0);
@@ -751,7 +788,11 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
                 os.stim[par ^ 1] = stimulus(a.dyn[cell], os.tstim, ri + 1);
             }
         }
-        cluster_arrive();
+        // Nothing an SSA thread wrote is read by another CTA through the barrier (the partials
+        // travel by st.async); the stimulus and the counters are read within the CTA, for which
+        // a CTA fence before a relaxed arrive suffices.  A release arrive would wait ~900 cycles.
+        __threadfence_block();
+        cluster_arrive_relaxed();
     }
     cluster_wait();
     if (!v.active) return;
@@ -783,7 +824,7 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
     }
     if (lane == 0) {
         if (my_events) atomicAdd(a.events, my_events);
-        if (my_err) atomicCAS(&a.status[cell], 0, (int)GW_ERR_EVENT_CAP);
+        if (my_err) atomicCAS(&a.status[cell], 0, (my_err & 2) ? (int)GW_ERR_SYNC_TIMEOUT : (int)GW_ERR_EVENT_CAP);
     }
 }
 
@@ -795,9 +836,15 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
 template <bool FP64, bool ODE64>
 __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const __grid_constant__ KernelArgs a) {
     using R = typename std::conditional<FP64, double, float>::type;
-    cluster_arrive_relaxed();
-    cluster_wait();
     const CtaView<FP64, ODE64> v(a);
+    // The partials' mbarriers (one arrival per phase: the ODE thread's expect_tx) are initialised
+    // before the cluster barrier that every CTA passes before its first remote write.
+    if (threadIdx.x == 0) {
+        for (uint32_t i = 0; i < 4; ++i) mbar_init(v.mbar + 8u * i, 1);
+        mbar_fence_init();
+    }
+    cluster_arrive();
+    cluster_wait();
     uint64_t step0 = 0;
     if (v.active) {
         const int cell = v.w.cell;

@@ -149,6 +149,12 @@ __device__ __forceinline__ uint32_t map_rank(const void *p, uint32_t rank) {
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
     return r;
 }
+// shared::cluster address of a local shared address (a 32-bit shared-window address) in CTA rank
+__device__ __forceinline__ uint32_t map_rank_addr(uint32_t a, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
 __device__ __forceinline__ void st_remote(uint32_t addr, double v) {
     asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(addr), "d"(v) : "memory");
 }
@@ -159,6 +165,51 @@ __device__ __forceinline__ void st_remote(uint32_t addr, uint4 v) {  // addr 16-
     asm volatile("st.shared::cluster.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x), "r"(v.y), "r"(v.z),
                  "r"(v.w)
                  : "memory");
+}
+
+// mbarriers (shared-memory arrival/transaction barriers) and asynchronous remote stores.  An
+// st.async writes 16 bytes into a CTA of the cluster and, once the bytes are there, counts them off
+// that CTA's mbarrier (complete_tx); the issuing thread does not wait for it, and a later fence
+// or release arrive of that thread does not either.  addr and mbar are shared::cluster addresses
+// (map_rank), addr 16-byte aligned.
+__device__ __forceinline__ void st_async(uint32_t addr, uint4 v, uint32_t mbar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(addr),
+                 "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "r"(mbar)
+                 : "memory");
+}
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+}
+// makes the initialisations visible to the cluster (before the cluster barrier that precedes
+// their first remote use)
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// one arrival on the local mbarrier, declaring tx more bytes to come in its current phase
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t mbar, uint32_t tx) {
+    uint64_t state;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;" : "=l"(state) : "r"(mbar), "r"(tx) : "memory");
+    (void)state;
+}
+// true once the phase of the given parity has completed; acquire at cluster scope, so the bytes
+// that completed it (written by other CTAs) are visible.  May suspend the thread for a while.
+__device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    return ok != 0u;
+}
+// Bounded wait: false if the phase did not complete within 2^31 cycles (about a second).
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    if (mbar_try_wait(mbar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(mbar, parity))
+        if (clock64() - t0 > (1ll << 31)) return false;
+    return true;
 }
 
 // ------------------------------------------------------------------------------------------

@@ -33,6 +33,7 @@ GW_ERR_NONFINITE = 5
 GW_ERR_NERNST = 6
 GW_ERR_UNSUPPORTED = 7
 GW_ERR_OUT_OF_MEMORY = 8
+GW_ERR_SYNC_TIMEOUT = 9
 
 PRECISION = {"fp64": 0, "fp32": 1}
 

@@ -38,7 +38,10 @@ typedef enum gw_status {
     GW_ERR_NERNST = 6,           /* non-positive concentration in a Nernst potential (the reference
                                     exits the process here, common.hpp:72-75) */
     GW_ERR_UNSUPPORTED = 7,      /* the requested launch shape does not fit this device */
-    GW_ERR_OUT_OF_MEMORY = 8
+    GW_ERR_OUT_OF_MEMORY = 8,
+    GW_ERR_SYNC_TIMEOUT = 9      /* a bounded wait inside the engine kernel ran out (about a second
+                                    for data that normally arrives within microseconds); the
+                                    launch finished, its results are not valid */
 } gw_status;
 
 /* Arithmetic of the CRU state and the SSA.  The global ODE is FP64 in both. */
