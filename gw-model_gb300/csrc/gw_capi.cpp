@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -54,6 +55,7 @@ struct DevBuf {
 
 struct gw_ctx {
     int device = 0;
+    int test_extra_tx = 0;  // see GWGB300_TEST_SYNC_TIMEOUT in gw_create
     int precision = GW_PRECISION_FP64;
     bool ode64 = true;
     int n_cells = 0;
@@ -273,6 +275,7 @@ KernelArgs base_args(gw_ctx *c) {
     a.status = c->d_status.as<int>();
     a.ssa_warps = c->ssa_warps;
     a.tile_cap = c->tile_cap;
+    a.test_extra_tx = c->test_extra_tx;
     a.max_cta_cell = c->max_cta_cell;
     a.tr_cell = -1;
     return a;
@@ -440,6 +443,13 @@ int gw_create(const gw_ensemble_desc *d, gw_ctx **out) {
     c->n_cells = d->n_cells;
     c->seed = d->seed;
     c->event_cap = d->event_cap > 0 ? d->event_cap : 65536;
+    // Test hook for the bounded waits of the engine kernel: GWGB300_TEST_SYNC_TIMEOUT=1 at context
+    // creation makes every launch's last wait for the warp partials expect 16 bytes that are never
+    // sent, so that it runs out (about a second) and the launch reports GW_ERR_SYNC_TIMEOUT.
+    {
+        const char *t = getenv("GWGB300_TEST_SYNC_TIMEOUT");
+        c->test_extra_tx = (t && t[0] == '1') ? 16 : 0;
+    }
     c->steps_per_launch = d->steps_per_launch > 0 ? d->steps_per_launch : 1000;
     c->rsize = c->precision == GW_PRECISION_FP64 ? 8 : 4;
     c->ncru.assign(d->ncru, d->ncru + d->n_cells);

@@ -612,7 +612,9 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
         cluster_wait();
         // the partials of step s will complete the next phase of mbarrier par (the previous one,
         // step s-2's, completed before this thread's wait in step s-1)
-        if (ot == 0) mbar_arrive_expect_tx(v.mbar + 8u * (uint32_t)par, part_bytes);
+        if (ot == 0 && os.status != GW_ERR_SYNC_TIMEOUT)
+            mbar_arrive_expect_tx(v.mbar + 8u * (uint32_t)par,
+                                  part_bytes + (s == a.n_steps - 1 ? (uint32_t)a.test_extra_tx : 0u));
         // fluxes of step s-1 (or the carry), then the global step s -> s+1
         if (ot == 0 && (not_positive(os.g[1]) || not_positive(os.g[2])) && os.status == 0)
             os.status = GW_ERR_NERNST;
@@ -646,7 +648,10 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
         // the new globals become the old ones of the next step's increments (read after the
         // next step's first barrier; no phase after this point reads XS_G)
         if (ot < kNumGlobals) X[XS_G + ot] = X[XS_GN + ot];
-        push_sv<FP64>(v.svbuf, v.svstage, par ^ 1, v.mbar + 16u + 8u * (uint32_t)(par ^ 1), v.w, ot);
+        // (no push after the launch's last step: no one would wait for those bytes, and a CTA
+        // must not exit while stores into its shared memory may still be in flight)
+        if (s + 1 < a.n_steps)
+            push_sv<FP64>(v.svbuf, v.svstage, par ^ 1, v.mbar + 16u + 8u * (uint32_t)(par ^ 1), v.w, ot);
         __threadfence_block();
         cluster_arrive_relaxed();
         // off the critical path: the phases the SSA does not need
@@ -711,7 +716,7 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
             // previous phase, step s-2's, completed before this CTA's waits of step s-2).  After
             // one wait has run out the results are void and no further waits are made.
             const uint32_t svm = v.mbar + 16u + 8u * (uint32_t)par;
-            if (threadIdx.x == 0) mbar_arrive_expect_tx(svm, (uint32_t)(kSvCount * sizeof(R)));
+            if (threadIdx.x == 0 && !(my_err & 2)) mbar_arrive_expect_tx(svm, (uint32_t)(kSvCount * sizeof(R)));
             if (!(my_err & 2) && !mbar_wait(svm, (uint32_t)(s >> 1) & 1u)) my_err |= 2;
             const R *sv = v.svbuf + par * kSvCount;
             const int nsw = n_ssa >> 5;

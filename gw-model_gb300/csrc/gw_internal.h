@@ -125,7 +125,8 @@ struct KernelArgs {
                         // other CTAs of a cell run SSA on all ssa_warps + kOdeWarps warps
     int tile_cap;       // CRU capacity of one CTA
     int max_cta_cell;   // max CTAs of one cell (partial slot stride)
-    int pad;
+    int test_extra_tx;  // test hook, 0 in use: bytes the leader adds to the last step's expected
+                        // partials (bytes no one sends), so that its bounded wait runs out
 };
 
 struct LaunchShape {

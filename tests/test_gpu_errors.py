@@ -78,3 +78,26 @@ def test_errors_are_per_cell():
     assert ex.value.code == _lib.GW_ERR_NERNST and "cell 1" in str(ex.value)
     assert np.all(np.isfinite(e.get_globals(0))) and not np.array_equal(e.get_globals(0), g0)
     e.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_bounded_wait_runs_out(monkeypatch, precision):
+    """The per-step data travel by st.async on mbarriers whose waits are bounded.  The test hook
+    makes the last wait of each launch expect 16 bytes that no one sends (a flag nothing sets):
+    the wait runs out after about a second, the launch finishes, the run reports
+    GW_ERR_SYNC_TIMEOUT, and the context answers; a context made without the hook runs normally."""
+    from gwgb300 import _lib
+
+    monkeypatch.setenv("GWGB300_TEST_SYNC_TIMEOUT", "1")
+    e = _cell(precision=precision, steps_per_launch=20)
+    with pytest.raises(_lib.GWError) as ex:
+        e.run(1e-3, 20)  # one launch: its final wait runs out
+    assert ex.value.code == _lib.GW_ERR_SYNC_TIMEOUT
+    assert "bounded wait" in str(ex.value)
+    assert np.all(np.isfinite(e.get_globals(0)))
+    e.close()
+    monkeypatch.delenv("GWGB300_TEST_SYNC_TIMEOUT")
+    f = _cell(precision=precision, steps_per_launch=20)
+    f.run(1e-3, 40)
+    assert np.all(np.isfinite(f.get_globals(0)))
+    f.close()
