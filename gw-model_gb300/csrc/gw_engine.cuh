@@ -3,16 +3,17 @@
 //
 // CTA = ssa_warps + kOdeWarps warps.  In a cell's leader CTA the last kOdeWarps warps run the
 // global step as the lane program of gw_ode_program.h; in the other CTAs of the cell every warp
-// runs SSA.  Per global step s, every thread does   wait(s) ... arrive(s+1):
-//   SSA warps : each warp owns a contiguous range of the CTA's CRU tile and runs the SSA of step
-//               s on it with the values sv[s&1], one CRU per lane at a time; a lane whose CRU has
-//               finished its step takes the warp's next CRU, so lanes with pending SSA events do
-//               not hold the others back.  Each warp pushes its flux partial into its slot in
-//               the leader's shared memory (DSMEM).  In a leader CTA the warp that finishes
-//               first also evaluates the stimulus of step s+1 for the ODE warps.
-//   ODE warps : reduce the warp partials of step s-1, increments and Euler update (globals
-//               s -> s+1), transcendental phases of the new state, push sv[(s+1)&1], arrive; the
-//               phases that the SSA does not need (general Jup exponents) run after the arrive.
+// runs SSA.  The CTAs of a cell are held together only by their data, which travel by st.async
+// and complete per-parity mbarriers of the receiver (no cluster barrier inside the launch):
+//   SSA warps : wait for sv[s&1] (the CTA's mbarrier), then each warp runs the SSA of step s on a
+//               contiguous range of the CTA's CRU tile, one CRU per lane at a time; a lane whose
+//               CRU has finished its step takes the warp's next CRU, so lanes with pending SSA
+//               events do not hold the others back.  Each warp pushes its flux partial into its
+//               slot in the leader's shared memory.
+//   ODE warps : wait for the warp partials of step s-1 (the leader's mbarrier), reduce them,
+//               increments and Euler update (globals s -> s+1), transcendental phases of the new
+//               state (an idle lane forms the stimulus of step s+1), push sv[(s+1)&1]; phases the
+//               SSA does not need run after the push.
 #pragma once
 
 #include <type_traits>
@@ -35,7 +36,7 @@ struct OdeShared {
     double g[kNumGlobals];  // the cell's globals (FP64 state)
     double t;               // accumulated time
     double sums[4];         // JLCC, ClCh, Jtr, Jxfer sums of the last reduced step (FP64)
-    double tstim;           // time of the next stimulus evaluation (the same sums as t)
+    double tstim;           // unused
     double stim[2];         // stimulus of step s in slot s & 1, from the leader's SSA warps
     int status;
     int pad;
@@ -45,7 +46,7 @@ constexpr int kMaxThreads = 512;  // SSA warps + ODE warps per CTA (128 register
 constexpr int kMaxWarps = kMaxThreads / 32;
 
 struct SmemLayout {
-    size_t cc, sv, ode, prog, x, math, svs, rtab, part, ctr, mbar, tile, total;
+    size_t cc, sv, ode, prog, x, math, svs, rtab, part, mbar, tile, total;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -72,8 +73,6 @@ __host__ __device__ inline SmemLayout smem_layout(int tile_cap, int max_cta_cell
     o += align16((size_t)kRateTab * sizeof(float2));
     L.part = o;  // [parity][rank in cell][warp]: warp partials (written by the cell's CTAs)
     o += align16((size_t)2 * max_cta_cell * kMaxWarps * sizeof(Partial));
-    L.ctr = o;   // warp completion counters [2 + parity]
-    o += 16;
     L.mbar = o;  // mbarriers: the warp partials of steps of parity 0 and 1 (leader CTA), then the
     o += 32;     // per-step SSA values of parity 0 and 1 (every CTA)
     L.tile = o;  // TileRec<R> per CRU
@@ -109,6 +108,20 @@ __device__ __forceinline__ void cluster_wait() {
 __device__ __forceinline__ void ode_bar() { asm volatile("bar.sync 1, %0;" ::"n"(kOdeLanes) : "memory"); }
 // barrier of a CTA's SSA warps (named barrier 2, n threads: the CTA's SSA threads 0 .. n-1)
 __device__ __forceinline__ void ssa_bar(int n) { asm volatile("bar.sync 2, %0;" ::"r"(n) : "memory"); }
+// named barrier `id` of n threads that also returns the OR of v over them: a decision that every
+// participating thread takes the same way (a bounded wait's outcome, which is per thread)
+__device__ __forceinline__ bool bar_or(int id, int n, bool v) {
+    int r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.s32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, %2, %3, p;\n\t"
+        "selp.s32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((int)v), "r"(id), "r"(n)
+        : "memory");
+    return r != 0;
+}
 
 // Stimulus of step ri at time t (pulse train or per-step samples).  Uses explicit round-to-nearest
 // operations so the host's evaluation of the same pulse train gives the same values.
@@ -492,7 +505,6 @@ struct CtaView {
     void *svstage;
     Partial *part;
     float2 *rtab;
-    int *ctr;
     uint32_t mbar;  // shared address of the partials' mbarrier of parity 0 (parity 1 at +8); the
                     // SSA values' mbarriers of parity 0 and 1 at +16 and +24
     TileRec<R> *tile;
@@ -519,7 +531,6 @@ struct CtaView {
         svstage = smem + L.svs;
         part = reinterpret_cast<Partial *>(smem + L.part);
         rtab = reinterpret_cast<float2 *>(smem + L.rtab);
-        ctr = reinterpret_cast<int *>(smem + L.ctr);
         mbar = smem_addr(smem + L.mbar);
         tile = reinterpret_cast<TileRec<R> *>(smem + L.tile);
         off = OdeOffsets{(uint32_t)L.prog, (uint32_t)L.x, (uint32_t)L.ode, (uint32_t)L.math, (uint32_t)L.svs};
@@ -582,6 +593,15 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
         if (ot == 0) stage_pair(stage, SV_CAI, SV_CAI_LO, os.g[3]);
         if (ot == 1) stage_pair(stage, SV_CANSR, SV_CANSR_LO, os.g[4]);
     }
+    // The next step's stimulus is formed by lane 0 of a warp without ops in the update phase (its
+    // t_{s+1} is os.t + dt, the same addition as the update's), else of one idle in the push
+    // phase (os.t is then t_{s+1}), else by thread 0 before the push.
+    int stim_q = -1, stim_warp = 0;
+    for (int w = kOdeWarps - 1; w >= 0; --w)
+        if (stim_q < 0 && P.wkind[P.upd_phase][w] == OK_NOP) stim_q = P.upd_phase, stim_warp = w;
+    for (int w = kOdeWarps - 1; w >= 0; --w)
+        if (stim_q < 0 && P.push_phase > P.upd_phase && P.wkind[P.push_phase][w] == OK_NOP)
+            stim_q = P.push_phase, stim_warp = w;
     // transcendental phases of the initial state, push sv[0]
     {
         const int reg = v_regime(os.g[0]);
@@ -590,11 +610,6 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
             ode_bar();
         }
         push_sv<FP64>(v.svbuf, v.svstage, 0, v.mbar + 16u, v.w, ot);
-        // nothing this thread wrote is read by another CTA through the barrier (the SSA values
-        // travel by st.async), and within the CTA a fence suffices: a relaxed arrive does not wait
-        // for the remote stores to land
-        __threadfence_block();
-        cluster_arrive_relaxed();
         for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
             ode_phase<T, R>(v.off, q, reg, ot);
             ode_bar();
@@ -603,30 +618,40 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
     // bytes of the cell's warp partials per step (every SSA warp of the cell pushes 32 B)
     const uint32_t part_bytes =
         (uint32_t)sizeof(Partial) * (uint32_t)(v.nw + (v.w.n_cta_cell - 1) * (v.nw + kOdeWarps));
+    bool stopped = false;  // a wait ran out (the same on every ODE thread)
     for (int s = 0; s < a.n_steps; ++s) {
         const int par = s & 1;
         const int64_t ri = a.run_step0 + s;
         const bool rec = a.record_every > 0 && (ri % a.record_every) == 0;
         const int64_t r_idx = rec ? ri / a.record_every - a.rec_base : -1;
         const bool rec_ok = rec && r_idx >= 0 && r_idx < a.rec_cap;
-        cluster_wait();
+        // After a wait has run out the cell stops for the rest of the launch (no waits, no
+        // declarations, no pushes): its CTAs then run out their own waits and stop too, so the
+        // launch ends within about a second per CTA and few stray bytes land on any mbarrier.
+        if (stopped) continue;
         // the partials of step s will complete the next phase of mbarrier par (the previous one,
         // step s-2's, completed before this thread's wait in step s-1)
-        if (ot == 0 && os.status != GW_ERR_SYNC_TIMEOUT)
+        if (ot == 0)
             mbar_arrive_expect_tx(v.mbar + 8u * (uint32_t)par,
                                   part_bytes + (s == a.n_steps - 1 ? (uint32_t)a.test_extra_tx : 0u));
         // fluxes of step s-1 (or the carry), then the global step s -> s+1
         if (ot == 0 && (not_positive(os.g[1]) || not_positive(os.g[2])) && os.status == 0)
             os.status = GW_ERR_NERNST;
-        // (after one wait has run out, the cell's results are void: no further waits)
-        if (s > 0 && os.status != GW_ERR_SYNC_TIMEOUT &&
-            !mbar_wait(v.mbar + 8u * (uint32_t)(par ^ 1), (uint32_t)((s - 1) >> 1) & 1u) && lane == 0)
-            atomicCAS(&os.status, 0, (int)GW_ERR_SYNC_TIMEOUT);
+        if (s > 0) {
+            const bool ok = mbar_wait(v.mbar + 8u * (uint32_t)(par ^ 1), (uint32_t)((s - 1) >> 1) & 1u);
+            if (bar_or(1, kOdeLanes, !ok)) {  // the same decision on all ODE threads
+                if (ot == 0) atomicCAS(&os.status, 0, (int)GW_ERR_SYNC_TIMEOUT);
+                stopped = true;
+                continue;
+            }
+        }
         if (s > 0) reduce_partials<FP64, T>(v.part + (par ^ 1) * pslot, v.w.n_cta_cell * kMaxWarps, ot >> 5, lane, os.sums, X);
-        if (s > 0 && ot == 0) X[XS_ISTIM] = (T)os.stim[par];
+        if (s > 0 && ot == 0) X[XS_ISTIM] = (T)os.stim[par];  // formed in step s-1 (below)
         ode_bar();
         const int reg_n = v_regime(os.g[0]);
         for (int q = 0; q <= P.upd_phase; ++q) {
+            if (q == stim_q && lane == 0 && (ot >> 5) == stim_warp)
+                os.stim[par ^ 1] = stimulus(a.dyn[cell], os.t + a.dt, ri + 1);
             ode_phase<T, R>(v.off, q, reg_n, ot);
             ode_bar();
         }
@@ -642,29 +667,32 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
         if (ot == kOdeLanes - 1) stage_pair(reinterpret_cast<R *>(v.svstage), SV_CAI, SV_CAI_LO, os.g[3]);
         if (ot == kOdeLanes - 2) stage_pair(reinterpret_cast<R *>(v.svstage), SV_CANSR, SV_CANSR_LO, os.g[4]);
         for (int q = P.upd_phase + 1; q <= P.push_phase; ++q) {
+            if (q == stim_q && lane == 0 && (ot >> 5) == stim_warp)
+                os.stim[par ^ 1] = stimulus(a.dyn[cell], os.t, ri + 1);
             ode_phase<T, R>(v.off, q, reg, ot);
             ode_bar();
         }
         // the new globals become the old ones of the next step's increments (read after the
-        // next step's first barrier; no phase after this point reads XS_G)
+        // next step's ode_bar; no phase after this point reads XS_G)
         if (ot < kNumGlobals) X[XS_G + ot] = X[XS_GN + ot];
+        // (no warp idle in either phase: the stimulus formed here)
+        if (stim_q < 0 && ot == 0) os.stim[par ^ 1] = stimulus(a.dyn[cell], os.t, ri + 1);
         // (no push after the launch's last step: no one would wait for those bytes, and a CTA
         // must not exit while stores into its shared memory may still be in flight)
         if (s + 1 < a.n_steps)
             push_sv<FP64>(v.svbuf, v.svstage, par ^ 1, v.mbar + 16u + 8u * (uint32_t)(par ^ 1), v.w, ot);
-        __threadfence_block();
-        cluster_arrive_relaxed();
         // off the critical path: the phases the SSA does not need
         for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
             ode_phase<T, R>(v.off, q, reg, ot);
             ode_bar();
         }
     }
-    cluster_wait();
     // carry of the last step's fluxes, globals and counters back to the cell block
-    if (a.n_steps > 0 && os.status != GW_ERR_SYNC_TIMEOUT &&
-        !mbar_wait(v.mbar + 8u * (uint32_t)((a.n_steps - 1) & 1), (uint32_t)((a.n_steps - 1) >> 1) & 1u) && lane == 0)
-        atomicCAS(&os.status, 0, (int)GW_ERR_SYNC_TIMEOUT);
+    if (a.n_steps > 0 && !stopped) {
+        const bool ok =
+            mbar_wait(v.mbar + 8u * (uint32_t)((a.n_steps - 1) & 1), (uint32_t)((a.n_steps - 1) >> 1) & 1u);
+        if (bar_or(1, kOdeLanes, !ok) && ot == 0) atomicCAS(&os.status, 0, (int)GW_ERR_SYNC_TIMEOUT);
+    }
     if (a.n_steps > 0)
         reduce_partials<FP64, T>(v.part + ((a.n_steps - 1) & 1) * pslot, v.w.n_cta_cell * kMaxWarps, ot >> 5, lane, os.sums, X);
     ode_bar();
@@ -679,6 +707,9 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
         d.step = step0 + (uint64_t)a.n_steps;
         if (os.status != 0) atomicCAS(&a.status[cell], 0, os.status);
     }
+    // the launch's one closing cluster barrier (every thread of every CTA of the cluster)
+    cluster_arrive();
+    cluster_wait();
 }
 
 // The SSA warps over a launch (every warp of a CTA that is not a leader's ODE warp, and every
@@ -694,35 +725,36 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
     const int warp = v.warp, lane = v.lane, cell = w.cell, n_ssa = v.n_ssa;
     const SsaConsts<R> &cc = *v.cc;
     TileRec<R> *tile = v.tile;
-    int *ctr = v.ctr;
     const int pslot = a.max_cta_cell * kMaxWarps;  // warp partials per parity slot
     const R dt = (R)a.dt;
     unsigned long long my_events = 0;
     int my_err = 0;  // bit 0: a CRU hit the event cap; bit 1: a wait for the SSA values ran out
-    cluster_arrive();
     for (int s = 0; s < a.n_steps; ++s) {
         const int par = s & 1;
         const int64_t ri = a.run_step0 + s;
         const bool rec = a.record_every > 0 && (ri % a.record_every) == 0;
         const int64_t r_idx = rec ? ri / a.record_every - a.rec_base : -1;
         const bool rec_ok = rec && r_idx >= 0 && r_idx < a.rec_cap;
-        cluster_wait();
-        if (v.active) {
-            // The counter of parity par^1 was last used in step s-1, which every warp of this
-            // CTA has left; it is next used in step s+1, after the cluster barrier.
-            if (threadIdx.x == 0) ctr[2 + (par ^ 1)] = 0;
+        if (v.active && !(my_err & 2)) {
             // The SSA values of step s arrive by st.async from the leader's ODE warps and complete
             // this CTA's mbarrier of parity par (thread 0 declares the bytes; that mbarrier's
-            // previous phase, step s-2's, completed before this CTA's waits of step s-2).  After
-            // one wait has run out the results are void and no further waits are made.
+            // previous phase, step s-2's, completed before this CTA's waits of step s-2).  The
+            // CTA's SSA threads then meet at named barrier 2 (all have left step s-1, so the rate
+            // table may be rebuilt; the CTAs of a cell are held together only by their data) and
+            // take the wait's outcome together: after a wait has run out the CTA stops for the
+            // rest of the launch (no more sends), so that its partners stop too.
             const uint32_t svm = v.mbar + 16u + 8u * (uint32_t)par;
-            if (threadIdx.x == 0 && !(my_err & 2)) mbar_arrive_expect_tx(svm, (uint32_t)(kSvCount * sizeof(R)));
-            if (!(my_err & 2) && !mbar_wait(svm, (uint32_t)(s >> 1) & 1u)) my_err |= 2;
+            if (threadIdx.x == 0) mbar_arrive_expect_tx(svm, (uint32_t)(kSvCount * sizeof(R)));
+            const bool ok = mbar_wait(svm, (uint32_t)(s >> 1) & 1u);
+            if (bar_or(2, n_ssa, !ok)) {
+                my_err |= 2;
+                continue;
+            }
             const R *sv = v.svbuf + par * kSvCount;
             const int nsw = n_ssa >> 5;
             if (!FP64) {
                 // The CTA's rate table for this step: entry e by SSA thread e, then the CTA's SSA
-                // warps meet at named barrier 2 (they leave the cluster barrier together).
+                // warps meet at named barrier 2.
                 for (int e = (int)threadIdx.x; e < kRateTab; e += n_ssa) build_rate_entry<R>(v.rtab, cc, sv, e);
                 ssa_bar(n_ssa);
             }
@@ -772,7 +804,6 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
             // sums the cell's warp partials in slot order (no reduction on this side of the
             // barrier).
             const Partial pv = acc.warp_total();
-            int done = 0;
             if (lane == 0) {
                 // two 16-byte asynchronous stores that count themselves off the leader's mbarrier
                 // of this parity: the arrive below does not wait for them to land
@@ -781,24 +812,11 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
                 const uint32_t rm = map_rank_addr(v.mbar + 8u * (uint32_t)par, (uint32_t)w.first);
                 st_async(rd, make_uint4(lo_of(pv.v[0]), hi_of(pv.v[0]), lo_of(pv.v[1]), hi_of(pv.v[1])), rm);
                 st_async(rd + 16u, make_uint4(lo_of(pv.v[2]), hi_of(pv.v[2]), lo_of(pv.v[3]), hi_of(pv.v[3])), rm);
-                done = atomicAdd(&ctr[2 + par], 1);  // the order of finishing (first warp below)
-            }
-            done = __shfl_sync(0xffffffffu, done, 0);
-            if (v.leader && done == 0 && lane == 0) {
-                // The stimulus of step s+1 at t_{s+1} (the ODE warps' t after this step's update,
-                // formed by the same additions), by the warp of the leader CTA that finishes first:
-                // it has slack, the ODE warps read it after the barrier.
-                OdeShared &os = *v.os;
-                os.tstim += a.dt;
-                os.stim[par ^ 1] = stimulus(a.dyn[cell], os.tstim, ri + 1);
             }
         }
-        // Nothing an SSA thread wrote is read by another CTA through the barrier (the partials
-        // travel by st.async); the stimulus and the counters are read within the CTA, for which
-        // a CTA fence before a relaxed arrive suffices.  A release arrive would wait ~900 cycles.
-        __threadfence_block();
-        cluster_arrive_relaxed();
     }
+    // the launch's one closing cluster barrier (every thread of every CTA of the cluster)
+    cluster_arrive();
     cluster_wait();
     if (!v.active) return;
     // the tile back to the cell's planes
@@ -833,11 +851,11 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
     }
 }
 
-// The engine kernel: every CTA of a cluster first waits for the whole cluster to be resident (it
-// writes into the other CTAs' shared memory from its first global step on), loads its CRU tile
-// and the cell's SSA constants, then splits into the ODE warps of a leader CTA and the SSA warps.
-// Both parts keep the same sequence of cluster barriers: one arrive after the setup, then one
-// wait and one arrive per global step, and one final wait.
+// The engine kernel: every CTA of a cluster initialises its mbarriers and waits for the whole
+// cluster to be resident (it writes into the other CTAs' shared memory from its first global step
+// on), loads its CRU tile and the cell's SSA constants, then splits into the ODE warps of a leader
+// CTA and the SSA warps.  Both parts end with one more cluster barrier, so that no CTA exits
+// while another may still write into its shared memory.
 template <bool FP64, bool ODE64>
 __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const __grid_constant__ KernelArgs a) {
     using R = typename std::conditional<FP64, double, float>::type;
@@ -855,8 +873,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const __grid_con
         const int cell = v.w.cell;
         if (threadIdx.x == 0) {
             load_ssa_consts<R>(*v.cc, a.cs[cell]);
-            v.ctr[0] = v.ctr[1] = v.ctr[2] = v.ctr[3] = 0;
-            if (v.leader) v.os->tstim = a.dyn[cell].t;
+
         }
         // The leader's warp-partial slots start at zero (slots of warps a CTA does not have stay
         // so); the cell's CTAs write them only after the first cluster barrier of the steps.
