@@ -214,15 +214,21 @@ int plan_shape(gw_ctx *c, int cluster_req, int tile_req) {
     }
     c->n_clusters = (int)used.size();
     c->work.assign((size_t)c->n_clusters * C, CtaWork{-1, 0, 0, 0, 0, 0, 0, 0});
-    // A cell's CRUs are split in proportion to the CTAs' SSA warps: the leader CTA has
-    // ssa_warps, the others ssa_warps + kOdeWarps.
-    const int64_t wl = c->ssa_warps, wo = c->ssa_warps + kOdeWarps;
+    // A cell's CRUs are split in proportion to the CTAs' SSA warps that take CRUs: the others have
+    // ssa_warps + kOdeWarps, the leader ssa_warps, or none when the cell is spread over several
+    // CTAs of under kLeaderFreeCrus CRUs each: the global step (~12 k cycles, on the leader's SM)
+    // then sets the step, and it runs ~10 % faster without SSA warps beside it (measured on one
+    // 12,500-CRU cell over 16 CTAs: 6.75 -> 6.15 us per step early in the beat, 7.52 -> 7.32 at
+    // 60-160 ms).  Larger CTA loads are SSA-bound and keep the leader's share.
+    constexpr int64_t kLeaderFreeCrus = 1024;
+    const int64_t wo = c->ssa_warps + kOdeWarps;
     int max_count = 0;
     for (int q = 0; q < c->n_clusters; ++q) {
         int rank = 0;
         for (int cell : members[q]) {
             const int64_t n = c->ncru[cell];
             const int k = std::max(1, (int)((n + tile - 1) / tile));
+            const int64_t wl = (k >= 2 && n < kLeaderFreeCrus * k) ? 0 : c->ssa_warps;
             const int64_t W = wl + (k - 1) * wo;
             auto cum = [&](int r) -> int64_t { return r == 0 ? 0 : wl + (r - 1) * wo; };
             for (int r = 0; r < k; ++r) {
@@ -233,6 +239,7 @@ int plan_shape(gw_ctx *c, int cluster_req, int tile_req) {
                 w.rank_in_cell = r;
                 w.first = rank;
                 w.n_cta_cell = k;
+                w.lead_warps = (int)wl;
                 max_count = std::max(max_count, w.cru_count);
             }
             rank += k;

@@ -760,8 +760,10 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
             }
             // This warp's CRUs [cursor, end).  A lane whose CRU has finished its step takes the
             // next one, so lanes with pending SSA events do not hold the others back.
-            const int beg = (int)((int64_t)w.cru_count * warp / nsw);
-            const int end = (int)((int64_t)w.cru_count * (warp + 1) / nsw);
+            // (a leader takes CRUs on its first lead_warps SSA warps only, possibly none)
+            const int nse = v.leader ? w.lead_warps : nsw;
+            const int beg = warp < nse ? (int)((int64_t)w.cru_count * warp / nse) : w.cru_count;
+            const int end = warp < nse ? (int)((int64_t)w.cru_count * (warp + 1) / nse) : w.cru_count;
             int cursor = beg;
             FluxAcc<FP64> acc;
             Cru<R> c;

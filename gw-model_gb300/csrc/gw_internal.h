@@ -78,7 +78,9 @@ struct CtaWork {
     int rank_in_cell;
     int first;
     int n_cta_cell;
-    int pad0, pad1;
+    int lead_warps;  // SSA warps of the cell's leader CTA that take CRUs (0: the leader runs only
+                     // the global step, for cells spread thinly enough that it sets the step)
+    int pad1;
 };
 
 struct OdeProgram;
