@@ -36,7 +36,6 @@ struct OdeShared {
     double g[kNumGlobals];  // the cell's globals (FP64 state)
     double t;               // accumulated time
     double sums[4];         // JLCC, ClCh, Jtr, Jxfer sums of the last reduced step (FP64)
-    double tstim;           // unused
     double stim[2];         // stimulus of step s in slot s & 1, from the leader's SSA warps
     int status;
     int pad;
@@ -538,9 +537,9 @@ struct CtaView {
 };
 
 // The leader CTA's ODE warps over a launch: the transcendental phases of the initial state and
-// the push of sv[0], then per global step s the reduction of the CTA partials of step s-1, the
-// global step s -> s+1 and the push of sv[(s+1)&1], and the carry back to the cell block at the
-// end.  A function of its own (not inlined into the kernel), so that its register allocation and
+// the push of sv[0], then per global step s the wait for and reduction of the warp partials of
+// step s-1, the global step s -> s+1 and the push of sv[(s+1)&1], and the carry back to the cell
+// block at the end.  A function of its own (not inlined into the kernel), so that its register allocation and
 // schedule do not depend on the SSA code.
 template <bool FP64, bool ODE64>
 __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
@@ -713,9 +712,9 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
 }
 
 // The SSA warps over a launch (every warp of a CTA that is not a leader's ODE warp, and every
-// warp of an idle CTA, which only keeps the cluster barriers): per global step the SSA of the
-// warp's CRUs, the record pass and the flux partials, and the tile back to the cell's planes at
-// the end.  Inlined into the kernel (out of line it spills).
+// warp of an idle CTA, which only keeps the closing cluster barrier): per global step the SSA of
+// the warp's CRUs, the record pass and the flux partials, and the tile back to the cell's planes
+// at the end.  Inlined into the kernel (out of line it spills).
 template <bool FP64, bool ODE64>
 __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
     using R = typename std::conditional<FP64, double, float>::type;
@@ -803,12 +802,11 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
             if (rec_ok && (cell == a.tr_cell || a.tr_sums != nullptr))
                 record_pass<R>(a, w, cell, r_idx, beg, end, lane, tile);
             // The warp partial, pushed straight into the leader's slot (rank, warp): the leader
-            // sums the cell's warp partials in slot order (no reduction on this side of the
-            // barrier).
+            // sums the cell's warp partials in slot order (no reduction on this side).
             const Partial pv = acc.warp_total();
             if (lane == 0) {
                 // two 16-byte asynchronous stores that count themselves off the leader's mbarrier
-                // of this parity: the arrive below does not wait for them to land
+                // of this parity (the warp goes on without waiting for them to land)
                 Partial *dst = v.part + par * pslot + w.rank_in_cell * kMaxWarps + warp;
                 const uint32_t rd = map_rank(dst, (uint32_t)w.first);
                 const uint32_t rm = map_rank_addr(v.mbar + 8u * (uint32_t)par, (uint32_t)w.first);
