@@ -50,7 +50,7 @@ METRIC = "CRU-steps/s and sim-ms/wall-s: batched vs plain GPU vs CPU, at KS/FP64
 BYTES_PER_CRU_STEP = 2 * 72
 # DRAM bytes (read + write) of one 1000-step launch of this workload, from the ncu capture in
 # profiles/engine_kernel_cell12500.txt (the bench's launches have exactly that shape).
-TRAFFIC_PER_LAUNCH = 1.048320e6
+TRAFFIC_PER_LAUNCH = 1.047296e6
 
 
 def parse():
