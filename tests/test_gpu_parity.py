@@ -120,6 +120,17 @@ def test_fp64_launch_shape_independent(oracle, shape):
     assert rel(g, m.globals().to_array()) <= 1e-12
 
 
+def test_fp64_leader_with_and_without_ssa(oracle):
+    """A cell over several CTAs of at least 1,024 CRUs each keeps SSA work on its leader CTA (the
+    split 12 : 16 warps); thinner cells give the leader none (the other parity cases).  Both are the
+    oracle's trajectory: 2,400 CRUs over two CTAs of up to 1,216."""
+    m, (g, s, st) = run_pair(oracle, 2400, 300, 6, "fp64", cluster_ctas=2, cta_crus=1216)
+    assert st["ctas"] == 2
+    for k in CHANNELS:
+        np.testing.assert_array_equal(getattr(s, k), getattr(m.crus(), k))
+    assert rel(g, m.globals().to_array()) <= 1e-12
+
+
 def _u24_state(oracle, n, seed, warm):
     """A state taken from an FP64 oracle run `warm` steps into an AP (open channels, raised CaSS)."""
     p = oracle.default_params()
