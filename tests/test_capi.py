@@ -32,6 +32,18 @@ def test_exports_every_declared_symbol(enginelib):
         assert hasattr(enginelib, n)
 
 
+def test_status_codes_match_bindings():
+    """Every gw_status the header declares has the same value in the Python mirror."""
+    from gwgb300 import _lib
+
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    body = re.search(r"typedef enum gw_status \{(.*?)\} gw_status;", src, flags=re.S).group(1)
+    codes = dict((n, int(v)) for n, v in re.findall(r"(GW_\w+)\s*=\s*(\d+)", body))
+    assert codes["GW_OK"] == 0 and "GW_ERR_SYNC_TIMEOUT" in codes
+    for name, value in codes.items():
+        assert getattr(_lib, name) == value, name
+
+
 def test_struct_layouts_match_bindings(enginelib):
     from gwgb300 import _lib
 
