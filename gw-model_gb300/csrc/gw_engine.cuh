@@ -68,8 +68,8 @@ __host__ __device__ inline SmemLayout smem_layout(int tile_cap, int max_cta_cell
     o += align16(sizeof(math64::Tables));
     L.svs = o;   // staging of the per-step SSA values before the push
     o += align16(kSvCount * sizeof(R));
-    L.rtab = o;  // the CTA's subunit rate table (FP32 SSA)
-    o += align16((size_t)kRateTab * sizeof(float2));
+    L.rtab = o;  // the CTA's subunit rate tables (FP32 SSA), one per step parity
+    o += align16((size_t)2 * kRateTab * sizeof(float2));
     L.part = o;  // [parity][rank in cell][warp]: warp partials (written by the cell's CTAs)
     o += align16((size_t)2 * max_cta_cell * kMaxWarps * sizeof(Partial));
     L.mbar = o;  // mbarriers: the warp partials of steps of parity 0 and 1 (leader CTA), then the
@@ -671,15 +671,15 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
             ode_phase<T, R>(v.off, q, reg, ot);
             ode_bar();
         }
-        // the new globals become the old ones of the next step's increments (read after the
-        // next step's ode_bar; no phase after this point reads XS_G)
-        if (ot < kNumGlobals) X[XS_G + ot] = X[XS_GN + ot];
         // (no warp idle in either phase: the stimulus formed here)
         if (stim_q < 0 && ot == 0) os.stim[par ^ 1] = stimulus(a.dyn[cell], os.t, ri + 1);
         // (no push after the launch's last step: no one would wait for those bytes, and a CTA
         // must not exit while stores into its shared memory may still be in flight)
         if (s + 1 < a.n_steps)
             push_sv<FP64>(v.svbuf, v.svstage, par ^ 1, v.mbar + 16u + 8u * (uint32_t)(par ^ 1), v.w, ot);
+        // the new globals become the old ones of the next step's increments (read after the
+        // next step's ode_bar; no phase after this point reads XS_G)
+        if (ot < kNumGlobals) X[XS_G + ot] = X[XS_GN + ot];
         // off the critical path: the phases the SSA does not need
         for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
             ode_phase<T, R>(v.off, q, reg, ot);
@@ -745,18 +745,18 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
             const uint32_t svm = v.mbar + 16u + 8u * (uint32_t)par;
             if (threadIdx.x == 0) mbar_arrive_expect_tx(svm, (uint32_t)(kSvCount * sizeof(R)));
             const bool ok = mbar_wait(svm, (uint32_t)(s >> 1) & 1u);
+            const R *sv = v.svbuf + par * kSvCount;
+            // FP32: the CTA's rate table of this step, entry e by SSA thread e, into the table of
+            // this parity (a warp still in step s-1 reads the other one; the barrier below, which
+            // every SSA thread reaches only after step s-1, publishes it)
+            float2 *rtab = v.rtab + par * kRateTab;
+            if (!FP64)
+                for (int e = (int)threadIdx.x; e < kRateTab; e += n_ssa) build_rate_entry<R>(rtab, cc, sv, e);
             if (bar_or(2, n_ssa, !ok)) {
                 my_err |= 2;
                 continue;
             }
-            const R *sv = v.svbuf + par * kSvCount;
             const int nsw = n_ssa >> 5;
-            if (!FP64) {
-                // The CTA's rate table for this step: entry e by SSA thread e, then the CTA's SSA
-                // warps meet at named barrier 2.
-                for (int e = (int)threadIdx.x; e < kRateTab; e += n_ssa) build_rate_entry<R>(v.rtab, cc, sv, e);
-                ssa_bar(n_ssa);
-            }
             // This warp's CRUs [cursor, end).  A lane whose CRU has finished its step takes the
             // next one, so lanes with pending SSA events do not hold the others back.
             // (a leader takes CRUs on its first lead_warps SSA warps only, possibly none)
@@ -788,7 +788,7 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
                 if (!__any_sync(0xffffffffu, m >= 0)) break;
                 if (m >= 0) {
                     int err = 0;
-                    if (sl.iterate(c, cc, sv, v.rtab, rng, dt, a.event_cap, err)) {
+                    if (sl.iterate(c, cc, sv, rtab, rng, dt, a.event_cap, err)) {
                         tile_put(tile[m], c);
                         my_events += (unsigned long long)sl.ev;
                         my_err |= err;
