@@ -166,7 +166,7 @@ int gw_destroy(gw_ctx *ctx);
 /* No counterpart in the reference (it has one CPU code path).  Measures the launch shape for an
  * ensemble: for each cluster size in {16, 9, 8, 6, 4, 3, 2, 1} that fits, and for two CTA capacities each
  * (the size rule's, cta_crus = 0, and the largest that fits shared memory: fewer, fuller CTAs
- * amortise the per-step cluster barrier and global step over more CRUs, which pays off for cells
+ * amortise the per-step exchange between CTAs and the global step over more CRUs, which pays off for cells
  * of uneven size), builds a throwaway context from *desc (its cluster_ctas and cta_crus are
  * ignored), paces it at 1 Hz and times trial_steps global steps after a short warm-up; returns the
  * fastest cluster size, its CTA capacity (0 = size rule; best_cta_crus may be NULL) and its
