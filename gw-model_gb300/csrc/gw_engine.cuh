@@ -608,6 +608,8 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
             ode_phase<T, R>(v.off, q, reg, ot);
             ode_bar();
         }
+        // (the SSA warps wait for these bytes in step 0: the host launches 1..steps_per_launch
+        // steps, never 0, so no CTA exits while they may be in flight)
         push_sv<FP64>(v.svbuf, v.svstage, 0, v.mbar + 16u, v.w, ot);
         for (int q = P.push_phase + 1; q < P.n_phases; ++q) {
             ode_phase<T, R>(v.off, q, reg, ot);
