@@ -847,6 +847,36 @@ int64_t orc_run(orc_model *m, double dt, int64_t num_steps, const double *Istim,
     return counter < max_records ? counter : max_records;
 }
 
+/* run<PRNG> with record_state (pyGW.hpp:56-122): the same loop as orc_run, and at each record the
+ * CRU arrays as well (record_state copies every CRU array, pyGW.hpp:84-98).  Any record pointer
+ * may be NULL.  Returns the number of records the reference's loop makes (ceil(num_steps /
+ * record_every)); only the first max_records of them are stored. */
+int64_t orc_run_record(orc_model *m, double dt, int64_t num_steps, const double *Istim,
+                       int record_every, int64_t max_records, double *rec_t,
+                       orc_globals *rec_globals, double *rec_CaSS, double *rec_CaJSR,
+                       int *rec_LCC, int *rec_LCCi, int *rec_RyR, int *rec_ClCh) {
+    const size_t n = (size_t)m->n;
+    double t = 0.0;
+    int64_t counter = 0;
+    for (int64_t i = 0; i < num_steps; ++i) {
+        orc_euler_step(m, dt, Istim ? Istim[i] : 0.0);
+        t += dt;
+        if (record_every > 0 && i % record_every == 0) {
+            if (counter < max_records) {
+                const size_t r = (size_t)counter;
+                if (rec_t) rec_t[r] = t;
+                if (rec_globals) rec_globals[r] = m->g;
+                orc_get_crus(m, rec_CaSS ? rec_CaSS + r * 4 * n : NULL,
+                             rec_CaJSR ? rec_CaJSR + r * n : NULL, rec_LCC ? rec_LCC + r * 4 * n : NULL,
+                             rec_LCCi ? rec_LCCi + r * 4 * n : NULL, rec_RyR ? rec_RyR + r * 24 * n : NULL,
+                             rec_ClCh ? rec_ClCh + r * 4 * n : NULL);
+            }
+            ++counter;
+        }
+    }
+    return counter;
+}
+
 void orc_cru_rates(const orc_params *p, const orc_consts *c, const int *LCC, const int *LCCi,
                    const int *RyR, const int *ClCh, const double *CaSS, double *LCC_rates,
                    double *LCCi_rates, double *RyR_rates, double *ClCh_rates,

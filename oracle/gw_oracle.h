@@ -148,6 +148,14 @@ void orc_euler_step(orc_model *m, double dt, double Istim);
  * as pyGW.hpp:113-121 does.  Returns the number of records written. */
 int64_t orc_run(orc_model *m, double dt, int64_t num_steps, const double *Istim, int record_every,
                 int64_t max_records, double *rec_t, orc_globals *rec_globals);
+/* orc_run recording the CRU arrays too (record_state, pyGW.hpp:56-99): record r of CaSS is
+ * rec_CaSS[r][n][4], of RyR rec_RyR[r][n][4][6], and so on; NULL skips a field.  Returns the
+ * number of records the reference's loop makes, ceil(num_steps / record_every); the first
+ * max_records are stored. */
+int64_t orc_run_record(orc_model *m, double dt, int64_t num_steps, const double *Istim,
+                       int record_every, int64_t max_records, double *rec_t,
+                       orc_globals *rec_globals, double *rec_CaSS, double *rec_CaJSR,
+                       int *rec_LCC, int *rec_LCCi, int *rec_RyR, int *rec_ClCh);
 /* Total SSA events (jumps) executed so far, and the worst per-CRU-step count. */
 int64_t orc_event_count(const orc_model *m);
 int orc_set_threads(int n);

@@ -85,13 +85,30 @@ _lib = None
 _ref = None
 
 
+def reference_dir() -> str:
+    """Checkout of the reference (lukeoloughlin/GW-model): $GW_REFERENCE_DIR, else the REF default
+    of oracle/Makefile, the recipe that compiles the reference's sources where they lie."""
+    env = os.environ.get("GW_REFERENCE_DIR")
+    if env:
+        return env
+    import re
+
+    with open(os.path.join(HERE, "Makefile")) as f:
+        m = re.search(r"^REF\s*\?=\s*(\S+)", f.read(), re.M)
+    return m.group(1) if m else ""
+
+
+def reference_sources_present() -> bool:
+    return os.path.isdir(os.path.join(reference_dir(), "src", "includes"))
+
+
 def build(force: bool = False) -> None:
     """Compile the oracle (and the reference harness when the reference sources are present)."""
     with _lock:
         if force or not os.path.exists(LIB_PATH):
             subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-        if os.path.isdir("/root/reference/src/includes") and (force or not os.path.exists(REF_PATH)):
-            subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        if reference_sources_present() and (force or not os.path.exists(REF_PATH)):
+            subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + reference_dir()], check=True)
 
 
 def _dp(a):
@@ -138,6 +155,10 @@ def lib():
         L.orc_run.restype = C.c_int64
         L.orc_run.argtypes = [vp, C.c_double, C.c_int64, P(C.c_double), C.c_int, C.c_int64,
                               P(C.c_double), P(OrcGlobals)]
+        L.orc_run_record.restype = C.c_int64
+        L.orc_run_record.argtypes = [vp, C.c_double, C.c_int64, P(C.c_double), C.c_int, C.c_int64,
+                                     P(C.c_double), P(OrcGlobals), P(C.c_double), P(C.c_double)] + \
+            [P(C.c_int)] * 4
         L.orc_event_count.restype = C.c_int64
         L.orc_event_count.argtypes = [vp]
         L.orc_set_threads.argtypes = [C.c_int]
@@ -306,6 +327,26 @@ class Model:
         got = self.L.orc_run(self.h, dt, n, _dp(istim), record_every, nrec, _dp(rec_t), rec_g)
         G = np.frombuffer(bytes(rec_g), dtype=np.float64).reshape(-1, 36)[:got].copy()
         return rec_t[:got].copy(), G
+
+    def run_record(self, dt: float, istim: np.ndarray, record_every: int, max_records=None):
+        """run<PRNG> + record_state (pyGW.hpp:56-122): records after every step i with
+        i % record_every == 0.  Returns (records the reference's loop makes, dict of the stored
+        records: t [R], globals [R, 36] and the CRU arrays [R, n, ...]); R = max_records, by
+        default num_steps // record_every, the reference's allocation (pyGW.hpp:109)."""
+        istim = np.ascontiguousarray(istim, dtype=np.float64)
+        n = self.n
+        R = istim.size // record_every if max_records is None else int(max_records)
+        Rb = max(R, 1)
+        out = {"t": np.zeros(Rb), "CaSS": np.zeros((Rb, n, 4)), "CaJSR": np.zeros((Rb, n)),
+               "LCC": np.zeros((Rb, n, 4), np.int32), "LCC_inactivation": np.zeros((Rb, n, 4), np.int32),
+               "RyR": np.zeros((Rb, n, 4, 6), np.int32), "ClCh": np.zeros((Rb, n, 4), np.int32)}
+        rec_g = (OrcGlobals * Rb)()
+        made = self.L.orc_run_record(self.h, dt, istim.size, _dp(istim), record_every, R, _dp(out["t"]), rec_g,
+                                     _dp(out["CaSS"]), _dp(out["CaJSR"]), _ip(out["LCC"]),
+                                     _ip(out["LCC_inactivation"]), _ip(out["RyR"]), _ip(out["ClCh"]))
+        out["globals"] = np.frombuffer(bytes(rec_g), dtype=np.float64).reshape(-1, 36).copy()
+        k = min(int(made), R)
+        return int(made), {key: v[:k] for key, v in out.items()}
 
     def events(self) -> int:
         return int(self.L.orc_event_count(self.h))

@@ -11,8 +11,16 @@ for p in (os.path.join(REPO, "gw-model_gb300"), os.path.join(REPO, "oracle"), RE
         sys.path.insert(0, p)
 
 GOLDEN = os.path.join(REPO, "tests", "golden")
-# the reference sources, present only where the reference was checked out next to this build
-REF = "/root/reference"
+
+
+def _reference_dir():
+    import pyoracle
+
+    return pyoracle.reference_dir()
+
+
+# the reference checkout, present only where it was checked out next to this build
+REF = _reference_dir()
 
 
 def pytest_configure(config):

@@ -74,8 +74,14 @@ def test_fp64_matches_reference_fixture(oracle, case):
     e.set_globals(0, z["g0"])
     e.set_crus(0, engine.CRUState(*(z["init_" + k] for k in ("CaSS", "CaJSR", "LCC", "LCC_inactivation", "RyR", "ClCh"))))
     e.set_samples(istim)
-    tr = e.run(DT, steps, record_every=rec)
-    # the engine records after steps i with i % rec == 0; the fixture after steps i with (i+1) % rec == 0
+    # the engine records after steps i with i % record_every == 0 (pyGW.hpp:117); the fixture holds
+    # the globals after steps i with (i + 1) % rec == 0: record every step and take those
+    tr = e.run(DT, steps, record_every=1)
+    assert tr.globals.shape == (1, steps, 36)
+    G = tr.globals[0, rec - 1::rec]
+    assert G.shape == z["globals_rec"].shape
+    assert rel(G, z["globals_rec"]) <= 1e-12
+    np.testing.assert_array_equal(tr.t, _accumulated_t(steps, DT))
     s = e.get_crus(0)
     for k in CHANNELS:
         np.testing.assert_array_equal(getattr(s, k), z["final_" + k], err_msg=k)
@@ -84,8 +90,17 @@ def test_fp64_matches_reference_fixture(oracle, case):
     assert rel(e.get_globals(0), z["globals_final"]) <= 1e-12
     jl = s.JLCC
     assert rel(jl, z["JLCC"]) <= 1e-12 if np.any(z["JLCC"]) else np.all(jl == 0)
-    assert tr.globals.shape[1] == steps // rec
     e.close()
+
+
+def _accumulated_t(steps, dt):
+    """t after each step, accumulated by t += dt as the reference's loop does (pyGW.hpp:116)."""
+    out = np.empty(steps)
+    t = 0.0
+    for i in range(steps):
+        t += dt
+        out[i] = t
+    return out
 
 
 @pytest.mark.parametrize("n,steps,seed", [(96, 6000, 1), (33, 12000, 2), (200, 3000, 3)])
@@ -147,6 +162,43 @@ def _u24_state(oracle, n, seed, warm):
     s.CaSS = s.CaSS.astype(np.float32).astype(np.float64)
     s.CaJSR = s.CaJSR.astype(np.float32).astype(np.float64)
     return p, m.globals(), s, m.fluxes()
+
+
+@pytest.mark.parametrize("warm", [2000, 15000, 60000])
+def test_fp64_one_step_matches_oracle_along_the_beat(oracle, warm):
+    """One FP64 CRU step and global step from an identical state (the oracle's after `warm` steps of
+    the 1,250-CRU paced cell: upstroke, Ca release, plateau), the same draws on both sides: channel
+    states bit-exact, CaSS, CaJSR, JLCC and the globals within 1e-12 relative."""
+    from gwgb300 import Ensemble, engine
+
+    po = oracle
+    po.lib().orc_set_threads(os.cpu_count() or 1)
+    n = 1250
+    p = po.default_params()
+    m = po.Model(p, n, seed=3)
+    m.set_globals(po.default_globals(py=True))
+    m.set_crus(po.initial_crus(p, n, seed=4))
+    istim = po.pulse_train(warm + 1, DT, 100.0, 0.5)
+    for i in range(warm):
+        m.euler_step(DT, istim[i])
+    g, s, (JLCC, Jxfer, Jtr) = m.globals(), m.crus(), m.fluxes()
+    t = float(_accumulated_t(warm, DT)[-1])
+    m.euler_step(DT, istim[warm])
+    e = Ensemble([n], params=engine.params_from(p), precision="fp64", seed=3)
+    e.set_globals(0, g.to_array())
+    e.set_crus(0, engine.CRUState(s.CaSS, s.CaJSR, s.LCC, s.LCC_inactivation, s.RyR, s.ClCh, JLCC),
+               with_jlcc=True)
+    e.set_flux_carry(0, float(JLCC.sum()), float(s.ClCh.sum()), float(Jtr.sum()), float(Jxfer.sum()))
+    e.set_time(0, t, warm)
+    e.set_samples(istim[warm:warm + 1])
+    e.run(DT, 1)
+    es, ms = e.get_crus(0), m.crus()
+    for k in CHANNELS:
+        np.testing.assert_array_equal(getattr(es, k), getattr(ms, k), err_msg=k)
+    assert rel(es.CaSS, ms.CaSS) <= 1e-12 and rel(es.CaJSR, ms.CaJSR) <= 1e-12
+    assert rel(es.JLCC[es.JLCC != 0], m.fluxes()[0][es.JLCC != 0]) <= 1e-12
+    assert rel(e.get_globals(0), m.globals().to_array()) <= 1e-12
+    e.close()
 
 
 @pytest.mark.parametrize("warm", [10, 3000, 8000])

@@ -39,3 +39,34 @@ def test_bit_exact(ref, seed, umode):
         assert np.array_equal(getattr(sm, k), getattr(s, k)), k
     for a, b in zip(m.fluxes(), fl):
         assert np.array_equal(a, b)
+
+
+def test_open_lcc_initial_state(ref):
+    """An initial state with open LCCs: the reference's ctor computes JLCC from its own random CRU
+    state (GW.hpp:104-112, states 1, 2 or 7, so JLCC = 0) before set_initial_value installs this one;
+    the oracle starts from JLCC = 0 too, and both runs agree bit for bit, JLCC included."""
+    po = ref
+    n, steps = 30, 400
+    p = po.default_params()
+    init = po.initial_crus(p, n, seed=3)
+    rng = np.random.default_rng(3)
+    pick = rng.random((n, 4)) < 0.3
+    init.LCC[pick] = rng.choice([6, 12], size=int(pick.sum()))
+    init.LCC_inactivation[pick] = 1
+    g0 = po.default_globals(py=True)
+    m = po.Model(p, n, seed=4)
+    m.set_globals(g0)
+    m.set_crus(init)
+    r = po.RefModel(p, n, seed=4)
+    r.set_state(g0, init)
+    assert not np.any(r.state()[2][0])  # the ctor's JLCC, before any step
+    istim = po.pulse_train(steps, 1e-3, 100.0, 0.5)
+    for i in range(steps):
+        m.euler_step(1e-3, istim[i])
+        r.euler_step(1e-3, istim[i])
+    g, s, fl = r.state()
+    assert np.array_equal(m.globals().to_array(), g.to_array())
+    for k in ("CaSS", "CaJSR", "LCC", "LCC_inactivation", "RyR", "ClCh"):
+        assert np.array_equal(getattr(m.crus(), k), getattr(s, k)), k
+    for a, b in zip(m.fluxes(), fl):
+        assert np.array_equal(a, b)
