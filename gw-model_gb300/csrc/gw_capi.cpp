@@ -174,7 +174,13 @@ int plan_shape(gw_ctx *c, int cluster_req, int tile_req) {
     const int max_n = *std::max_element(c->ncru.begin(), c->ncru.end());
     int C = cluster_req > 0 ? cluster_req : 0;
     int tile = tile_req > 0 ? tile_req : 0;
-    if (C == 0 && tile == 0) {
+    if (C == 0 && tile == 0 && c->precision == GW_PRECISION_FP64) {
+        // Default FP64: the SSA is bound by the FP64 pipe (one warp instruction per ~64 cycles per
+        // sub-partition), so a cell is spread over up to 16 CTAs of at most 96 CRUs: three full
+        // warps per CTA on three sub-partitions.
+        C = std::min(kMaxClusterCtas, std::max(1, (max_n + 95) / 96));
+        tile = (max_n + C - 1) / C;
+    } else if (C == 0 && tile == 0) {
         // Default: one CRU per SSA thread where possible, at most 16 CTAs per cell.
         C = 1;
         while (C < kMaxClusterCtas && (max_n + C - 1) / C > 32 * kMaxSsaWarps) C *= 2;

@@ -762,7 +762,12 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
             // This warp's CRUs [cursor, end).  A lane whose CRU has finished its step takes the
             // next one, so lanes with pending SSA events do not hold the others back.
             // (a leader takes CRUs on its first lead_warps SSA warps only, possibly none)
-            const int nse = v.leader ? w.lead_warps : nsw;
+            // FP64: no more working warps than ceil(CRUs / 32).  An FP64 warp instruction takes its
+            // sub-partition's FP64 pipe for ~64 cycles whatever its active lanes, so two warps of
+            // 16 CRUs cost twice one warp of 32; the first warps of a CTA sit on distinct
+            // sub-partitions.
+            int nse = v.leader ? w.lead_warps : nsw;
+            if (FP64) nse = min(nse, (w.cru_count + 31) >> 5);
             const int beg = warp < nse ? (int)((int64_t)w.cru_count * warp / nse) : w.cru_count;
             const int end = warp < nse ? (int)((int64_t)w.cru_count * (warp + 1) / nse) : w.cru_count;
             int cursor = beg;
