@@ -6,23 +6,38 @@ each simulated CRU stands for one real CRU), reference default parameters, GW::G
 globals, the reference's random initial CRU distributions, dt = 1e-3 ms, 1 Hz pacing with a
 +100 pA/pF, 0.5 ms stimulus (the reference integrates dV = dt (Istim - sum I), so the usual
 -100 pA/pF inward stimulus is +100 here).  CRU state FP32, global ODE FP64 with compensated flux
-reduction.  Synthetic seeded input.  A bench step is `--span-ms` of simulated time of that paced
-cell; the timed steps continue the protocol.
+reduction.  Synthetic seeded input.
 
-  value        CRU-steps/s, state resident on the device, CUDA events around the engine kernel
-  e2e          the same through the reference-facing C ABI (gw_simulate: host arrays in and out,
-               the per-step stimulus samples uploaded, a fresh context per call)
-  paths        plain GPU (the same cell, one kernel launch per global step) and batched GPU (256
-               cells of 2,000-12,500 CRUs, log-normal per-cell parameters and 400-1000 ms cycle
-               lengths in one launch), each as CRU-steps/s and simulated ms per wall-second
-  roofline     the engine kernel against HBM, algorithmic bytes = the 72-byte FP32 CRU state read
-               and written once per CRU-step; the kernel keeps the state on chip between steps, so
-               the bound that binds is the per-step dependency chain (see profiles/)
-  cpu_baseline the oracle port of the reference's C++ (OpenMP over CRUs) on the host cores,
-               bounded sample
+Timed window: one whole beat.  The K timed steps are K consecutive windows of 1000/K ms that cover
+0-1000 ms of the beat (upstroke, Ca release, plateau, repolarisation, rest); the W warm-up steps
+run the same windows first on the same context, which is then restored to its t = 0 checkpoint.
+Between timed steps a 256 MB buffer is written (L2 flush; the cell's 0.9 MB state would otherwise
+stay in L2 between launches).
 
---impl reference times the reference's CPU implementation of the path (the oracle port) on the
-host cores with all threads.
+  value        CRU-steps/s over the beat, state resident on the device, CUDA events on the
+               engine's stream around every engine launch
+  e2e          the same beat through the reference-facing C ABI (gw_simulate: host arrays in, the
+               per-step stimulus samples uploaded, the last step's state copied back and passed to
+               the next call, a fresh context per call, as chained run() calls of the reference)
+  paths        plain GPU (the same cell, one launch and one host synchronisation per global step,
+               sampled at every window start of the beat), batched GPU (256 cells of 2,000-12,500
+               CRUs, log-normal per-cell parameters and 400-1000 ms cycle lengths, one launch,
+               0-400 ms of every cell's beat), the large ensemble (1,024 x 12,500 CRUs, 2 Hz,
+               0-50 ms), and config 1 (one 1,250-CRU cell, FP64 throughout, 500 ms) on the GPU
+               beside the CPU port running the same config in full
+  roofline     the engine kernel against HBM (algorithmic bytes = the 72-byte FP32 CRU state read
+               and written once per CRU-step); issue_roofline: warp instructions issued against
+               the issue rate of the SMs the cell uses (what binds a single cell)
+  accuracy     the FP32 path's error against the FP64 oracle at the headline config with common
+               random numbers (1 and 200 steps from the same 12,500-CRU state at four points of
+               the beat), and FP32 vs FP64 ensemble statistics (64 cells x 500 CRUs, 450 ms)
+  cpu_baseline the oracle port of the reference's C++ built with the reference's Release flags,
+               OpenMP over CRUs on all host cores, timed on the same beat phases: a 1,250-CRU cell
+               runs the beat on the CPU, its state at each window start is tiled to 12,500 CRUs,
+               and a bounded sample is timed from each
+
+--impl reference times that CPU implementation alone (the oracle port; the reference's own C++
+cannot be built on the GPU host, which has no copy of its sources).
 """
 from __future__ import annotations
 
@@ -48,9 +63,12 @@ METRIC = "CRU-steps/s and sim-ms/wall-s: batched vs plain GPU vs CPU, at KS/FP64
 # FP32 CRU state per CRU: LCC states 4 B, gate + ClCh bits 4 B, RyR counts 24 B, CaSS 16 B,
 # JLCC 16 B, CaJSR 4 B, CaJSR compensation 4 B = 72 B, read and written once per CRU-step.
 BYTES_PER_CRU_STEP = 2 * 72
-# DRAM bytes (read + write) of one 1000-step launch of this workload, from the ncu capture in
-# profiles/engine_kernel_cell12500.txt (the bench's launches have exactly that shape).
+# From the ncu captures of the engine kernel on this workload (profiles/engine_kernel_cell12500.txt
+# and profiles/engine_kernel_cell12500_instmix.txt): DRAM bytes (read + write) of one 1000-step
+# launch, and warp instructions issued per CRU-step.
 TRAFFIC_PER_LAUNCH = 1.047296e6
+WARP_INST_PER_CRU_STEP = 28.4
+CPU_PRE_NCRU = 1250   # the CPU's beat run, tiled x10 to 12,500 CRUs at each window start
 
 
 def parse():
@@ -59,10 +77,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--span-ms", type=float, default=20.0)
+    ap.add_argument("--beat-ms", type=float, default=PERIOD, help="simulated time the K timed steps cover")
     ap.add_argument("--cells", type=int, default=1, help="replicate cells per GPU (1 = plain path)")
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU time of the timed samples")
     return ap.parse_args()
 
 
@@ -112,6 +130,30 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+class L2Flush:
+    """Writes a 256 MB device buffer (twice the 129 MB L2) between timed steps."""
+
+    def __init__(self, device):
+        self.buf = None
+        try:
+            import torch
+
+            if torch.cuda.is_available():
+                self.buf = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{device}")
+                self.torch = torch
+        except Exception:
+            self.buf = None
+
+    def __call__(self, k=0):
+        if self.buf is not None:
+            self.buf.fill_(k & 0xFF)
+            self.torch.cuda.synchronize(self.buf.device)
+
+    def note(self):
+        return "256 MB buffer written between timed steps (L2 flush)" if self.buf is not None else \
+            "no L2 flush (torch CUDA unavailable)"
+
+
 def peaks():
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
@@ -120,42 +162,97 @@ def peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def cpu_baseline(seconds: float, ncru: int = NCRU):
-    """The oracle port (C restatement of the reference, OpenMP over CRUs) timed on the host cores on
-    a bounded sample of the paced cell: the first steps after the stimulus."""
+def pulse(t: float) -> float:
+    """The 1 Hz stimulus at time t, the engine's pulse-train formula."""
+    tb = t - PERIOD * float(int(t / PERIOD))
+    return STIM_AMP if tb < STIM_DUR else 0.0
+
+
+def window_steps(K: int, beat_ms: float) -> int:
+    return max(1, int(round(beat_ms / K / DT)))
+
+
+# ---------------------------------------------------------------------------------------------
+# CPU: the oracle port of the reference (Release flags), timed at matching beat phases
+# ---------------------------------------------------------------------------------------------
+
+def cpu_phase_states(K: int, span: int, threads: int):
+    """A 1,250-CRU cell (NCaRU 12,500) through K windows of `span` steps on the CPU; its state (globals,
+    CRU arrays, per-CRU fluxes) at each window start."""
     import pyoracle as po
 
     po.build()
-    threads = os.cpu_count() or 1
-    po.lib().orc_set_threads(threads)
+    po.timed_lib().orc_set_threads(threads)
     p = po.default_params()
-    m = po.Model(p, ncru, seed=0)
+    m = po.Model(p, CPU_PRE_NCRU, seed=0, timed=True)
     m.sample_initial_crus()
     m.set_globals(po.default_globals(py=False))
-    t0 = time.perf_counter()
-    steps = 0
+    states = []
     t = 0.0
-    while True:
-        tb = t - PERIOD * float(int(t / PERIOD))
-        m.euler_step(DT, STIM_AMP if tb < STIM_DUR else 0.0)
+    for k in range(K):
+        states.append((m.globals(), m.crus(), m.fluxes(), t, k * span))
+        for _ in range(span):
+            m.euler_step(DT, pulse(t))
+            t += DT
+    return states
+
+
+def cpu_window_sample(state, steps: int, threads: int, seed: int):
+    """Times `steps` steps of a 12,500-CRU cell (the state tiled x10) on the CPU; returns seconds."""
+    import numpy as np
+
+    import pyoracle as po
+
+    g, s, (JLCC, Jxfer, Jtr), t, step = state
+    f = NCRU // CPU_PRE_NCRU
+    tile = po.CRUArrays(NCRU)
+    for k in ("CaSS", "CaJSR", "LCC", "LCC_inactivation", "RyR", "ClCh"):
+        setattr(tile, k, np.concatenate([getattr(s, k)] * f))
+    po.timed_lib().orc_set_threads(threads)
+    m = po.Model(po.default_params(), NCRU, seed=seed, timed=True)
+    m.set_globals(g)
+    m.set_crus(tile)
+    # per-CRU fluxes tiled as they are: the global step scales their sum by CRU_factor, which is
+    # 10 for the 1,250-CRU run and 1 here, so the sums the global step sees are the same
+    m.set_fluxes(np.concatenate([JLCC] * f), np.concatenate([Jxfer] * f), np.concatenate([Jtr] * f))
+    m.set_step(step)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        m.euler_step(DT, pulse(t))
         t += DT
-        steps += 1
-        el = time.perf_counter() - t0
-        if el >= seconds:
-            break
-    rate = ncru * steps / el
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(K: int, span: int, seconds: float, warmup: int = 0):
+    """Whole-beat CPU rate: K samples, one per window start, each ~seconds/K of CPU work."""
+    threads = os.cpu_count() or 1
+    states = cpu_phase_states(K, span, threads)
+    per = max(50, int(seconds / K * 5e7 / NCRU))   # ~seconds/K each at ~5e7 CRU-steps/s
+    for w in range(warmup):
+        cpu_window_sample(states[w % K], per, threads, seed=900 + w)
+    times = [cpu_window_sample(states[k], per, threads, seed=k) for k in range(K)]
+    total = sum(times)
+    rate = NCRU * per * K / total
     return {"value": rate, "unit": "CRU-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{ncru} CRUs x {steps} steps ({steps * DT:.3f} ms from the stimulus) in {el:.1f} s"}
+            "build": "oracle/_build/liboracle_timed.so (-Ofast -funroll-loops, OpenMP over CRUs)",
+            "sample": f"{K} samples of {per} steps x {NCRU} CRUs, one at each {span * DT:g} ms window start of "
+                      f"the 1 Hz beat (0-{K * span * DT:g} ms; states from a {CPU_PRE_NCRU}-CRU CPU run of the "
+                      f"beat tiled x{NCRU // CPU_PRE_NCRU}), {total:.1f} s",
+            "per_window_cru_steps_per_s": [NCRU * per / x for x in times]}
 
 
-def workload_config(args, world=1):
+def workload_config(args, world=1, K=None, flush_note=None):
     cells = max(args.cells, 1)
+    K = K or args.steps
+    span = window_steps(K, args.beat_ms)
     return {"workload": f"{'single cell' if cells == 1 else f'{cells} replicate cells'} of {NCRU} CRUs, "
                         f"1 Hz pacing (+{STIM_AMP:g} pA/pF, {STIM_DUR:g} ms), dt 1e-3 ms, "
                         f"FP32 CRU state, FP64 global ODE",
-            "ncru": NCRU, "cells_per_gpu": cells, "span_ms_per_step": args.span_ms,
+            "ncru": NCRU, "cells_per_gpu": cells, "window_ms_per_step": span * DT,
+            "timed_span_ms": f"0-{K * span * DT:g} of the beat (warm-up on the same windows, then the t = 0 "
+                             "state restored)",
             "parallelism": f"replicas x{world}",
-            "l2": "CRU state (0.9 MB per cell) stays in shared memory across steps; no L2 flush"}
+            "l2": flush_note or "256 MB buffer written between timed steps (L2 flush)"}
 
 
 def run_reference(args):
@@ -165,51 +262,62 @@ def run_reference(args):
     if rank != 0:
         return 0
     K, W = args.steps, args.warmup
-    per = max(args.cpu_seconds / max(K + W, 1), 2.0)
-    for _ in range(W):
-        cpu_baseline(per)
-    vals = [cpu_baseline(per) for _ in range(K)]
-    v = statistics.median(x["value"] for x in vals)
+    span = window_steps(K, args.beat_ms)
+    cb = cpu_baseline(K, span, args.cpu_seconds, warmup=W)
+    v = cb["value"]
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "CRU-steps/s",
             "n_gpus": args.gpus, "steps": K, "warmup": W, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": workload_config(args, world),
-            "cpu_baseline": {"value": v, "unit": "CRU-steps/s", "cores": vals[0]["cores"], "kind": "port",
-                             "sample": vals[0]["sample"]},
+            "config": workload_config(args, world, K, "CPU run; no GPU"),
+            "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "CRU-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
+# ---------------------------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------------------------
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
-    import numpy as np
-
     from gwgb300 import Ensemble
     from gwgb300 import dist as gd
 
     rank, local_rank, world = gd.env_rank()
     d = gd.init()
-    span = int(round(args.span_ms / DT))
     K, W = args.steps, max(args.warmup, 3)
+    span = window_steps(K, args.beat_ms)
     cells = max(args.cells, 1)
     e = Ensemble([NCRU] * cells, precision="fp32", seed=1000 + rank, device=local_rank)
     for c in range(cells):
         e.sample_initial_crus(c)
     e.set_pulse(0.0, PERIOD, STIM_DUR, STIM_AMP)
+    ck0 = [e.checkpoint(c) for c in range(cells)]
     for _ in range(W):
         e.run(DT, span)
+    for c in range(cells):
+        e.restore(c, ck0[c])
+    flush = L2Flush(local_rank)
+    windows = []       # window-start checkpoints of cell 0 (plain path, accuracy)
+    per_step = []
     gd.barrier(d)
     st0 = e.stats()
     t0 = time.perf_counter()
     with ClockSampler(local_rank) as clk:
-        for _ in range(K):
+        for k in range(K):
+            if rank == 0 and not args.no_extras:
+                windows.append(e.checkpoint(0))
+            flush(k)
+            a = e.stats()
             e.run(DT, span)
+            b = e.stats()
+            per_step.append(b["kernel_ms"] - a["kernel_ms"])
     wall = time.perf_counter() - t0
     st1 = e.stats()
-    kernel_s = (st1["kernel_ms"] - st0["kernel_ms"]) / 1e3
+    kernel_s = sum(per_step) / 1e3
     kernel_s = gd.max_over_ranks(d, kernel_s)
     wall = gd.max_over_ranks(d, wall)
     cru_steps = NCRU * cells * span * K * world
@@ -218,13 +326,18 @@ def main():
     pk, pk_kind = peaks()
     per_launch_steps = span * K / max(launches, 1)
     achieved_gbs = BYTES_PER_CRU_STEP * NCRU * cells * span * K / kernel_s / 1e9
+    clocks = clk.summary()
+    sm_hz = (clocks.get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)) * 1e6
+    sms_used = st1["cluster_ctas"] * (st1["n_clusters"])
+    warp_rate = WARP_INST_PER_CRU_STEP * value / world
     line = {"metric": METRIC, "value": value, "unit": "CRU-steps/s", "n_gpus": world,
             "steps": K, "warmup": W, "ms_per_step": kernel_s / K * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": workload_config(args, world),
+            "config": workload_config(args, world, K, flush.note()),
             "launch_shape": {k: st1[k] for k in ("cluster_ctas", "cta_crus", "threads_per_cta", "n_clusters")},
             "sim_ms_per_wall_s": cells * world * span * K * DT / kernel_s,
             "events_per_cru_step": (st1["events"] - st0["events"]) / max(NCRU * cells * span * K, 1),
+            "per_window_us_per_step": [ms * 1e3 / span for ms in per_step],
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
                          "frac": achieved_gbs / pk["hbm_gbs"],
@@ -232,55 +345,71 @@ def main():
                          "traffic_unit": "bytes per launch (ncu dram read + write)",
                          "peak_kind": pk_kind, "bytes_per_cru_step": BYTES_PER_CRU_STEP,
                          "steps_per_launch": per_launch_steps},
-            "clocks": clk.summary(), "wall_s": wall}
+            "issue_roofline": {"warp_inst_per_cru_step": WARP_INST_PER_CRU_STEP,
+                               "achieved_warp_inst_per_s": warp_rate,
+                               "peak_cell_sms": sms_used * 4 * sm_hz, "frac_cell_sms": warp_rate / (sms_used * 4 * sm_hz),
+                               "peak_gpu": 152 * 4 * sm_hz, "frac_gpu": warp_rate / (152 * 4 * sm_hz),
+                               "sms_used": sms_used, "sm_hz": sm_hz,
+                               "note": "issue slots = 4 schedulers x SM clock per SM; warp instructions per "
+                                       "CRU-step from the ncu instruction mix of this workload"},
+            "clocks": clocks, "wall_s": wall}
     e.close()
     if rank == 0 and not args.no_extras:
-        line["e2e"] = e2e_measure(span, K)
-        line["paths"] = {"plain_gpu": plain_measure(local_rank), "batched_gpu": batched_measure(local_rank),
-                         "large_ensemble_gpu": large_measure(local_rank)}
-        line["accuracy"] = accuracy_vs_fp64(local_rank)
-        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
-        line["paths"]["cpu"] = {"cru_steps_per_s": line["cpu_baseline"]["value"],
-                                "sim_ms_per_wall_s": line["cpu_baseline"]["value"] / NCRU * DT,
+        del flush
+        line["e2e"] = e2e_measure(K, span)
+        line["paths"] = {"plain_gpu": plain_measure(local_rank, windows),
+                         "batched_gpu": batched_measure(local_rank),
+                         "large_ensemble_gpu": large_measure(local_rank),
+                         "config1_fp64": config1_measure(local_rank)}
+        line["accuracy"] = {"fp32_vs_fp64_oracle_crn": accuracy_crn(local_rank, windows, K, span),
+                            "fp32_vs_fp64_ensemble": accuracy_ks(local_rank)}
+        line["cpu_baseline"] = cpu_baseline(K, span, args.cpu_seconds)
+        cpu = line["cpu_baseline"]["value"]
+        line["paths"]["cpu"] = {"cru_steps_per_s": cpu, "sim_ms_per_wall_s": cpu / NCRU * DT,
                                 "cores": line["cpu_baseline"]["cores"]}
+        b = line["paths"]["batched_gpu"]["cru_steps_per_s"]
+        line["ratios"] = {"batched_over_plain_launch_per_step": b / line["paths"]["plain_gpu"]["cru_steps_per_s"],
+                          "batched_over_single_cell": b / value, "batched_over_cpu": b / cpu,
+                          "single_cell_over_cpu": value / cpu, "e2e_over_cpu": line["e2e"]["value"] / cpu}
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
 
 
-def plain_measure(device, steps=3000):
-    """The same paced cell with one engine launch (and one host synchronisation) per global step."""
+def plain_measure(device, windows, steps=200):
+    """The paced cell with one engine launch (and one host synchronisation) per global step, timed
+    from each window start of the beat (the headline run's checkpoints) for `steps` steps."""
     from gwgb300 import Ensemble
 
-    e = Ensemble([NCRU], precision="fp32", seed=7, device=device, steps_per_launch=1)
-    e.sample_initial_crus(0)
+    e = Ensemble([NCRU], precision="fp32", seed=1000, device=device, steps_per_launch=1)
     e.set_pulse(0.0, PERIOD, STIM_DUR, STIM_AMP)
-    e.run(DT, 300)
-    st0 = e.stats()
-    t0 = time.perf_counter()
-    e.run(DT, steps)
-    wall = time.perf_counter() - t0
-    st1 = e.stats()
+    e.restore(0, windows[0])
+    e.run(DT, 50)
+    wall = 0.0
+    kern = 0.0
+    for ck in windows:
+        e.restore(0, ck)
+        st0 = e.stats()
+        t0 = time.perf_counter()
+        e.run(DT, steps)
+        wall += time.perf_counter() - t0
+        kern += (e.stats()["kernel_ms"] - st0["kernel_ms"]) / 1e3
     e.close()
-    kern = (st1["kernel_ms"] - st0["kernel_ms"]) / 1e3
-    return {"cru_steps_per_s": NCRU * steps / wall, "sim_ms_per_wall_s": steps * DT / wall,
-            "kernel_cru_steps_per_s": NCRU * steps / kern, "launches": int(st1["launches"] - st0["launches"]),
-            "workload": f"1 cell x {NCRU} CRUs, 1 launch per global step, {steps} steps, wall clock"}
+    n = NCRU * steps * len(windows)
+    return {"cru_steps_per_s": n / wall, "sim_ms_per_wall_s": steps * len(windows) * DT / wall,
+            "kernel_cru_steps_per_s": n / kern,
+            "workload": f"1 cell x {NCRU} CRUs, 1 launch + 1 host sync per global step, {steps} steps from each "
+                        f"of {len(windows)} window starts across the beat, wall clock"}
 
 
-def batched_config(seed=3, n_cells=256):
-    """256 cells, CRU counts uniform in 2,000..12,500, per-cell PCaL, GKr, GKs, Vmaxf = Vmaxr and
-    rRyR scaled by log-normal(sigma 0.1) factors, cycle lengths uniform in 400..1000 ms."""
-    import numpy as np
-
+def lognormal_params(rng, n_cells, sigma):
+    """Per-cell PCaL, GKr, GKs, Vmaxf = Vmaxr and rRyR scaled by log-normal(sigma) factors."""
     from gwgb300 import _lib
 
-    rng = np.random.default_rng(seed)
-    ncru = rng.integers(2000, 12501, size=n_cells)
     params = []
     for _ in range(n_cells):
         p = _lib.default_params()
-        f = rng.lognormal(0.0, 0.1, size=5)
+        f = rng.lognormal(0.0, sigma, size=5)
         p.PCaL *= f[0]
         p.GKr *= f[1]
         p.GKs *= f[2]
@@ -288,11 +417,24 @@ def batched_config(seed=3, n_cells=256):
         p.Vmaxr *= f[3]
         p.rRyR *= f[4]
         params.append(p)
+    return params
+
+
+def batched_config(seed=3, n_cells=256):
+    """256 cells, CRU counts uniform in 2,000..12,500, per-cell log-normal(0.1) parameters, cycle
+    lengths uniform in 400..1000 ms."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    ncru = rng.integers(2000, 12501, size=n_cells)
+    params = lognormal_params(rng, n_cells, 0.1)
     cl = rng.uniform(400.0, 1000.0, size=n_cells)
     return ncru, params, cl
 
 
-def batched_measure(device, steps=2000, cluster_ctas="auto"):
+def batched_measure(device, window_ms=400.0, cluster_ctas="auto"):
+    """Config 3 over 0-400 ms of every cell's first beat (upstroke, release, plateau,
+    repolarisation; a whole beat for the cells paced at 400 ms)."""
     from gwgb300 import Ensemble
 
     ncru, params, cl = batched_config()
@@ -300,7 +442,7 @@ def batched_measure(device, steps=2000, cluster_ctas="auto"):
     for c in range(len(ncru)):
         e.sample_initial_crus(c)
         e.set_pulse(0.0, float(cl[c]), STIM_DUR, STIM_AMP, cell=c)
-    e.run(DT, 500)
+    steps = int(round(window_ms / DT))
     st0 = e.stats()
     t0 = time.perf_counter()
     e.run(DT, steps)
@@ -311,68 +453,28 @@ def batched_measure(device, steps=2000, cluster_ctas="auto"):
     total = int(ncru.sum()) * steps
     return {"cru_steps_per_s": total / kern, "sim_ms_per_wall_s": len(ncru) * steps * DT / kern,
             "wall_cru_steps_per_s": total / wall, "cells": len(ncru), "crus": int(ncru.sum()),
-            "autotuned": cluster_ctas == "auto",
+            "algorithmic_GBps": total * BYTES_PER_CRU_STEP / kern / 1e9,
+            "autotuned": cluster_ctas == "auto", "tuned_us_per_step": e.tuned_us_per_step,
             "launch_shape": {k: st1[k] for k in ("cluster_ctas", "cta_crus", "threads_per_cta", "n_clusters")},
             "workload": f"{len(ncru)} cells, 2,000-12,500 CRUs, log-normal(0.1) PCaL/GKr/GKs/Vmax/rRyR, "
-                        f"CL 400-1000 ms, {steps} steps"}
+                        f"CL 400-1000 ms, 0-{window_ms:g} ms of the beat ({steps} steps)"}
 
 
-def accuracy_vs_fp64(device, cells=64, ncru=200, t_ms=200.0):
-    """Error of the FP32 engine (the measured path) against the FP64 engine (reference arithmetic,
-    checked bit-exact against the oracle): replicate-cell ensembles of one paced beat, two-sample
-    KS p-values and relative differences of the ensemble means of peak Cai, its time and V."""
+def large_measure(device, cells=1024, ncru=12500, window_ms=50.0):
+    """Config 5: 1,024 cells of 12,500 CRUs (12.8M CRUs), per-cell log-normal(0.15) parameters, 2 Hz
+    pacing; timed over 0-50 ms of the beat (upstroke and Ca release, the event-heaviest part)."""
     import numpy as np
-    from scipy.stats import ks_2samp
 
     from gwgb300 import Ensemble
 
-    every = 500
-    out = {}
-    for prec, seed in (("fp32", 31), ("fp64", 32)):
-        e = Ensemble([ncru] * cells, precision=prec, seed=seed, device=device)
-        for c in range(cells):
-            e.sample_initial_crus(c)
-        e.set_pulse(0.0, PERIOD, STIM_DUR, STIM_AMP)
-        tr = e.run(DT, int(t_ms / DT), record_every=every)
-        e.close()
-        V, Cai = tr.var("V"), tr.var("Cai")
-        i100 = int(100.0 / (every * DT)) - 1
-        out[prec] = {"peak_Cai": Cai.max(axis=1), "t_peak_Cai": Cai.argmax(axis=1) * every * DT,
-                     "V_100ms": V[:, i100], "Cai_150ms": Cai[:, int(150.0 / (every * DT)) - 1]}
-    res = {"reference": "FP64 engine (reference arithmetic)", "cells": cells, "ncru": ncru,
-           "window_ms": t_ms, "ks_pvalue": {}, "rel_diff_of_means": {}}
-    for k in out["fp32"]:
-        a, b = out["fp32"][k], out["fp64"][k]
-        res["ks_pvalue"][k] = float(ks_2samp(a, b).pvalue)
-        res["rel_diff_of_means"][k] = float(abs(a.mean() - b.mean()) / max(abs(b.mean()), 1e-30))
-    return res
-
-
-def large_measure(device, cells=1024, ncru=12500, steps=1000):
-    """Large ensemble: 1,024 cells of 12,500 CRUs (12.8M CRUs), per-cell PCaL, GKr, GKs,
-    Vmaxf = Vmaxr and rRyR scaled by log-normal(sigma 0.15) factors, 2 Hz pacing (CL 500 ms)."""
-    import numpy as np
-
-    from gwgb300 import Ensemble, _lib
-
     rng = np.random.default_rng(5)
-    params = []
-    for _ in range(cells):
-        p = _lib.default_params()
-        f = rng.lognormal(0.0, 0.15, size=5)
-        p.PCaL *= f[0]
-        p.GKr *= f[1]
-        p.GKs *= f[2]
-        p.Vmaxf *= f[3]
-        p.Vmaxr *= f[3]
-        p.rRyR *= f[4]
-        params.append(p)
+    params = lognormal_params(rng, cells, 0.15)
     e = Ensemble([ncru] * cells, params, precision="fp32", seed=17, device=device, cluster_ctas="auto",
                  tune_steps=100)
     for c in range(cells):
         e.sample_initial_crus(c)
     e.set_pulse(0.0, 500.0, STIM_DUR, STIM_AMP)
-    e.run(DT, 200)
+    steps = int(round(window_ms / DT))
     st0 = e.stats()
     e.run(DT, steps)
     st1 = e.stats()
@@ -382,58 +484,215 @@ def large_measure(device, cells=1024, ncru=12500, steps=1000):
     return {"cru_steps_per_s": total / kern, "sim_ms_per_wall_s": cells * steps * DT / kern,
             "algorithmic_GBps": total * BYTES_PER_CRU_STEP / kern / 1e9, "cells": cells, "crus": cells * ncru,
             "launch_shape": {k: st1[k] for k in ("cluster_ctas", "cta_crus", "threads_per_cta", "n_clusters")},
-            "workload": f"{cells} cells x {ncru} CRUs, log-normal(0.15) PCaL/GKr/GKs/Vmax/rRyR, CL 500 ms, {steps} steps"}
+            "workload": f"{cells} cells x {ncru} CRUs, log-normal(0.15) PCaL/GKr/GKs/Vmax/rRyR, CL 500 ms, "
+                        f"0-{window_ms:g} ms of the beat ({steps} steps)"}
 
 
-def e2e_measure(span, K):
-    """The reference-facing path: GreensteinWinslow.run-equivalent C call with host buffers."""
+def config1_measure(device):
+    """Config 1 in full: one cell of 1,250 CRUs (NCaRU 12,500), FP64 throughout, one +100 pA/pF
+    stimulus of 0.5 ms, 500 ms, seed 0 -- on the GPU (FP64 engine) and on the CPU (the oracle port,
+    Release flags, all cores), the reference's own CPU-runnable case."""
+    from gwgb300 import Ensemble, _lib, engine
+
+    import pyoracle as po
+
+    n, steps = 1250, 500_000
+    e = Ensemble([n], precision="fp64", seed=0, device=device)
+    e.sample_initial_crus(0)
+    e.set_globals(0, engine.globals_to_array(_lib.default_globals(py=True)))
+    e.set_pulse(0.0, 0.0, STIM_DUR, STIM_AMP)
+    st0 = e.stats()
+    t0 = time.perf_counter()
+    e.run(DT, steps)
+    wall = time.perf_counter() - t0
+    st1 = e.stats()
+    e.close()
+    kern = (st1["kernel_ms"] - st0["kernel_ms"]) / 1e3
+    threads = os.cpu_count() or 1
+    po.build()
+    po.timed_lib().orc_set_threads(threads)
+    m = po.Model(po.default_params(), n, seed=0, timed=True)
+    m.sample_initial_crus()
+    m.set_globals(po.default_globals(py=True))
+    istim = po.pulse_train(steps, DT, STIM_AMP, STIM_DUR)
+    t1 = time.perf_counter()
+    m.run(DT, istim, 0)
+    cpu_s = time.perf_counter() - t1
+    return {"gpu_fp64_cru_steps_per_s": n * steps / kern, "gpu_fp64_wall_cru_steps_per_s": n * steps / wall,
+            "gpu_sim_ms_per_wall_s": steps * DT / wall,
+            "cpu_cru_steps_per_s": n * steps / cpu_s, "cpu_sim_ms_per_wall_s": steps * DT / cpu_s,
+            "cpu_cores": threads, "gpu_over_cpu": (n * steps / wall) / (n * steps / cpu_s),
+            "launch_shape": {k: st1[k] for k in ("cluster_ctas", "cta_crus", "threads_per_cta", "n_clusters")},
+            "workload": "1 cell x 1,250 CRUs (NCaRU 12,500), FP64, +100 pA/pF 0.5 ms, 500 ms, seed 0, in full"}
+
+
+def phase_checkpoint(device, windows, span, t_ms):
+    """The headline cell's state at t_ms: the latest window start at or before it, advanced on a
+    copy of the cell."""
+    from gwgb300 import Ensemble
+
+    k = min(int(t_ms / (span * DT)), len(windows) - 1)
+    extra = int(round(t_ms / DT)) - k * span
+    if extra <= 0:
+        return windows[k]
+    e = Ensemble([NCRU], precision="fp32", seed=1000, device=device)
+    e.set_pulse(0.0, PERIOD, STIM_DUR, STIM_AMP)
+    e.restore(0, windows[k])
+    e.run(DT, extra)
+    ck = e.checkpoint(0)
+    e.close()
+    return ck
+
+
+def accuracy_crn(device, windows, K, span, steps=200, points_ms=(0.0, 15.0, 150.0, 350.0)):
+    """North-star check (c) at the headline config: the FP32 engine against the FP64 oracle from
+    the same 12,500-CRU state with common random numbers (the oracle in 24-bit-uniform mode draws
+    the engine's FP32 uniforms), after 1 and `steps` global steps, at rest before the stimulus,
+    in the Ca release (15 ms), on the plateau (150 ms) and in repolarisation (350 ms)."""
+    import numpy as np
+
+    import pyoracle as po
+    from gwgb300 import Ensemble
+
+    po.build()
+    po.lib().orc_set_threads(os.cpu_count() or 1)
+    out = []
+    for t_ms in points_ms:
+        if t_ms >= K * span * DT:
+            continue
+        ck = phase_checkpoint(device, windows, span, t_ms)
+        s = ck["crus"]
+        rec = {"t_ms": ck["t"]}
+        for n in (1, steps):
+            e = Ensemble([NCRU], precision="fp32", seed=1000, device=device)
+            e.set_pulse(0.0, PERIOD, STIM_DUR, STIM_AMP)
+            e.restore(0, ck)
+            e.run(DT, n)
+            g32, s32 = e.get_globals(0), e.get_crus(0)
+            e.close()
+            m = po.Model(po.default_params(), NCRU, seed=1000, umode=po.U24)
+            m.set_globals(po.OrcGlobals.from_array(ck["globals"]))
+            o = po.CRUArrays(NCRU)
+            for key in ("CaSS", "CaJSR", "LCC", "LCC_inactivation", "RyR", "ClCh"):
+                setattr(o, key, getattr(s, key))
+            m.set_crus(o)
+            jl, cl, jt, jx = ck["carry"]
+            m.set_fluxes(s.JLCC, np.full((NCRU, 4), jx / (4 * NCRU)), np.full(NCRU, jt / NCRU))
+            m.set_step(ck["step"])
+            t = ck["t"]
+            for _ in range(n):
+                m.euler_step(DT, pulse(t))
+                t += DT
+            g64, s64 = m.globals().to_array(), m.crus()
+            same = np.ones(NCRU, bool)
+            for key in ("LCC", "LCC_inactivation", "RyR", "ClCh"):
+                same &= np.all(getattr(s32, key).reshape(NCRU, -1) == getattr(s64, key).reshape(NCRU, -1), axis=1)
+            relg = np.abs(g32 - g64) / np.maximum(np.abs(g64), 1e-300)
+            rec[f"after_{n}"] = {
+                "globals_max_rel": float(relg.max()), "V_rel": float(relg[0]), "Cai_rel": float(relg[3]),
+                "crus_with_other_channel_state": int((~same).sum()),
+                "CaSS_max_rel_same_channels": float(np.max(np.abs(s32.CaSS[same] - s64.CaSS[same]) /
+                                                           s64.CaSS[same])) if same.any() else None,
+                "CaJSR_max_rel_same_channels": float(np.max(np.abs(s32.CaJSR[same] - s64.CaJSR[same]) /
+                                                            s64.CaJSR[same])) if same.any() else None}
+        out.append(rec)
+    return {"reference": "FP64 oracle (C restatement pinned bit-exact to the reference's C++), 24-bit uniforms "
+                         "= the engine's draws", "ncru": NCRU, "points": out}
+
+
+def accuracy_ks(device, cells=64, ncru=500, t_ms=450.0, every=500):
+    """FP32 vs FP64 engine (FP64 = reference arithmetic, bit-exact with the oracle): replicate
+    ensembles of one paced beat, KS p-values and relative differences of the means of APD90, peak
+    Cai, its time and V at 100 ms."""
+    import numpy as np
+    from scipy.stats import ks_2samp
+
+    from gwgb300 import Ensemble, analysis
+
+    out = {}
+    for prec, seed in (("fp32", 31), ("fp64", 32)):
+        e = Ensemble([ncru] * cells, precision=prec, seed=seed, device=device)
+        for c in range(cells):
+            e.sample_initial_crus(c)
+        e.set_pulse(0.0, PERIOD, STIM_DUR, STIM_AMP)
+        tr = e.run(DT, int(t_ms / DT), record_every=every)
+        e.close()
+        V, Cai = tr.var("V"), tr.var("Cai")
+        t = (np.arange(V.shape[1]) + 1) * every * DT
+        mk = analysis.ap_markers(t, V, v_rest=-91.382)
+        out[prec] = {"APD90": mk["APD90"], "peak_Cai": Cai.max(axis=1), "t_peak_Cai": t[Cai.argmax(axis=1)],
+                     "V_100ms": V[:, int(100.0 / (every * DT)) - 1]}
+    res = {"reference": "FP64 engine (reference arithmetic, bit-exact channel sequences vs the oracle)",
+           "cells": cells, "ncru": ncru, "window_ms": t_ms, "ks_pvalue": {}, "rel_diff_of_means": {}}
+    for k in out["fp32"]:
+        a, b = out["fp32"][k], out["fp64"][k]
+        res["ks_pvalue"][k] = float(ks_2samp(a, b).pvalue)
+        res["rel_diff_of_means"][k] = float(abs(a.mean() - b.mean()) / max(abs(b.mean()), 1e-30))
+    return res
+
+
+def e2e_measure(K, span):
+    """The same beat through the reference-facing C ABI: K chained gw_simulate calls of `span` steps
+    (host arrays in; per-step stimulus samples at the global t; the last step's state read back and
+    passed to the next call; a fresh context per call, as chained run() calls of the reference)."""
     import ctypes as C
 
     import numpy as np
 
+    import GreensteinWinslow as GW
     from gwgb300 import _lib
 
     L = _lib.load()
     p = _lib.default_params()
     g = _lib.default_globals(py=True)
-    import GreensteinWinslow as GW
-
     rng = np.random.default_rng(0)
     LCC, LCCi, RyR, ClCh = GW._initial_cru_arrays(NCRU, rng)
     CaSS = np.full((NCRU, 4), 1.45370e-4)
     CaJSR = np.full(NCRU, 0.908408)
-    t = np.arange(span) * DT
-    istim = np.where(t - PERIOD * np.floor(t / PERIOD) < STIM_DUR, STIM_AMP, 0.0)
-    rec_every = span
-    out = {k: np.zeros((1, NCRU, 4)) for k in ("CaSS",)}
-    tr = _lib.GwTrace()
-    rec_t = np.zeros(1)
-    recG = np.zeros(36)
-    rCaSS = np.zeros((1, NCRU, 4))
-    rCaJSR = np.zeros((1, NCRU))
-    rI = [np.zeros((1, NCRU, 4), np.int32) for _ in range(3)]
-    rRyR = np.zeros((1, NCRU, 4, 6), np.int32)
-    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
-    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
+    rec_t = np.zeros(2)
+    recG = np.zeros((2, 36))
+    rCaSS = np.zeros((2, NCRU, 4))
+    rCaJSR = np.zeros((2, NCRU))
+    rI = [np.zeros((2, NCRU, 4), np.int32) for _ in range(3)]
+    rRyR = np.zeros((2, NCRU, 4, 6), np.int32)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))  # noqa: E731
+    # the stimulus at t_i = sum_{k<i} dt (t += dt), window k's samples istim_all[k*span:(k+1)*span]
+    istim_all = np.empty(K * span)
+    t = 0.0
+    for i in range(K * span):
+        istim_all[i] = pulse(t)
+        t += DT
 
-    def once():
-        tr.max_records = 1
+    def once(k, state):
+        CaSS_, CaJSR_, LCC_, LCCi_, RyR_, ClCh_, g_ = state
+        tr = _lib.GwTrace()
+        tr.max_records = 2
         tr.t, tr.globals, tr.cru_cell = dp(rec_t), dp(recG), 0
         tr.CaSS, tr.CaJSR = dp(rCaSS), dp(rCaJSR)
         tr.LCC, tr.LCC_inactivation, tr.ClCh, tr.RyR = ip(rI[0]), ip(rI[1]), ip(rI[2]), ip(rRyR)
-        rc = L.gw_simulate(C.byref(p), NCRU, DT, span, dp(istim), rec_every, dp(CaSS), dp(CaJSR), ip(LCC),
-                           ip(LCCi), ip(RyR), ip(ClCh), C.byref(g), b"xoshiro256++", 1, 1, C.byref(tr))
+        istim = np.ascontiguousarray(istim_all[k * span:(k + 1) * span])
+        rc = L.gw_simulate(C.byref(p), NCRU, DT, span, dp(istim), max(span - 1, 1), dp(CaSS_), dp(CaJSR_), ip(LCC_),
+                           ip(LCCi_), ip(RyR_), ip(ClCh_), C.byref(g_), b"xoshiro256++", 1 + k, 1, C.byref(tr))
         _lib.check(rc)
+        last = 1 if span > 1 else 0
+        gn = _lib.GwGlobals.from_buffer_copy(recG[last].tobytes())
+        return (rCaSS[last].copy(), rCaJSR[last].copy(), rI[0][last].copy(), rI[1][last].copy(), rRyR[last].copy(),
+                rI[2][last].copy(), gn)
 
-    once()
+    state0 = (CaSS, CaJSR, LCC, LCCi, RyR, ClCh, g)
+    once(0, state0)   # warm-up call (module and context set-up)
+    state = state0
     t0 = time.perf_counter()
-    for _ in range(K):
-        once()
+    for k in range(K):
+        state = once(k, state)
     el = time.perf_counter() - t0
-    h2d = CaSS.nbytes + CaJSR.nbytes + LCC.nbytes + LCCi.nbytes + RyR.nbytes + ClCh.nbytes + istim.nbytes
+    h2d = CaSS.nbytes + CaJSR.nbytes + LCC.nbytes + LCCi.nbytes + RyR.nbytes + ClCh.nbytes + 8 * span + 288
     d2h = rec_t.nbytes + recG.nbytes + rCaSS.nbytes + rCaJSR.nbytes + sum(a.nbytes for a in rI) + rRyR.nbytes
     return {"value": NCRU * span * K / el, "unit": "CRU-steps/s", "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h), "path": "gw_simulate (C ABI, host arrays, fresh context per call)"}
+            "d2h_bytes_per_step": int(d2h), "wall_s": el,
+            "path": f"gw_simulate (C ABI, host arrays, a fresh context per call), {K} chained calls of {span} steps "
+                    f"covering 0-{K * span * DT:g} ms of the beat"}
 
 
 if __name__ == "__main__":

@@ -16,6 +16,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+# the same C source built with the reference's Release flags (CPU baseline timings only)
+TIMED_LIB_PATH = os.path.join(HERE, "_build", "liboracle_timed.so")
 REF_PATH = os.path.join(HERE, "_ref", "libgwref.so")
 REF_TIMED_PATH = os.path.join(HERE, "_ref", "libgwref_timed.so")
 
@@ -82,6 +84,7 @@ class OrcCurrents(C.Structure):
 
 _lock = threading.Lock()
 _lib = None
+_timed = None
 _ref = None
 
 
@@ -124,7 +127,23 @@ def lib():
     if _lib is None:
         if not os.path.exists(LIB_PATH):
             build()
-        L = C.CDLL(LIB_PATH)
+        _lib = _bind(C.CDLL(LIB_PATH))
+    return _lib
+
+
+def timed_lib():
+    """gw_oracle.c built with the reference's Release flags (-Ofast -funroll-loops): the CPU
+    baseline's timings use it; its results are not bit-exact with the parity build."""
+    global _timed
+    if _timed is None:
+        if not os.path.exists(TIMED_LIB_PATH):
+            build(force=True)
+        _timed = _bind(C.CDLL(TIMED_LIB_PATH))
+    return _timed
+
+
+def _bind(L):
+    if True:
         vp = C.c_void_p
         P = C.POINTER
         L.orc_params_default.argtypes = [P(OrcParams)]
@@ -163,8 +182,7 @@ def lib():
         L.orc_event_count.argtypes = [vp]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_param_count.restype = C.c_int
-        _lib = L
-    return _lib
+    return L
 
 
 def ref_available() -> bool:
@@ -249,10 +267,11 @@ class CRUArrays:
 
 
 class Model:
-    """One cell in the C restatement (orc_model)."""
+    """One cell in the C restatement (orc_model); timed=True uses the Release-flag build."""
 
-    def __init__(self, p: OrcParams, ncru: int, seed: int = 0, cell: int = 0, umode: int = U53):
-        self.L = lib()
+    def __init__(self, p: OrcParams, ncru: int, seed: int = 0, cell: int = 0, umode: int = U53,
+                 timed: bool = False):
+        self.L = timed_lib() if timed else lib()
         self.n = ncru
         self.p = p
         self.h = self.L.orc_create(C.byref(p), ncru, seed, cell, umode)
