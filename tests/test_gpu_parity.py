@@ -277,3 +277,83 @@ def test_initial_state_sampler_matches_oracle(oracle):
             for k in CHANNELS:
                 np.testing.assert_array_equal(getattr(s, k), getattr(r, k))
         e.close()
+
+
+def _flips_and_errors(es, ms, n):
+    same = np.ones(n, bool)
+    for k in CHANNELS:
+        a, b = getattr(es, k).reshape(n, -1), getattr(ms, k).reshape(n, -1)
+        same &= np.all(a == b, axis=1)
+    cass = rel(es.CaSS[same], ms.CaSS[same]) if same.any() else 0.0
+    cajsr = rel(es.CaJSR[same], ms.CaJSR[same]) if same.any() else 0.0
+    return int(np.sum(~same)), cass, cajsr
+
+
+def test_fp32_matches_reference_u24_fixture(oracle):
+    """The FP32 engine over the reference's own 4,000-step trajectory with 24-bit uniforms (48 CRUs,
+    an AP upstroke and the start of the release, recorded from the reference's C++ with the same
+    draws): CRUs whose final channel state differs are counted and bounded (an FP32 partial sum
+    can put a draw on the other side of a boundary); the globals over the run stay within 1e-6."""
+    from gwgb300 import Ensemble, engine
+
+    z = np.load(os.path.join(GOLDEN, "traj_ap_u24.npz"))
+    p = oracle.default_params()
+    n, steps, rec = int(z["ncru"]), int(z["steps"]), int(z["rec"])
+    e = Ensemble([n], params=engine.params_from(p), precision="fp32", seed=int(z["seed"]))
+    e.set_globals(0, z["g0"])
+    e.set_crus(0, engine.CRUState(*(z["init_" + k] for k in ("CaSS", "CaJSR", "LCC", "LCC_inactivation", "RyR", "ClCh"))))
+    e.set_samples(oracle.pulse_train(steps, DT, float(z["amp"]), float(z["dur"])))
+    tr = e.run(DT, steps, record_every=1)
+    s = e.get_crus(0)
+    e.close()
+    final = oracle.CRUArrays(n)
+    for k in ("CaSS", "CaJSR") + CHANNELS:
+        setattr(final, k, z["final_" + k])
+    flips, cass, cajsr = _flips_and_errors(s, final, n)
+    err_g = rel(tr.globals[0, rec - 1::rec], z["globals_rec"])
+    # measured on GB300: no flips, CaSS 1.2e-6, CaJSR 7.7e-11, globals 2.1e-8
+    print(f"u24 fixture: flips {flips}/{n}, CaSS {cass:.2e}, CaJSR {cajsr:.2e}, globals {err_g:.2e}")
+    assert flips <= 1
+    assert err_g <= 1e-6
+    if flips == 0:
+        assert cass <= 3e-5 and cajsr <= 1e-8
+
+
+@pytest.mark.parametrize("warm", [10, 3000, 8000])
+def test_fp32_multistep_matches_u24_oracle(oracle, warm):
+    """2,000 FP32 steps of 4,000 CRUs from the oracle's state at three points of the AP (rest,
+    upstroke and release, plateau), against the oracle in FP64 with the same 24-bit uniforms:
+    CRUs with another final channel state counted and bounded, the globals and the CRU Ca of the
+    agreeing CRUs bounded."""
+    from gwgb300 import Ensemble, engine
+
+    po = oracle
+    po.lib().orc_set_threads(os.cpu_count() or 1)
+    n, steps = 4000, 2000
+    p, g, s, (JLCC, Jxfer, Jtr) = _u24_state(oracle, n, 21, warm)
+    JLCC = JLCC.astype(np.float32).astype(np.float64)
+    step0 = 12345
+    istim = po.pulse_train(warm + steps, DT, 100.0, 0.5)[warm:]
+    m = po.Model(p, n, seed=5, umode=po.U24)
+    m.set_globals(g)
+    m.set_crus(s)
+    m.set_fluxes(JLCC, Jxfer, Jtr)
+    m.set_step(step0)
+    for i in range(steps):
+        m.euler_step(DT, istim[i])
+    e = Ensemble([n], params=engine.params_from(p), precision="fp32", seed=5)
+    e.set_globals(0, g.to_array())
+    e.set_crus(0, engine.CRUState(s.CaSS, s.CaJSR, s.LCC, s.LCC_inactivation, s.RyR, s.ClCh, JLCC), with_jlcc=True)
+    e.set_flux_carry(0, float(JLCC.sum()), float(s.ClCh.sum()), float(Jtr.sum()), float(Jxfer.sum()))
+    e.set_time(0, 0.0, step0)
+    e.set_samples(istim)
+    e.run(DT, steps)
+    flips, cass, cajsr = _flips_and_errors(e.get_crus(0), m.crus(), n)
+    err_g = rel(e.get_globals(0), m.globals().to_array())
+    e.close()
+    # measured on GB300 (warm 10 / 3000 / 8000): no flips; CaSS 4.0e-6 / 2.2e-6 / 3.0e-6, CaJSR
+    # 1.3e-10 / 7.9e-10 / 1.9e-9, globals 4.4e-9 / 3.8e-8 / 3.6e-8
+    print(f"warm {warm}: flips {flips}/{n}, CaSS {cass:.2e}, CaJSR {cajsr:.2e}, globals {err_g:.2e}")
+    assert flips <= max(2, n // 1000)
+    assert err_g <= 1e-6
+    assert cass <= 1e-4 and cajsr <= 5e-8
