@@ -1039,7 +1039,7 @@ int gw_run(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_trace *tr
         }
         CK(c, cudaEventSynchronize(c->ev1));
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        CK(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
         total_ms += ms;
         done += n;
     }
@@ -1202,7 +1202,7 @@ int gw_run_noalloc(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_t
         }
         CK(c, cudaEventSynchronize(c->ev1));
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        CK(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
         total_ms += ms;
         done += n;
     }

@@ -620,6 +620,7 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
     const uint32_t part_bytes =
         (uint32_t)sizeof(Partial) * (uint32_t)(v.nw + (v.w.n_cta_cell - 1) * (v.nw + kOdeWarps));
     bool stopped = false;  // a wait ran out (the same on every ODE thread)
+    int s_stop = -1;       // the step whose wait (for the partials of step s_stop - 1) ran out
     for (int s = 0; s < a.n_steps; ++s) {
         const int par = s & 1;
         const int64_t ri = a.run_step0 + s;
@@ -643,6 +644,7 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
             if (bar_or(1, kOdeLanes, !ok)) {  // the same decision on all ODE threads
                 if (ot == 0) atomicCAS(&os.status, 0, (int)GW_ERR_SYNC_TIMEOUT);
                 stopped = true;
+                s_stop = s;
                 continue;
             }
         }
@@ -694,6 +696,15 @@ __device__ __noinline__ void ode_warps(const KernelArgs &a, uint64_t step0) {
             mbar_wait(v.mbar + 8u * (uint32_t)((a.n_steps - 1) & 1), (uint32_t)((a.n_steps - 1) >> 1) & 1u);
         if (bar_or(1, kOdeLanes, !ok) && ot == 0) atomicCAS(&os.status, 0, (int)GW_ERR_SYNC_TIMEOUT);
     }
+    // After a wait ran out in step s_stop, warp partials of steps s_stop - 1 and s_stop may still
+    // land here (the cell's CTAs send step s + 1 only after the SSA values of step s + 1, which the
+    // leader pushes only after the partials of step s - 1): thread 0 waits, bounded, for both
+    // declared phases, so that no store into this CTA is in flight when it exits (an st.async
+    // completes only on its mbarrier; the closing cluster barrier does not order it).
+    if (stopped && ot == 0 && s_stop >= 1) {
+        mbar_wait(v.mbar + 8u * (uint32_t)((s_stop - 1) & 1), (uint32_t)((s_stop - 1) >> 1) & 1u);
+        mbar_wait(v.mbar + 8u * (uint32_t)(s_stop & 1), (uint32_t)(s_stop >> 1) & 1u);
+    }
     if (a.n_steps > 0)
         reduce_partials<FP64, T>(v.part + ((a.n_steps - 1) & 1) * pslot, v.w.n_cta_cell * kMaxWarps, ot >> 5, lane, os.sums, X);
     ode_bar();
@@ -730,6 +741,7 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
     const R dt = (R)a.dt;
     unsigned long long my_events = 0;
     int my_err = 0;  // bit 0: a CRU hit the event cap; bit 1: a wait for the SSA values ran out
+    int s_stop = -1;  // the step whose wait ran out
     for (int s = 0; s < a.n_steps; ++s) {
         const int par = s & 1;
         const int64_t ri = a.run_step0 + s;
@@ -740,22 +752,24 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
             // The SSA values of step s arrive by st.async from the leader's ODE warps and complete
             // this CTA's mbarrier of parity par (thread 0 declares the bytes; that mbarrier's
             // previous phase, step s-2's, completed before this CTA's waits of step s-2).  The
-            // CTA's SSA threads then meet at named barrier 2 (all have left step s-1, so the rate
-            // table may be rebuilt; the CTAs of a cell are held together only by their data) and
-            // take the wait's outcome together: after a wait has run out the CTA stops for the
-            // rest of the launch (no more sends), so that its partners stop too.
+            // CTA's SSA threads then meet at named barrier 2 (bar_or below; the CTAs of a cell are
+            // held together only by their data) and take the wait's outcome together: after a
+            // wait has run out the CTA stops for the rest of the launch (no more sends), so that
+            // its partners stop too.
             const uint32_t svm = v.mbar + 16u + 8u * (uint32_t)par;
             if (threadIdx.x == 0) mbar_arrive_expect_tx(svm, (uint32_t)(kSvCount * sizeof(R)));
             const bool ok = mbar_wait(svm, (uint32_t)(s >> 1) & 1u);
             const R *sv = v.svbuf + par * kSvCount;
             // FP32: the CTA's rate table of this step, entry e by SSA thread e, into the table of
-            // this parity (a warp still in step s-1 reads the other one; the barrier below, which
-            // every SSA thread reaches only after step s-1, publishes it)
+            // this parity, before bar_or(2) of step s, which publishes it.  No reader of that
+            // table (step s-2's) can remain: every SSA thread passed bar_or of step s-1 after its
+            // last iteration of step s-2.  A warp still in step s-1 reads the other table.
             float2 *rtab = v.rtab + par * kRateTab;
             if (!FP64)
                 for (int e = (int)threadIdx.x; e < kRateTab; e += n_ssa) build_rate_entry<R>(rtab, cc, sv, e);
             if (bar_or(2, n_ssa, !ok)) {
                 my_err |= 2;
+                s_stop = s;
                 continue;
             }
             const int nsw = n_ssa >> 5;
@@ -820,6 +834,22 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
                 st_async(rd, make_uint4(lo_of(pv.v[0]), hi_of(pv.v[0]), lo_of(pv.v[1]), hi_of(pv.v[1])), rm);
                 st_async(rd + 16u, make_uint4(lo_of(pv.v[2]), hi_of(pv.v[2]), lo_of(pv.v[3]), hi_of(pv.v[3])), rm);
             }
+        }
+    }
+    // A CTA that stopped at step s_stop may still receive the SSA values of steps s_stop and
+    // s_stop + 1, stores the leader issued before it stopped in turn (it pushes step s + 2 only
+    // after this CTA's partials of step s, which a stopped CTA does not send).  Nothing orders the
+    // landing of an st.async with the closing cluster barrier; its completion shows only on the
+    // receiving mbarrier.  So thread 0 waits, bounded, for those two phases before the barrier
+    // (declaring the bytes of step s_stop + 1, whose phase was not declared yet): no store into
+    // this CTA's shared memory is in flight when it exits.
+    if ((my_err & 2) && threadIdx.x == 0 && s_stop >= 0) {
+        const uint32_t m0 = v.mbar + 16u + 8u * (uint32_t)(s_stop & 1);
+        mbar_wait(m0, (uint32_t)(s_stop >> 1) & 1u);
+        if (s_stop + 1 < a.n_steps) {
+            const uint32_t m1 = v.mbar + 16u + 8u * (uint32_t)((s_stop + 1) & 1);
+            mbar_arrive_expect_tx(m1, (uint32_t)(kSvCount * sizeof(R)));
+            mbar_wait(m1, (uint32_t)((s_stop + 1) >> 1) & 1u);
         }
     }
     // the launch's one closing cluster barrier (every thread of every CTA of the cluster)

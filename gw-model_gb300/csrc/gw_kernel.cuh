@@ -1,4 +1,5 @@
-// gw_kernel.cuh -- the GB300 engine kernel for the Greenstein-Winslow hybrid SSA.
+// gw_kernel.cuh -- the per-CRU hybrid SSA of the GB300 engine (device functions; the engine
+// kernel that runs them is in gw_engine.cuh).
 //
 // One launch advances every cell of an ensemble by n_steps global steps.  A cell's CRUs are
 // spread over the CTAs of one thread-block cluster; each CTA keeps its CRU tile in shared memory
@@ -6,11 +7,12 @@
 //
 //   SSA warps   : per-CRU hybrid SSA of step n (SSA.tpp:286-310) with V, Cai, CaNSR of step n,
 //                 then per-warp flux partials pushed into the leader CTA's shared memory (DSMEM).
-//   ODE warp    : (leader CTA of each cell only, concurrently with the SSA warps) reduces the
-//                 partials of step n-1 and takes the FP64 global step n -> n+1
-//                 (GW.tpp:237-272), then pushes the per-step SSA values of step n+1 to every CTA
+//   ODE warps   : (the four last warps of each cell's leader CTA, concurrently with the SSA warps)
+//                 reduce the partials of step n-1 and take the FP64 global step n -> n+1
+//                 (GW.tpp:237-272), then push the per-step SSA values of step n+1 to every CTA
 //                 of the cell.
-//   one barrier.cluster per step separates producers and consumers (double-buffered slots).
+//   No cluster barrier inside a launch: the step's data travel by st.async into double-buffered
+//   slots and complete the receiver's mbarrier of that slot (bounded waits).
 //
 // The reference's ordering is preserved: the global derivatives of step n use the fluxes left by
 // the SSA of step n-1 (GW.tpp:188-198) and the SSA of step n uses the globals of step n.
