@@ -6,12 +6,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
-#include <mutex>
 #include <string>
 #include <memory>
 #include <vector>
@@ -29,6 +29,9 @@ constexpr double kGasConst = 8.314; // common.hpp:10
 constexpr int kMaxSsaWarps = 12;    // + kOdeWarps ODE warps = 512 threads per CTA
 
 thread_local std::string g_create_error;
+// cudaMalloc calls of this library in this process (gw_stats.device_allocs); every device
+// allocation goes through DevBuf::alloc or dev_alloc
+std::atomic<uint64_t> g_device_allocs{0};
 
 struct DevBuf {
     void *p = nullptr;
@@ -41,6 +44,7 @@ struct DevBuf {
         p = nullptr;
         n = bytes;
         if (bytes == 0) return cudaSuccess;
+        g_device_allocs.fetch_add(1, std::memory_order_relaxed);
         cudaError_t e = cudaMalloc(&p, bytes);
         if (e == cudaSuccess) e = cudaMemset(p, 0, bytes);
         return e;
@@ -325,9 +329,6 @@ int plane_put(gw_ctx *c, DevBuf &b, int plane, int64_t s0, int64_t n, const T *i
 // One array per device, in the module image.  Nothing in it has to start at zero: every record
 // slot the trace unpack reads was written by the engine launch just before it.
 constexpr size_t kNoallocScratchBytes = GW_NOALLOC_SCRATCH_BYTES;
-constexpr int kNoallocMaxDevices = 64;
-std::mutex g_noalloc_mu;
-unsigned char *g_noalloc_ptr[kNoallocMaxDevices];  // device address per device, set once
 
 }  // namespace
 
@@ -335,19 +336,15 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[GW_NOALLOC_SCRA
 
 namespace {
 
-// Device address of the scratch on the current device (c->device), looked up once per device.
+// Device address of the scratch in the current device's context, looked up on every call (it
+// allocates nothing once the module is loaded; an address cached across calls would go stale if
+// the host application reset the device and the module were loaded again).
 int noalloc_scratch(gw_ctx *c, unsigned char **out) {
-    if (c->device < 0 || c->device >= kNoallocMaxDevices)
-        return fail(c, GW_ERR_UNSUPPORTED, "gw_run_noalloc supports devices 0..%d", kNoallocMaxDevices - 1);
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[c->device]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p)
-            return fail(c, GW_ERR_CUDA, "cudaGetSymbolAddress(no-allocation scratch): %s", cudaGetErrorString(e));
-        g_noalloc_ptr[c->device] = static_cast<unsigned char *>(p);
-    }
-    *out = g_noalloc_ptr[c->device];
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+        return fail(c, GW_ERR_CUDA, "cudaGetSymbolAddress(no-allocation scratch): %s", cudaGetErrorString(e));
+    *out = static_cast<unsigned char *>(p);
     return GW_OK;
 }
 
@@ -1114,11 +1111,18 @@ int gw_run_noalloc(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_t
     int64_t chunk = c->steps_per_launch;
     int64_t rec_cap = 0;
     if (recording) {
-        if (bytes_for(3) > kNoallocScratchBytes)
+        if (bytes_for(3) > kNoallocScratchBytes) {
+            if (tr_cell < 0)
+                return fail(c, GW_ERR_INVALID_ARGUMENT,
+                            "a trace record of the globals of %d cells needs about %zu bytes of staging and "
+                            "gw_run_noalloc stages at least 3 records in its %zu-byte scratch; split the cells "
+                            "over several contexts or use gw_run",
+                            c->n_cells, bytes_for(1), kNoallocScratchBytes);
             return fail(c, GW_ERR_INVALID_ARGUMENT,
                         "a trace record of this context needs about %zu bytes of staging and gw_run_noalloc stages at "
                         "least 3 records in its %zu-byte scratch; record fewer CRU fields or use gw_run",
                         bytes_for(1), kNoallocScratchBytes);
+        }
         while (bytes_for(chunk / record_every + 2) > kNoallocScratchBytes) chunk = std::max<int64_t>(1, chunk / 2);
         rec_cap = std::min<int64_t>(tr->max_records, chunk / record_every + 2);
     }
@@ -1271,6 +1275,7 @@ int gw_set_time(gw_ctx *c, int cell, double t, uint64_t step) {
 int gw_get_stats(gw_ctx *c, gw_stats *s) {
     if (!c || !s) return GW_ERR_INVALID_ARGUMENT;
     *s = c->stats;
+    s->device_allocs = g_device_allocs.load(std::memory_order_relaxed);
     return GW_OK;
 }
 

@@ -73,7 +73,8 @@ SUM_FIELDS = ["LCC_open", "LCC_conducting", "CaSS_conducting", "RyR_open", "ClCh
 class GwStats(C.Structure):
     _fields_ = [("steps", C.c_uint64), ("launches", C.c_uint64), ("kernel_ms", C.c_double),
                 ("events", C.c_uint64), ("cluster_ctas", C.c_int), ("cta_crus", C.c_int),
-                ("threads_per_cta", C.c_int), ("n_clusters", C.c_int), ("ctas", C.c_int)]
+                ("threads_per_cta", C.c_int), ("n_clusters", C.c_int), ("ctas", C.c_int),
+                ("device_allocs", C.c_uint64)]
 
 
 # Exported entry points and their signatures (all return int status unless noted).

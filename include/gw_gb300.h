@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define GW_ABI_VERSION 3
+#define GW_ABI_VERSION 4
 
 /* Status codes. */
 typedef enum gw_status {
@@ -87,9 +87,10 @@ typedef struct gw_ensemble_desc {
     uint64_t seed;
     int device;               /* CUDA device ordinal */
     int event_cap;            /* max jumps per CRU per step; 0 -> 65536 */
-    int cluster_ctas;         /* CTAs per thread-block cluster; 0 -> the smallest power of two that
-                                 keeps a cell's CTAs at <= 384 CRUs, at most 16 (gw_autotune
-                                 measures the best choice instead) */
+    int cluster_ctas;         /* CTAs per thread-block cluster; 0 -> FP32: the smallest power of two
+                                 that keeps a cell's CTAs at <= 384 CRUs, FP64: enough CTAs of at
+                                 most 96 CRUs; at most 16 either way (gw_autotune measures the best
+                                 choice instead) */
     int cta_crus;             /* CRU capacity of one CTA; 0 -> derived from cluster_ctas */
     int steps_per_launch;     /* global steps fused in one launch; 0 -> 1000 */
     int ode_fp32_rhs;         /* GW_PRECISION_FP32 only: 1 evaluates the global right-hand side in
@@ -146,6 +147,7 @@ typedef struct gw_stats {
     double kernel_ms;        /* device time of the engine kernels (CUDA events) */
     uint64_t events;         /* SSA jumps (all CRUs, all cells) */
     int cluster_ctas, cta_crus, threads_per_cta, n_clusters, ctas;
+    uint64_t device_allocs;  /* cudaMalloc calls made by this library in this process so far */
 } gw_stats;
 
 typedef struct gw_ctx gw_ctx;
@@ -221,9 +223,12 @@ int gw_run(gw_ctx *ctx, double dt, int64_t n_steps, int record_every, gw_trace *
  *
  * Limit: the records of one launch must fit the scratch.  Launches are shortened until they do;
  * if even 3 records do not fit, the call returns GW_ERR_INVALID_ARGUMENT with the size needed
- * (record fewer CRU fields, or use gw_run).  Without a trace it uses no scratch at all.
- * Set-up: the first call on a device looks the array up (cudaGetSymbolAddress, which may load the
- * module); make that first call before any stream capture begins.
+ * (record fewer CRU fields, or use gw_run).  A record always holds the 36 globals of every cell,
+ * so a globals-only trace also scales with n_cells (about 19,400 cells or more do not fit).
+ * Without a trace it uses no scratch at all.
+ * Set-up: every call looks the array's device address up in the current device's context
+ * (cudaGetSymbolAddress; the first call on a device may load the module); make the first call on
+ * each device before any stream capture begins.
  * Nothing in the scratch has to start at zero: each record slot is written by the engine before
  * it is read.  The per-cell status words are zeroed by the call itself, as gw_run does.
  * Concurrency: the scratch is shared by every context on the device.  Calls that overlap in time

@@ -58,7 +58,7 @@ int main(void) {
   O(gw_params, NCaRU) O(gw_params, Ko) O(gw_params, Hr) O(gw_globals, Kr) O(gw_globals, Kv43)
   O(gw_globals, Kv14) O(gw_ensemble_desc, seed) O(gw_ensemble_desc, ode_fp32_rhs)
   O(gw_trace, cru_cell) O(gw_trace, n_written) O(gw_trace, cru_sums) O(gw_trace, CaJSR_f32)
-  O(gw_stats, kernel_ms) O(gw_stats, ctas)
+  O(gw_stats, kernel_ms) O(gw_stats, ctas) O(gw_stats, device_allocs)
   return 0;
 }
 """
@@ -101,7 +101,7 @@ def test_global_defaults(enginelib, oracle):
 
 
 def test_abi_version(enginelib):
-    assert enginelib.gw_abi_version() == 3
+    assert enginelib.gw_abi_version() == 4
 
 
 def test_invalid_arguments_without_device(enginelib):

@@ -54,13 +54,10 @@ def _run(e, fn, dt, n, every, cru_cell):
 
 
 def _same(ra, rb):
+    # the same engine launches on the same state and draws: bit for bit the same records
     assert ra.keys() == rb.keys()
     for k in ra:
-        if ra[k].dtype == np.int32:
-            assert np.array_equal(ra[k], rb[k]), k
-        else:
-            # the same engine launches on the same state: equal up to 1e-12 relative
-            np.testing.assert_allclose(rb[k], ra[k], rtol=1e-12, atol=0, err_msg=k)
+        assert np.array_equal(ra[k], rb[k]), k
 
 
 def _state(e, cell=0):
@@ -80,12 +77,27 @@ def test_noalloc_matches_gw_run_on_two_calls(precision):
         assert np.all(ra["LCC"] >= 1) and np.all(ra["LCC"] <= 12)
         ga, sa = _state(a)
         gb, sb = _state(b)
-        np.testing.assert_allclose(gb, ga, rtol=1e-12, atol=0)
-        for f in ("LCC", "LCC_inactivation", "RyR", "ClCh"):
+        assert np.array_equal(gb, ga)
+        for f in ("CaSS", "CaJSR", "JLCC", "LCC", "LCC_inactivation", "RyR", "ClCh"):
             assert np.array_equal(getattr(sa, f), getattr(sb, f)), (call, f)
         assert a.time(0) == b.time(0)
     a.close()
     b.close()
+
+
+def test_noalloc_allocates_no_device_memory():
+    """After its first call on a device, gw_run_noalloc makes no cudaMalloc (the library counts
+    every one it makes, gw_stats.device_allocs); gw_run, for comparison, allocates its record
+    staging on every call."""
+    e = _ensemble([1500, 700], "fp64", seed=8)
+    _run(e, "gw_run_noalloc", 1e-3, 200, 40, cru_cell=1)
+    n0 = e.stats()["device_allocs"]
+    for _ in range(2):
+        _run(e, "gw_run_noalloc", 1e-3, 200, 40, cru_cell=1)
+    assert e.stats()["device_allocs"] == n0
+    _run(e, "gw_run", 1e-3, 200, 40, cru_cell=1)
+    assert e.stats()["device_allocs"] > n0
+    e.close()
 
 
 def test_noalloc_shortens_launches_to_fit_its_scratch():
