@@ -1,0 +1,1185 @@
+// gw_adjoint.cu -- pathwise gradients of a voltage-trace loss for an ensemble of cells (gw_grad_*
+// in gw_gb300.h).  No counterpart in the reference, which has no derivatives.
+//
+// Forward.  Per global step s, two kernels: k_ssa runs every CRU's hybrid SSA of step s (the FP64
+// lane of the engine, SsaLane<double, true>, with the engine's counter-based draws keyed on (seed,
+// cell, CRU, step), so the jump trajectory is the one gw_run draws); k_global sums each cell's CRU
+// fluxes and takes the FP64 global step (gw_adjoint_math.h, the reference's formulas and order).
+// The state of every CRU and cell is checkpointed every `checkpoint_every` steps.
+//
+// Backward, one checkpoint segment at a time from the last: the segment is recomputed from its
+// checkpoint with every step's start state stored, then stepped in reverse:
+//   k_cru_adj     one thread per CRU: re-runs the CRU's step from its stored start state with the
+//                 same draws (hence the same jump times and transitions), keeps the sub-steps in
+//                 blocks of kRec and walks them backwards through the adjoint of the sub-step and
+//                 event arithmetic; a block reduction gives the cell's adjoints of the step inputs
+//                 (Cai, CaNSR, the JLCC factors) and of rRyR and CSQN.
+//   k_global_adj  one thread per cell: the adjoint of the global increment plus the CRU inputs'
+//                 contributions, and the parameters' relative sensitivities.
+// Memory: (steps / checkpoint_every) checkpoints + checkpoint_every step states of every CRU.
+//
+// Replay (gw_grad_replay) re-runs chosen cells with other parameters on the recorded jump
+// trajectory (frozen jump times and transitions): a copy of the source cell runs as in the forward
+// pass and drives a variant whose continuous state follows the same sub-steps and events.  At the
+// source's own parameters the replay reproduces the forward pass bit for bit, so central
+// differences of replays measure exactly the derivative the adjoint computes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gw_adjoint_math.h"
+#include "gw_gb300.h"
+#include "gw_internal.h"
+#include "gw_kernel.cuh"
+
+using namespace gw;
+using namespace gw::adj;
+
+namespace {
+
+constexpr int kBlk = 128;     // threads per block of the CRU kernels (one cell per block)
+constexpr int kRec = 8;       // sub-steps a CRU keeps per block of its reverse sweep
+constexpr int kAdjIn = 6;     // per-cell CRU adjoints: Cai, CaNSR, JM, JE, rRyR (relative), CSQN_const
+constexpr int kLamX = 9;      // CRU adjoint state: CaSS[4], CaJSR, JLCC[4]
+using CruD = dev::Cru<double>;
+
+struct Buf {
+    void *p = nullptr;
+    size_t n = 0;
+    Buf() = default;
+    Buf(const Buf &) = delete;
+    Buf &operator=(const Buf &) = delete;
+    ~Buf() {
+        if (p) cudaFree(p);
+    }
+    int alloc(size_t bytes) {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = bytes;
+        return dev_alloc(&p, bytes);
+    }
+    template <typename T>
+    T *as() const {
+        return reinterpret_cast<T *>(p);
+    }
+};
+
+// Arguments of the forward kernels for one set of cells (the ensemble, or a replay's source copies
+// or variants).
+struct GradArgs {
+    const CellStatic *cs;       // [n_cells]
+    const int *blk_cell;        // [blocks] cell of each CRU block
+    const int *blk_lo;          // [blocks] first CRU (within the cell) of each block
+    const int64_t *cru0;        // [n_cells] first CRU of each cell in the CRU arrays
+    const int *ncru;            // [n_cells]
+    const int *rng_cell;        // [n_cells] cell index that keys the cell's random streams
+    CruD *x;                    // [n_crus] CRU state
+    double *out;                // [n_crus][4] the step's per-CRU sum JLCC, sum Jxfer, Jtr, open ClCh
+    double *G;                  // [n_cells][36]
+    double *carry;              // [n_cells][4] sum JLCC, sum ClCh, sum Jtr, sum Jxfer
+    double *t;                  // [n_cells] accumulated time
+    double *sv;                 // [n_cells][kSvCount] SSA values of the current step
+    const double *stim;         // [n_cells][4] pulse start, period, duration, amplitude
+    int *status;                // [n_cells]
+    unsigned long long *events; // [n_cells] or null
+    double *V;                  // [n_cells][n_samples] or null
+    unsigned long long *regime; // [n_cells] steps begun at V >= -40 mV, or null
+    int64_t n_samples;
+    int sample_every;
+    uint64_t seed;
+    double dt;
+    int event_cap;
+    int n_cells;
+    int64_t n_crus;
+    // Recording of a segment's step states (null: not recording): slot = step - segment start.
+    CruD *seg_x;                // [slots][n_crus]
+    double *seg_G;              // [slots][n_cells][36]
+    double *seg_carry;          // [slots][n_cells][4]
+    double *seg_sv;             // [slots][n_cells][kSvCount]
+    // Replay: the variant's continuous CRU state driven by this set's jump trajectory (null: none).
+    const CellStatic *var_cs;   // [n_cells]
+    double *var_x;              // [n_crus][9] CaSS[4], CaJSR, JLCC[4]
+    double *var_out;            // [n_crus][4]
+    const double *var_sv;       // [n_cells][kSvCount]
+};
+
+// Adjoint arrays.
+struct AdjArgs {
+    double *lam_x;      // [n_crus][9]
+    double *lam_G;      // [n_cells][36]
+    double *lam_cy;     // [n_cells][3] adjoints of the carry sums JLCC, Jtr, Jxfer
+    double *lam_th;     // [n_cells][8] relative sensitivities
+    double *part;       // [blocks][kAdjIn]
+    const int *blk0;    // [n_cells + 1] first block of each cell
+    const double *dLdV; // [n_cells][n_samples]
+};
+
+__device__ __forceinline__ double pulse_at(double t, const double *s) {
+    double tb = __dsub_rn(t, s[0]);
+    if (tb >= 0.0) {
+        if (s[1] > 0.0) tb = __dsub_rn(tb, __dmul_rn(s[1], trunc(__ddiv_rn(tb, s[1]))));
+        if (tb < s[2]) return s[3];
+    }
+    return 0.0;
+}
+
+// Sum of N values over the block (warp shuffles, then warp totals in order); thread 0 holds it.
+template <int N>
+__device__ __forceinline__ void block_sum(double (&v)[N], double *sh) {
+#pragma unroll
+    for (int q = 0; q < N; ++q)
+        for (int off = 16; off > 0; off >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], off);
+    const int w = (int)threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int q = 0; q < N; ++q) sh[w * N + q] = v[q];
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int q = 0; q < N; ++q) {
+            double s = 0.0;
+            for (int k = 0; k < kBlk / 32; ++k) s += sh[k * N + q];
+            v[q] = s;
+        }
+}
+
+__device__ __forceinline__ void open_counts(const CruD &c, int o[4]) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) o[j] = dev::byte_s(c.ryr[2], j) + dev::byte_s(c.ryr[3], j);
+}
+
+// The continuous effect of the transition an iteration applied (apply_event in gw_kernel.cuh),
+// from the channel state before (lcc0, fl0) and after (c) it.
+__device__ __forceinline__ void classify(const dev::IterInfo<double> &f, uint32_t lcc0, uint32_t fl0, const CruD &c,
+                                         int &ev, int &j, int &onew) {
+    ev = EV_NONE;
+    j = f.aj;
+    onew = 0;
+    const uint32_t sh = 8u * (uint32_t)j;
+    if (f.act == 1) {
+        const int from = (int)((lcc0 >> sh) & 0xFFu), to = (int)((c.lcc >> sh) & 0xFFu);
+        if (from >= 1 && from <= 12) {
+            if ((from == 5 && to == 6) || (from == 11 && to == 12))
+                ev = ((fl0 >> j) & 1u) ? EV_JLCC_SET : EV_JLCC_ZERO;
+            else if (from == 6 || from == 12)
+                ev = EV_JLCC_ZERO;
+        }
+    } else if (f.act == 2) {
+        const int st = (int)((c.lcc >> sh) & 0xFFu);
+        if (((c.flags >> j) & 1u) == 0u)
+            ev = EV_JLCC_ZERO;
+        else if (st == 6 || st == 12)
+            ev = EV_JLCC_SET;
+    } else if (f.act == 3) {
+        ev = EV_JREL;
+        onew = dev::byte_s(c.ryr[2], j) + dev::byte_s(c.ryr[3], j);
+    }
+}
+
+__device__ __forceinline__ CruIn cru_in(const double *sv) {
+    return CruIn{sv[SV_CAI], sv[SV_CANSR], sv[SV_JMUL], sv[SV_JEXP]};
+}
+
+// Forward SSA of step `step` for every CRU (one block per 128 CRUs of one cell).
+__global__ void __launch_bounds__(kBlk) k_ssa(const GradArgs a, int64_t step, int slot) {
+    __shared__ dev::SsaConsts<double> cc;
+    __shared__ double sv[kSvCount];
+    __shared__ double vsv[kSvCount];
+    const int cell = a.blk_cell[blockIdx.x];
+    if (threadIdx.x == 0) dev::load_ssa_consts<double>(cc, a.cs[cell]);
+    if (threadIdx.x < kSvCount) {
+        sv[threadIdx.x] = a.sv[(int64_t)cell * kSvCount + threadIdx.x];
+        if (a.var_x) vsv[threadIdx.x] = a.var_sv[(int64_t)cell * kSvCount + threadIdx.x];
+    }
+    __syncthreads();
+    const int m = a.blk_lo[blockIdx.x] + (int)threadIdx.x;
+    const bool active = m < a.ncru[cell] && a.status[cell] == 0;
+    unsigned int ev = 0;
+    int err = 0;
+    if (active) {
+        const int64_t i = a.cru0[cell] + m;
+        CruD c = a.x[i];
+        if (a.seg_x) a.seg_x[(int64_t)slot * a.n_crus + i] = c;
+        dev::Stream rng;
+        rng.open(a.seed, (uint32_t)a.rng_cell[cell], (uint32_t)m, (uint64_t)step, 0);
+        dev::SsaLane<double, true> L;
+        L.begin(c, cc);
+        if (!a.var_x) {
+            while (!L.iterate(c, cc, sv, nullptr, rng, a.dt, a.event_cap, err)) {
+            }
+        } else {
+            // the variant follows the same sub-steps and events with its own parameters and inputs
+            const CruPar P = cru_par(a.var_cs[cell]);
+            const CruIn in = cru_in(vsv);
+            double *vx = a.var_x + (int64_t)kLamX * i;
+            CruCont v;
+            for (int j = 0; j < 4; ++j) {
+                v.c[j] = vx[j];
+                v.L[j] = vx[5 + j];
+            }
+            v.J = vx[4];
+            int o[4];
+            open_counts(c, o);
+            cru_begin(v, o, P);
+            double vjtr = 0.0, vjx = 0.0;
+            for (;;) {
+                const uint32_t lcc0 = c.lcc, fl0 = c.flags;
+                dev::IterInfo<double> f;
+                const bool done = L.iterate(c, cc, sv, nullptr, rng, a.dt, a.event_cap, err, &f);
+                cru_substep(v, f.h, in, P, vjtr, vjx);
+                int e, j, onew;
+                classify(f, lcc0, fl0, c, e, j, onew);
+                cru_event(v, e, j, onew, in, P);
+                if (done) break;
+            }
+            for (int j = 0; j < 4; ++j) {
+                vx[j] = v.c[j];
+                vx[5 + j] = v.L[j];
+            }
+            vx[4] = v.J;
+            double *vo = a.var_out + 4 * i;
+            vo[0] = v.L[0] + v.L[1] + v.L[2] + v.L[3];
+            vo[1] = vjx;
+            vo[2] = vjtr;
+            vo[3] = (double)__popc((c.flags >> 4) & 0xFu);
+        }
+        a.x[i] = c;
+        double *o = a.out + 4 * i;
+        o[0] = c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3];
+        o[1] = L.jxfer_sum;
+        o[2] = L.jtr;
+        o[3] = (double)__popc((c.flags >> 4) & 0xFu);
+        ev = (unsigned int)L.ev;
+    }
+    const unsigned int wev = __reduce_add_sync(0xffffffffu, ev);
+    if (a.events && (threadIdx.x & 31) == 0 && wev) atomicAdd(&a.events[cell], (unsigned long long)wev);
+    if (err) atomicExch(&a.status[cell], (int)GW_ERR_EVENT_CAP);
+}
+
+// The cell's flux sums of the step and its global step (one block per cell).
+__global__ void __launch_bounds__(kBlk) k_global(const GradArgs a, int64_t step, int slot, int use_var) {
+    __shared__ double sh[(kBlk / 32) * 4];
+    const int cell = blockIdx.x;
+    const int n = a.ncru[cell];
+    const double *o = (use_var ? a.var_out : a.out) + 4 * a.cru0[cell];
+    double s[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int m = (int)threadIdx.x; m < n; m += kBlk)
+        for (int q = 0; q < 4; ++q) s[q] += o[4 * m + q];
+    block_sum<4>(s, sh);
+    if (threadIdx.x != 0 || a.status[cell] != 0) return;
+    const CellStatic &C = use_var ? a.var_cs[cell] : a.cs[cell];
+    double *g = a.G + (int64_t)kNumGlobals * cell;
+    double *cy = a.carry + 4 * (int64_t)cell;
+    double *svo = (use_var ? const_cast<double *>(a.var_sv) : a.sv) + (int64_t)kSvCount * cell;
+    double gl[kNumGlobals], d[kNumGlobals];
+    for (int k = 0; k < kNumGlobals; ++k) gl[k] = g[k];
+    const Carry c0{cy[0], cy[1], cy[2], cy[3]};
+    const double istim = pulse_at(a.t[cell], a.stim + 4 * (int64_t)cell);
+    if (a.seg_G) {
+        const int64_t r = (int64_t)slot * a.n_cells + cell;
+        for (int k = 0; k < kNumGlobals; ++k) a.seg_G[r * kNumGlobals + k] = gl[k];
+        for (int k = 0; k < 4; ++k) a.seg_carry[r * 4 + k] = cy[k];
+        for (int k = 0; k < kSvCount; ++k) a.seg_sv[r * kSvCount + k] = svo[k];
+    }
+    if (a.regime && gl[0] >= -40.0) a.regime[cell] += 1ull;
+    if (!glob_increment(C, gl, c0, istim, a.dt, d)) {
+        a.status[cell] = GW_ERR_NERNST;
+        return;
+    }
+    bool fin = true;
+    for (int k = 0; k < kNumGlobals; ++k) {
+        gl[k] += d[k];
+        fin = fin && isfinite(gl[k]);
+    }
+    if (!fin) {
+        a.status[cell] = GW_ERR_NONFINITE;
+        return;
+    }
+    for (int k = 0; k < kNumGlobals; ++k) g[k] = gl[k];
+    // carry order {JLCC, ClCh, Jtr, Jxfer} from the per-CRU {JLCC, Jxfer, Jtr, ClCh}
+    cy[0] = s[0];
+    cy[1] = s[3];
+    cy[2] = s[2];
+    cy[3] = s[1];
+    a.t[cell] += a.dt;
+    step_values(C, gl, svo);
+    if (a.V && (step + 1) % a.sample_every == 0) {
+        const int64_t si = (step + 1) / a.sample_every - 1;
+        if (si < a.n_samples) a.V[(int64_t)cell * a.n_samples + si] = gl[0];
+    }
+}
+
+// One recorded sub-step of a CRU's step: the state at its start and what ended it.
+struct Rec {
+    CruCont s;
+    double h;
+    int ev, j, onew;
+};
+
+// Re-runs a CRU's step from x0 and keeps iterations [lo, hi) in rec[k % kRec]; stops after hi
+// iterations or at the end of the step.  Returns the iterations run.
+__device__ int run_rec(const CruD &x0, const dev::SsaConsts<double> &cc, const double *sv, uint64_t seed,
+                       uint32_t rcell, uint32_t m, uint64_t step, double dt, int cap, int lo, int hi, Rec *rec) {
+    CruD c = x0;
+    dev::Stream rng;
+    rng.open(seed, rcell, m, step, 0);
+    dev::SsaLane<double, true> L;
+    L.begin(c, cc);
+    int k = 0, err = 0;
+    for (;;) {
+        CruCont s;
+        const bool keep = k >= lo && k < hi;
+        if (keep) {
+            for (int j = 0; j < 4; ++j) {
+                s.c[j] = c.cass[j];
+                s.L[j] = c.jlcc[j];
+                s.rel[j] = L.jrel[j];
+            }
+            s.J = c.cajsr;
+        }
+        const uint32_t lcc0 = c.lcc, fl0 = c.flags;
+        dev::IterInfo<double> f;
+        const bool done = L.iterate(c, cc, sv, nullptr, rng, dt, cap, err, &f);
+        if (keep) {
+            Rec &r = rec[k % kRec];
+            r.s = s;
+            r.h = f.h;
+            classify(f, lcc0, fl0, c, r.ev, r.j, r.onew);
+        }
+        ++k;
+        if (done || k >= hi) break;
+    }
+    return k;
+}
+
+// Reverse of step `step` for every CRU: lam_x from after the step to before it, and the block's
+// sums of the step-input and parameter adjoints into part[block].
+__global__ void __launch_bounds__(kBlk) k_cru_adj(const GradArgs a, const AdjArgs b, int64_t step, int slot) {
+    __shared__ dev::SsaConsts<double> cc;
+    __shared__ double sv[kSvCount];
+    __shared__ double sh[(kBlk / 32) * kAdjIn];
+    const int cell = a.blk_cell[blockIdx.x];
+    if (threadIdx.x == 0) dev::load_ssa_consts<double>(cc, a.cs[cell]);
+    if (threadIdx.x < kSvCount)
+        sv[threadIdx.x] = a.seg_sv[((int64_t)slot * a.n_cells + cell) * kSvCount + threadIdx.x];
+    __syncthreads();
+    const int m = a.blk_lo[blockIdx.x] + (int)threadIdx.x;
+    double acc[kAdjIn] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    if (m < a.ncru[cell]) {
+        const int64_t i = a.cru0[cell] + m;
+        const CruD x0 = a.seg_x[(int64_t)slot * a.n_crus + i];
+        const CruPar P = cru_par(a.cs[cell]);
+        const CruIn in = cru_in(sv);
+        const double *lc = b.lam_cy + 3 * (int64_t)cell;
+        double *lx = b.lam_x + (int64_t)kLamX * i;
+        CruCont la;
+        for (int j = 0; j < 4; ++j) {
+            la.c[j] = lx[j];
+            la.L[j] = lx[5 + j] + lc[0];
+            la.rel[j] = 0.0;
+        }
+        la.J = lx[4];
+        CruAdjIn ai{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        Rec rec[kRec];
+        const uint32_t rc = (uint32_t)a.rng_cell[cell];
+        const int n = run_rec(x0, cc, sv, a.seed, rc, (uint32_t)m, (uint64_t)step, a.dt, a.event_cap, 0, 1 << 30,
+                              rec);
+        for (int blk = (n - 1) / kRec; blk >= 0; --blk) {
+            const int lo = blk * kRec, hi = min(n, lo + kRec);
+            if (blk != (n - 1) / kRec)
+                run_rec(x0, cc, sv, a.seed, rc, (uint32_t)m, (uint64_t)step, a.dt, a.event_cap, lo, hi, rec);
+            for (int k = hi - 1; k >= lo; --k) {
+                const Rec &r = rec[k % kRec];
+                CruCont s1 = r.s;
+                double jt, jx;
+                cru_substep(s1, r.h, in, P, jt, jx);
+                cru_event_adj(s1, r.ev, r.j, r.onew, in, P, la, ai);
+                const bool last = k == n - 1;
+                cru_substep_adj(r.s, r.h, in, P, last ? lc[1] : 0.0, last ? lc[2] : 0.0, la, ai);
+            }
+        }
+        CruCont s0;
+        for (int j = 0; j < 4; ++j) {
+            s0.c[j] = x0.cass[j];
+            s0.L[j] = x0.jlcc[j];
+            s0.rel[j] = 0.0;
+        }
+        s0.J = x0.cajsr;
+        int o[4];
+        open_counts(x0, o);
+        cru_begin_adj(s0, o, P, la, ai);
+        for (int j = 0; j < 4; ++j) {
+            lx[j] = la.c[j];
+            lx[5 + j] = la.L[j];
+        }
+        lx[4] = la.J;
+        acc[0] = ai.Cai;
+        acc[1] = ai.CaNSR;
+        acc[2] = ai.JM;
+        acc[3] = ai.JE;
+        acc[4] = ai.rRyR_rel;
+        acc[5] = ai.CSQN;
+    }
+    block_sum<kAdjIn>(acc, sh);
+    if (threadIdx.x == 0)
+        for (int q = 0; q < kAdjIn; ++q) b.part[(int64_t)blockIdx.x * kAdjIn + q] = acc[q];
+}
+
+// Reverse of the global step `step` for every cell (one thread per cell).
+__global__ void k_global_adj(const GradArgs a, const AdjArgs b, int64_t step, int slot) {
+    const int cell = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (cell >= a.n_cells) return;
+    const CellStatic &C = a.cs[cell];
+    const int64_t r = (int64_t)slot * a.n_cells + cell;
+    const double *g = a.seg_G + r * kNumGlobals;
+    const double *cyv = a.seg_carry + r * 4;
+    const double *sv = a.seg_sv + r * kSvCount;
+    const Carry cy{cyv[0], cyv[1], cyv[2], cyv[3]};
+    double ai[kAdjIn] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int k = b.blk0[cell]; k < b.blk0[cell + 1]; ++k)
+        for (int q = 0; q < kAdjIn; ++q) ai[q] += b.part[(int64_t)k * kAdjIn + q];
+    double *lgp = b.lam_G + (int64_t)kNumGlobals * cell;
+    double lam[kNumGlobals], lg[kNumGlobals];
+    for (int k = 0; k < kNumGlobals; ++k) {
+        lam[k] = lgp[k];
+        lg[k] = 0.0;
+    }
+    if ((step + 1) % a.sample_every == 0) {
+        const int64_t si = (step + 1) / a.sample_every - 1;
+        if (si < a.n_samples) lam[0] += b.dLdV[(int64_t)cell * a.n_samples + si];
+    }
+    double lcy[3] = {0.0, 0.0, 0.0};
+    double *th = b.lam_th + (int64_t)kTheta * cell;
+    double lth[kTheta];
+    for (int k = 0; k < kTheta; ++k) lth[k] = th[k];
+    glob_increment_adj(C, g, cy, a.dt, lam, lg, lcy, lth);
+    // the CRUs' step inputs: Cai, CaNSR and the JLCC factors of V
+    lg[3] += ai[0];
+    lg[4] += ai[1];
+    double dJM, dJE;
+    jlcc_factor_derivs(C, g[0], sv[SV_JEXP], dJM, dJE);
+    lg[0] += ai[2] * dJM + ai[3] * dJE;
+    lth[TH_PCAL] += ai[2] * sv[SV_JMUL];
+    lth[TH_RRYR] += ai[4];
+    lth[TH_CSQNT] += ai[5] * C.CSQN_const;
+    for (int k = 0; k < kNumGlobals; ++k) lgp[k] = lg[k];
+    for (int k = 0; k < 3; ++k) b.lam_cy[3 * (int64_t)cell + k] = lcy[k];
+    for (int k = 0; k < kTheta; ++k) th[k] = lth[k];
+}
+
+int fail_to(std::string &err, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    err = buf;
+    return code;
+}
+
+thread_local std::string g_grad_create_error;
+
+// Host CRU record of the reference's arrays for one CRU (JLCC zero, as the reference's ctor).
+int pack_cru(const double *CaSS, const double *CaJSR, const int32_t *LCC, const int32_t *LCCi, const int32_t *RyR,
+             const int32_t *ClCh, int i, CruD &c, double &clch) {
+    std::memset(&c, 0, sizeof c);
+    for (int j = 0; j < 4; ++j) {
+        const int s = LCC[4 * i + j], li = LCCi[4 * i + j], ch = ClCh[4 * i + j];
+        if (s < 1 || s > 12 || (li != 0 && li != 1) || (ch != 0 && ch != 1)) return 1;
+        c.lcc |= (uint32_t)(s & 0xFF) << (8 * j);
+        c.flags |= (uint32_t)li << j;
+        c.flags |= (uint32_t)ch << (4 + j);
+        clch += ch;
+        for (int k = 0; k < 6; ++k) {
+            const int v = RyR[24 * i + 6 * j + k];
+            if (v < -128 || v > 127) return 1;
+            c.ryr[k] |= (uint32_t)(v & 0xFF) << (8 * j);
+        }
+        c.cass[j] = CaSS[4 * i + j];
+        c.jlcc[j] = 0.0;
+    }
+    c.cajsr = CaJSR[i];
+    return 0;
+}
+
+}  // namespace
+
+struct gw_grad {
+    int device = 0;
+    int n_cells = 0;
+    int64_t n_crus = 0;
+    int n_blocks = 0;
+    std::vector<int> ncru, blk_cell, blk_lo, blk0;
+    std::vector<int64_t> cru0;
+    std::vector<CellStatic> cs;
+    std::vector<double> stim;
+    double dt = 0.0;
+    int64_t n_steps = 0, n_samples = 0, n_ck = 0;
+    int ck_every = 200, sample_every = 1, event_cap = 65536;
+    uint64_t seed = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string err;
+    std::vector<char> have_state;
+    bool forwarded = false;
+    gw_grad_stats stats{};
+    std::vector<double> G_final;
+    // tables
+    Buf d_cs, d_blk_cell, d_blk_lo, d_blk0, d_cru0, d_ncru, d_rng_cell, d_stim;
+    // initial state
+    Buf x_init, G_init, carry_init, sv_init;
+    // state
+    Buf x, out, G, carry, t, sv, status, events, V, regime;
+    // checkpoints and segment
+    Buf ck_x, ck_G, ck_carry, ck_t, ck_sv;
+    Buf seg_x, seg_G, seg_carry, seg_sv;
+    // adjoint
+    Buf lam_x, lam_G, lam_cy, lam_th, part, dLdV;
+
+    ~gw_grad() {
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+    int cuda(cudaError_t e, const char *what) {
+        if (e == cudaSuccess) return GW_OK;
+        cudaGetLastError();
+        return fail_to(err, e == cudaErrorMemoryAllocation ? GW_ERR_OUT_OF_MEMORY : GW_ERR_CUDA, "%s: %s", what,
+                       cudaGetErrorString(e));
+    }
+    int alloc(Buf &b, size_t bytes, const char *what) {
+        const int e = b.alloc(bytes);
+        return cuda((cudaError_t)e, what);
+    }
+    GradArgs args() const {
+        GradArgs a{};
+        a.cs = d_cs.as<CellStatic>();
+        a.blk_cell = d_blk_cell.as<int>();
+        a.blk_lo = d_blk_lo.as<int>();
+        a.cru0 = d_cru0.as<int64_t>();
+        a.ncru = d_ncru.as<int>();
+        a.rng_cell = d_rng_cell.as<int>();
+        a.x = x.as<CruD>();
+        a.out = out.as<double>();
+        a.G = G.as<double>();
+        a.carry = carry.as<double>();
+        a.t = t.as<double>();
+        a.sv = sv.as<double>();
+        a.stim = d_stim.as<double>();
+        a.status = status.as<int>();
+        a.events = events.as<unsigned long long>();
+        a.V = V.as<double>();
+        a.regime = regime.as<unsigned long long>();
+        a.n_samples = n_samples;
+        a.sample_every = sample_every;
+        a.seed = seed;
+        a.dt = dt;
+        a.event_cap = event_cap;
+        a.n_cells = n_cells;
+        a.n_crus = n_crus;
+        return a;
+    }
+    AdjArgs adj_args() const {
+        AdjArgs b{};
+        b.lam_x = lam_x.as<double>();
+        b.lam_G = lam_G.as<double>();
+        b.lam_cy = lam_cy.as<double>();
+        b.lam_th = lam_th.as<double>();
+        b.part = part.as<double>();
+        b.blk0 = d_blk0.as<int>();
+        b.dLdV = dLdV.as<double>();
+        return b;
+    }
+    // Restores the state of step s0 = k * ck_every from checkpoint k (k = -1: the initial state).
+    int restore(int64_t k) {
+        const size_t xb = sizeof(CruD) * n_crus, gb = sizeof(double) * kNumGlobals * n_cells;
+        const size_t cb = sizeof(double) * 4 * n_cells, tb = sizeof(double) * n_cells;
+        const size_t sb = sizeof(double) * kSvCount * n_cells;
+        int rc;
+        if (k < 0) {
+            if ((rc = cuda(cudaMemcpyAsync(x.p, x_init.p, xb, cudaMemcpyDeviceToDevice, stream), "restore"))) return rc;
+            if ((rc = cuda(cudaMemcpyAsync(G.p, G_init.p, gb, cudaMemcpyDeviceToDevice, stream), "restore"))) return rc;
+            if ((rc = cuda(cudaMemcpyAsync(carry.p, carry_init.p, cb, cudaMemcpyDeviceToDevice, stream), "restore")))
+                return rc;
+            if ((rc = cuda(cudaMemsetAsync(t.p, 0, tb, stream), "restore"))) return rc;
+            return cuda(cudaMemcpyAsync(sv.p, sv_init.p, sb, cudaMemcpyDeviceToDevice, stream), "restore");
+        }
+        auto at = [](const Buf &b, size_t bytes, int64_t k) { return (char *)b.p + bytes * (size_t)k; };
+        if ((rc = cuda(cudaMemcpyAsync(x.p, at(ck_x, xb, k), xb, cudaMemcpyDeviceToDevice, stream), "restore")))
+            return rc;
+        if ((rc = cuda(cudaMemcpyAsync(G.p, at(ck_G, gb, k), gb, cudaMemcpyDeviceToDevice, stream), "restore")))
+            return rc;
+        if ((rc = cuda(cudaMemcpyAsync(carry.p, at(ck_carry, cb, k), cb, cudaMemcpyDeviceToDevice, stream), "restore")))
+            return rc;
+        if ((rc = cuda(cudaMemcpyAsync(t.p, at(ck_t, tb, k), tb, cudaMemcpyDeviceToDevice, stream), "restore")))
+            return rc;
+        return cuda(cudaMemcpyAsync(sv.p, at(ck_sv, sb, k), sb, cudaMemcpyDeviceToDevice, stream), "restore");
+    }
+    int save(int64_t k) {
+        const size_t xb = sizeof(CruD) * n_crus, gb = sizeof(double) * kNumGlobals * n_cells;
+        const size_t cb = sizeof(double) * 4 * n_cells, tb = sizeof(double) * n_cells;
+        const size_t sb = sizeof(double) * kSvCount * n_cells;
+        auto at = [](const Buf &b, size_t bytes, int64_t k) { return (char *)b.p + bytes * (size_t)k; };
+        int rc;
+        if ((rc = cuda(cudaMemcpyAsync(at(ck_x, xb, k), x.p, xb, cudaMemcpyDeviceToDevice, stream), "checkpoint")))
+            return rc;
+        if ((rc = cuda(cudaMemcpyAsync(at(ck_G, gb, k), G.p, gb, cudaMemcpyDeviceToDevice, stream), "checkpoint")))
+            return rc;
+        if ((rc = cuda(cudaMemcpyAsync(at(ck_carry, cb, k), carry.p, cb, cudaMemcpyDeviceToDevice, stream),
+                       "checkpoint")))
+            return rc;
+        if ((rc = cuda(cudaMemcpyAsync(at(ck_t, tb, k), t.p, tb, cudaMemcpyDeviceToDevice, stream), "checkpoint")))
+            return rc;
+        return cuda(cudaMemcpyAsync(at(ck_sv, sb, k), sv.p, sb, cudaMemcpyDeviceToDevice, stream), "checkpoint");
+    }
+    int check_status(const Buf &st, int n, const char *what) {
+        std::vector<int> s(n);
+        int rc = cuda(cudaMemcpyAsync(s.data(), st.p, sizeof(int) * n, cudaMemcpyDeviceToHost, stream), what);
+        if (rc) return rc;
+        if ((rc = cuda(cudaStreamSynchronize(stream), what))) return rc;
+        for (int c = 0; c < n; ++c)
+            if (s[c] != 0)
+                return fail_to(err, s[c], "%s: cell %d stopped with status %d (%s)", what, c, s[c],
+                               s[c] == GW_ERR_NERNST      ? "non-positive Nernst argument"
+                               : s[c] == GW_ERR_NONFINITE ? "non-finite global state"
+                                                          : "jump cap exceeded");
+        return GW_OK;
+    }
+};
+
+extern "C" {
+
+int gw_grad_create(const gw_grad_desc *d, gw_grad **out) {
+    g_grad_create_error.clear();
+    if (!out) return fail_to(g_grad_create_error, GW_ERR_INVALID_ARGUMENT, "null output pointer");
+    *out = nullptr;
+    if (!d || d->n_cells < 1 || !d->ncru || !d->params || !d->stim)
+        return fail_to(g_grad_create_error, GW_ERR_INVALID_ARGUMENT, "null descriptor field or n_cells < 1");
+    if (!(d->dt > 0.0) || d->n_steps < 1 || d->sample_every < 1 || d->checkpoint_every < 0 || d->event_cap < 0)
+        return fail_to(g_grad_create_error, GW_ERR_INVALID_ARGUMENT,
+                       "need dt > 0, n_steps >= 1, sample_every >= 1, checkpoint_every >= 0, event_cap >= 0");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail_to(g_grad_create_error, GW_ERR_NO_DEVICE, "no CUDA device");
+    }
+    if (d->device < 0 || d->device >= ndev)
+        return fail_to(g_grad_create_error, GW_ERR_INVALID_ARGUMENT, "device %d of %d", d->device, ndev);
+    int major = 0, minor = 0;
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, d->device);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, d->device);
+    if (major != 10 || minor != 3)
+        return fail_to(g_grad_create_error, GW_ERR_NO_DEVICE, "device %d is sm_%d%d; this build targets sm_103a",
+                       d->device, major, minor);
+    cudaSetDevice(d->device);
+    gw_grad *g = new gw_grad;
+    g->device = d->device;
+    g->n_cells = d->n_cells;
+    g->dt = d->dt;
+    g->n_steps = d->n_steps;
+    g->sample_every = d->sample_every;
+    g->n_samples = d->n_steps / d->sample_every;
+    g->ck_every = d->checkpoint_every > 0 ? d->checkpoint_every : 200;
+    g->n_ck = (d->n_steps + g->ck_every - 1) / g->ck_every;
+    g->event_cap = d->event_cap > 0 ? d->event_cap : 65536;
+    g->seed = d->seed;
+    g->stim.assign(d->stim, d->stim + 4 * (size_t)d->n_cells);
+    g->have_state.assign(d->n_cells, 0);
+    g->cs.resize(d->n_cells);
+    g->ncru.resize(d->n_cells);
+    g->cru0.resize(d->n_cells);
+    g->blk0.resize(d->n_cells + 1);
+    for (int c = 0; c < d->n_cells; ++c) {
+        const int n = d->ncru[c];
+        if (n < 1) {
+            delete g;
+            return fail_to(g_grad_create_error, GW_ERR_INVALID_ARGUMENT, "cell %d: ncru %d < 1", c, n);
+        }
+        g->ncru[c] = n;
+        g->cru0[c] = g->n_crus;
+        g->n_crus += n;
+        make_cell_static(d->params[d->params_per_cell ? c : 0], n, g->cs[c]);
+        g->blk0[c] = (int)g->blk_cell.size();
+        for (int lo = 0; lo < n; lo += kBlk) {
+            g->blk_cell.push_back(c);
+            g->blk_lo.push_back(lo);
+        }
+    }
+    g->blk0[d->n_cells] = (int)g->blk_cell.size();
+    g->n_blocks = (int)g->blk_cell.size();
+    std::vector<int> rng_cell(d->n_cells);
+    for (int c = 0; c < d->n_cells; ++c) rng_cell[c] = c;
+    const int64_t C = d->n_cells, N = g->n_crus, S = g->ck_every, K = g->n_ck;
+    int rc = 0;
+    auto up = [&](Buf &b, const void *src, size_t bytes) {
+        if (rc) return;
+        rc = g->alloc(b, bytes, "gw_grad_create");
+        if (!rc && src) rc = g->cuda(cudaMemcpy(b.p, src, bytes, cudaMemcpyHostToDevice), "gw_grad_create");
+    };
+    up(g->d_cs, g->cs.data(), sizeof(CellStatic) * C);
+    up(g->d_blk_cell, g->blk_cell.data(), sizeof(int) * g->n_blocks);
+    up(g->d_blk_lo, g->blk_lo.data(), sizeof(int) * g->n_blocks);
+    up(g->d_blk0, g->blk0.data(), sizeof(int) * (C + 1));
+    up(g->d_cru0, g->cru0.data(), sizeof(int64_t) * C);
+    up(g->d_ncru, g->ncru.data(), sizeof(int) * C);
+    up(g->d_rng_cell, rng_cell.data(), sizeof(int) * C);
+    up(g->d_stim, g->stim.data(), sizeof(double) * 4 * C);
+    up(g->x_init, nullptr, sizeof(CruD) * N);
+    up(g->G_init, nullptr, sizeof(double) * kNumGlobals * C);
+    up(g->carry_init, nullptr, sizeof(double) * 4 * C);
+    up(g->sv_init, nullptr, sizeof(double) * kSvCount * C);
+    up(g->x, nullptr, sizeof(CruD) * N);
+    up(g->out, nullptr, sizeof(double) * 4 * N);
+    up(g->G, nullptr, sizeof(double) * kNumGlobals * C);
+    up(g->carry, nullptr, sizeof(double) * 4 * C);
+    up(g->t, nullptr, sizeof(double) * C);
+    up(g->sv, nullptr, sizeof(double) * kSvCount * C);
+    up(g->status, nullptr, sizeof(int) * C);
+    up(g->events, nullptr, sizeof(unsigned long long) * C);
+    up(g->V, nullptr, sizeof(double) * std::max<int64_t>(1, g->n_samples) * C);
+    up(g->regime, nullptr, sizeof(unsigned long long) * C);
+    up(g->ck_x, nullptr, sizeof(CruD) * N * K);
+    up(g->ck_G, nullptr, sizeof(double) * kNumGlobals * C * K);
+    up(g->ck_carry, nullptr, sizeof(double) * 4 * C * K);
+    up(g->ck_t, nullptr, sizeof(double) * C * K);
+    up(g->ck_sv, nullptr, sizeof(double) * kSvCount * C * K);
+    up(g->seg_x, nullptr, sizeof(CruD) * N * S);
+    up(g->seg_G, nullptr, sizeof(double) * kNumGlobals * C * S);
+    up(g->seg_carry, nullptr, sizeof(double) * 4 * C * S);
+    up(g->seg_sv, nullptr, sizeof(double) * kSvCount * C * S);
+    up(g->lam_x, nullptr, sizeof(double) * kLamX * N);
+    up(g->lam_G, nullptr, sizeof(double) * kNumGlobals * C);
+    up(g->lam_cy, nullptr, sizeof(double) * 3 * C);
+    up(g->lam_th, nullptr, sizeof(double) * kTheta * C);
+    up(g->part, nullptr, sizeof(double) * kAdjIn * g->n_blocks);
+    up(g->dLdV, nullptr, sizeof(double) * std::max<int64_t>(1, g->n_samples) * C);
+    if (!rc) rc = g->cuda(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking), "gw_grad_create");
+    if (!rc) rc = g->cuda(cudaEventCreate(&g->ev0), "gw_grad_create");
+    if (!rc) rc = g->cuda(cudaEventCreate(&g->ev1), "gw_grad_create");
+    if (rc) {
+        g_grad_create_error = g->err;
+        delete g;
+        return rc;
+    }
+    g->stats.checkpoint_bytes = (int64_t)(g->ck_x.n + g->ck_G.n + g->ck_carry.n + g->ck_t.n + g->ck_sv.n);
+    g->stats.segment_bytes = (int64_t)(g->seg_x.n + g->seg_G.n + g->seg_carry.n + g->seg_sv.n);
+    *out = g;
+    return GW_OK;
+}
+
+int gw_grad_destroy(gw_grad *g) {
+    if (!g) return GW_OK;
+    cudaSetDevice(g->device);
+    delete g;
+    return GW_OK;
+}
+
+int gw_grad_set_state(gw_grad *g, int cell, const gw_globals *globals, const double *CaSS, const double *CaJSR,
+                      const int32_t *LCC, const int32_t *LCC_inactivation, const int32_t *RyR, const int32_t *ClCh) {
+    if (!g) return GW_ERR_INVALID_ARGUMENT;
+    if (cell < 0 || cell >= g->n_cells) return fail_to(g->err, GW_ERR_INVALID_ARGUMENT, "cell %d of %d", cell, g->n_cells);
+    if (!globals || !CaSS || !CaJSR || !LCC || !LCC_inactivation || !RyR || !ClCh)
+        return fail_to(g->err, GW_ERR_INVALID_ARGUMENT, "null state array");
+    cudaSetDevice(g->device);
+    const int n = g->ncru[cell];
+    std::vector<CruD> xs(n);
+    double clch = 0.0;
+    for (int i = 0; i < n; ++i)
+        if (pack_cru(CaSS, CaJSR, LCC, LCC_inactivation, RyR, ClCh, i, xs[i], clch))
+            return fail_to(g->err, GW_ERR_INVALID_ARGUMENT,
+                           "CRU %d: LCC not in 1..12, LCC_inactivation/ClCh not 0/1 or RyR count out of int8 range", i);
+    double G0[kNumGlobals];
+    std::memcpy(G0, globals, sizeof G0);
+    double cy[4] = {0.0, clch, 0.0, 0.0};
+    ctor_flux_carry(g->cs[cell].p, n, cy[2], cy[3]);
+    double sv0[kSvCount];
+    step_values(g->cs[cell], G0, sv0);
+    int rc;
+    if ((rc = g->cuda(cudaMemcpy(g->x_init.as<CruD>() + g->cru0[cell], xs.data(), sizeof(CruD) * n,
+                                 cudaMemcpyHostToDevice), "gw_grad_set_state")))
+        return rc;
+    if ((rc = g->cuda(cudaMemcpy(g->G_init.as<double>() + kNumGlobals * cell, G0, sizeof G0, cudaMemcpyHostToDevice),
+                      "gw_grad_set_state")))
+        return rc;
+    if ((rc = g->cuda(cudaMemcpy(g->carry_init.as<double>() + 4 * cell, cy, sizeof cy, cudaMemcpyHostToDevice),
+                      "gw_grad_set_state")))
+        return rc;
+    if ((rc = g->cuda(cudaMemcpy(g->sv_init.as<double>() + kSvCount * cell, sv0, sizeof sv0, cudaMemcpyHostToDevice),
+                      "gw_grad_set_state")))
+        return rc;
+    g->have_state[cell] = 1;
+    g->forwarded = false;
+    return GW_OK;
+}
+
+int gw_grad_forward(gw_grad *g, double *V_samples) {
+    if (!g) return GW_ERR_INVALID_ARGUMENT;
+    for (int c = 0; c < g->n_cells; ++c)
+        if (!g->have_state[c]) return fail_to(g->err, GW_ERR_INVALID_ARGUMENT, "cell %d has no state", c);
+    cudaSetDevice(g->device);
+    int rc;
+    if ((rc = g->restore(-1))) return rc;
+    if ((rc = g->cuda(cudaMemsetAsync(g->status.p, 0, g->status.n, g->stream), "gw_grad_forward"))) return rc;
+    if ((rc = g->cuda(cudaMemsetAsync(g->events.p, 0, g->events.n, g->stream), "gw_grad_forward"))) return rc;
+    if ((rc = g->cuda(cudaMemsetAsync(g->regime.p, 0, g->regime.n, g->stream), "gw_grad_forward"))) return rc;
+    if ((rc = g->cuda(cudaMemsetAsync(g->V.p, 0, g->V.n, g->stream), "gw_grad_forward"))) return rc;
+    GradArgs a = g->args();
+    cudaEventRecord(g->ev0, g->stream);
+    for (int64_t s = 0; s < g->n_steps; ++s) {
+        if (s % g->ck_every == 0 && (rc = g->save(s / g->ck_every))) return rc;
+        k_ssa<<<g->n_blocks, kBlk, 0, g->stream>>>(a, s, 0);
+        k_global<<<g->n_cells, kBlk, 0, g->stream>>>(a, s, 0, 0);
+    }
+    cudaEventRecord(g->ev1, g->stream);
+    if ((rc = g->cuda(cudaGetLastError(), "gw_grad_forward launch"))) return rc;
+    if ((rc = g->check_status(g->status, g->n_cells, "gw_grad_forward"))) return rc;
+    float ms = 0.f;
+    if ((rc = g->cuda(cudaEventElapsedTime(&ms, g->ev0, g->ev1), "gw_grad_forward"))) return rc;
+    g->stats.forward_ms = ms;
+    std::vector<unsigned long long> ev(g->n_cells);
+    if ((rc = g->cuda(cudaMemcpy(ev.data(), g->events.p, g->events.n, cudaMemcpyDeviceToHost), "gw_grad_forward")))
+        return rc;
+    g->stats.events = 0;
+    for (auto e : ev) g->stats.events += (int64_t)e;
+    g->G_final.resize((size_t)kNumGlobals * g->n_cells);
+    if ((rc = g->cuda(cudaMemcpy(g->G_final.data(), g->G.p, g->G.n, cudaMemcpyDeviceToHost), "gw_grad_forward")))
+        return rc;
+    if (V_samples && g->n_samples > 0 &&
+        (rc = g->cuda(cudaMemcpy(V_samples, g->V.p, sizeof(double) * g->n_samples * g->n_cells, cudaMemcpyDeviceToHost),
+                      "gw_grad_forward")))
+        return rc;
+    g->forwarded = true;
+    return GW_OK;
+}
+
+int gw_grad_backward(gw_grad *g, const double *dL_dV, double *sens) {
+    if (!g) return GW_ERR_INVALID_ARGUMENT;
+    if (!g->forwarded) return fail_to(g->err, GW_ERR_INVALID_ARGUMENT, "gw_grad_backward before gw_grad_forward");
+    if (!dL_dV || !sens) return fail_to(g->err, GW_ERR_INVALID_ARGUMENT, "null dL_dV or sens");
+    cudaSetDevice(g->device);
+    int rc;
+    if (g->n_samples > 0 &&
+        (rc = g->cuda(cudaMemcpy(g->dLdV.p, dL_dV, sizeof(double) * g->n_samples * g->n_cells, cudaMemcpyHostToDevice),
+                      "gw_grad_backward")))
+        return rc;
+    for (Buf *b : {&g->lam_x, &g->lam_G, &g->lam_cy, &g->lam_th})
+        if ((rc = g->cuda(cudaMemsetAsync(b->p, 0, b->n, g->stream), "gw_grad_backward"))) return rc;
+    GradArgs a = g->args();
+    a.events = nullptr;
+    a.V = nullptr;
+    a.regime = nullptr;
+    a.seg_x = g->seg_x.as<CruD>();
+    a.seg_G = g->seg_G.as<double>();
+    a.seg_carry = g->seg_carry.as<double>();
+    a.seg_sv = g->seg_sv.as<double>();
+    const AdjArgs b = g->adj_args();
+    const int cb = std::min(128, ((g->n_cells + 31) / 32) * 32);
+    const int cg = (g->n_cells + cb - 1) / cb;
+    cudaEventRecord(g->ev0, g->stream);
+    for (int64_t k = g->n_ck - 1; k >= 0; --k) {
+        const int64_t s0 = k * g->ck_every, s1 = std::min(s0 + g->ck_every, g->n_steps);
+        if ((rc = g->restore(k))) return rc;
+        for (int64_t s = s0; s < s1; ++s) {
+            k_ssa<<<g->n_blocks, kBlk, 0, g->stream>>>(a, s, (int)(s - s0));
+            k_global<<<g->n_cells, kBlk, 0, g->stream>>>(a, s, (int)(s - s0), 0);
+        }
+        for (int64_t s = s1 - 1; s >= s0; --s) {
+            k_cru_adj<<<g->n_blocks, kBlk, 0, g->stream>>>(a, b, s, (int)(s - s0));
+            k_global_adj<<<cg, cb, 0, g->stream>>>(a, b, s, (int)(s - s0));
+        }
+    }
+    cudaEventRecord(g->ev1, g->stream);
+    if ((rc = g->cuda(cudaGetLastError(), "gw_grad_backward launch"))) return rc;
+    if ((rc = g->check_status(g->status, g->n_cells, "gw_grad_backward"))) return rc;
+    float ms = 0.f;
+    if ((rc = g->cuda(cudaEventElapsedTime(&ms, g->ev0, g->ev1), "gw_grad_backward"))) return rc;
+    g->stats.backward_ms = ms;
+    return g->cuda(cudaMemcpy(sens, g->lam_th.p, sizeof(double) * kTheta * g->n_cells, cudaMemcpyDeviceToHost),
+                   "gw_grad_backward");
+}
+
+int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_params *params, double *V_samples,
+                   int64_t *regime_steps) {
+    if (!g) return GW_ERR_INVALID_ARGUMENT;
+    if (n_var < 1 || !src_cell || !params || !V_samples)
+        return fail_to(g->err, GW_ERR_INVALID_ARGUMENT, "need n_var >= 1 and non-null src_cell, params, V_samples");
+    for (int v = 0; v < n_var; ++v) {
+        if (src_cell[v] < 0 || src_cell[v] >= g->n_cells)
+            return fail_to(g->err, GW_ERR_INVALID_ARGUMENT, "variant %d: source cell %d of %d", v, src_cell[v], g->n_cells);
+        if (!g->have_state[src_cell[v]])
+            return fail_to(g->err, GW_ERR_INVALID_ARGUMENT, "variant %d: source cell %d has no state", v, src_cell[v]);
+    }
+    cudaSetDevice(g->device);
+    // tables of the source copies (cell v = a copy of src_cell[v]) and the variants
+    std::vector<int> ncru(n_var), bc, bl, rngc(n_var);
+    std::vector<int64_t> c0(n_var);
+    std::vector<CellStatic> vcs(n_var);
+    std::vector<double> stim(4 * (size_t)n_var), vsv(kSvCount * (size_t)n_var);
+    int64_t N = 0;
+    for (int v = 0; v < n_var; ++v) {
+        const int s = src_cell[v];
+        ncru[v] = g->ncru[s];
+        c0[v] = N;
+        N += ncru[v];
+        rngc[v] = s;
+        for (int k = 0; k < 4; ++k) stim[4 * v + k] = g->stim[4 * s + k];
+        make_cell_static(params[v], ncru[v], vcs[v]);
+        for (int lo = 0; lo < ncru[v]; lo += kBlk) {
+            bc.push_back(v);
+            bl.push_back(lo);
+        }
+    }
+    const int nb = (int)bc.size();
+    std::vector<CellStatic> scs(n_var);
+    for (int v = 0; v < n_var; ++v) scs[v] = g->cs[src_cell[v]];
+    // initial states: the source's
+    std::vector<double> G0((size_t)kNumGlobals * g->n_cells), cy0(4 * (size_t)g->n_cells),
+        sv0((size_t)kSvCount * g->n_cells);
+    int rc;
+    if ((rc = g->cuda(cudaMemcpy(G0.data(), g->G_init.p, g->G_init.n, cudaMemcpyDeviceToHost), "gw_grad_replay")))
+        return rc;
+    if ((rc = g->cuda(cudaMemcpy(cy0.data(), g->carry_init.p, g->carry_init.n, cudaMemcpyDeviceToHost), "gw_grad_replay")))
+        return rc;
+    if ((rc = g->cuda(cudaMemcpy(sv0.data(), g->sv_init.p, g->sv_init.n, cudaMemcpyDeviceToHost), "gw_grad_replay")))
+        return rc;
+    std::vector<double> G(kNumGlobals * (size_t)n_var), cy(4 * (size_t)n_var), sv(kSvCount * (size_t)n_var);
+    for (int v = 0; v < n_var; ++v) {
+        const int s = src_cell[v];
+        std::memcpy(&G[kNumGlobals * (size_t)v], &G0[kNumGlobals * (size_t)s], sizeof(double) * kNumGlobals);
+        std::memcpy(&cy[4 * (size_t)v], &cy0[4 * (size_t)s], sizeof(double) * 4);
+        std::memcpy(&sv[kSvCount * (size_t)v], &sv0[kSvCount * (size_t)s], sizeof(double) * kSvCount);
+        step_values(vcs[v], &G0[kNumGlobals * (size_t)s], &vsv[kSvCount * (size_t)v]);
+    }
+    Buf d_cs, d_vcs, d_bc, d_bl, d_c0, d_n, d_rng, d_stim, x, out, vx, vout, dG, dvG, dcy, dvcy, dt_, dvt, dsv, dvsv,
+        dst, dvst, dV, dreg;
+    auto up = [&](Buf &b, const void *src, size_t bytes) {
+        if (rc) return;
+        rc = g->alloc(b, bytes, "gw_grad_replay");
+        if (!rc && src) rc = g->cuda(cudaMemcpy(b.p, src, bytes, cudaMemcpyHostToDevice), "gw_grad_replay");
+    };
+    up(d_cs, scs.data(), sizeof(CellStatic) * n_var);
+    up(d_vcs, vcs.data(), sizeof(CellStatic) * n_var);
+    up(d_bc, bc.data(), sizeof(int) * nb);
+    up(d_bl, bl.data(), sizeof(int) * nb);
+    up(d_c0, c0.data(), sizeof(int64_t) * n_var);
+    up(d_n, ncru.data(), sizeof(int) * n_var);
+    up(d_rng, rngc.data(), sizeof(int) * n_var);
+    up(d_stim, stim.data(), sizeof(double) * 4 * n_var);
+    up(x, nullptr, sizeof(CruD) * N);
+    up(out, nullptr, sizeof(double) * 4 * N);
+    up(vx, nullptr, sizeof(double) * kLamX * N);
+    up(vout, nullptr, sizeof(double) * 4 * N);
+    up(dG, G.data(), sizeof(double) * kNumGlobals * n_var);
+    up(dvG, G.data(), sizeof(double) * kNumGlobals * n_var);
+    up(dcy, cy.data(), sizeof(double) * 4 * n_var);
+    up(dvcy, cy.data(), sizeof(double) * 4 * n_var);
+    up(dt_, nullptr, sizeof(double) * n_var);
+    up(dvt, nullptr, sizeof(double) * n_var);
+    up(dsv, sv.data(), sizeof(double) * kSvCount * n_var);
+    up(dvsv, vsv.data(), sizeof(double) * kSvCount * n_var);
+    up(dst, nullptr, sizeof(int) * n_var);
+    up(dvst, nullptr, sizeof(int) * n_var);
+    up(dV, nullptr, sizeof(double) * std::max<int64_t>(1, g->n_samples) * n_var);
+    up(dreg, nullptr, sizeof(unsigned long long) * n_var);
+    if (rc) return rc;
+    // CRU states of the sources, and the variants' continuous part of them
+    {
+        std::vector<CruD> xs(g->n_crus), xr(N);
+        if ((rc = g->cuda(cudaMemcpy(xs.data(), g->x_init.p, g->x_init.n, cudaMemcpyDeviceToHost), "gw_grad_replay")))
+            return rc;
+        std::vector<double> xv(kLamX * (size_t)N);
+        for (int v = 0; v < n_var; ++v)
+            for (int m = 0; m < ncru[v]; ++m) {
+                const CruD &c = xs[g->cru0[src_cell[v]] + m];
+                xr[c0[v] + m] = c;
+                double *p = &xv[kLamX * (size_t)(c0[v] + m)];
+                for (int j = 0; j < 4; ++j) {
+                    p[j] = c.cass[j];
+                    p[5 + j] = c.jlcc[j];
+                }
+                p[4] = c.cajsr;
+            }
+        if ((rc = g->cuda(cudaMemcpy(x.p, xr.data(), x.n, cudaMemcpyHostToDevice), "gw_grad_replay"))) return rc;
+        if ((rc = g->cuda(cudaMemcpy(vx.p, xv.data(), vx.n, cudaMemcpyHostToDevice), "gw_grad_replay"))) return rc;
+    }
+    GradArgs a{};
+    a.cs = d_cs.as<CellStatic>();
+    a.blk_cell = d_bc.as<int>();
+    a.blk_lo = d_bl.as<int>();
+    a.cru0 = d_c0.as<int64_t>();
+    a.ncru = d_n.as<int>();
+    a.rng_cell = d_rng.as<int>();
+    a.x = x.as<CruD>();
+    a.out = out.as<double>();
+    a.G = dG.as<double>();
+    a.carry = dcy.as<double>();
+    a.t = dt_.as<double>();
+    a.sv = dsv.as<double>();
+    a.stim = d_stim.as<double>();
+    a.status = dst.as<int>();
+    a.n_samples = g->n_samples;
+    a.sample_every = g->sample_every;
+    a.seed = g->seed;
+    a.dt = g->dt;
+    a.event_cap = g->event_cap;
+    a.n_cells = n_var;
+    a.n_crus = N;
+    a.var_cs = d_vcs.as<CellStatic>();
+    a.var_x = vx.as<double>();
+    a.var_out = vout.as<double>();
+    a.var_sv = dvsv.as<double>();
+    // the variants' global step: the same kernel on the variant arrays
+    GradArgs va = a;
+    va.G = dvG.as<double>();
+    va.carry = dvcy.as<double>();
+    va.t = dvt.as<double>();
+    va.status = dvst.as<int>();
+    va.V = dV.as<double>();
+    va.regime = dreg.as<unsigned long long>();
+    cudaEventRecord(g->ev0, g->stream);
+    for (int64_t s = 0; s < g->n_steps; ++s) {
+        k_ssa<<<nb, kBlk, 0, g->stream>>>(a, s, 0);
+        k_global<<<n_var, kBlk, 0, g->stream>>>(a, s, 0, 0);
+        k_global<<<n_var, kBlk, 0, g->stream>>>(va, s, 0, 1);
+    }
+    cudaEventRecord(g->ev1, g->stream);
+    if ((rc = g->cuda(cudaGetLastError(), "gw_grad_replay launch"))) return rc;
+    if ((rc = g->check_status(dst, n_var, "gw_grad_replay (source copy)"))) return rc;
+    if ((rc = g->check_status(dvst, n_var, "gw_grad_replay (variant)"))) return rc;
+    float ms = 0.f;
+    if ((rc = g->cuda(cudaEventElapsedTime(&ms, g->ev0, g->ev1), "gw_grad_replay"))) return rc;
+    g->stats.replay_ms = ms;
+    if (g->n_samples > 0 &&
+        (rc = g->cuda(cudaMemcpy(V_samples, dV.p, sizeof(double) * g->n_samples * n_var, cudaMemcpyDeviceToHost),
+                      "gw_grad_replay")))
+        return rc;
+    if (regime_steps) {
+        std::vector<unsigned long long> r(n_var);
+        if ((rc = g->cuda(cudaMemcpy(r.data(), dreg.p, dreg.n, cudaMemcpyDeviceToHost), "gw_grad_replay"))) return rc;
+        for (int v = 0; v < n_var; ++v) regime_steps[v] = (int64_t)r[v];
+    }
+    return GW_OK;
+}
+
+int gw_grad_regime_steps(gw_grad *g, int64_t *regime_steps) {
+    if (!g || !regime_steps) return GW_ERR_INVALID_ARGUMENT;
+    if (!g->forwarded) return fail_to(g->err, GW_ERR_INVALID_ARGUMENT, "no forward pass yet");
+    cudaSetDevice(g->device);
+    std::vector<unsigned long long> r(g->n_cells);
+    const int rc = g->cuda(cudaMemcpy(r.data(), g->regime.p, g->regime.n, cudaMemcpyDeviceToHost), "gw_grad_regime_steps");
+    if (rc) return rc;
+    for (int c = 0; c < g->n_cells; ++c) regime_steps[c] = (int64_t)r[c];
+    return GW_OK;
+}
+
+int gw_grad_get_globals(gw_grad *g, int cell, gw_globals *out) {
+    if (!g || !out) return GW_ERR_INVALID_ARGUMENT;
+    if (cell < 0 || cell >= g->n_cells) return fail_to(g->err, GW_ERR_INVALID_ARGUMENT, "cell %d of %d", cell, g->n_cells);
+    if (!g->forwarded) return fail_to(g->err, GW_ERR_INVALID_ARGUMENT, "no forward pass yet");
+    std::memcpy(out, &g->G_final[(size_t)kNumGlobals * cell], sizeof(double) * kNumGlobals);
+    return GW_OK;
+}
+
+int gw_grad_get_stats(gw_grad *g, gw_grad_stats *s) {
+    if (!g || !s) return GW_ERR_INVALID_ARGUMENT;
+    *s = g->stats;
+    return GW_OK;
+}
+
+int gw_grad_last_error(gw_grad *g, char *msg, size_t len) {
+    if (!msg || len == 0) return GW_ERR_INVALID_ARGUMENT;
+    const std::string &e = g ? g->err : g_grad_create_error;
+    std::snprintf(msg, len, "%s", e.c_str());
+    return GW_OK;
+}
+
+int gw_grad_check_global(const gw_params *p, int nCRU, const double *G, const double *carry, double Istim, double dt,
+                         const double *lam, double *d, double *lam_G, double *lam_carry, double *lam_theta) {
+    if (!p || nCRU < 1 || !G || !carry || !lam || !d || !lam_G || !lam_carry || !lam_theta)
+        return GW_ERR_INVALID_ARGUMENT;
+    CellStatic C;
+    make_cell_static(*p, nCRU, C);
+    const Carry cy{carry[0], carry[1], carry[2], carry[3]};
+    if (!glob_increment(C, G, cy, Istim, dt, d)) return GW_ERR_NERNST;
+    for (int k = 0; k < kNumGlobals; ++k) lam_G[k] = 0.0;
+    for (int k = 0; k < 3; ++k) lam_carry[k] = 0.0;
+    for (int k = 0; k < kTheta; ++k) lam_theta[k] = 0.0;
+    glob_increment_adj(C, G, cy, dt, lam, lam_G, lam_carry, lam_theta);
+    return GW_OK;
+}
+
+int gw_grad_check_cru(const gw_params *p, int nCRU, const double *x, const int32_t *open, const double *in, int n_sub,
+                      const double *h, const int32_t *ev, const int32_t *sub, const int32_t *onew, const double *lam_x,
+                      const double *lam_carry, double *x_out, double *carry_out, double *lam_x0, double *lam_in,
+                      double *lam_par) {
+    if (!p || nCRU < 1 || !x || !open || !in || n_sub < 1 || !h || !ev || !sub || !onew || !lam_x || !lam_carry ||
+        !x_out || !carry_out || !lam_x0 || !lam_in || !lam_par)
+        return GW_ERR_INVALID_ARGUMENT;
+    for (int k = 0; k < n_sub; ++k)
+        if (ev[k] < EV_NONE || ev[k] > EV_JREL || sub[k] < 0 || sub[k] > 3) return GW_ERR_INVALID_ARGUMENT;
+    CellStatic C;
+    make_cell_static(*p, nCRU, C);
+    const CruPar P = cru_par(C);
+    const CruIn ci{in[0], in[1], in[2], in[3]};
+    int o[4];
+    CruCont s0;
+    for (int j = 0; j < 4; ++j) {
+        o[j] = open[j];
+        s0.c[j] = x[j];
+        s0.L[j] = x[5 + j];
+    }
+    s0.J = x[4];
+    // forward, keeping every sub-step's start state
+    std::vector<CruCont> st(n_sub);
+    CruCont s = s0;
+    cru_begin(s, o, P);
+    double jt = 0.0, jx = 0.0;
+    for (int k = 0; k < n_sub; ++k) {
+        st[k] = s;
+        cru_substep(s, h[k], ci, P, jt, jx);
+        cru_event(s, ev[k], sub[k], onew[k], ci, P);
+    }
+    for (int j = 0; j < 4; ++j) {
+        x_out[j] = s.c[j];
+        x_out[5 + j] = s.L[j];
+    }
+    x_out[4] = s.J;
+    carry_out[0] = jt;
+    carry_out[1] = jx;
+    // reverse
+    CruCont la;
+    for (int j = 0; j < 4; ++j) {
+        la.c[j] = lam_x[j];
+        la.L[j] = lam_x[5 + j];
+        la.rel[j] = 0.0;
+    }
+    la.J = lam_x[4];
+    CruAdjIn ai{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int k = n_sub - 1; k >= 0; --k) {
+        CruCont s1 = st[k];
+        double a1, a2;
+        cru_substep(s1, h[k], ci, P, a1, a2);
+        cru_event_adj(s1, ev[k], sub[k], onew[k], ci, P, la, ai);
+        const bool last = k == n_sub - 1;
+        cru_substep_adj(st[k], h[k], ci, P, last ? lam_carry[0] : 0.0, last ? lam_carry[1] : 0.0, la, ai);
+    }
+    cru_begin_adj(s0, o, P, la, ai);
+    for (int j = 0; j < 4; ++j) {
+        lam_x0[j] = la.c[j];
+        lam_x0[5 + j] = la.L[j];
+    }
+    lam_x0[4] = la.J;
+    lam_in[0] = ai.Cai;
+    lam_in[1] = ai.CaNSR;
+    lam_in[2] = ai.JM;
+    lam_in[3] = ai.JE;
+    lam_par[0] = ai.rRyR_rel;
+    lam_par[1] = ai.CSQN;
+    return GW_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,717 @@
+// gw_adjoint_math.h -- the continuous dynamics of one cell and their hand-written adjoints, for
+// the pathwise gradients of gw_grad_* (gw_adjoint.cu).  Host and device.
+//
+// What is differentiated.  One global step of a cell (GW.tpp:237-272) is
+//   G[s+1] = G[s] + d(G[s], carry[s], Istim[s]; theta)          (GW.tpp:26-212, 163-168, 127-160)
+//   x[s+1] = Phi(x[s]; Cai[s], CaNSR[s], JM(V[s]), JE(V[s]); theta)    per CRU (SSA.tpp:286-310)
+// where carry[s] = the flux sums the SSA of step s-1 left (sum JLCC, sum ClCh, sum Jtr, sum Jxfer;
+// GW.tpp:188-198) and x = a CRU's continuous state (CaSS[4], CaJSR, JLCC[4]).  Conditional on the
+// recorded jump trajectory (jump times, chosen transitions, binomial re-splits), Phi is a chain
+// of explicit Euler sub-steps of CaSS and CaJSR (update_CaSS SSA.tpp:87-99, update_CaJSR
+// SSA.hpp:68-71) whose lengths are the jump times, separated by events that reset JLCC
+// (sample_LCC / sample_new_state, SSA.tpp:103-197, 262-283) or Jrel (sample_RyR, SSA.tpp:200-259).
+// This pathwise estimator ignores the dependence of the jump times and of the chosen transitions
+// on the parameters.  A binomial re-split of a lumped RyR pair changes no open count, so it has no
+// effect on the continuous state.
+//
+// theta: the 8 parameters of the fit, each reported as a relative sensitivity theta_k dL/dtheta_k
+//   PCaL (JLCC_const, through JLCC at LCC openings), GKr (IKr), GKs (IKs), GK1 (IK1),
+//   INaKmax (INaK), Vmax (Vmaxf and Vmaxr scaled together: Jup), rRyR (Jrel), CSQNT (CaJSR buffer).
+#pragma once
+
+#include <cmath>
+
+#include "gw_internal.h"
+
+#ifdef __CUDACC__
+#define GW_HD __host__ __device__ __forceinline__
+#else
+#define GW_HD inline
+#endif
+
+namespace gw {
+namespace adj {
+
+constexpr int kTheta = 8;
+enum Theta { TH_PCAL = 0, TH_GKR = 1, TH_GKS = 2, TH_GK1 = 3, TH_INAK = 4, TH_VMAX = 5, TH_RRYR = 6, TH_CSQNT = 7 };
+constexpr double kFaradayA = 96.5;  // common.hpp:9
+
+// Flux sums of the previous step's SSA (the global step's inputs from the CRUs).
+struct Carry {
+    double jlcc, clch, jtr, jxfer;
+};
+
+GW_HD double sqd(double x) { return x * x; }
+GW_HD double cubed(double x) { return x * x * x; }
+
+// ---------------------------------------------------------------------------------------------
+// The global increment d = G[s+1] - G[s] (update_V_and_concentration_derivatives GW.tpp:171-212,
+// update_gate_derivatives :163-168, update_Kr/Kv_derivatives :127-160 with update_QKr/QKv
+// :26-123), in the reference's formulas and operation order.
+// ---------------------------------------------------------------------------------------------
+
+// Rates of the Kv1.4 / Kv4.3 chains (update_QKv, GW.tpp:65-123): aa, ai, ba, bi.
+GW_HD void kv_rates(const gw_params &p, int ch, double V, double r[4]) {
+    if (ch == 0) {
+        r[0] = p.alphaa0Kv14 * exp(p.aaKv14 * V);
+        r[1] = p.alphai0Kv14 * exp(-p.aiKv14 * V);
+        r[2] = p.betaa0Kv14 * exp(-p.baKv14 * V);
+        r[3] = p.betai0Kv14 * exp(p.biKv14 * V);
+    } else {
+        r[0] = p.alphaa0Kv43 * exp(p.aaKv43 * V);
+        r[1] = p.alphai0Kv43 * exp(-p.aiKv43 * V);
+        r[2] = p.betaa0Kv43 * exp(-p.baKv43 * V);
+        r[3] = p.betai0Kv43 * exp(p.biKv43 * V);
+    }
+}
+
+// The off-diagonal transitions of a 10-state Kv chain: from, to, coefficient, rate (0 aa, 1 ai,
+// 2 ba, 3 bi), as update_QKv builds them; the diagonal is minus the row sum.
+struct KvEdge {
+    int a, b;
+    double coef;
+    int rate;
+};
+GW_HD void kv_edges(const gw_params &p, int ch, KvEdge e[26]) {
+    const double f1 = ch == 0 ? p.f1Kv14 : p.f1Kv43, f2 = ch == 0 ? p.f2Kv14 : p.f2Kv43;
+    const double f3 = ch == 0 ? p.f3Kv14 : p.f3Kv43, f4 = ch == 0 ? p.f4Kv14 : p.f4Kv43;
+    const double b1 = ch == 0 ? p.b1Kv14 : p.b1Kv43, b2 = ch == 0 ? p.b2Kv14 : p.b2Kv43;
+    const double b3 = ch == 0 ? p.b3Kv14 : p.b3Kv43, b4 = ch == 0 ? p.b4Kv14 : p.b4Kv43;
+    int n = 0;
+    auto E = [&](int a, int b, double c, int r) { e[n++] = KvEdge{a, b, c, r}; };
+    E(0, 1, 4.0, 0); E(0, 5, 1.0, 3);
+    E(1, 0, 1.0, 2); E(1, 2, 3.0, 0); E(1, 6, f1, 3);
+    E(2, 1, 2.0, 2); E(2, 3, 2.0, 0); E(2, 7, f2, 3);
+    E(3, 2, 3.0, 2); E(3, 4, 1.0, 0); E(3, 8, f3, 3);
+    E(4, 3, 4.0, 2); E(4, 9, f4, 3);
+    E(5, 6, 4.0 * b1, 0); E(5, 0, 1.0, 1);
+    E(6, 5, 1.0 / f1, 2); E(6, 7, 3.0 * b2 / b1, 0); E(6, 1, 1.0 / b1, 1);
+    E(7, 6, 2.0 * f1 / f2, 2); E(7, 8, 2.0 * b3 / b2, 0); E(7, 2, 1.0 / b2, 1);
+    E(8, 7, 3.0 * f2 / f3, 2); E(8, 9, b4 / b3, 0); E(8, 3, 1.0 / b3, 1);
+    E(9, 8, 4.0 * f3 / f4, 2); E(9, 4, 1.0 / b4, 1);
+}
+
+// Q matrix of one Kv chain in the reference's arithmetic (fill order of update_QKv).
+GW_HD void kv_matrix(const gw_params &p, int ch, double V, double Q[10][10]) {
+    double r[4];
+    kv_rates(p, ch, V, r);
+    const double aa = r[0], ai = r[1], ba = r[2], bi = r[3];
+    const double f1 = ch == 0 ? p.f1Kv14 : p.f1Kv43, f2 = ch == 0 ? p.f2Kv14 : p.f2Kv43;
+    const double f3 = ch == 0 ? p.f3Kv14 : p.f3Kv43, f4 = ch == 0 ? p.f4Kv14 : p.f4Kv43;
+    const double b1 = ch == 0 ? p.b1Kv14 : p.b1Kv43, b2 = ch == 0 ? p.b2Kv14 : p.b2Kv43;
+    const double b3 = ch == 0 ? p.b3Kv14 : p.b3Kv43, b4 = ch == 0 ? p.b4Kv14 : p.b4Kv43;
+    Q[0][1] = 4 * aa; Q[0][5] = bi; Q[0][0] = -(Q[0][1] + Q[0][5]);
+    Q[1][0] = ba; Q[1][2] = 3 * aa; Q[1][6] = f1 * bi; Q[1][1] = -(Q[1][0] + Q[1][2] + Q[1][6]);
+    Q[2][1] = 2 * ba; Q[2][3] = 2 * aa; Q[2][7] = f2 * bi; Q[2][2] = -(Q[2][1] + Q[2][3] + Q[2][7]);
+    Q[3][2] = 3 * ba; Q[3][4] = aa; Q[3][8] = f3 * bi; Q[3][3] = -(Q[3][2] + Q[3][4] + Q[3][8]);
+    Q[4][3] = 4 * ba; Q[4][9] = f4 * bi; Q[4][4] = -(Q[4][3] + Q[4][9]);
+    Q[5][6] = 4 * aa * b1; Q[5][0] = ai; Q[5][5] = -(Q[5][6] + Q[5][0]);
+    Q[6][5] = ba / f1; Q[6][7] = 3 * aa * b2 / b1; Q[6][1] = ai / b1;
+    Q[6][6] = -(Q[6][5] + Q[6][7] + Q[6][1]);
+    Q[7][6] = 2 * ba * f1 / f2; Q[7][8] = 2 * aa * b3 / b2; Q[7][2] = ai / b2;
+    Q[7][7] = -(Q[7][6] + Q[7][8] + Q[7][2]);
+    Q[8][7] = 3 * ba * f2 / f3; Q[8][9] = aa * b4 / b3; Q[8][3] = ai / b3;
+    Q[8][8] = -(Q[8][7] + Q[8][9] + Q[8][3]);
+    Q[9][8] = 4 * ba * f3 / f4; Q[9][4] = ai / b4; Q[9][9] = -(Q[9][8] + Q[9][4]);
+}
+
+// Stencil of update_Kv_derivatives (GW.tpp:136-160): d = dt * (incoming + diagonal) per state.
+GW_HD void kv_deriv(const double Q[10][10], const double *x, double *d, double dt) {
+    d[0] = dt * (Q[1][0] * x[1] + Q[5][0] * x[5] + Q[0][0] * x[0]);
+    d[1] = dt * (Q[0][1] * x[0] + Q[2][1] * x[2] + Q[6][1] * x[6] + Q[1][1] * x[1]);
+    d[2] = dt * (Q[1][2] * x[1] + Q[3][2] * x[3] + Q[7][2] * x[7] + Q[2][2] * x[2]);
+    d[3] = dt * (Q[2][3] * x[2] + Q[4][3] * x[4] + Q[8][3] * x[8] + Q[3][3] * x[3]);
+    d[4] = dt * (Q[3][4] * x[3] + Q[9][4] * x[9] + Q[4][4] * x[4]);
+    d[5] = dt * (Q[6][5] * x[6] + Q[0][5] * x[0] + Q[5][5] * x[5]);
+    d[6] = dt * (Q[5][6] * x[5] + Q[7][6] * x[7] + Q[1][6] * x[1] + Q[6][6] * x[6]);
+    d[7] = dt * (Q[6][7] * x[6] + Q[8][7] * x[8] + Q[2][7] * x[2] + Q[7][7] * x[7]);
+    d[8] = dt * (Q[7][8] * x[7] + Q[9][8] * x[9] + Q[3][8] * x[3] + Q[8][8] * x[8]);
+    d[9] = dt * (Q[8][9] * x[8] + Q[4][9] * x[4] + Q[9][9] * x[9]);
+}
+
+// IKr chain (update_QKr, GW.tpp:26-44): the V-dependent entries Q01 Q10 Q23 Q24 Q32 Q34 Q43 and
+// Q42 = Q32 Q43 Q24 / (Q23 Q34).
+struct KrQ {
+    double q01, q10, q23, q24, q32, q34, q43, q42;
+};
+GW_HD KrQ kr_q(double V) {
+    KrQ q;
+    q.q01 = 0.0069 * exp(0.0272 * V);
+    q.q10 = 0.0227 * exp(-0.0431 * V);
+    q.q23 = 0.0218 * exp(0.0262 * V);
+    q.q24 = 1.29e-5 * exp(2.71e-6 * V);
+    q.q32 = 0.0009 * exp(-0.0269 * V);
+    q.q34 = 0.0622 * exp(0.0120 * V);
+    q.q43 = 0.0059 * exp(-0.0443 * V);
+    q.q42 = q.q32 * q.q43 * q.q24 / (q.q23 * q.q34);
+    return q;
+}
+
+// The gate rate functions of update_gate_derivatives (common.hpp:175-218, GW_utils.hpp:358-362)
+// and their V derivatives.  The h and j rates change form at V = -40 mV (a discontinuity of the
+// reference's model).
+struct Gates {
+    double am, bm, ah, bh, aj, bj, xinf, tinv;
+    double dam, dbm, dah, dbh, daj, dbj, dxinf, dtinv;
+};
+GW_HD Gates gate_rates(double V, bool derivs) {
+    Gates r{};
+    const bool hi = V >= -40.0;
+    {
+        const double w = V + 47.13, E = exp(-0.1 * w);
+        r.am = (V == -47.13) ? 3.2 : 0.32 * w / (1.0 - E);
+        if (derivs) r.dam = (V == -47.13) ? 0.16 : 0.32 * ((1.0 - E) - w * 0.1 * E) / sqd(1.0 - E);
+    }
+    r.bm = 0.08 * exp(-V / 11.0);
+    r.dbm = -r.bm / 11.0;
+    if (hi) {
+        r.ah = 0.0;
+        const double X = exp(-(V + 10.66) / 11.1);
+        r.bh = 1.0 / (0.13 * (1.0 + X));
+        r.dbh = r.bh * X / (11.1 * (1.0 + X));
+        r.aj = 0.0;
+        const double Z = exp(-0.1 * (V + 32.0)), y0 = 0.3 * exp(-2.535e-7 * V);
+        r.bj = y0 / (1.0 + Z);
+        r.dbj = r.bj * (-2.535e-7 + 0.1 * Z / (1.0 + Z));
+    } else {
+        r.ah = 0.135 * exp(-(V + 80.0) / 6.8);
+        r.dah = -r.ah / 6.8;
+        const double e1 = exp(0.079 * V), e2 = exp(0.35 * V);
+        r.bh = 3.56 * e1 + 3.1e5 * e2;
+        r.dbh = 3.56 * 0.079 * e1 + 3.1e5 * 0.35 * e2;
+        const double ea = exp(0.2444 * V), eb = exp(-0.04391 * V);
+        const double P = -127140.0 * ea - 3.474e-5 * eb, Qv = V + 37.78;
+        const double D = 1.0 + exp(0.311 * (V + 79.23));
+        r.aj = P * Qv / D;
+        const double dP = -127140.0 * 0.2444 * ea + 3.474e-5 * 0.04391 * eb, dD = 0.311 * (D - 1.0);
+        r.daj = (dP * Qv + P) / D - P * Qv * dD / sqd(D);
+        const double Z = exp(-0.1378 * (V + 40.14)), y0 = 0.1212 * exp(-0.01052 * V);
+        r.bj = y0 / (1.0 + Z);
+        r.dbj = r.bj * (-0.01052 + 0.1378 * Z / (1.0 + Z));
+    }
+    {
+        const double X = exp(-(V - 24.7) / 13.6);
+        r.xinf = 1.0 / (1.0 + X);
+        r.dxinf = r.xinf * r.xinf * X / 13.6;
+    }
+    {
+        const double u = V - 10.0, E1 = exp(-0.148 * u), E2 = exp(0.0687 * u);
+        r.tinv = 0.0000719 * u / (1.0 - E1) + 0.000131 * u / (E2 - 1.0);
+        r.dtinv = 0.0000719 * ((1.0 - E1) - u * 0.148 * E1) / sqd(1.0 - E1) +
+                  0.000131 * ((E2 - 1.0) - u * 0.0687 * E2) / sqd(E2 - 1.0);
+    }
+    return r;
+}
+
+// The global increment (the same formulas and order as the reference).  Returns false for a
+// non-positive Nernst argument, where the reference exits (common.hpp:72-75).
+GW_HD bool glob_increment(const CellStatic &C, const double *g, const Carry &cy, double Istim, double dt,
+                          double *d) {
+    const gw_params &p = C.p;
+    const double V = g[0], Nai = g[1], Ki = g[2], Cai = g[3], CaNSR = g[4], CaLT = g[5], CaHT = g[6];
+    const double m = g[7], h = g[8], jg = g[9], xKs = g[10];
+    const double *Kr = g + 11, *Kv43 = g + 16, *Kv14 = g + 26;
+    if (!(Nai > 0.0) || !(Ki > 0.0)) return false;
+    const double VF_RT = V * C.F_RT, e = exp(-VF_RT);
+    const double ENa = log(p.Nao / Nai) * C.RT_F / 1.0;
+    const double EK = log(p.Ko / Ki) * C.RT_F / 1.0;
+    const double ECa = log(p.Ko / Ki) * C.RT_F / 2.0;
+    const double INa = p.GNa * cubed(m) * h * jg * (V - ENa);
+    const double INab = p.GNab * (V - ENa);
+    const double e1 = exp(p.eta * VF_RT), e2 = e1 * e;
+    const double INaCa = C.INaCa_const * (e1 * cubed(Nai) * p.Cao - e2 * C.Nao3 * Cai) / (1.0 + p.ksat * e2);
+    const double fNaK = 1.0 / (1.0 + 0.1245 * exp(-0.1 * VF_RT) + 0.0365 * C.sigma * e);
+    const double INaK = C.INaK_const * fNaK / (1.0 + pow(p.KmNai / Nai, 1.5));
+    const double RKr = 1.0 / (1.0 + 1.4945 * exp(0.0446 * V));
+    const double IKr = p.GKr * C.sqrtKo * RKr * Kr[3] * (V - EK) * 0.5;
+    const double EKs = log((p.Ko + 0.01833 * p.Nao) / (Ki + 0.01833 * Nai)) * C.RT_F;
+    const double IKs = p.GKs * sqd(xKs) * (V - EKs);
+    const double mm = C.PKv14_Csc * (kFaradayA * VF_RT) * Kv14[4] / (1 - e);
+    const double IKv14 = mm * ((Ki - p.Ko * e) + 0.02 * (Nai - p.Nao * e)) * 1.0e9;
+    const double IKv43 = p.GKv43 * Kv43[4] * (V - EK);
+    const double Ito1 = IKv14 + IKv43;
+    const double Ito2 = cy.clch * C.Ito2_const * VF_RT * (p.Clcyto * e - p.Clo) / (e - 1.0);
+    const double K1inf = 1.0 / (2.0 + exp(1.5 * (V - EK) * C.F_RT));
+    const double IK1 = p.GK1 * K1inf * C.IK1_const * (V - EK);
+    const double Kp = 1. / (1. + exp((7.488 - V) / 5.98));
+    const double IKp = p.GKp * Kp * (V - EK);
+    const double ICaL = cy.jlcc * C.ICaL_const;
+    const double ICab = p.GCab * (V - ECa);
+    const double IpCa = p.IpCamax * (Cai / (p.KmpCa + Cai));
+    const double fu = pow(Cai / p.Kmf, p.Hf), ru = pow(CaNSR / p.Kmr, p.Hr);
+    const double Jup = (p.Vmaxf * fu - p.Vmaxr * ru) / (1.0 + fu + ru);
+    const double Jtr_tot = cy.jtr * C.CRU_factor, Jxfer_tot = cy.jxfer * C.CRU_factor;
+    const double beta_cyto = 1.0 / (1.0 + C.CMDN_const / sqd(p.KCMDN + Cai));
+    double dLT = p.kLTRPNp * Cai * (p.LTRPNtot - CaLT) - p.kLTRPNm * CaLT;
+    double dHT = p.kHTRPNp * Cai * (p.HTRPNtot - CaHT) - p.kHTRPNm * CaHT;
+    d[1] = -dt * C.CSA_FVcyto * (INa + INab + 3 * INaCa + 3 * INaK);
+    d[2] = -dt * C.CSA_FVcyto * (IKr + IKs + Ito1 + IK1 + IKp - 2 * INaK);
+    d[3] = dt * beta_cyto *
+           (-0.5 * C.CSA_FVcyto * (ICab + IpCa - 2 * INaCa) + C.VSS_Vcyto * Jxfer_tot - Jup - (dLT + dHT));
+    d[4] = dt * (C.Vcyto_VNSR * Jup - C.VJSR_VNSR * Jtr_tot);
+    d[5] = dLT * dt;
+    d[6] = dHT * dt;
+    d[0] = dt * (Istim - (INa + ICaL + IKr + IKs + Ito1 + IK1 + IKp + Ito2 + INaK + INaCa + IpCa + ICab + INab));
+    const Gates gr = gate_rates(V, false);
+    d[7] = dt * (gr.am * (1.0 - m) - gr.bm * m);
+    d[8] = dt * (gr.ah * (1.0 - h) - gr.bh * h);
+    d[9] = dt * (gr.aj * (1.0 - jg) - gr.bj * jg);
+    d[10] = dt * (gr.xinf - xKs) * gr.tinv;
+    const KrQ q = kr_q(V);
+    const double Q00 = -q.q01, Q11 = -(q.q10 + p.Kf), Q22 = -(p.Kb + q.q23 + q.q24), Q33 = -(q.q32 + q.q34);
+    const double Q44 = -(q.q42 + q.q43);
+    d[11] = dt * (q.q10 * Kr[1] + Q00 * Kr[0]);
+    d[12] = dt * (q.q01 * Kr[0] + p.Kb * Kr[2] + Q11 * Kr[1]);
+    d[13] = dt * (p.Kf * Kr[1] + q.q32 * Kr[3] + q.q42 * Kr[4] + Q22 * Kr[2]);
+    d[14] = dt * (q.q23 * Kr[2] + q.q43 * Kr[4] + Q33 * Kr[3]);
+    d[15] = dt * (q.q24 * Kr[2] + q.q34 * Kr[3] + Q44 * Kr[4]);
+    double Q[10][10];
+    kv_matrix(p, 1, V, Q);
+    kv_deriv(Q, Kv43, d + 16, dt);
+    kv_matrix(p, 0, V, Q);
+    kv_deriv(Q, Kv14, d + 26, dt);
+    return true;
+}
+
+// Per-step SSA values of a state (the lane's sv[], gw_internal.h SvIndex) in the reference's
+// arithmetic: update_LCC_rates (GW_utils.tpp:118-186), update_LCC_inactivation_rates
+// (GW_utils.hpp:378-383) and the JLCC factors (GW.tpp:216-221).
+GW_HD void step_values(const CellStatic &C, const double *g, double *sv) {
+    const double V = g[0];
+    const double e = exp(-(V * C.F_RT));
+    const double al = 2.0 * exp(0.012 * (V - 35.0));
+    const double be = 0.0882 * exp(-0.05 * (V - 35.0));
+    const double yinf = 0.4 / (1.0 + exp((V + 12.5) / 5.0)) + 0.6;
+    const double tau = 340.0 / (1.0 + exp((V + 30.0) / 12.0)) + 60.0;
+    const double JE = sqd(1.0 / e);
+    for (int i = 0; i < kSvCount; ++i) sv[i] = 0.0;
+    sv[SV_A4] = 4 * al; sv[SV_A3] = 3 * al; sv[SV_A2] = 2 * al; sv[SV_A1] = al;
+    sv[SV_B1] = be; sv[SV_B2] = 2 * be; sv[SV_B3] = 3 * be; sv[SV_B4] = 4 * be;
+    sv[SV_A4a] = 4 * al * C.a; sv[SV_A3a] = 3 * al * C.a; sv[SV_A2a] = 2 * al * C.a; sv[SV_A1a] = al * C.a;
+    sv[SV_B1bi] = be * C.binv; sv[SV_B2bi] = 2 * be * C.binv; sv[SV_B3bi] = 3 * be * C.binv;
+    sv[SV_B4bi] = 4 * be * C.binv;
+    sv[SV_F] = C.p.f; sv[SV_G] = C.p.g; sv[SV_OM] = C.omega;
+    sv[SV_OMB1] = C.omega_b; sv[SV_OMB2] = C.omega_b2; sv[SV_OMB3] = C.omega_b3; sv[SV_OMB4] = C.omega_b4;
+    sv[SV_F1] = C.p.f1; sv[SV_G1] = C.p.g1;
+    sv[SV_INACT0] = yinf / tau;
+    sv[SV_INACT1] = (1.0 - yinf) / tau;
+    sv[SV_JEXP] = JE;
+    sv[SV_JMUL] = C.JLCC_const * V * C.F_RT / (JE - 1);
+    sv[SV_CAI] = g[3];
+    sv[SV_CANSR] = g[4];
+}
+
+// dJM/dV and dJE/dV of the JLCC factors: JE = exp(2 V F/RT), JM = JLCC_const V F/RT / (JE - 1).
+GW_HD void jlcc_factor_derivs(const CellStatic &C, double V, double JE, double &dJM, double &dJE) {
+    dJE = 2.0 * C.F_RT * JE;
+    dJM = C.JLCC_const * C.F_RT * ((JE - 1.0) - V * dJE) / sqd(JE - 1.0);
+}
+
+// The adjoint of one global increment: with lam = dL/dG[s+1] and G[s+1] = G[s] + d, adds
+// dL/dG[s] (the identity included) to lam_g, dL/d(carry jlcc, jtr, jxfer) to lam_cy[0..2] and the
+// relative sensitivities of GKr, GKs, GK1, INaKmax and Vmax to lam_th.
+GW_HD void glob_increment_adj(const CellStatic &C, const double *g, const Carry &cy, double dt, const double *lam,
+                              double *lam_g, double *lam_cy, double *lam_th) {
+    const gw_params &p = C.p;
+    const double V = g[0], Nai = g[1], Ki = g[2], Cai = g[3], CaNSR = g[4], CaLT = g[5], CaHT = g[6];
+    const double m = g[7], h = g[8], jg = g[9], xKs = g[10];
+    const double *Kr = g + 11, *Kv43 = g + 16, *Kv14 = g + 26;
+    for (int i = 0; i < kNumGlobals; ++i) lam_g[i] += lam[i];
+    // forward values
+    const double F_RT = C.F_RT, RT_F = C.RT_F;
+    const double VF_RT = V * F_RT, e = exp(-VF_RT);
+    const double ENa = log(p.Nao / Nai) * RT_F, EK = log(p.Ko / Ki) * RT_F, ECa = log(p.Ko / Ki) * RT_F / 2.0;
+    const double m3hj = cubed(m) * h * jg;
+    const double e1 = exp(p.eta * VF_RT), e2 = e1 * e;
+    const double numNC = e1 * cubed(Nai) * p.Cao - e2 * C.Nao3 * Cai, denNC = 1.0 + p.ksat * e2;
+    const double INaCa = C.INaCa_const * numNC / denNC;
+    const double E1k = exp(-0.1 * VF_RT);
+    const double fNaK = 1.0 / (1.0 + 0.1245 * E1k + 0.0365 * C.sigma * e);
+    const double qNaK = 1.0 + pow(p.KmNai / Nai, 1.5);
+    const double INaK = C.INaK_const * fNaK / qNaK;
+    const double ERk = exp(0.0446 * V), RKr = 1.0 / (1.0 + 1.4945 * ERk);
+    const double IKr = p.GKr * C.sqrtKo * RKr * Kr[3] * (V - EK) * 0.5;
+    const double sKs = Ki + 0.01833 * Nai;
+    const double EKs = log((p.Ko + 0.01833 * p.Nao) / sKs) * RT_F;
+    const double IKs = p.GKs * sqd(xKs) * (V - EKs);
+    const double P14 = C.PKv14_Csc * kFaradayA;
+    const double A14 = (Ki - p.Ko * e) + 0.02 * (Nai - p.Nao * e);
+    const double mm = P14 * VF_RT * Kv14[4] / (1 - e);
+    const double uK1 = V - EK, EK1 = exp(1.5 * uK1 * F_RT), K1inf = 1.0 / (2.0 + EK1);
+    const double IK1 = p.GK1 * K1inf * C.IK1_const * uK1;
+    const double EKp = exp((7.488 - V) / 5.98), Kp = 1. / (1. + EKp);
+    const double fu = pow(Cai / p.Kmf, p.Hf), ru = pow(CaNSR / p.Kmr, p.Hr), den = 1.0 + fu + ru;
+    const double Jup = (p.Vmaxf * fu - p.Vmaxr * ru) / den;
+    const double Jxfer_tot = cy.jxfer * C.CRU_factor;
+    const double beta = 1.0 / (1.0 + C.CMDN_const / sqd(p.KCMDN + Cai));
+    const double dLT = p.kLTRPNp * Cai * (p.LTRPNtot - CaLT) - p.kLTRPNm * CaLT;
+    const double dHT = p.kHTRPNp * Cai * (p.HTRPNtot - CaHT) - p.kHTRPNm * CaHT;
+    const double ICab = p.GCab * (V - ECa), IpCa = p.IpCamax * (Cai / (p.KmpCa + Cai));
+    const double Q3 = -0.5 * C.CSA_FVcyto * (ICab + IpCa - 2 * INaCa) + C.VSS_Vcyto * Jxfer_tot - Jup - (dLT + dHT);
+    const double CSA = C.CSA_FVcyto;
+
+    // adjoints of the currents
+    double lINa = 0, lINab = 0, lINaCa = 0, lINaK = 0, lIKr = 0, lIKs = 0, lIto1 = 0, lIK1 = 0, lIKp = 0;
+    double lIto2 = 0, lICaL = 0, lICab = 0, lIpCa = 0, lJup = 0, lJtr = 0, lJxfer = 0, lbeta = 0, ldLT = 0, ldHT = 0;
+    // d[1], d[2]
+    lINa += -dt * CSA * lam[1]; lINab += -dt * CSA * lam[1]; lINaCa += -3 * dt * CSA * lam[1];
+    lINaK += -3 * dt * CSA * lam[1];
+    lIKr += -dt * CSA * lam[2]; lIKs += -dt * CSA * lam[2]; lIto1 += -dt * CSA * lam[2];
+    lIK1 += -dt * CSA * lam[2]; lIKp += -dt * CSA * lam[2]; lINaK += 2 * dt * CSA * lam[2];
+    // d[3]
+    lbeta += lam[3] * dt * Q3;
+    {
+        const double lQ = lam[3] * dt * beta;
+        lICab += -0.5 * CSA * lQ; lIpCa += -0.5 * CSA * lQ; lINaCa += CSA * lQ;
+        lJxfer += C.VSS_Vcyto * lQ; lJup -= lQ; ldLT -= lQ; ldHT -= lQ;
+    }
+    // d[4], d[5], d[6]
+    lJup += dt * C.Vcyto_VNSR * lam[4];
+    lJtr += -dt * C.VJSR_VNSR * lam[4];
+    ldLT += dt * lam[5];
+    ldHT += dt * lam[6];
+    // d[0]
+    {
+        const double l0 = -dt * lam[0];
+        lINa += l0; lICaL += l0; lIKr += l0; lIKs += l0; lIto1 += l0; lIK1 += l0; lIKp += l0;
+        lIto2 += l0; lINaK += l0; lINaCa += l0; lIpCa += l0; lICab += l0; lINab += l0;
+    }
+    // state adjoints from the currents
+    double lV = 0, lNai = 0, lKi = 0, lCai = 0, lCaNSR = 0, lVF = 0, le = 0, lENa = 0, lEK = 0, lECa = 0;
+    // INa, INab
+    lam_g[7] += lINa * 3 * p.GNa * sqd(m) * h * jg * (V - ENa);
+    lam_g[8] += lINa * p.GNa * cubed(m) * jg * (V - ENa);
+    lam_g[9] += lINa * p.GNa * cubed(m) * h * (V - ENa);
+    lV += lINa * p.GNa * m3hj;
+    lENa -= lINa * p.GNa * m3hj;
+    lV += lINab * p.GNab;
+    lENa -= lINab * p.GNab;
+    // INaCa
+    {
+        const double lnum = lINaCa * C.INaCa_const / denNC;
+        const double lden = -lINaCa * INaCa / denNC;
+        double le1 = lnum * cubed(Nai) * p.Cao;
+        lNai += lnum * 3 * e1 * sqd(Nai) * p.Cao;
+        double le2 = -lnum * C.Nao3 * Cai + lden * p.ksat;
+        lCai += -lnum * e2 * C.Nao3;
+        le1 += le2 * e;
+        le += le2 * e1;
+        lVF += le1 * p.eta * e1;
+    }
+    // INaK
+    {
+        const double lf = lINaK * C.INaK_const / qNaK;
+        const double lq = -lINaK * INaK / qNaK;
+        lNai += lq * (-1.5 * pow(p.KmNai / Nai, 1.5) / Nai);
+        const double lD = -lf * sqd(fNaK);
+        lVF += lD * 0.1245 * (-0.1) * E1k;
+        le += lD * 0.0365 * C.sigma;
+        lam_th[TH_INAK] += lINaK * INaK;
+    }
+    // IKr
+    {
+        const double k = p.GKr * C.sqrtKo * 0.5;
+        lam_g[14] += lIKr * k * RKr * (V - EK);
+        const double dRKr = -sqd(RKr) * 1.4945 * 0.0446 * ERk;
+        lV += lIKr * k * Kr[3] * (RKr + (V - EK) * dRKr);
+        lEK -= lIKr * k * RKr * Kr[3];
+        lam_th[TH_GKR] += lIKr * IKr;
+    }
+    // IKs
+    {
+        lam_g[10] += lIKs * 2 * p.GKs * xKs * (V - EKs);
+        lV += lIKs * p.GKs * sqd(xKs);
+        const double lEKs = -lIKs * p.GKs * sqd(xKs);
+        lKi += lEKs * (-RT_F / sKs);
+        lNai += lEKs * (-0.01833 * RT_F / sKs);
+        lam_th[TH_GKS] += lIKs * IKs;
+    }
+    // Ito1 = IKv14 + IKv43
+    {
+        const double lI14 = lIto1, lI43 = lIto1;
+        const double lmm = lI14 * A14 * 1.0e9, lA = lI14 * mm * 1.0e9;
+        lKi += lA;
+        lNai += 0.02 * lA;
+        le += lA * (-p.Ko - 0.02 * p.Nao);
+        lam_g[30] += lmm * P14 * VF_RT / (1 - e);
+        lVF += lmm * P14 * Kv14[4] / (1 - e);
+        le += lmm * P14 * VF_RT * Kv14[4] / sqd(1 - e);
+        lam_g[20] += lI43 * p.GKv43 * (V - EK);
+        lV += lI43 * p.GKv43 * Kv43[4];
+        lEK -= lI43 * p.GKv43 * Kv43[4];
+    }
+    // Ito2 = clch Ito2_const VF (Clcyto e - Clo) / (e - 1)
+    {
+        const double B = (p.Clcyto * e - p.Clo) / (e - 1.0);
+        const double k = cy.clch * C.Ito2_const;
+        lVF += lIto2 * k * B;
+        le += lIto2 * k * VF_RT * (p.Clo - p.Clcyto) / sqd(e - 1.0);
+    }
+    // IK1
+    {
+        const double dK1 = -sqd(K1inf) * 1.5 * F_RT * EK1;
+        const double dIdu = p.GK1 * C.IK1_const * (K1inf + uK1 * dK1);
+        lV += lIK1 * dIdu;
+        lEK -= lIK1 * dIdu;
+        lam_th[TH_GK1] += lIK1 * IK1;
+    }
+    // IKp
+    {
+        const double dKp = sqd(Kp) * EKp / 5.98;
+        lV += lIKp * p.GKp * (Kp + (V - EK) * dKp);
+        lEK -= lIKp * p.GKp * Kp;
+    }
+    // ICaL, ICab, IpCa
+    lam_cy[0] += lICaL * C.ICaL_const;
+    lV += lICab * p.GCab;
+    lECa -= lICab * p.GCab;
+    lCai += lIpCa * p.IpCamax * p.KmpCa / sqd(p.KmpCa + Cai);
+    // Jup
+    {
+        const double dJdf = (p.Vmaxf * (1.0 + ru) + p.Vmaxr * ru) / sqd(den);
+        const double dJdr = -(p.Vmaxr * (1.0 + fu) + p.Vmaxf * fu) / sqd(den);
+        lCai += lJup * dJdf * p.Hf * fu / Cai;
+        lCaNSR += lJup * dJdr * p.Hr * ru / CaNSR;
+        lam_th[TH_VMAX] += lJup * Jup;
+    }
+    lam_cy[1] += lJtr * C.CRU_factor;
+    lam_cy[2] += lJxfer * C.CRU_factor;
+    // beta_cyto, troponin
+    lCai += lbeta * sqd(beta) * 2.0 * C.CMDN_const / cubed(p.KCMDN + Cai);
+    lCai += ldLT * p.kLTRPNp * (p.LTRPNtot - CaLT) + ldHT * p.kHTRPNp * (p.HTRPNtot - CaHT);
+    lam_g[5] += ldLT * (-p.kLTRPNp * Cai - p.kLTRPNm);
+    lam_g[6] += ldHT * (-p.kHTRPNp * Cai - p.kHTRPNm);
+    // Nernst potentials
+    lNai += lENa * (-RT_F / Nai);
+    lKi += lEK * (-RT_F / Ki) + lECa * (-RT_F / (2.0 * Ki));
+    // gates
+    {
+        const Gates gr = gate_rates(V, true);
+        lam_g[7] += lam[7] * dt * (-gr.am - gr.bm);
+        lam_g[8] += lam[8] * dt * (-gr.ah - gr.bh);
+        lam_g[9] += lam[9] * dt * (-gr.aj - gr.bj);
+        lam_g[10] += -lam[10] * dt * gr.tinv;
+        lV += lam[7] * dt * (gr.dam * (1.0 - m) - gr.dbm * m);
+        lV += lam[8] * dt * (gr.dah * (1.0 - h) - gr.dbh * h);
+        lV += lam[9] * dt * (gr.daj * (1.0 - jg) - gr.dbj * jg);
+        lV += lam[10] * dt * (gr.dxinf * gr.tinv + (gr.xinf - xKs) * gr.dtinv);
+    }
+    // IKr chain: d_k = dt (sum over edges a->b of q x_a into b, minus out of a)
+    {
+        const KrQ q = kr_q(V);
+        const double *l = lam + 11;
+        double *lx = lam_g + 11;
+        double lq01 = 0, lq10 = 0, lq23 = 0, lq24 = 0, lq32 = 0, lq34 = 0, lq43 = 0, lq42 = 0;
+        auto edge = [&](int a, int b, double qv, double *lqv) {
+            const double w = dt * (l[b] - l[a]);
+            lx[a] += qv * w;
+            if (lqv) *lqv += Kr[a] * w;
+        };
+        edge(0, 1, q.q01, &lq01);
+        edge(1, 0, q.q10, &lq10);
+        edge(1, 2, p.Kf, nullptr);
+        edge(2, 1, p.Kb, nullptr);
+        edge(2, 3, q.q23, &lq23);
+        edge(2, 4, q.q24, &lq24);
+        edge(3, 2, q.q32, &lq32);
+        edge(3, 4, q.q34, &lq34);
+        edge(4, 3, q.q43, &lq43);
+        edge(4, 2, q.q42, &lq42);
+        // q42 = q32 q43 q24 / (q23 q34)
+        lq32 += lq42 * q.q42 / q.q32;
+        lq43 += lq42 * q.q42 / q.q43;
+        lq24 += lq42 * q.q42 / q.q24;
+        lq23 -= lq42 * q.q42 / q.q23;
+        lq34 -= lq42 * q.q42 / q.q34;
+        lV += lq01 * 0.0272 * q.q01 + lq10 * (-0.0431) * q.q10 + lq23 * 0.0262 * q.q23 + lq24 * 2.71e-6 * q.q24 +
+              lq32 * (-0.0269) * q.q32 + lq34 * 0.0120 * q.q34 + lq43 * (-0.0443) * q.q43;
+    }
+    // Kv chains
+    for (int ch = 0; ch < 2; ++ch) {
+        const double *x = ch == 0 ? Kv14 : Kv43;
+        const double *l = lam + (ch == 0 ? 26 : 16);
+        double *lx = lam_g + (ch == 0 ? 26 : 16);
+        double r[4], lr[4] = {0, 0, 0, 0};
+        kv_rates(p, ch, V, r);
+        KvEdge E[26];
+        kv_edges(p, ch, E);
+        for (int k = 0; k < 26; ++k) {
+            const double qv = E[k].coef * r[E[k].rate];
+            const double w = dt * (l[E[k].b] - l[E[k].a]);
+            lx[E[k].a] += qv * w;
+            lr[E[k].rate] += E[k].coef * x[E[k].a] * w;
+        }
+        const double ka = ch == 0 ? p.aaKv14 : p.aaKv43, ki = ch == 0 ? p.aiKv14 : p.aiKv43;
+        const double kb = ch == 0 ? p.baKv14 : p.baKv43, kbi = ch == 0 ? p.biKv14 : p.biKv43;
+        lV += lr[0] * ka * r[0] - lr[1] * ki * r[1] - lr[2] * kb * r[2] + lr[3] * kbi * r[3];
+    }
+    // VF_RT and e = exp(-VF_RT) back to V
+    lV += F_RT * lVF - F_RT * e * le;
+    lam_g[0] += lV;
+    lam_g[1] += lNai;
+    lam_g[2] += lKi;
+    lam_g[3] += lCai;
+    lam_g[4] += lCaNSR;
+}
+
+// ---------------------------------------------------------------------------------------------
+// One CRU over one global step, given its jump trajectory: sub-steps of lengths h_k separated by
+// events.  The arithmetic of the sub-step and of the events is the FP64 SSA lane's
+// (SsaLane<double, true> in gw_kernel.cuh, the reference's order), so that a replay of the
+// trajectory at the recording's parameters gives the recording's values bit for bit.
+// ---------------------------------------------------------------------------------------------
+
+// Continuous state of a CRU within a step.
+struct CruCont {
+    double c[4], J, L[4], rel[4];
+};
+
+// Per-step inputs of a CRU from its cell, and the parameters it uses.
+struct CruIn {
+    double Cai, CaNSR, JM, JE;
+};
+struct CruPar {
+    double rRyR, rtr, riss, rxfer, KBSR, KBSL, BSR_const, BSL_const, KCSQN, CSQN_const, VSS_VJSR, Cao_scaled;
+};
+GW_HD CruPar cru_par(const CellStatic &C) {
+    return CruPar{C.p.rRyR, C.p.rtr, C.p.riss, C.p.rxfer, C.p.KBSR, C.p.KBSL, C.BSR_const, C.BSL_const,
+                  C.p.KCSQN, C.CSQN_const, C.VSS_VJSR, C.Cao_scaled};
+}
+
+// Event effects on the continuous state (sample_new_state, SSA.tpp:262-283): a subunit starting
+// to conduct (LCC open, voltage gate not inactivated) sets JLCC from CaSS; one that stops sets
+// it to 0; a RyR transition resets Jrel with the new open count; other events change nothing
+// continuous but end a sub-step.
+enum CruEvent { EV_NONE = 0, EV_JLCC_SET = 1, EV_JLCC_ZERO = 2, EV_JREL = 3 };
+
+// Jrel at the start of the step from the open counts o (copy_from_CRUState, SSA.tpp:10-33).
+GW_HD void cru_begin(CruCont &s, const int o[4], const CruPar &P) {
+    for (int j = 0; j < 4; ++j) s.rel[j] = P.rRyR * (double)o[j] * (s.J - s.c[j]);
+}
+
+// One sub-step of length h (update_fluxes, update_CaSS, update_CaJSR); returns the fluxes taken at
+// its start (the step's carry when it is the last one).
+GW_HD void cru_substep(CruCont &s, double h, const CruIn &in, const CruPar &P, double &jtr, double &jxfer_sum) {
+    double jiss[4], jxf[4];
+    jtr = P.rtr * (in.CaNSR - s.J);
+    jiss[0] = P.riss * (s.c[1] + s.c[3] - 2.0 * s.c[0]);
+    jiss[1] = P.riss * (s.c[2] + s.c[0] - 2.0 * s.c[1]);
+    jiss[2] = P.riss * (s.c[3] + s.c[1] - 2.0 * s.c[2]);
+    jiss[3] = P.riss * (s.c[0] + s.c[2] - 2.0 * s.c[3]);
+    for (int j = 0; j < 4; ++j) jxf[j] = P.rxfer * (s.c[j] - in.Cai);
+    double cn[4];
+    for (int j = 0; j < 4; ++j) {
+        const double x = s.c[j];
+        const double beta = 1.0 / (1.0 + (P.BSR_const / ((P.KBSR + x) * (P.KBSR + x))) +
+                                   (P.BSL_const / ((P.KBSL + x) * (P.KBSL + x))));
+        cn[j] = x + h * (s.L[j] + s.rel[j] - jxf[j] + jiss[j]) * beta;
+    }
+    {
+        const double x = s.J;
+        const double beta = 1.0 / (1.0 + P.CSQN_const / ((P.KCSQN + x) * (P.KCSQN + x)));
+        s.J += h * beta * (jtr - P.VSS_VJSR * (s.rel[0] + s.rel[1] + s.rel[2] + s.rel[3]));
+    }
+    for (int j = 0; j < 4; ++j) s.c[j] = cn[j];
+    jxfer_sum = jxf[0] + jxf[1] + jxf[2] + jxf[3];
+}
+
+GW_HD void cru_event(CruCont &s, int ev, int j, int onew, const CruIn &in, const CruPar &P) {
+    if (ev == EV_JLCC_SET)
+        s.L[j] = in.JM * (P.Cao_scaled - in.JE * s.c[j]);
+    else if (ev == EV_JLCC_ZERO)
+        s.L[j] = 0.0;
+    else if (ev == EV_JREL)
+        s.rel[j] = P.rRyR * (double)onew * (s.J - s.c[j]);
+}
+
+// Adjoint accumulators of a CRU's per-step inputs and parameters.
+struct CruAdjIn {
+    double Cai, CaNSR, JM, JE, rRyR_rel, CSQN;  // rRyR_rel: rRyR dL/drRyR; CSQN: dL/dCSQN_const
+};
+
+// Adjoint of cru_event; s is the state the event acts on (after the sub-step; an event changes
+// neither CaSS nor CaJSR).  la: adjoints of the state after the event; on return, before it.
+GW_HD void cru_event_adj(const CruCont &s, int ev, int j, int onew, const CruIn &in, const CruPar &P, CruCont &la,
+                         CruAdjIn &ai) {
+    if (ev == EV_JLCC_SET) {
+        const double l = la.L[j];
+        ai.JM += l * (P.Cao_scaled - in.JE * s.c[j]);
+        ai.JE += l * (-in.JM * s.c[j]);
+        la.c[j] += l * (-in.JM * in.JE);
+        la.L[j] = 0.0;
+    } else if (ev == EV_JLCC_ZERO) {
+        la.L[j] = 0.0;
+    } else if (ev == EV_JREL) {
+        const double l = la.rel[j], k = P.rRyR * (double)onew;
+        ai.rRyR_rel += l * k * (s.J - s.c[j]);
+        la.J += l * k;
+        la.c[j] -= l * k;
+        la.rel[j] = 0.0;
+    }
+}
+
+// Adjoint of cru_substep from its start state s0 (the state before the sub-step).  la holds the
+// adjoints after the sub-step (c, J, L, rel); l_jtr / l_jxfer are the adjoints of the returned
+// fluxes (non-zero for the step's last sub-step, whose fluxes are the carry).
+GW_HD void cru_substep_adj(const CruCont &s0, double h, const CruIn &in, const CruPar &P, double l_jtr,
+                           double l_jxfer, CruCont &la, CruAdjIn &ai) {
+    double jiss[4], jxf[4];
+    const double jtr = P.rtr * (in.CaNSR - s0.J);
+    jiss[0] = P.riss * (s0.c[1] + s0.c[3] - 2.0 * s0.c[0]);
+    jiss[1] = P.riss * (s0.c[2] + s0.c[0] - 2.0 * s0.c[1]);
+    jiss[2] = P.riss * (s0.c[3] + s0.c[1] - 2.0 * s0.c[2]);
+    jiss[3] = P.riss * (s0.c[0] + s0.c[2] - 2.0 * s0.c[3]);
+    for (int j = 0; j < 4; ++j) jxf[j] = P.rxfer * (s0.c[j] - in.Cai);
+    double lc[4], liss[4], lxf[4];
+    for (int j = 0; j < 4; ++j) {
+        const double x = s0.c[j];
+        const double uR = P.KBSR + x, uL = P.KBSL + x;
+        const double beta = 1.0 / (1.0 + P.BSR_const / (uR * uR) + P.BSL_const / (uL * uL));
+        const double dbeta = 2.0 * beta * beta * (P.BSR_const / (uR * uR * uR) + P.BSL_const / (uL * uL * uL));
+        const double A = s0.L[j] + s0.rel[j] - jxf[j] + jiss[j];
+        const double lcn = la.c[j];
+        const double lA = lcn * h * beta;
+        lc[j] = lcn + lcn * h * A * dbeta;
+        la.L[j] += lA;
+        la.rel[j] += lA;
+        lxf[j] = -lA + l_jxfer;
+        liss[j] = lA;
+    }
+    double lJ, ljtr = l_jtr;
+    {
+        const double x = s0.J, u = P.KCSQN + x;
+        const double beta = 1.0 / (1.0 + P.CSQN_const / (u * u));
+        const double G = jtr - P.VSS_VJSR * (s0.rel[0] + s0.rel[1] + s0.rel[2] + s0.rel[3]);
+        const double lJn = la.J;
+        lJ = lJn + lJn * h * G * (2.0 * beta * beta * P.CSQN_const / (u * u * u));
+        ljtr += lJn * h * beta;
+        for (int j = 0; j < 4; ++j) la.rel[j] -= lJn * h * beta * P.VSS_VJSR;
+        ai.CSQN += lJn * h * G * (-beta * beta / (u * u));
+    }
+    for (int j = 0; j < 4; ++j) {
+        lc[j] += P.rxfer * lxf[j];
+        ai.Cai -= P.rxfer * lxf[j];
+    }
+    lc[1] += P.riss * liss[0]; lc[3] += P.riss * liss[0]; lc[0] -= 2.0 * P.riss * liss[0];
+    lc[2] += P.riss * liss[1]; lc[0] += P.riss * liss[1]; lc[1] -= 2.0 * P.riss * liss[1];
+    lc[3] += P.riss * liss[2]; lc[1] += P.riss * liss[2]; lc[2] -= 2.0 * P.riss * liss[2];
+    lc[0] += P.riss * liss[3]; lc[2] += P.riss * liss[3]; lc[3] -= 2.0 * P.riss * liss[3];
+    ai.CaNSR += P.rtr * ljtr;
+    lJ -= P.rtr * ljtr;
+    for (int j = 0; j < 4; ++j) la.c[j] = lc[j];
+    la.J = lJ;
+}
+
+// Adjoint of cru_begin: the step's Jrel from its start state.
+GW_HD void cru_begin_adj(const CruCont &s0, const int o[4], const CruPar &P, CruCont &la, CruAdjIn &ai) {
+    for (int j = 0; j < 4; ++j) {
+        const double l = la.rel[j], k = P.rRyR * (double)o[j];
+        ai.rRyR_rel += l * k * (s0.J - s0.c[j]);
+        la.J += l * k;
+        la.c[j] -= l * k;
+        la.rel[j] = 0.0;
+    }
+}
+
+}  // namespace adj
+}  // namespace gw

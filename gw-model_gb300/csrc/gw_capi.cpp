@@ -115,8 +115,10 @@ int fail(gw_ctx *c, int code, const char *fmt, ...) {
                         "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);  \
     } while (0)
 
+}  // namespace
+
 // Constants ctor (GW_utils.tpp:67-116), FP64, reference expression order.
-void make_static(const gw_params &p, int nCRU, CellStatic &c) {
+void gw::make_cell_static(const gw_params &p, int nCRU, CellStatic &c) {
     std::memset(&c, 0, sizeof c);
     c.p = p;
     c.RT_F = kGasConst * p.T / kFaraday;
@@ -157,11 +159,19 @@ void make_static(const gw_params &p, int nCRU, CellStatic &c) {
     c.CMDN_const = p.KCMDN * p.CMDNT;
 }
 
-int byte_of(int v) { return v & 0xFF; }
+// Device allocation for the other translation units (gw_adjoint.cu), counted like DevBuf's.
+int gw::dev_alloc(void **p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) return (int)cudaSuccess;
+    g_device_allocs.fetch_add(1, std::memory_order_relaxed);
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) e = cudaMemset(*p, 0, bytes);
+    return (int)e;
+}
 
 // Flux carry of the reference's ctor (GW.hpp:73-74): initialise_Jxfer / initialise_Jtr from the
 // default GlobalState and the ctor's CRU constants, summed over CRUs in order.
-void ctor_carry(const gw_params &p, int n, double &sum_jtr, double &sum_jxfer) {
+void gw::ctor_flux_carry(const gw_params &p, int n, double &sum_jtr, double &sum_jxfer) {
     gw_globals g;
     gw_globals_default(&g);
     const double jx = p.rxfer * (1.45370e-4 - g.Cai);
@@ -171,6 +181,10 @@ void ctor_carry(const gw_params &p, int n, double &sum_jtr, double &sum_jxfer) {
     for (int i = 0; i < n; ++i) sum_jtr += jt;
     for (int i = 0; i < 4 * n; ++i) sum_jxfer += jx;
 }
+
+namespace {
+
+int byte_of(int v) { return v & 0xFF; }
 
 // Launch shape: cluster size C, CRU tile per CTA and SSA warps per CTA.  A cell needs
 // ceil(ncru / tile) <= C CTAs.
@@ -489,7 +503,7 @@ int gw_create(const gw_ensemble_desc *d, gw_ctx **out) {
     }
     for (int i = 0; i < c->n_cells; ++i) {
         const gw_params &p = d->params[d->params_per_cell ? i : 0];
-        make_static(p, c->ncru[i], c->cs[i]);
+        make_cell_static(p, c->ncru[i], c->cs[i]);
         if (!ode_program_build(c->cs[i], pow_fast, i == 0 ? &c->prog : nullptr, c->cs[i].ode_consts)) {
             g_create_error = "global-step program does not fit its tables";
             delete c;
@@ -500,7 +514,7 @@ int gw_create(const gw_ensemble_desc *d, gw_ctx **out) {
         gw_globals g;
         gw_globals_default(&g);
         std::memcpy(y.g, &g, sizeof g);
-        ctor_carry(p, c->ncru[i], y.sum_jtr, y.sum_jxfer);
+        ctor_flux_carry(p, c->ncru[i], y.sum_jtr, y.sum_jxfer);
     }
     auto alloc_all = [&]() -> int {
         CK(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
@@ -1290,7 +1304,7 @@ int gw_global_step_host(const gw_params *p, int nCRU, double *g, const double *s
                         double dt, double *sv) {
     if (!p || nCRU <= 0 || !g || !sums) return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "bad arguments");
     CellStatic cs;
-    make_static(*p, nCRU, cs);
+    make_cell_static(*p, nCRU, cs);
     static thread_local OdeProgram prog;
     static thread_local double consts[kOdeMaxConsts];
     const bool fast = p->Hf == 0.75 && p->Hr == 0.75;

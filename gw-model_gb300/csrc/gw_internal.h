@@ -138,6 +138,15 @@ struct LaunchShape {
     size_t smem;      // dynamic shared memory per CTA
 };
 
+// The reference's Constants ctor (GW_utils.tpp:67-116) into a cell block (gw_capi.cpp); the
+// global-step program's constants (ode_consts) are left zero.
+void make_cell_static(const gw_params &p, int nCRU, CellStatic &c);
+// The flux carry (sum Jtr, sum Jxfer) of the reference's ctor for n CRUs (GW.hpp:73-74).
+void ctor_flux_carry(const gw_params &p, int n, double &sum_jtr, double &sum_jxfer);
+// cudaMalloc of `bytes` zeroed bytes, counted in gw_stats.device_allocs (gw_capi.cpp); returns a
+// cudaError_t.
+int dev_alloc(void **p, size_t bytes);
+
 // Implemented per precision in gw_kernel_fp64.cu / gw_kernel_fp32.cu.
 int launch_engine_fp64(const KernelArgs &a, const LaunchShape &s, void *stream, bool ode64);
 int launch_engine_fp32(const KernelArgs &a, const LaunchShape &s, void *stream, bool ode64);

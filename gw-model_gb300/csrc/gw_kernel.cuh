@@ -704,6 +704,15 @@ __device__ __forceinline__ void apply_event(Cru<R> &s, const SsaConsts<R> &c, co
     }
 }
 
+// What one iteration of the event loop did: its sub-step length (the jump time, or the rest of the
+// global step for the last one) and the event chosen after it (act 0: none; else act, subunit aj
+// and transition atr as select_event returns them).  Read by the pathwise adjoint (gw_adjoint.cu).
+template <typename R>
+struct IterInfo {
+    R h;
+    int act, aj, atr;
+};
+
 template <typename R, bool EXACT>
 struct SsaLane {
     R t;          // time reached within the global step
@@ -727,7 +736,7 @@ struct SsaLane {
     // One iteration of the event loop; true when the CRU's step is complete (the jump passed the
     // end of the step, or the event cap was exceeded, which sets err).
     __device__ __forceinline__ bool iterate(Cru<R> &s, const SsaConsts<R> &c, const R *sv, const float2 *tab,
-                                            Stream &rng, R dt, int cap, int &err) {
+                                            Stream &rng, R dt, int cap, int &err, IterInfo<R> *info = nullptr) {
         const R Cai = sv[SV_CAI], CaNSR = sv[SV_CANSR];
         const R Cai_lo = EXACT ? (R)0 : sv[SV_CAI_LO], CaNSR_lo = EXACT ? (R)0 : sv[SV_CANSR_LO];
         R jxfer[4], jiss[4];
@@ -830,6 +839,12 @@ struct SsaLane {
 
         // Apply the transition to the updated state.
         if (act != 0) apply_event<R>(s, c, sv, act, aj, atr, jrel);
+        if (info) {
+            info->h = h;
+            info->act = act;
+            info->aj = aj;
+            info->atr = atr;
+        }
         jxfer_sum = jxfer[0] + jxfer[1] + jxfer[2] + jxfer[3];
         k = kk;
         if (last) return true;

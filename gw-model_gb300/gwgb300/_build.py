@@ -1,7 +1,8 @@
 """Builds the engine's shared library (libgwgb300.so) in-tree with nvcc for sm_103a.
 
-Three translation units compile in parallel: the FP64 engine (-fmad=false, reference rounding),
-the FP32 engine, and the host runtime behind the C ABI.  The CUDA runtime is linked statically so
+The translation units compile in parallel: the FP64 engine and the FP64 gradient path
+(-fmad=false, reference rounding), the FP32 engine, the global-step program builder and the host
+runtime behind the C ABI.  The CUDA runtime is linked statically so
 the library loads without torch.
 """
 from __future__ import annotations
@@ -23,6 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-I" + INCLUDE, "-I" + CSRC, "-Xcompiler", "-fPIC"]
 UNITS = [
     ("gw_kernel_fp64.cu", ["-fmad=false"]),
+    ("gw_adjoint.cu", ["-fmad=false"]),
     ("gw_kernel_fp32.cu", []),
     ("gw_capi.cpp", ["-x", "cu"]),
     ("gw_ode_program.cpp", []),

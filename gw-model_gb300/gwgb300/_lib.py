@@ -77,6 +77,24 @@ class GwStats(C.Structure):
                 ("device_allocs", C.c_uint64)]
 
 
+# Parameters of the gradient path (GW_TH_* order) and the gw_params fields each one scales.
+GRAD_THETA = ("PCaL", "GKr", "GKs", "GK1", "INaKmax", "Vmax", "rRyR", "CSQNT")
+GRAD_THETA_FIELDS = (("PCaL",), ("GKr",), ("GKs",), ("GK1",), ("INaKmax",), ("Vmaxf", "Vmaxr"), ("rRyR",),
+                     ("CSQNT",))
+
+
+class GwGradDesc(C.Structure):
+    _fields_ = [("n_cells", C.c_int), ("ncru", C.POINTER(C.c_int32)), ("params", C.POINTER(GwParams)),
+                ("params_per_cell", C.c_int), ("seed", C.c_uint64), ("device", C.c_int), ("dt", C.c_double),
+                ("n_steps", C.c_int64), ("checkpoint_every", C.c_int), ("sample_every", C.c_int),
+                ("stim", C.POINTER(C.c_double)), ("event_cap", C.c_int)]
+
+
+class GwGradStats(C.Structure):
+    _fields_ = [("forward_ms", C.c_double), ("backward_ms", C.c_double), ("replay_ms", C.c_double),
+                ("events", C.c_int64), ("checkpoint_bytes", C.c_int64), ("segment_bytes", C.c_int64)]
+
+
 # Exported entry points and their signatures (all return int status unless noted).
 _P = C.POINTER
 _SIGS = {
@@ -111,6 +129,25 @@ _SIGS = {
                      _P(C.c_double), _P(C.c_double), _P(C.c_int32), _P(C.c_int32), _P(C.c_int32),
                      _P(C.c_int32), _P(GwGlobals), C.c_char_p, C.c_uint64, C.c_int, _P(GwTrace)],
                     C.c_int),
+    "gw_grad_create": ([_P(GwGradDesc), _P(C.c_void_p)], C.c_int),
+    "gw_grad_destroy": ([C.c_void_p], C.c_int),
+    "gw_grad_set_state": ([C.c_void_p, C.c_int, _P(GwGlobals), _P(C.c_double), _P(C.c_double), _P(C.c_int32),
+                           _P(C.c_int32), _P(C.c_int32), _P(C.c_int32)], C.c_int),
+    "gw_grad_forward": ([C.c_void_p, _P(C.c_double)], C.c_int),
+    "gw_grad_backward": ([C.c_void_p, _P(C.c_double), _P(C.c_double)], C.c_int),
+    "gw_grad_replay": ([C.c_void_p, C.c_int, _P(C.c_int32), _P(GwParams), _P(C.c_double), _P(C.c_int64)],
+                       C.c_int),
+    "gw_grad_regime_steps": ([C.c_void_p, _P(C.c_int64)], C.c_int),
+    "gw_grad_get_globals": ([C.c_void_p, C.c_int, _P(GwGlobals)], C.c_int),
+    "gw_grad_get_stats": ([C.c_void_p, _P(GwGradStats)], C.c_int),
+    "gw_grad_last_error": ([C.c_void_p, C.c_char_p, C.c_size_t], C.c_int),
+    "gw_grad_check_global": ([_P(GwParams), C.c_int, _P(C.c_double), _P(C.c_double), C.c_double, C.c_double,
+                              _P(C.c_double), _P(C.c_double), _P(C.c_double), _P(C.c_double), _P(C.c_double)],
+                             C.c_int),
+    "gw_grad_check_cru": ([_P(GwParams), C.c_int, _P(C.c_double), _P(C.c_int32), _P(C.c_double), C.c_int,
+                           _P(C.c_double), _P(C.c_int32), _P(C.c_int32), _P(C.c_int32), _P(C.c_double),
+                           _P(C.c_double), _P(C.c_double), _P(C.c_double), _P(C.c_double), _P(C.c_double),
+                           _P(C.c_double)], C.c_int),
 }
 
 _lock = threading.Lock()

@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define GW_ABI_VERSION 4
+#define GW_ABI_VERSION 5
 
 /* Status codes. */
 typedef enum gw_status {
@@ -272,6 +272,98 @@ int gw_simulate(const gw_params *p, int nCRU, double step_size, int64_t num_step
                 const int32_t *init_LCC_inactivation, const int32_t *init_RyR,
                 const int32_t *init_ClCh, const gw_globals *init_globals, const char *prng,
                 uint64_t seed, int precision, gw_trace *trace);
+
+/* ---------------------------------------------------------------------------------------------
+ * Pathwise gradients of a voltage-trace loss.  No counterpart in the reference (it has no
+ * derivatives); this is the differentiation path of the model's parameter fits.
+ *
+ * An ensemble of cells is run forward for n_steps global steps (the same FP64 SSA lane, draws and
+ * global step as gw_run with GW_PRECISION_FP64) with V sampled after every step s for which
+ * (s + 1) % sample_every == 0.  gw_grad_backward takes dL/dV at the samples and returns, per cell,
+ * the relative sensitivities theta_k dL/dtheta_k of the 8 parameters below, conditional on the
+ * forward pass's jump trajectory: the jump times, the transitions chosen and the RyR re-splits are
+ * held fixed, and the derivative of the continuous CRU updates (update_fluxes SSA.tpp:37-45,
+ * update_CaSS SSA.tpp:87-99, update_CaJSR SSA.hpp:68-71, JLCC and Jrel at transitions
+ * SSA.tpp:103-283) and of the global step (GW.tpp:171-212, 237-272) is taken exactly.  This
+ * estimator ignores the dependence of the jump times and transition choices on the parameters.
+ * Memory is bounded by checkpoints every checkpoint_every steps and a recompute of each segment.
+ * ------------------------------------------------------------------------------------------- */
+#define GW_GRAD_THETA 8
+enum {
+    GW_TH_PCAL = 0,    /* PCaL (JLCC at LCC openings) */
+    GW_TH_GKR = 1,     /* GKr */
+    GW_TH_GKS = 2,     /* GKs */
+    GW_TH_GK1 = 3,     /* GK1 */
+    GW_TH_INAKMAX = 4, /* INaKmax */
+    GW_TH_VMAX = 5,    /* Vmaxf and Vmaxr scaled together (SERCA) */
+    GW_TH_RRYR = 6,    /* rRyR (RyR release rate) */
+    GW_TH_CSQNT = 7    /* CSQNT (JSR calsequestrin) */
+};
+
+typedef struct gw_grad_desc {
+    int n_cells;
+    const int32_t *ncru;      /* [n_cells] CRUs per cell */
+    const gw_params *params;  /* [n_cells] if params_per_cell, else [1] */
+    int params_per_cell;
+    uint64_t seed;
+    int device;
+    double dt;                /* global step [ms] */
+    int64_t n_steps;
+    int checkpoint_every;     /* steps between checkpoints; 0 -> 200 */
+    int sample_every;         /* V sampled after step s when (s + 1) % sample_every == 0 */
+    const double *stim;       /* [n_cells][4] pulse train start, period (<= 0: single pulse),
+                                 duration, amplitude, as gw_set_stimulus_pulse */
+    int event_cap;            /* max jumps per CRU per step; 0 -> 65536 */
+} gw_grad_desc;
+
+typedef struct gw_grad_stats {
+    double forward_ms, backward_ms, replay_ms; /* device time of the last call of each */
+    int64_t events;                            /* SSA jumps of the last forward pass */
+    int64_t checkpoint_bytes, segment_bytes;   /* device memory of the checkpoints and of a segment */
+} gw_grad_stats;
+
+typedef struct gw_grad gw_grad;
+
+int gw_grad_create(const gw_grad_desc *desc, gw_grad **out);
+int gw_grad_destroy(gw_grad *g);
+/* Initial state of one cell: the 36 globals and the reference's CRU arrays.  JLCC starts at zero
+ * and the flux carry at the reference ctor's (GW.hpp:73-74), as gw_create leaves a cell. */
+int gw_grad_set_state(gw_grad *g, int cell, const gw_globals *globals, const double *CaSS, const double *CaJSR,
+                      const int32_t *LCC, const int32_t *LCC_inactivation, const int32_t *RyR, const int32_t *ClCh);
+/* Runs the forward pass from the initial states; V_samples [n_cells][n_steps / sample_every] (or NULL). */
+int gw_grad_forward(gw_grad *g, double *V_samples);
+/* dL_dV [n_cells][n_steps / sample_every] -> sens [n_cells][GW_GRAD_THETA] relative sensitivities. */
+int gw_grad_backward(gw_grad *g, const double *dL_dV, double *sens);
+/* Frozen-trajectory replay: variant v re-runs cell src_cell[v] from its initial state with
+ * params[v] on the jump trajectory that cell draws with its own parameters.  V_samples
+ * [n_var][n_steps / sample_every]; regime_steps [n_var] (or NULL): steps begun at V >= -40 mV,
+ * where the reference's h and j gate rates change form (common.hpp:176-218). */
+int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_params *params, double *V_samples,
+                   int64_t *regime_steps);
+/* Steps begun at V >= -40 mV in the last forward pass, per cell. */
+int gw_grad_regime_steps(gw_grad *g, int64_t *regime_steps);
+/* Globals of a cell at the end of the last forward pass. */
+int gw_grad_get_globals(gw_grad *g, int cell, gw_globals *out);
+int gw_grad_get_stats(gw_grad *g, gw_grad_stats *stats);
+/* Message of the last failing call on g (g may be NULL for gw_grad_create failures). */
+int gw_grad_last_error(gw_grad *g, char *msg, size_t len);
+
+/* Host checks of the hand-written adjoints (no device).  gw_grad_check_global: the global
+ * increment d of one step (G: 36 globals; carry: sum JLCC, sum ClCh, sum Jtr, sum Jxfer) and, for
+ * a cotangent lam of G + d, the adjoints of G (identity included), of the carry sums JLCC, Jtr and
+ * Jxfer, and the relative sensitivities of GKr, GKs, GK1, INaKmax and Vmax (others zero).
+ * gw_grad_check_cru: one CRU step of n_sub sub-steps h[k], each followed by event ev[k] (0 none,
+ * 1 subunit sub[k] starts conducting, 2 it stops, 3 its RyR open count becomes onew[k]); x =
+ * CaSS[4], CaJSR, JLCC[4], open = open RyRs per subunit at the start, in = Cai, CaNSR, JLCC factors
+ * JM and JE.  Returns x_out, carry_out = Jtr and the sum of Jxfer of the last sub-step, and for
+ * the cotangents lam_x (of x_out) and lam_carry (of carry_out): lam_x0, lam_in (Cai, CaNSR, JM,
+ * JE) and lam_par (rRyR dL/drRyR, dL/dCSQN_const). */
+int gw_grad_check_global(const gw_params *p, int nCRU, const double *G, const double *carry, double Istim, double dt,
+                         const double *lam, double *d, double *lam_G, double *lam_carry, double *lam_theta);
+int gw_grad_check_cru(const gw_params *p, int nCRU, const double *x, const int32_t *open, const double *in, int n_sub,
+                      const double *h, const int32_t *ev, const int32_t *sub, const int32_t *onew, const double *lam_x,
+                      const double *lam_carry, double *x_out, double *carry_out, double *lam_x0, double *lam_in,
+                      double *lam_par);
 
 #ifdef __cplusplus
 }

@@ -54,11 +54,13 @@ def test_struct_layouts_match_bindings(enginelib):
 #define P(T) printf(#T " %zu\n", sizeof(T));
 #define O(T, f) printf(#T "." #f " %zu\n", offsetof(T, f));
 int main(void) {
-  P(gw_params) P(gw_globals) P(gw_ensemble_desc) P(gw_trace) P(gw_stats)
+  P(gw_params) P(gw_globals) P(gw_ensemble_desc) P(gw_trace) P(gw_stats) P(gw_grad_desc) P(gw_grad_stats)
   O(gw_params, NCaRU) O(gw_params, Ko) O(gw_params, Hr) O(gw_globals, Kr) O(gw_globals, Kv43)
   O(gw_globals, Kv14) O(gw_ensemble_desc, seed) O(gw_ensemble_desc, ode_fp32_rhs)
   O(gw_trace, cru_cell) O(gw_trace, n_written) O(gw_trace, cru_sums) O(gw_trace, CaJSR_f32)
   O(gw_stats, kernel_ms) O(gw_stats, ctas) O(gw_stats, device_allocs)
+  O(gw_grad_desc, seed) O(gw_grad_desc, dt) O(gw_grad_desc, n_steps) O(gw_grad_desc, stim)
+  O(gw_grad_desc, event_cap) O(gw_grad_stats, events) O(gw_grad_stats, segment_bytes)
   return 0;
 }
 """
@@ -70,7 +72,8 @@ int main(void) {
         lines = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
     got = dict(l.split() for l in lines if l.strip())
     types = {"gw_params": _lib.GwParams, "gw_globals": _lib.GwGlobals, "gw_ensemble_desc": _lib.GwEnsembleDesc,
-             "gw_trace": _lib.GwTrace, "gw_stats": _lib.GwStats}
+             "gw_trace": _lib.GwTrace, "gw_stats": _lib.GwStats, "gw_grad_desc": _lib.GwGradDesc,
+             "gw_grad_stats": _lib.GwGradStats}
     for k, v in got.items():
         if "." in k:
             t, f = k.split(".")
@@ -101,7 +104,7 @@ def test_global_defaults(enginelib, oracle):
 
 
 def test_abi_version(enginelib):
-    assert enginelib.gw_abi_version() == 4
+    assert enginelib.gw_abi_version() == 5
 
 
 def test_invalid_arguments_without_device(enginelib):
@@ -116,6 +119,27 @@ def test_invalid_arguments_without_device(enginelib):
     assert enginelib.gw_run(None, 1e-3, 10, 0, None) == _lib.GW_ERR_INVALID_ARGUMENT
     assert enginelib.gw_run_noalloc(None, 1e-3, 10, 0, None) == _lib.GW_ERR_INVALID_ARGUMENT
     assert enginelib.gw_autotune(None, 10, None, None, None) == _lib.GW_ERR_INVALID_ARGUMENT
+    g = C.c_void_p()
+    gd = _lib.GwGradDesc()
+    assert enginelib.gw_grad_create(C.byref(gd), C.byref(g)) == _lib.GW_ERR_INVALID_ARGUMENT
+    buf = C.create_string_buffer(256)
+    enginelib.gw_grad_last_error(None, buf, len(buf))
+    assert b"n_cells" in buf.value
+    assert enginelib.gw_grad_forward(None, None) == _lib.GW_ERR_INVALID_ARGUMENT
+    assert enginelib.gw_grad_backward(None, None, None) == _lib.GW_ERR_INVALID_ARGUMENT
+
+
+def test_grad_theta_enum_matches_bindings():
+    from gwgb300 import _lib
+
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    codes = dict((n, int(v)) for n, v in re.findall(r"(GW_TH_\w+)\s*=\s*(\d+)", src))
+    assert sorted(codes.values()) == list(range(len(_lib.GRAD_THETA)))
+    assert int(re.search(r"#define GW_GRAD_THETA (\d+)", src).group(1)) == len(_lib.GRAD_THETA)
+    names = {"PCAL": "PCaL", "GKR": "GKr", "GKS": "GKs", "GK1": "GK1", "INAKMAX": "INaKmax", "VMAX": "Vmax",
+             "RRYR": "rRyR", "CSQNT": "CSQNT"}
+    for n, v in codes.items():
+        assert _lib.GRAD_THETA[v] == names[n[len("GW_TH_"):]]
 
 
 def test_unknown_prng_rejected_before_any_device_work(enginelib):
