@@ -78,7 +78,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--beat-ms", type=float, default=PERIOD, help="simulated time the K timed steps cover")
-    ap.add_argument("--cells", type=int, default=1, help="replicate cells per GPU (1 = plain path)")
+    ap.add_argument("--cells", type=int, default=1, help="cells of the headline configuration per GPU")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU time of the timed samples")
     return ap.parse_args()
@@ -245,13 +245,15 @@ def workload_config(args, world=1, K=None, flush_note=None):
     cells = max(args.cells, 1)
     K = K or args.steps
     span = window_steps(K, args.beat_ms)
-    return {"workload": f"{'single cell' if cells == 1 else f'{cells} replicate cells'} of {NCRU} CRUs, "
+    return {"workload": f"{'single cell' if cells == 1 else f'{cells} cells'} of {NCRU} CRUs per GPU, "
                         f"1 Hz pacing (+{STIM_AMP:g} pA/pF, {STIM_DUR:g} ms), dt 1e-3 ms, "
                         f"FP32 CRU state, FP64 global ODE",
             "ncru": NCRU, "cells_per_gpu": cells, "window_ms_per_step": span * DT,
             "timed_span_ms": f"0-{K * span * DT:g} of the beat (warm-up on the same windows, then the t = 0 "
                              "state restored)",
-            "parallelism": f"replicas x{world}",
+            "parallelism": (f"{cells * world} cells partitioned over {world} ranks (contiguous shares, streams "
+                            "keyed on the global cell index, no collective on the data path)" if world > 1
+                            else "1 GPU"),
             "l2": flush_note or "256 MB buffer written between timed steps (L2 flush)"}
 
 
@@ -291,7 +293,10 @@ def main():
     K, W = args.steps, max(args.warmup, 3)
     span = window_steps(K, args.beat_ms)
     cells = max(args.cells, 1)
-    e = Ensemble([NCRU] * cells, precision="fp32", seed=1000 + rank, device=local_rank)
+    # one ensemble of cells x world cells, split into contiguous shares (rank r holds global cells
+    # r*cells ..), each keyed on its global cell index: the union is the 1-GPU run of all cells
+    e = Ensemble.partitioned([NCRU] * (cells * world), world=world, rank=rank, precision="fp32", seed=1000,
+                             device=local_rank)
     for c in range(cells):
         e.sample_initial_crus(c)
     e.set_pulse(0.0, PERIOD, STIM_DUR, STIM_AMP)

@@ -519,7 +519,7 @@ struct gw_grad {
     std::vector<double> stim;
     double dt = 0.0;
     int64_t n_steps = 0, n_samples = 0, n_ck = 0;
-    int ck_every = 200, sample_every = 1, event_cap = 65536;
+    int ck_every = 200, sample_every = 1, event_cap = 65536, cell_base = 0;
     uint64_t seed = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -662,6 +662,9 @@ int gw_grad_create(const gw_grad_desc *d, gw_grad **out) {
     if (!(d->dt > 0.0) || d->n_steps < 1 || d->sample_every < 1 || d->checkpoint_every < 0 || d->event_cap < 0)
         return fail_to(g_grad_create_error, GW_ERR_INVALID_ARGUMENT,
                        "need dt > 0, n_steps >= 1, sample_every >= 1, checkpoint_every >= 0, event_cap >= 0");
+    if (d->cell_base < 0 || (int64_t)d->cell_base + d->n_cells > (int64_t)(1 << 28))
+        return fail_to(g_grad_create_error, GW_ERR_INVALID_ARGUMENT,
+                       "need 0 <= cell_base and cell_base + n_cells <= 2^28");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
@@ -687,6 +690,7 @@ int gw_grad_create(const gw_grad_desc *d, gw_grad **out) {
     g->n_ck = (d->n_steps + g->ck_every - 1) / g->ck_every;
     g->event_cap = d->event_cap > 0 ? d->event_cap : 65536;
     g->seed = d->seed;
+    g->cell_base = d->cell_base;
     g->stim.assign(d->stim, d->stim + 4 * (size_t)d->n_cells);
     g->have_state.assign(d->n_cells, 0);
     g->cs.resize(d->n_cells);
@@ -712,7 +716,7 @@ int gw_grad_create(const gw_grad_desc *d, gw_grad **out) {
     g->blk0[d->n_cells] = (int)g->blk_cell.size();
     g->n_blocks = (int)g->blk_cell.size();
     std::vector<int> rng_cell(d->n_cells);
-    for (int c = 0; c < d->n_cells; ++c) rng_cell[c] = c;
+    for (int c = 0; c < d->n_cells; ++c) rng_cell[c] = d->cell_base + c;
     const int64_t C = d->n_cells, N = g->n_crus, S = g->ck_every, K = g->n_ck;
     int rc = 0;
     auto up = [&](Buf &b, const void *src, size_t bytes) {
@@ -925,7 +929,7 @@ int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_para
         ncru[v] = g->ncru[s];
         c0[v] = N;
         N += ncru[v];
-        rngc[v] = s;
+        rngc[v] = g->cell_base + s;
         for (int k = 0; k < 4; ++k) stim[4 * v + k] = g->stim[4 * s + k];
         make_cell_static(params[v], ncru[v], vcs[v]);
         for (int lo = 0; lo < ncru[v]; lo += kBlk) {

@@ -64,6 +64,7 @@ struct gw_ctx {
     bool ode64 = true;
     int n_cells = 0;
     uint64_t seed = 0;
+    int cell_base = 0;  // global index of cell 0 (random streams)
     int event_cap = 65536;
     int steps_per_launch = 1000;
     std::vector<int32_t> ncru;
@@ -188,11 +189,13 @@ int byte_of(int v) { return v & 0xFF; }
 
 // Launch shape: cluster size C, CRU tile per CTA and SSA warps per CTA.  A cell needs
 // ceil(ncru / tile) <= C CTAs.
-int plan_shape(gw_ctx *c, int cluster_req, int tile_req) {
-    const int max_n = *std::max_element(c->ncru.begin(), c->ncru.end());
-    int C = cluster_req > 0 ? cluster_req : 0;
-    int tile = tile_req > 0 ? tile_req : 0;
-    if (C == 0 && tile == 0 && c->precision == GW_PRECISION_FP64) {
+// The size rule: cluster size C and CTA capacity (tile) for cells of at most max_n CRUs, from the
+// requested values (0 = derive).  Depends on nothing else, so contexts holding shares of an
+// ensemble reach the whole ensemble's shape when given its max_n.
+void shape_rule(int precision, int max_n, int cluster_req, int tile_req, int &C, int &tile) {
+    C = cluster_req > 0 ? cluster_req : 0;
+    tile = tile_req > 0 ? tile_req : 0;
+    if (C == 0 && tile == 0 && precision == GW_PRECISION_FP64) {
         // Default FP64: the SSA is bound by the FP64 pipe (one warp instruction per ~64 cycles per
         // sub-partition), so a cell is spread over up to 16 CTAs of at most 96 CRUs: three full
         // warps per CTA on three sub-partitions.
@@ -209,6 +212,12 @@ int plan_shape(gw_ctx *c, int cluster_req, int tile_req) {
         tile = (max_n + C - 1) / C;
     }
     tile = std::max(32, ((tile + 31) / 32) * 32);
+}
+
+int plan_shape(gw_ctx *c, int cluster_req, int tile_req) {
+    const int max_n = *std::max_element(c->ncru.begin(), c->ncru.end());
+    int C = 0, tile = 0;
+    shape_rule(c->precision, max_n, cluster_req, tile_req, C, tile);
     if (C > kMaxClusterCtas || C < 1) return fail(c, GW_ERR_UNSUPPORTED, "cluster size %d not in [1,16]", C);
     const int need = (max_n + tile - 1) / tile;
     if (need > C)
@@ -300,6 +309,7 @@ KernelArgs base_args(gw_ctx *c) {
     a.cajsr = c->d_cajsr.p;
     a.cajsr_lo = c->d_cajsr_lo.as<float>();
     a.seed = c->seed;
+    a.cell_base = c->cell_base;
     a.event_cap = c->event_cap;
     a.n_cells = c->n_cells;
     a.events = c->d_events.as<unsigned long long>();
@@ -450,7 +460,8 @@ int gw_create(const gw_ensemble_desc *d, gw_ctx **out) {
         return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "unknown precision %d", d->precision);
     for (int i = 0; i < d->n_cells; ++i)
         if (d->ncru[i] <= 0) return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "cell %d: nCRU must be > 0", i);
-    if (d->n_cells > (1 << 28)) return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "too many cells");
+    if (d->cell_base < 0 || (int64_t)d->cell_base + d->n_cells > (int64_t)(1 << 28))
+        return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "need 0 <= cell_base and cell_base + n_cells <= 2^28");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return fail(nullptr, GW_ERR_NO_DEVICE, "no CUDA device");
@@ -466,6 +477,7 @@ int gw_create(const gw_ensemble_desc *d, gw_ctx **out) {
     c->ode64 = d->precision == GW_PRECISION_FP64 || d->ode_fp32_rhs == 0;
     c->n_cells = d->n_cells;
     c->seed = d->seed;
+    c->cell_base = d->cell_base;
     c->event_cap = d->event_cap > 0 ? d->event_cap : 65536;
     // Test hook for the bounded waits of the engine kernel: GWGB300_TEST_SYNC_TIMEOUT=1 at context
     // creation makes every launch's last wait for the warp partials expect 16 bytes that are never
@@ -572,6 +584,18 @@ int gw_destroy(gw_ctx *c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     delete c;
+    return GW_OK;
+}
+
+int gw_default_shape(const gw_ensemble_desc *d, int *cluster_ctas, int *cta_crus) {
+    if (!d || !cluster_ctas || !cta_crus || d->n_cells <= 0 || !d->ncru)
+        return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "gw_default_shape: null descriptor/output or n_cells <= 0");
+    int max_n = 0;
+    for (int i = 0; i < d->n_cells; ++i) {
+        if (d->ncru[i] <= 0) return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "cell %d: nCRU must be > 0", i);
+        max_n = std::max(max_n, (int)d->ncru[i]);
+    }
+    shape_rule(d->precision, max_n, d->cluster_ctas, d->cta_crus, *cluster_ctas, *cta_crus);
     return GW_OK;
 }
 

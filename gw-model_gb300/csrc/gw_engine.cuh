@@ -799,7 +799,7 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
                         if (nm < end) {
                             m = nm;
                             tile_get(c, tile[m]);
-                            rng.open(a.seed, (uint32_t)cell, (uint32_t)(w.cru_begin + m), step0 + s, 0);
+                            rng.open(a.seed, (uint32_t)(a.cell_base + cell), (uint32_t)(w.cru_begin + m), step0 + s, 0);
                             sl.begin(c, cc);
                         } else {
                             m = -2;
@@ -958,7 +958,7 @@ __global__ void init_crus_kernel(const KernelArgs a, int cell, int ncru) {
     const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (i >= ncru) return;
     Stream s;
-    s.open(a.seed, (uint32_t)cell, (uint32_t)i, 0, 1);
+    s.open(a.seed, (uint32_t)(a.cell_base + cell), (uint32_t)i, 0, 1);
     uint32_t k = 0;
     auto pick = [&](const double *w, int n) {
         const double u = FP64 ? s.u53(k) : (double)s.u24(k);

@@ -119,6 +119,7 @@ struct KernelArgs {
     float *tr_cass_f, *tr_cajsr_f;         // codec: [rec][ncru][4], [rec][ncru]
     unsigned long long *tr_sums;           // [n_cells][rec_cap][8] CRU sums (int64; Ca in 2^-40 mM)
     uint64_t seed;
+    int cell_base;      // global index of cell 0: cell i draws from the streams of cell_base + i
     int event_cap;
     int n_cells;
     unsigned long long *events;

@@ -51,7 +51,8 @@ class GwEnsembleDesc(C.Structure):
     _fields_ = [("n_cells", C.c_int), ("ncru", C.POINTER(C.c_int32)), ("params", C.POINTER(GwParams)),
                 ("params_per_cell", C.c_int), ("precision", C.c_int), ("seed", C.c_uint64),
                 ("device", C.c_int), ("event_cap", C.c_int), ("cluster_ctas", C.c_int),
-                ("cta_crus", C.c_int), ("steps_per_launch", C.c_int), ("ode_fp32_rhs", C.c_int)]
+                ("cta_crus", C.c_int), ("steps_per_launch", C.c_int), ("ode_fp32_rhs", C.c_int),
+                ("cell_base", C.c_int)]
 
 
 class GwTrace(C.Structure):
@@ -87,7 +88,7 @@ class GwGradDesc(C.Structure):
     _fields_ = [("n_cells", C.c_int), ("ncru", C.POINTER(C.c_int32)), ("params", C.POINTER(GwParams)),
                 ("params_per_cell", C.c_int), ("seed", C.c_uint64), ("device", C.c_int), ("dt", C.c_double),
                 ("n_steps", C.c_int64), ("checkpoint_every", C.c_int), ("sample_every", C.c_int),
-                ("stim", C.POINTER(C.c_double)), ("event_cap", C.c_int)]
+                ("stim", C.POINTER(C.c_double)), ("event_cap", C.c_int), ("cell_base", C.c_int)]
 
 
 class GwGradStats(C.Structure):
@@ -118,6 +119,7 @@ _SIGS = {
     "gw_run": ([C.c_void_p, C.c_double, C.c_int64, C.c_int, _P(GwTrace)], C.c_int),
     "gw_run_noalloc": ([C.c_void_p, C.c_double, C.c_int64, C.c_int, _P(GwTrace)], C.c_int),
     "gw_autotune": ([_P(GwEnsembleDesc), C.c_int, _P(C.c_int), _P(C.c_int), _P(C.c_double)], C.c_int),
+    "gw_default_shape": ([_P(GwEnsembleDesc), _P(C.c_int), _P(C.c_int)], C.c_int),
     "gw_math_check": ([_P(C.c_double), C.c_int64, _P(C.c_double), _P(C.c_double)], C.c_int),
     "gw_get_time": ([C.c_void_p, C.c_int, _P(C.c_double), _P(C.c_uint64)], C.c_int),
     "gw_set_time": ([C.c_void_p, C.c_int, C.c_double, C.c_uint64], C.c_int),

@@ -77,7 +77,7 @@ class GradEngine:
     def __init__(self, ncru: Sequence[int], params=None, *, n_steps: int, dt: float = 1e-3, seed: int = 0,
                  checkpoint_every: int = 200, sample_every: int = 500,
                  stim: Sequence[float] | np.ndarray = (0.0, 0.0, 0.5, 100.0), device: int = 0,
-                 event_cap: int = 0):
+                 event_cap: int = 0, cell_base: int = 0):
         """params: one GwParams (or mapping) for all cells, or a list with one per cell.  stim: the
         pulse train (start, period, duration, amplitude) of every cell, or one row per cell."""
         self.L = _lib.load()
@@ -114,6 +114,7 @@ class GradEngine:
         d.sample_every = self.sample_every
         d.stim = _dp(self.stim)
         d.event_cap = event_cap
+        d.cell_base = int(cell_base)
         h = C.c_void_p()
         _check(self.L, self.L.gw_grad_create(C.byref(d), C.byref(h)), None)
         self.h = h

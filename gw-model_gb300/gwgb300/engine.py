@@ -92,10 +92,12 @@ class Ensemble:
 
     def __init__(self, ncru: Sequence[int], params=None, *, precision: str = "fp32", seed: int = 0,
                  device: int = 0, event_cap: int = 0, cluster_ctas=0, cta_crus: int = 0,
-                 steps_per_launch: int = 0, ode_fp32_rhs: bool = False, tune_steps: int = 200):
+                 steps_per_launch: int = 0, ode_fp32_rhs: bool = False, tune_steps: int = 200,
+                 cell_base: int = 0):
         """cluster_ctas: CTAs per cluster, 0 for the size rule, or "auto" to measure the fastest
         shape (cluster size and CTA capacity) for these cells first (gw_autotune, tune_steps trial
-        steps per candidate)."""
+        steps per candidate).  cell_base: global index of this ensemble's cell 0 in a larger
+        ensemble split over contexts (random streams are keyed on the global index)."""
         self.L = _lib.load()
         self.ncru = np.ascontiguousarray(ncru, dtype=np.int32)
         self.n_cells = int(self.ncru.size)
@@ -120,6 +122,9 @@ class Ensemble:
         d.seed = seed & 0xFFFFFFFFFFFFFFFF
         d.device = device
         d.event_cap = event_cap
+        d.cell_base = int(cell_base)
+        self.cell_base = int(cell_base)
+        self.global_cells = range(self.cell_base, self.cell_base + self.n_cells)
         self.tuned_us_per_step = None
         if cluster_ctas == "auto":
             best, tile, us = C.c_int(), C.c_int(), C.c_double()
@@ -133,6 +138,45 @@ class Ensemble:
         h = C.c_void_p()
         check(self.L.gw_create(C.byref(d), C.byref(h)))
         self.h = h
+
+    @staticmethod
+    def partition_spec(ncru: Sequence[int], world: int, rank: int, precision: str = "fp32",
+                       cluster_ctas: int = 0, cta_crus: int = 0):
+        """(begin, end, cluster_ctas, cta_crus) of this rank's contiguous share of an ensemble of
+        len(ncru) cells (dist.partition) and the launch shape every share takes: the whole
+        ensemble's (gw_default_shape), since a cell's CRU split depends on the shape.  No device."""
+        from .dist import partition
+
+        if cluster_ctas == "auto":
+            raise ValueError("tune the whole ensemble once (gw_autotune) and pass its cluster_ctas and cta_crus")
+        b, e = partition(len(ncru), world, rank)
+        n_all = np.ascontiguousarray(ncru, dtype=np.int32)
+        d = GwEnsembleDesc()
+        d.n_cells = int(n_all.size)
+        d.ncru = n_all.ctypes.data_as(C.POINTER(C.c_int32))
+        d.precision = _lib.PRECISION[precision]
+        d.cluster_ctas = int(cluster_ctas)
+        d.cta_crus = int(cta_crus)
+        cl, tile = C.c_int(), C.c_int()
+        check(_lib.load().gw_default_shape(C.byref(d), C.byref(cl), C.byref(tile)))
+        return b, e, cl.value, tile.value
+
+    @classmethod
+    def partitioned(cls, ncru: Sequence[int], params=None, *, world: int, rank: int, **kw) -> "Ensemble":
+        """This rank's share of an ensemble of len(ncru) cells (partition_spec), keyed on the cells'
+        global indices (cell_base): the union over ranks reproduces one context holding every cell,
+        bit for bit.  ``params``: one set for all cells or one per cell (the share is taken);
+        ``global_cells`` on the result gives the share's global indices."""
+        b, e, cl, tile = cls.partition_spec(ncru, world, rank, kw.get("precision", "fp32"),
+                                            kw.get("cluster_ctas", 0), kw.get("cta_crus", 0))
+        if e <= b:
+            raise ValueError(f"rank {rank} of {world} has no cells of {len(ncru)}")
+        if isinstance(params, (list, tuple)):
+            if len(params) != len(ncru):
+                raise ValueError("need one parameter set per cell")
+            params = list(params[b:e])
+        kw = dict(kw, cluster_ctas=cl, cta_crus=tile)
+        return cls(list(ncru)[b:e], params, cell_base=b, **kw)
 
     def close(self):
         if getattr(self, "h", None):

@@ -95,6 +95,10 @@ typedef struct gw_ensemble_desc {
     int steps_per_launch;     /* global steps fused in one launch; 0 -> 1000 */
     int ode_fp32_rhs;         /* GW_PRECISION_FP32 only: 1 evaluates the global right-hand side in
                                  FP32 (state and Euler update stay FP64); 0 (default) keeps it FP64 */
+    int cell_base;            /* global index of this context's cell 0: cell i draws from the streams
+                                 of cell cell_base + i, so an ensemble split into contexts (one per
+                                 GPU, contiguous shares) gives the results of one context holding all
+                                 its cells; 0 for a whole ensemble.  cell_base + n_cells <= 2^28 */
 } gw_ensemble_desc;
 
 /* Optional recording for gw_run, mirroring record_state (pyGW.hpp:56-99): after step i of the
@@ -176,6 +180,13 @@ int gw_destroy(gw_ctx *ctx);
  * gw_create.  The contexts it builds draw their own initial states; no caller state is touched. */
 int gw_autotune(const gw_ensemble_desc *desc, int trial_steps, int *best_cluster_ctas, int *best_cta_crus,
                 double *best_us_per_step);
+
+/* No counterpart in the reference.  The launch shape gw_create derives for *desc (its size rule,
+ * or desc's own cluster_ctas / cta_crus where set): CTAs per cluster and CTA capacity.  Needs no
+ * device.  Results depend on the shape only through each cell's CRU split, so contexts that hold
+ * shares of an ensemble (cell_base) and are created with the whole ensemble's shape reproduce the
+ * one-context results bit for bit. */
+int gw_default_shape(const gw_ensemble_desc *desc, int *cluster_ctas, int *cta_crus);
 
 /* Replaces GW_model::set_initial_value (GW.tpp:6-10) for one cell.  JLCC may be NULL: the
  * reference then keeps the ctor's JLCC, which is zero (GW.hpp:107-112). */
@@ -314,6 +325,7 @@ typedef struct gw_grad_desc {
     const double *stim;       /* [n_cells][4] pulse train start, period (<= 0: single pulse),
                                  duration, amplitude, as gw_set_stimulus_pulse */
     int event_cap;            /* max jumps per CRU per step; 0 -> 65536 */
+    int cell_base;            /* global index of cell 0 (random streams), as in gw_ensemble_desc */
 } gw_grad_desc;
 
 typedef struct gw_grad_stats {

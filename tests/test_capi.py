@@ -163,3 +163,17 @@ def test_create_reports_missing_device_cleanly(enginelib):
     with pytest.raises(_lib.GWError) as e:
         Ensemble([16])
     assert e.value.code == _lib.GW_ERR_NO_DEVICE
+
+
+def test_cell_base_validated_without_device(enginelib):
+    from gwgb300 import _lib
+
+    d = _lib.GwEnsembleDesc()
+    n = (C.c_int32 * 1)(16)
+    p = _lib.default_params()
+    d.n_cells, d.ncru, d.params = 1, n, C.pointer(p)
+    h = C.c_void_p()
+    for base in (-1, 1 << 28):
+        d.cell_base = base
+        assert enginelib.gw_create(C.byref(d), C.byref(h)) == _lib.GW_ERR_INVALID_ARGUMENT
+        assert "cell_base" in _lib.last_error()

@@ -91,3 +91,45 @@ def test_heterogeneous_ensemble_matches_per_cell_oracle(oracle):
     # 405,000 lie either side of its second upstroke
     V0 = tr.globals[0, :, 0]
     assert V0[405_000 // every] - V0[395_000 // every] > 30.0, V0[-4:]
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_partition_contexts_reproduce_one_context(oracle, precision):
+    """The ensemble split into contiguous shares (Ensemble.partitioned: cell_base = the share's first
+    global cell, the whole ensemble's launch shape), one context per share as one rank per GPU
+    would hold them, gives the one-context results bit for bit: globals at every record, final
+    CRU arrays including JLCC, and the flux carries."""
+    from gwgb300 import Ensemble, engine
+
+    po = oracle
+    seed, steps, every = 5, 3000, 500
+    ncru, ncaru, cl, scale = ensemble_case()
+    params = [engine.params_from(cell_params(po, ncaru[c], scale[c])) for c in range(len(ncru))]
+
+    def run(e, cells):
+        for i, c in enumerate(cells):
+            e.sample_initial_crus(i)
+            e.set_pulse(0.0, cl[c], 0.5, 100.0, cell=i)
+        tr = e.run(DT, steps, record_every=every)
+        crus = [e.get_crus(i) for i in range(len(cells))]
+        carry = [e.get_flux_carry(i) for i in range(len(cells))]
+        return tr.globals, crus, carry
+
+    whole = Ensemble(ncru, params, precision=precision, seed=seed)
+    Gw, Cw, Fw = run(whole, range(len(ncru)))
+    whole.close()
+    for world in (2, 3):
+        got_G, got_C, got_F = [], [], []
+        for rank in range(world):
+            part = Ensemble.partitioned(ncru, params, world=world, rank=rank, precision=precision, seed=seed)
+            cells = list(part.global_cells)
+            G, Cr, F = run(part, cells)
+            part.close()
+            got_G.append(G)
+            got_C += Cr
+            got_F += F
+        np.testing.assert_array_equal(np.concatenate(got_G, axis=0), Gw)
+        for c in range(len(ncru)):
+            for k in ("CaSS", "CaJSR", "JLCC") + CHANNELS:
+                np.testing.assert_array_equal(getattr(got_C[c], k), getattr(Cw[c], k), err_msg=f"{world} {c} {k}")
+            assert got_F[c] == Fw[c]

@@ -61,3 +61,51 @@ def test_partition_bounds():
             assert spans[0][0] == 0 and spans[-1][1] == n
             assert all(spans[i][1] == spans[i + 1][0] for i in range(w - 1))
             assert max(e - b for b, e in spans) - min(e - b for b, e in spans) <= 1
+
+
+def _spec_worker(rank, world, port, ncru, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
+                      WORLD_SIZE=str(world), LOCAL_RANK=str(rank))
+    import torch
+    import torch.distributed as dist
+    from gwgb300 import dist as gd
+    from gwgb300.engine import Ensemble
+
+    d = gd.init("gloo")
+    out = {}
+    for prec in ("fp32", "fp64"):
+        b, e, cl, tile = Ensemble.partition_spec(ncru, world, rank, prec)
+        t = torch.tensor([b, e, cl, tile], dtype=torch.int64)
+        got = [torch.zeros(4, dtype=torch.int64) for _ in range(world)]
+        dist.all_gather(got, t)
+        out[prec] = [g.tolist() for g in got]
+    gd.barrier(d)
+    q.put((rank, out))
+    dist.destroy_process_group()
+
+
+def test_two_rank_ensemble_partition_spec_gloo(enginelib):
+    """Two ranks take contiguous, complete shares of a heterogeneous ensemble, and both shares get
+    the launch shape of one context holding every cell (so the split reproduces it bit for bit);
+    the cell_base of a share is its first global cell."""
+    from gwgb300.engine import Ensemble
+
+    ncru = [2000, 12500, 500, 7000, 64, 3000, 9000]
+    world = 2
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_spec_worker, args=(r, world, port, ncru, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=120) for _ in range(world)]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for prec in ("fp32", "fp64"):
+        whole = Ensemble.partition_spec(ncru, 1, 0, prec)
+        assert whole[:2] == (0, len(ncru))
+        for rank, out in res:
+            specs = out[prec]
+            assert specs[0][0] == 0 and specs[-1][1] == len(ncru) and specs[0][1] == specs[1][0]
+            assert all(s[2:] == list(whole[2:]) for s in specs)
