@@ -22,8 +22,10 @@ stay in L2 between launches).
   paths        plain GPU (the same cell, one launch and one host synchronisation per global step,
                sampled at every window start of the beat), batched GPU (256 cells of 2,000-12,500
                CRUs, log-normal per-cell parameters and 400-1000 ms cycle lengths, one launch,
-               0-400 ms of every cell's beat), the large ensemble (1,024 x 12,500 CRUs, 2 Hz,
-               0-50 ms), and config 1 (one 1,250-CRU cell, FP64 throughout, 500 ms) on the GPU
+               0-400 ms of every cell's beat), config 5 (1,024 x 12,500 CRUs, 2 Hz, cells spread over
+               16 phases of the beat from a one-beat phase library, timed over one 31.25 ms stratum
+               so that the whole beat is covered once), and config 1 (one 1,250-CRU cell, FP64
+               throughout, 500 ms) on the GPU
                beside the CPU port running the same config in full
   roofline     the engine kernel against HBM (algorithmic bytes = the 72-byte FP32 CRU state read
                and written once per CRU-step); issue_roofline: warp instructions issued against
@@ -81,6 +83,16 @@ def parse():
     ap.add_argument("--cells", type=int, default=1, help="cells of the headline configuration per GPU")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU time of the timed samples")
+    ap.add_argument("--config4", type=float, default=0.0, metavar="MS",
+                    help="only run config 4 (32 cells x 5,000 CRUs, adjoint of a V-trace MSE) over MS ms after "
+                         "one stimulus and print its timing as one JSON line")
+    ap.add_argument("--config4-cells", type=int, default=32)
+    ap.add_argument("--profile-batched", type=int, default=0, metavar="LAUNCHES",
+                    help="only run config 3's ensemble with 100 steps per launch: 200 launches (0-20 ms), then "
+                         "LAUNCHES more (the launches an ncu capture takes)")
+    ap.add_argument("--config5-accuracy", type=int, default=0, metavar="BEATS",
+                    help="only run config 5's FP32 vs FP64 APD90 / peak-Cai comparison over BEATS beats at 2 Hz "
+                         "(64 cells) and print it as one JSON line")
     return ap.parse_args()
 
 
@@ -285,6 +297,15 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config4:
+        print(json.dumps({"config4": config4_measure(0, args.config4, args.config4_cells)}), flush=True)
+        return 0
+    if args.profile_batched:
+        profile_batched(0, args.profile_batched)
+        return 0
+    if args.config5_accuracy:
+        print(json.dumps({"config5_accuracy": config5_accuracy(0, beats=args.config5_accuracy)}), flush=True)
+        return 0
     from gwgb300 import Ensemble
     from gwgb300 import dist as gd
 
@@ -364,7 +385,7 @@ def main():
         line["e2e"] = e2e_measure(K, span)
         line["paths"] = {"plain_gpu": plain_measure(local_rank, windows),
                          "batched_gpu": batched_measure(local_rank),
-                         "large_ensemble_gpu": large_measure(local_rank),
+                         "config5_gpu": config5_measure(local_rank),
                          "config1_fp64": config1_measure(local_rank)}
         line["accuracy"] = {"fp32_vs_fp64_oracle_crn": accuracy_crn(local_rank, windows, K, span),
                             "fp32_vs_fp64_ensemble": accuracy_ks(local_rank)}
@@ -465,32 +486,192 @@ def batched_measure(device, window_ms=400.0, cluster_ctas="auto"):
                         f"CL 400-1000 ms, 0-{window_ms:g} ms of the beat ({steps} steps)"}
 
 
-def large_measure(device, cells=1024, ncru=12500, window_ms=50.0):
+def config5_measure(device, cells=1024, ncru=12500, lib_cells=64, strata=16):
     """Config 5: 1,024 cells of 12,500 CRUs (12.8M CRUs), per-cell log-normal(0.15) parameters, 2 Hz
-    pacing; timed over 0-50 ms of the beat (upstroke and Ca release, the event-heaviest part)."""
+    pacing, timed over a window in which the cells together cover every phase of the beat.
+
+    A phase library comes first: lib_cells cells (their own parameter sets) run one whole 500 ms
+    beat and are checkpointed at `strata` evenly spaced phases.  Cell c of the ensemble takes
+    parameter set c % lib_cells and the library state at phase (c // lib_cells) * 500 / strata ms
+    (time and RNG step included, so it continues its own beat).  The timed window is one stratum
+    long (500 / strata ms): over it the strata tile the whole beat once, so the rate is the
+    beat-averaged rate of the ensemble, without simulating every cell's beat first."""
     import numpy as np
 
     from gwgb300 import Ensemble
 
+    if cells % lib_cells:
+        raise ValueError("cells must be a multiple of lib_cells")
+    period = 500.0
     rng = np.random.default_rng(5)
-    params = lognormal_params(rng, cells, 0.15)
-    e = Ensemble([ncru] * cells, params, precision="fp32", seed=17, device=device, cluster_ctas="auto",
-                 tune_steps=100)
+    params = lognormal_params(rng, lib_cells, 0.15)
+    lib = Ensemble([ncru] * lib_cells, params, precision="fp32", seed=17, device=device)
+    for c in range(lib_cells):
+        lib.sample_initial_crus(c)
+    lib.set_pulse(0.0, period, STIM_DUR, STIM_AMP)
+    span = int(round(period / strata / DT))
+    states = []
+    t0 = time.perf_counter()
+    for k in range(strata):
+        states.append([lib.checkpoint(c) for c in range(lib_cells)])
+        lib.run(DT, span)
+    lib.close()
+    t_lib = time.perf_counter() - t0
+    reps = cells // lib_cells
+    e = Ensemble([ncru] * cells, [params[c % lib_cells] for c in range(cells)], precision="fp32", seed=19,
+                 device=device, cluster_ctas="auto", tune_steps=100)
+    e.set_pulse(0.0, period, STIM_DUR, STIM_AMP)
     for c in range(cells):
-        e.sample_initial_crus(c)
-    e.set_pulse(0.0, 500.0, STIM_DUR, STIM_AMP)
-    steps = int(round(window_ms / DT))
+        e.restore(c, states[(c // lib_cells) % strata][c % lib_cells])
+    del states
     st0 = e.stats()
-    e.run(DT, steps)
+    e.run(DT, span)
     st1 = e.stats()
     e.close()
     kern = (st1["kernel_ms"] - st0["kernel_ms"]) / 1e3
-    total = cells * ncru * steps
-    return {"cru_steps_per_s": total / kern, "sim_ms_per_wall_s": cells * steps * DT / kern,
+    total = cells * ncru * span
+    return {"cru_steps_per_s": total / kern, "sim_ms_per_wall_s": cells * span * DT / kern,
             "algorithmic_GBps": total * BYTES_PER_CRU_STEP / kern / 1e9, "cells": cells, "crus": cells * ncru,
+            "events_per_cru_step": (st1["events"] - st0["events"]) / total,
             "launch_shape": {k: st1[k] for k in ("cluster_ctas", "cta_crus", "threads_per_cta", "n_clusters")},
-            "workload": f"{cells} cells x {ncru} CRUs, log-normal(0.15) PCaL/GKr/GKs/Vmax/rRyR, CL 500 ms, "
-                        f"0-{window_ms:g} ms of the beat ({steps} steps)"}
+            "phase_library_s": t_lib,
+            "workload": f"{cells} cells x {ncru} CRUs, {lib_cells} log-normal(0.15) PCaL/GKr/GKs/Vmax/rRyR sets x "
+                        f"{reps} phases, CL {period:g} ms; cells start at {strata} phases spaced "
+                        f"{period / strata:g} ms apart (states from a one-beat library run) and the timed "
+                        f"{span * DT:g} ms window covers the whole beat once across them"}
+
+
+def config4_measure(device, ms=400.0, cells=32, ncru=5000, sample_every=500, checkpoint_every=200):
+    """Config 4: 32 cells x 5,000 CRUs, one stimulus, `ms` ms; loss = MSE of V sampled every 0.5 ms
+    against a target trace from the same cells with the 8 parameters scaled by 1 + U(-0.2, 0.2);
+    the pathwise adjoint with a checkpoint every 200 global steps.  Times the target's forward pass,
+    the forward pass at the base parameters and the backward pass (device time, CUDA events)."""
+    import numpy as np
+
+    from gwgb300 import _lib
+    from gwgb300.adjoint import THETA, GradEngine, initial_states, scaled_params
+
+    steps = int(round(ms / DT))
+    base = _lib.default_params()
+    g0 = np.frombuffer(bytes(_lib.default_globals(py=True)), dtype=np.float64).copy()
+    states = initial_states([ncru] * cells, seed=7, device=device)
+    kw = dict(n_steps=steps, seed=7, checkpoint_every=checkpoint_every, sample_every=sample_every, device=device)
+    scales = 1.0 + np.random.default_rng(4).uniform(-0.2, 0.2, (cells, len(THETA)))
+    with GradEngine([ncru] * cells, [scaled_params(base, s) for s in scales], **kw) as t:
+        for c in range(cells):
+            t.set_state(c, g0, states[c])
+        Vt = t.forward()
+        target_ms = t.stats()["forward_ms"]
+    with GradEngine([ncru] * cells, base, **kw) as e:
+        for c in range(cells):
+            e.set_state(c, g0, states[c])
+        w0 = time.perf_counter()
+        V = e.forward()
+        w1 = time.perf_counter()
+        sens = e.backward(2.0 * (V - Vt) / Vt.size)
+        w2 = time.perf_counter()
+        st = e.stats()
+    crus = cells * ncru * steps
+    return {"workload": f"{cells} cells x {ncru} CRUs, {ms:g} ms after one stimulus (+100 pA/pF, 0.5 ms), V "
+                        f"sampled every {sample_every * DT:g} ms, checkpoint every {checkpoint_every} steps",
+            "steps": steps, "forward_s": st["forward_ms"] / 1e3, "backward_s": st["backward_ms"] / 1e3,
+            "target_forward_s": target_ms / 1e3, "wall_forward_s": w1 - w0, "wall_backward_s": w2 - w1,
+            "forward_cru_steps_per_s": crus / (st["forward_ms"] / 1e3),
+            "gradient_cru_steps_per_s": crus / ((st["forward_ms"] + st["backward_ms"]) / 1e3),
+            "backward_over_forward": st["backward_ms"] / st["forward_ms"],
+            "events_per_cru_step": st["events"] / crus,
+            "checkpoint_GB": st["checkpoint_bytes"] / 1e9, "segment_GB": st["segment_bytes"] / 1e9,
+            "loss": float(np.mean((V - Vt) ** 2)),
+            "sens_mean_abs": dict(zip(THETA, np.abs(sens).mean(axis=0).tolist()))}
+
+
+def profile_batched(device, launches):
+    """Config 3's ensemble (the fixed shape its autotune picks: clusters of 6 CTAs of 2,336 CRUs)
+    with 100 global steps per launch: 200 launches bring it to 20 ms (Ca release), then `launches`
+    more.  For ncu: -k regex:engine_kernel -s 200 -c <n>."""
+    from gwgb300 import Ensemble
+
+    ncru, params, cl = batched_config()
+    e = Ensemble(list(ncru), params, precision="fp32", seed=11, device=device, cluster_ctas=6, cta_crus=2336,
+                 steps_per_launch=100)
+    for c in range(len(ncru)):
+        e.sample_initial_crus(c)
+        e.set_pulse(0.0, float(cl[c]), STIM_DUR, STIM_AMP, cell=c)
+    e.run(DT, 200 * 100)
+    st0 = e.stats()
+    e.run(DT, launches * 100)
+    st1 = e.stats()
+    e.close()
+    total = int(ncru.sum()) * launches * 100
+    print(json.dumps({"profile_batched": {"launches": launches, "crus": int(ncru.sum()),
+                                          "us_per_step": (st1["kernel_ms"] - st0["kernel_ms"]) * 1e3 / (launches * 100),
+                                          "cru_steps_per_s": total / ((st1["kernel_ms"] - st0["kernel_ms"]) / 1e3),
+                                          "events_per_cru_step": (st1["events"] - st0["events"]) / total}}),
+          flush=True)
+
+
+def _lib_globals():
+    from gwgb300 import _lib
+
+    return _lib.default_globals()
+
+
+def config5_accuracy(device, cells=64, ncru=500, beats=10, every=500):
+    """Config 5 accuracy: APD90 and peak Cai of every beat of a 64-cell subset, FP32 engine vs FP64
+    engine (reference arithmetic), same seeds and parameter sets (log-normal(0.15), as config 5),
+    2 Hz for `beats` beats.  The cells hold ncru CRUs standing for NCaRU = 12,500 (CRU_factor
+    12,500 / ncru) so that the FP64 runs fit; both precisions see the same cells.  Reports per beat
+    and pooled over beats: KS p-values of the two distributions, relative differences of their means
+    and standard deviations, and the mean absolute per-cell difference."""
+    import numpy as np
+    from scipy.stats import ks_2samp
+
+    from gwgb300 import Ensemble, analysis
+
+    period = 500.0
+    rng = np.random.default_rng(5)
+    params = lognormal_params(rng, cells, 0.15)
+    steps = int(round(beats * period / DT))
+    per_beat = int(round(period / (every * DT)))
+    out, secs = {}, {}
+    for prec in ("fp32", "fp64"):
+        e = Ensemble([ncru] * cells, params, precision=prec, seed=23, device=device)
+        for c in range(cells):
+            e.sample_initial_crus(c)
+        e.set_pulse(0.0, period, STIM_DUR, STIM_AMP)
+        st0 = e.stats()
+        tr = e.run(DT, steps, record_every=every)
+        secs[prec] = (e.stats()["kernel_ms"] - st0["kernel_ms"]) / 1e3
+        e.close()
+        V, Cai = tr.var("V"), tr.var("Cai")
+        v0 = np.frombuffer(bytes(_lib_globals()), dtype=np.float64)[0]
+        apd, pk = [], []
+        t = np.arange(per_beat + 1) * every * DT  # from the beat's stimulus onset
+        for b in range(beats):
+            sl = slice(b * per_beat, (b + 1) * per_beat)
+            # the beat's trace with V just before its stimulus in front (the rest level of APD90)
+            before = np.full((cells, 1), v0) if b == 0 else V[:, b * per_beat - 1:b * per_beat]
+            mk = analysis.ap_markers(t, np.concatenate([before, V[:, sl]], axis=1))
+            apd.append(mk["APD90"])
+            pk.append(Cai[:, sl].max(axis=1))
+        out[prec] = {"APD90": np.array(apd), "peak_Cai": np.array(pk)}
+
+    def compare(a, b):
+        return {"ks_pvalue": float(ks_2samp(a.ravel(), b.ravel()).pvalue),
+                "rel_diff_mean": float(abs(a.mean() - b.mean()) / abs(b.mean())),
+                "rel_diff_std": float(abs(a.std() - b.std()) / max(b.std(), 1e-300)),
+                "mean_abs_cell_diff_rel": float(np.mean(np.abs(a - b)) / abs(b.mean()))}
+
+    res = {"reference": "FP64 engine (reference arithmetic, bit-exact channel sequences vs the oracle)",
+           "cells": cells, "ncru": ncru, "NCaRU": 12500, "beats": beats, "cycle_ms": period,
+           "kernel_s": secs, "pooled": {}, "per_beat": {}}
+    for k in ("APD90", "peak_Cai"):
+        a, b = out["fp32"][k], out["fp64"][k]
+        res["pooled"][k] = compare(a, b)
+        res["per_beat"][k] = [compare(a[i], b[i]) for i in range(beats)]
+        res["pooled"][k]["fp64_mean"] = float(b.mean())
+        res["pooled"][k]["fp64_std"] = float(b.std())
+    return res
 
 
 def config1_measure(device):
