@@ -586,13 +586,14 @@ def config4_measure(device, ms=400.0, cells=32, ncru=5000, sample_every=500, che
 
 
 def profile_batched(device, launches):
-    """Config 3's ensemble (the fixed shape its autotune picks: clusters of 6 CTAs of 2,336 CRUs)
-    with 100 global steps per launch: 200 launches bring it to 20 ms (Ca release), then `launches`
-    more.  For ncu: -k regex:engine_kernel -s 200 -c <n>."""
+    """Config 3's ensemble in the shape its autotune picks (clusters of 6 CTAs, the size rule's CTA
+    capacity; the planner then gives the CTAs up to 2,336 CRUs) with 100 global steps per launch:
+    200 launches bring it to 20 ms (Ca release), then `launches` more.  For ncu:
+    -k regex:engine_kernel -s 200 -c <n>."""
     from gwgb300 import Ensemble
 
     ncru, params, cl = batched_config()
-    e = Ensemble(list(ncru), params, precision="fp32", seed=11, device=device, cluster_ctas=6, cta_crus=2336,
+    e = Ensemble(list(ncru), params, precision="fp32", seed=11, device=device, cluster_ctas=6, cta_crus=0,
                  steps_per_launch=100)
     for c in range(len(ncru)):
         e.sample_initial_crus(c)

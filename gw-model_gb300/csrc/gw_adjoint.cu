@@ -8,14 +8,22 @@
 // The state of every CRU and cell is checkpointed every `checkpoint_every` steps.
 //
 // Backward, one checkpoint segment at a time from the last: the segment is recomputed from its
-// checkpoint with every step's start state stored, then stepped in reverse:
-//   k_cru_adj     one thread per CRU: re-runs the CRU's step from its stored start state with the
-//                 same draws (hence the same jump times and transitions), keeps the sub-steps in
-//                 blocks of kRec and walks them backwards through the adjoint of the sub-step and
-//                 event arithmetic; a block reduction gives the cell's adjoints of the step inputs
-//                 (Cai, CaNSR, the JLCC factors) and of rRyR and CSQN.
-//   k_global_adj  one thread per cell: the adjoint of the global increment plus the CRU inputs'
-//                 contributions, and the parameters' relative sensitivities.
+// checkpoint with every step's start state stored, and the CRUs whose step had a jump listed per
+// step; then it is stepped in reverse:
+//   k_cru_quiet   the CRUs without a jump in the step (most of them): their step is one sub-step of
+//                 length dt, reversed directly from the stored start state.
+//   k_cru_busy    the listed CRUs, densely packed: each re-runs its step from its stored start state
+//                 with the same draws (hence the same jump times and transitions), keeps the
+//                 sub-steps in blocks of kRec and walks them backwards through the adjoint of the
+//                 sub-step and event arithmetic.
+//   Both write per CRU its adjoint state and its adjoints of the step inputs (Cai, CaNSR, the JLCC
+//   factors) and of rRyR and CSQN.
+//   k_global_adj  one block per cell: sums the cell's CRU rows in a fixed order, then the adjoint
+//                 of the global increment plus the CRU inputs' contributions, and the parameters'
+//                 relative sensitivities.
+// The SSA of a step runs with lane refill: a warp's lane whose CRU has finished its step takes the
+// next CRU of the warp's range, so a CRU with many jumps does not hold 31 idle lanes.  Results do
+// not depend on the order in which CRUs are processed or listed.
 // Memory: (steps / checkpoint_every) checkpoints + checkpoint_every step states of every CRU.
 //
 // Replay (gw_grad_replay) re-runs chosen cells with other parameters on the recorded jump
@@ -44,7 +52,7 @@ using namespace gw::adj;
 namespace {
 
 constexpr int kBlk = 128;     // threads per block of the CRU kernels (one cell per block)
-constexpr int kRec = 8;       // sub-steps a CRU keeps per block of its reverse sweep
+constexpr int kRec = 16;      // sub-steps a CRU keeps per block of its reverse sweep
 constexpr int kAdjIn = 6;     // per-cell CRU adjoints: Cai, CaNSR, JM, JE, rRyR (relative), CSQN_const
 constexpr int kLamX = 9;      // CRU adjoint state: CaSS[4], CaJSR, JLCC[4]
 using CruD = dev::Cru<double>;
@@ -76,6 +84,8 @@ struct GradArgs {
     const CellStatic *cs;       // [n_cells]
     const int *blk_cell;        // [blocks] cell of each CRU block
     const int *blk_lo;          // [blocks] first CRU (within the cell) of each block
+    const int *blk_hi;          // [blocks] end of the block's CRU range (within the cell)
+    const int *cru_cell;        // [n_crus] cell of each CRU (backward kernels)
     const int64_t *cru0;        // [n_cells] first CRU of each cell in the CRU arrays
     const int *ncru;            // [n_cells]
     const int *rng_cell;        // [n_cells] cell index that keys the cell's random streams
@@ -102,6 +112,9 @@ struct GradArgs {
     double *seg_G;              // [slots][n_cells][36]
     double *seg_carry;          // [slots][n_cells][4]
     double *seg_sv;             // [slots][n_cells][kSvCount]
+    uint8_t *quiet;             // [slots][n_crus] 1: the CRU's step had no jump (one sub-step of dt)
+    int *busy;                  // [slots][n_crus] the other CRUs of the step, in completion order
+    int *busy_n;                // [slots] their count
     // Replay: the variant's continuous CRU state driven by this set's jump trajectory (null: none).
     const CellStatic *var_cs;   // [n_cells]
     double *var_x;              // [n_crus][9] CaSS[4], CaJSR, JLCC[4]
@@ -115,8 +128,8 @@ struct AdjArgs {
     double *lam_G;      // [n_cells][36]
     double *lam_cy;     // [n_cells][3] adjoints of the carry sums JLCC, Jtr, Jxfer
     double *lam_th;     // [n_cells][8] relative sensitivities
-    double *part;       // [blocks][kAdjIn]
-    const int *blk0;    // [n_cells + 1] first block of each cell
+    double *ai_row;     // [n_crus][kAdjIn] each CRU's adjoints of its step inputs and parameters
+    const dev::SsaConsts<double> *cc;  // [n_cells] SSA constants (k_cru_busy)
     const double *dLdV; // [n_cells][n_samples]
 };
 
@@ -184,133 +197,248 @@ __device__ __forceinline__ CruIn cru_in(const double *sv) {
     return CruIn{sv[SV_CAI], sv[SV_CANSR], sv[SV_JMUL], sv[SV_JEXP]};
 }
 
-// Forward SSA of step `step` for every CRU (one block per 128 CRUs of one cell).
+// Forward SSA of step `step`: block b takes CRUs [blk_lo, blk_hi) of cell blk_cell, split evenly
+// over its warps; each warp runs its range with lane refill (one SSA iteration per pass; a lane
+// whose CRU finished its step takes the warp's next CRU).
 __global__ void __launch_bounds__(kBlk) k_ssa(const GradArgs a, int64_t step, int slot) {
     __shared__ dev::SsaConsts<double> cc;
     __shared__ double sv[kSvCount];
     __shared__ double vsv[kSvCount];
     const int cell = a.blk_cell[blockIdx.x];
+    const bool var = a.var_x != nullptr;
     if (threadIdx.x == 0) dev::load_ssa_consts<double>(cc, a.cs[cell]);
     if (threadIdx.x < kSvCount) {
         sv[threadIdx.x] = a.sv[(int64_t)cell * kSvCount + threadIdx.x];
-        if (a.var_x) vsv[threadIdx.x] = a.var_sv[(int64_t)cell * kSvCount + threadIdx.x];
+        if (var) vsv[threadIdx.x] = a.var_sv[(int64_t)cell * kSvCount + threadIdx.x];
     }
     __syncthreads();
-    const int m = a.blk_lo[blockIdx.x] + (int)threadIdx.x;
-    const bool active = m < a.ncru[cell] && a.status[cell] == 0;
+    const int lane = (int)threadIdx.x & 31, warp = (int)threadIdx.x >> 5;
+    constexpr int nw = kBlk / 32;
+    const int lo = a.blk_lo[blockIdx.x], span = a.blk_hi[blockIdx.x] - lo;
+    const int end = lo + (int)((int64_t)span * (warp + 1) / nw);
+    int cursor = lo + (int)((int64_t)span * warp / nw);
+    const int64_t c0 = a.cru0[cell];
+    const uint32_t rc = (uint32_t)a.rng_cell[cell];
+    CruPar P{};
+    CruIn in{};
+    if (var) {
+        P = cru_par(a.var_cs[cell]);
+        in = cru_in(vsv);
+    }
+    CruD c;
+    dev::SsaLane<double, true> L;
+    dev::Stream rng;
+    CruCont v;
+    double vjtr = 0.0, vjx = 0.0;
+    int m = a.status[cell] == 0 ? -1 : -2;  // CRU of this lane; -1 none yet, -2 none left
     unsigned int ev = 0;
     int err = 0;
-    if (active) {
-        const int64_t i = a.cru0[cell] + m;
-        CruD c = a.x[i];
-        if (a.seg_x) a.seg_x[(int64_t)slot * a.n_crus + i] = c;
-        dev::Stream rng;
-        rng.open(a.seed, (uint32_t)a.rng_cell[cell], (uint32_t)m, (uint64_t)step, 0);
-        dev::SsaLane<double, true> L;
-        L.begin(c, cc);
-        if (!a.var_x) {
-            while (!L.iterate(c, cc, sv, nullptr, rng, a.dt, a.event_cap, err)) {
+    for (;;) {
+        const unsigned need = __ballot_sync(0xffffffffu, m == -1);
+        if (need) {
+            const int nm = cursor + __popc(need & ((1u << lane) - 1u));
+            cursor += __popc(need);
+            if (m == -1) {
+                if (nm < end) {
+                    m = nm;
+                    const int64_t i = c0 + m;
+                    c = a.x[i];
+                    if (a.seg_x) a.seg_x[(int64_t)slot * a.n_crus + i] = c;
+                    rng.open(a.seed, rc, (uint32_t)m, (uint64_t)step, 0);
+                    L.begin(c, cc);
+                    if (var) {
+                        // the variant follows the same sub-steps and events with its own parameters
+                        const double *vx = a.var_x + (int64_t)kLamX * i;
+                        for (int j = 0; j < 4; ++j) {
+                            v.c[j] = vx[j];
+                            v.L[j] = vx[5 + j];
+                        }
+                        v.J = vx[4];
+                        int o[4];
+                        open_counts(c, o);
+                        cru_begin(v, o, P);
+                    }
+                } else {
+                    m = -2;
+                }
             }
-        } else {
-            // the variant follows the same sub-steps and events with its own parameters and inputs
-            const CruPar P = cru_par(a.var_cs[cell]);
-            const CruIn in = cru_in(vsv);
-            double *vx = a.var_x + (int64_t)kLamX * i;
-            CruCont v;
-            for (int j = 0; j < 4; ++j) {
-                v.c[j] = vx[j];
-                v.L[j] = vx[5 + j];
-            }
-            v.J = vx[4];
-            int o[4];
-            open_counts(c, o);
-            cru_begin(v, o, P);
-            double vjtr = 0.0, vjx = 0.0;
-            for (;;) {
-                const uint32_t lcc0 = c.lcc, fl0 = c.flags;
-                dev::IterInfo<double> f;
-                const bool done = L.iterate(c, cc, sv, nullptr, rng, a.dt, a.event_cap, err, &f);
+        }
+        if (!__any_sync(0xffffffffu, m >= 0)) break;
+        if (m >= 0) {
+            const uint32_t lcc0 = c.lcc, fl0 = c.flags;
+            dev::IterInfo<double> f;
+            const bool done = L.iterate(c, cc, sv, nullptr, rng, a.dt, a.event_cap, err, var ? &f : nullptr);
+            if (var) {
                 cru_substep(v, f.h, in, P, vjtr, vjx);
                 int e, j, onew;
                 classify(f, lcc0, fl0, c, e, j, onew);
                 cru_event(v, e, j, onew, in, P);
-                if (done) break;
             }
-            for (int j = 0; j < 4; ++j) {
-                vx[j] = v.c[j];
-                vx[5 + j] = v.L[j];
+            if (done) {
+                const int64_t i = c0 + m;
+                a.x[i] = c;
+                double *o = a.out + 4 * i;
+                o[0] = c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3];
+                o[1] = L.jxfer_sum;
+                o[2] = L.jtr;
+                o[3] = (double)__popc((c.flags >> 4) & 0xFu);
+                if (var) {
+                    double *vx = a.var_x + (int64_t)kLamX * i;
+                    for (int j = 0; j < 4; ++j) {
+                        vx[j] = v.c[j];
+                        vx[5 + j] = v.L[j];
+                    }
+                    vx[4] = v.J;
+                    double *vo = a.var_out + 4 * i;
+                    vo[0] = v.L[0] + v.L[1] + v.L[2] + v.L[3];
+                    vo[1] = vjx;
+                    vo[2] = vjtr;
+                    vo[3] = o[3];
+                }
+                if (a.quiet) {
+                    const bool q = L.ev == 0;
+                    a.quiet[(int64_t)slot * a.n_crus + i] = q ? 1 : 0;
+                    if (!q) a.busy[(int64_t)slot * a.n_crus + atomicAdd(&a.busy_n[slot], 1)] = (int)i;
+                }
+                ev += (unsigned int)L.ev;
+                m = -1;
             }
-            vx[4] = v.J;
-            double *vo = a.var_out + 4 * i;
-            vo[0] = v.L[0] + v.L[1] + v.L[2] + v.L[3];
-            vo[1] = vjx;
-            vo[2] = vjtr;
-            vo[3] = (double)__popc((c.flags >> 4) & 0xFu);
         }
-        a.x[i] = c;
-        double *o = a.out + 4 * i;
-        o[0] = c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3];
-        o[1] = L.jxfer_sum;
-        o[2] = L.jtr;
-        o[3] = (double)__popc((c.flags >> 4) & 0xFu);
-        ev = (unsigned int)L.ev;
     }
     const unsigned int wev = __reduce_add_sync(0xffffffffu, ev);
-    if (a.events && (threadIdx.x & 31) == 0 && wev) atomicAdd(&a.events[cell], (unsigned long long)wev);
+    if (a.events && lane == 0 && wev) atomicAdd(&a.events[cell], (unsigned long long)wev);
     if (err) atomicExch(&a.status[cell], (int)GW_ERR_EVENT_CAP);
 }
 
-// The cell's flux sums of the step and its global step (one block per cell).
+// The cell's flux sums of the step and its global step (one block per cell): the transcendental
+// terms of the increment, then of the new state's SSA values, on one thread each; the rest on
+// thread 0.
 __global__ void __launch_bounds__(kBlk) k_global(const GradArgs a, int64_t step, int slot, int use_var) {
     __shared__ double sh[(kBlk / 32) * 4];
+    __shared__ double T[kNT];
+    __shared__ double gn[kNumGlobals];
+    __shared__ double S[kNS];
+    __shared__ int ok;
     const int cell = blockIdx.x;
+    if (a.status[cell] != 0) return;  // the same for the whole block
     const int n = a.ncru[cell];
     const double *o = (use_var ? a.var_out : a.out) + 4 * a.cru0[cell];
     double s[4] = {0.0, 0.0, 0.0, 0.0};
     for (int m = (int)threadIdx.x; m < n; m += kBlk)
         for (int q = 0; q < 4; ++q) s[q] += o[4 * m + q];
     block_sum<4>(s, sh);
-    if (threadIdx.x != 0 || a.status[cell] != 0) return;
     const CellStatic &C = use_var ? a.var_cs[cell] : a.cs[cell];
     double *g = a.G + (int64_t)kNumGlobals * cell;
-    double *cy = a.carry + 4 * (int64_t)cell;
+    if (threadIdx.x < kNT) T[threadIdx.x] = glob_term(C, g, (int)threadIdx.x);
+    __syncthreads();
     double *svo = (use_var ? const_cast<double *>(a.var_sv) : a.sv) + (int64_t)kSvCount * cell;
-    double gl[kNumGlobals], d[kNumGlobals];
-    for (int k = 0; k < kNumGlobals; ++k) gl[k] = g[k];
-    const Carry c0{cy[0], cy[1], cy[2], cy[3]};
-    const double istim = pulse_at(a.t[cell], a.stim + 4 * (int64_t)cell);
-    if (a.seg_G) {
-        const int64_t r = (int64_t)slot * a.n_cells + cell;
-        for (int k = 0; k < kNumGlobals; ++k) a.seg_G[r * kNumGlobals + k] = gl[k];
-        for (int k = 0; k < 4; ++k) a.seg_carry[r * 4 + k] = cy[k];
-        for (int k = 0; k < kSvCount; ++k) a.seg_sv[r * kSvCount + k] = svo[k];
+    if (threadIdx.x == 0) {
+        ok = 0;
+        double *cy = a.carry + 4 * (int64_t)cell;
+        double gl[kNumGlobals], d[kNumGlobals];
+        for (int k = 0; k < kNumGlobals; ++k) gl[k] = g[k];
+        const Carry c0{cy[0], cy[1], cy[2], cy[3]};
+        const double istim = pulse_at(a.t[cell], a.stim + 4 * (int64_t)cell);
+        if (a.seg_G) {
+            const int64_t r = (int64_t)slot * a.n_cells + cell;
+            for (int k = 0; k < kNumGlobals; ++k) a.seg_G[r * kNumGlobals + k] = gl[k];
+            for (int k = 0; k < 4; ++k) a.seg_carry[r * 4 + k] = cy[k];
+            for (int k = 0; k < kSvCount; ++k) a.seg_sv[r * kSvCount + k] = svo[k];
+        }
+        if (a.regime && gl[0] >= -40.0) a.regime[cell] += 1ull;
+        if (!glob_increment(C, gl, c0, istim, a.dt, T, d)) {
+            a.status[cell] = GW_ERR_NERNST;
+        } else {
+            bool fin = true;
+            for (int k = 0; k < kNumGlobals; ++k) {
+                gl[k] += d[k];
+                fin = fin && isfinite(gl[k]);
+            }
+            if (!fin) {
+                a.status[cell] = GW_ERR_NONFINITE;
+            } else {
+                for (int k = 0; k < kNumGlobals; ++k) g[k] = gn[k] = gl[k];
+                // carry order {JLCC, ClCh, Jtr, Jxfer} from the per-CRU {JLCC, Jxfer, Jtr, ClCh}
+                cy[0] = s[0];
+                cy[1] = s[3];
+                cy[2] = s[2];
+                cy[3] = s[1];
+                a.t[cell] += a.dt;
+                ok = 1;
+            }
+        }
     }
-    if (a.regime && gl[0] >= -40.0) a.regime[cell] += 1ull;
-    if (!glob_increment(C, gl, c0, istim, a.dt, d)) {
-        a.status[cell] = GW_ERR_NERNST;
-        return;
+    __syncthreads();
+    if (!ok) return;
+    if (threadIdx.x < kNS) S[threadIdx.x] = sv_term(C, gn, (int)threadIdx.x);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        step_values(C, gn, S, svo);
+        if (a.V && (step + 1) % a.sample_every == 0) {
+            const int64_t si = (step + 1) / a.sample_every - 1;
+            if (si < a.n_samples) a.V[(int64_t)cell * a.n_samples + si] = gn[0];
+        }
     }
-    bool fin = true;
-    for (int k = 0; k < kNumGlobals; ++k) {
-        gl[k] += d[k];
-        fin = fin && isfinite(gl[k]);
+}
+
+// The adjoint state of CRU i after its step (its lam_x row, and the carry adjoints: the step's
+// sum of JLCC is the sum of the final JLCC).
+__device__ __forceinline__ CruCont lam_after(const double *lx, const double *lc) {
+    CruCont la;
+    for (int j = 0; j < 4; ++j) {
+        la.c[j] = lx[j];
+        la.L[j] = lx[5 + j] + lc[0];
+        la.rel[j] = 0.0;
     }
-    if (!fin) {
-        a.status[cell] = GW_ERR_NONFINITE;
-        return;
+    la.J = lx[4];
+    return la;
+}
+
+__device__ __forceinline__ CruCont cont_of(const CruD &x) {
+    CruCont s;
+    for (int j = 0; j < 4; ++j) {
+        s.c[j] = x.cass[j];
+        s.L[j] = x.jlcc[j];
+        s.rel[j] = 0.0;
     }
-    for (int k = 0; k < kNumGlobals; ++k) g[k] = gl[k];
-    // carry order {JLCC, ClCh, Jtr, Jxfer} from the per-CRU {JLCC, Jxfer, Jtr, ClCh}
-    cy[0] = s[0];
-    cy[1] = s[3];
-    cy[2] = s[2];
-    cy[3] = s[1];
-    a.t[cell] += a.dt;
-    step_values(C, gl, svo);
-    if (a.V && (step + 1) % a.sample_every == 0) {
-        const int64_t si = (step + 1) / a.sample_every - 1;
-        if (si < a.n_samples) a.V[(int64_t)cell * a.n_samples + si] = gl[0];
+    s.J = x.cajsr;
+    return s;
+}
+
+__device__ __forceinline__ void store_adj(const CruCont &la, const CruAdjIn &ai, double *lx, double *row) {
+    for (int j = 0; j < 4; ++j) {
+        lx[j] = la.c[j];
+        lx[5 + j] = la.L[j];
     }
+    lx[4] = la.J;
+    row[0] = ai.Cai;
+    row[1] = ai.CaNSR;
+    row[2] = ai.JM;
+    row[3] = ai.JE;
+    row[4] = ai.rRyR_rel;
+    row[5] = ai.CSQN;
+}
+
+// Reverse of step `slot` for the CRUs whose step had no jump: one sub-step of length dt (the
+// iteration's h = dt - 0) and no transition.
+__global__ void __launch_bounds__(kBlk) k_cru_quiet(const GradArgs a, const AdjArgs b, int slot) {
+    const int64_t i = (int64_t)blockIdx.x * kBlk + threadIdx.x;
+    if (i >= a.n_crus || !a.quiet[(int64_t)slot * a.n_crus + i]) return;
+    const int cell = a.cru_cell[i];
+    const CruD x0 = a.seg_x[(int64_t)slot * a.n_crus + i];
+    const CruPar P = cru_par(a.cs[cell]);
+    const CruIn in = cru_in(a.seg_sv + ((int64_t)slot * a.n_cells + cell) * kSvCount);
+    const double *lc = b.lam_cy + 3 * (int64_t)cell;
+    double *lx = b.lam_x + (int64_t)kLamX * i;
+    CruCont la = lam_after(lx, lc);
+    CruAdjIn ai{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    int o[4];
+    open_counts(x0, o);
+    CruCont s0 = cont_of(x0);
+    cru_begin(s0, o, P);
+    cru_substep_adj(s0, a.dt, in, P, lc[1], lc[2], la, ai);
+    cru_begin_adj(s0, o, P, la, ai);
+    store_adj(la, ai, lx, b.ai_row + (int64_t)kAdjIn * i);
 }
 
 // One recorded sub-step of a CRU's step: the state at its start and what ended it.
@@ -356,92 +484,68 @@ __device__ int run_rec(const CruD &x0, const dev::SsaConsts<double> &cc, const d
     return k;
 }
 
-// Reverse of step `step` for every CRU: lam_x from after the step to before it, and the block's
-// sums of the step-input and parameter adjoints into part[block].
-__global__ void __launch_bounds__(kBlk) k_cru_adj(const GradArgs a, const AdjArgs b, int64_t step, int slot) {
-    __shared__ dev::SsaConsts<double> cc;
-    __shared__ double sv[kSvCount];
-    __shared__ double sh[(kBlk / 32) * kAdjIn];
-    const int cell = a.blk_cell[blockIdx.x];
-    if (threadIdx.x == 0) dev::load_ssa_consts<double>(cc, a.cs[cell]);
-    if (threadIdx.x < kSvCount)
-        sv[threadIdx.x] = a.seg_sv[((int64_t)slot * a.n_cells + cell) * kSvCount + threadIdx.x];
-    __syncthreads();
-    const int m = a.blk_lo[blockIdx.x] + (int)threadIdx.x;
-    double acc[kAdjIn] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    if (m < a.ncru[cell]) {
-        const int64_t i = a.cru0[cell] + m;
+// Reverse of step `step` for the CRUs the recompute listed (their step had jumps), one thread per
+// listed CRU: the step is re-run from its stored start state (same draws, same trajectory) to
+// recover the sub-steps, kRec at a time from the last block, and each block is reversed.
+__global__ void __launch_bounds__(kBlk) k_cru_busy(const GradArgs a, const AdjArgs b, int64_t step, int slot) {
+    const int nb = a.busy_n[slot];
+    for (int k = (int)(blockIdx.x * kBlk + threadIdx.x); k < nb; k += (int)(gridDim.x * kBlk)) {
+        const int64_t i = a.busy[(int64_t)slot * a.n_crus + k];
+        const int cell = a.cru_cell[i];
+        const uint32_t m = (uint32_t)(i - a.cru0[cell]);
+        const dev::SsaConsts<double> &cc = b.cc[cell];
+        const double *sv = a.seg_sv + ((int64_t)slot * a.n_cells + cell) * kSvCount;
         const CruD x0 = a.seg_x[(int64_t)slot * a.n_crus + i];
         const CruPar P = cru_par(a.cs[cell]);
         const CruIn in = cru_in(sv);
         const double *lc = b.lam_cy + 3 * (int64_t)cell;
         double *lx = b.lam_x + (int64_t)kLamX * i;
-        CruCont la;
-        for (int j = 0; j < 4; ++j) {
-            la.c[j] = lx[j];
-            la.L[j] = lx[5 + j] + lc[0];
-            la.rel[j] = 0.0;
-        }
-        la.J = lx[4];
+        CruCont la = lam_after(lx, lc);
         CruAdjIn ai{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         Rec rec[kRec];
         const uint32_t rc = (uint32_t)a.rng_cell[cell];
-        const int n = run_rec(x0, cc, sv, a.seed, rc, (uint32_t)m, (uint64_t)step, a.dt, a.event_cap, 0, 1 << 30,
-                              rec);
+        const int n = run_rec(x0, cc, sv, a.seed, rc, m, (uint64_t)step, a.dt, a.event_cap, 0, 1 << 30, rec);
         for (int blk = (n - 1) / kRec; blk >= 0; --blk) {
             const int lo = blk * kRec, hi = min(n, lo + kRec);
-            if (blk != (n - 1) / kRec)
-                run_rec(x0, cc, sv, a.seed, rc, (uint32_t)m, (uint64_t)step, a.dt, a.event_cap, lo, hi, rec);
-            for (int k = hi - 1; k >= lo; --k) {
-                const Rec &r = rec[k % kRec];
+            if (blk != (n - 1) / kRec) run_rec(x0, cc, sv, a.seed, rc, m, (uint64_t)step, a.dt, a.event_cap, lo, hi, rec);
+            for (int q = hi - 1; q >= lo; --q) {
+                const Rec &r = rec[q % kRec];
                 CruCont s1 = r.s;
                 double jt, jx;
                 cru_substep(s1, r.h, in, P, jt, jx);
                 cru_event_adj(s1, r.ev, r.j, r.onew, in, P, la, ai);
-                const bool last = k == n - 1;
+                const bool last = q == n - 1;
                 cru_substep_adj(r.s, r.h, in, P, last ? lc[1] : 0.0, last ? lc[2] : 0.0, la, ai);
             }
         }
-        CruCont s0;
-        for (int j = 0; j < 4; ++j) {
-            s0.c[j] = x0.cass[j];
-            s0.L[j] = x0.jlcc[j];
-            s0.rel[j] = 0.0;
-        }
-        s0.J = x0.cajsr;
         int o[4];
         open_counts(x0, o);
-        cru_begin_adj(s0, o, P, la, ai);
-        for (int j = 0; j < 4; ++j) {
-            lx[j] = la.c[j];
-            lx[5 + j] = la.L[j];
-        }
-        lx[4] = la.J;
-        acc[0] = ai.Cai;
-        acc[1] = ai.CaNSR;
-        acc[2] = ai.JM;
-        acc[3] = ai.JE;
-        acc[4] = ai.rRyR_rel;
-        acc[5] = ai.CSQN;
+        cru_begin_adj(cont_of(x0), o, P, la, ai);
+        store_adj(la, ai, lx, b.ai_row + (int64_t)kAdjIn * i);
     }
-    block_sum<kAdjIn>(acc, sh);
-    if (threadIdx.x == 0)
-        for (int q = 0; q < kAdjIn; ++q) b.part[(int64_t)blockIdx.x * kAdjIn + q] = acc[q];
 }
 
-// Reverse of the global step `step` for every cell (one thread per cell).
-__global__ void k_global_adj(const GradArgs a, const AdjArgs b, int64_t step, int slot) {
-    const int cell = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    if (cell >= a.n_cells) return;
+// Reverse of the global step `step` (one block per cell): the cell's CRU rows summed in a fixed
+// order, then the adjoint of the global increment by thread 0.
+__global__ void __launch_bounds__(kBlk) k_global_adj(const GradArgs a, const AdjArgs b, int64_t step, int slot) {
+    __shared__ double sh[(kBlk / 32) * kAdjIn];
+    __shared__ double T[kNT];
+    const int cell = blockIdx.x;
+    const int n = a.ncru[cell];
+    const double *rows = b.ai_row + (int64_t)kAdjIn * a.cru0[cell];
+    double ai[kAdjIn] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int m = (int)threadIdx.x; m < n; m += kBlk)
+        for (int q = 0; q < kAdjIn; ++q) ai[q] += rows[(int64_t)kAdjIn * m + q];
+    block_sum<kAdjIn>(ai, sh);
     const CellStatic &C = a.cs[cell];
     const int64_t r = (int64_t)slot * a.n_cells + cell;
     const double *g = a.seg_G + r * kNumGlobals;
+    if (threadIdx.x < kNT) T[threadIdx.x] = glob_term(C, g, (int)threadIdx.x);
+    __syncthreads();
+    if (threadIdx.x != 0) return;
     const double *cyv = a.seg_carry + r * 4;
     const double *sv = a.seg_sv + r * kSvCount;
     const Carry cy{cyv[0], cyv[1], cyv[2], cyv[3]};
-    double ai[kAdjIn] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int k = b.blk0[cell]; k < b.blk0[cell + 1]; ++k)
-        for (int q = 0; q < kAdjIn; ++q) ai[q] += b.part[(int64_t)k * kAdjIn + q];
     double *lgp = b.lam_G + (int64_t)kNumGlobals * cell;
     double lam[kNumGlobals], lg[kNumGlobals];
     for (int k = 0; k < kNumGlobals; ++k) {
@@ -456,7 +560,7 @@ __global__ void k_global_adj(const GradArgs a, const AdjArgs b, int64_t step, in
     double *th = b.lam_th + (int64_t)kTheta * cell;
     double lth[kTheta];
     for (int k = 0; k < kTheta; ++k) lth[k] = th[k];
-    glob_increment_adj(C, g, cy, a.dt, lam, lg, lcy, lth);
+    glob_increment_adj(C, g, cy, a.dt, T, lam, lg, lcy, lth);
     // the CRUs' step inputs: Cai, CaNSR and the JLCC factors of V
     lg[3] += ai[0];
     lg[4] += ai[1];
@@ -469,6 +573,12 @@ __global__ void k_global_adj(const GradArgs a, const AdjArgs b, int64_t step, in
     for (int k = 0; k < kNumGlobals; ++k) lgp[k] = lg[k];
     for (int k = 0; k < 3; ++k) b.lam_cy[3 * (int64_t)cell + k] = lcy[k];
     for (int k = 0; k < kTheta; ++k) th[k] = lth[k];
+}
+
+// SSA constants of every cell, for the kernels whose threads mix cells.
+__global__ void k_init_consts(const CellStatic *cs, dev::SsaConsts<double> *cc, int n_cells) {
+    const int c = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (c < n_cells) dev::load_ssa_consts<double>(cc[c], cs[c]);
 }
 
 int fail_to(std::string &err, int code, const char *fmt, ...) {
@@ -506,6 +616,28 @@ int pack_cru(const double *CaSS, const double *CaJSR, const int32_t *LCC, const 
     return 0;
 }
 
+// Blocks of k_ssa for cells of ncru[] CRUs: a cell gets blocks in proportion to its CRUs, rounded
+// down so that all of them fit the device's `slots` resident blocks in one wave (at least one, at
+// most one per 32 CRUs); block r of bpc takes CRUs [ncru r / bpc, ncru (r + 1) / bpc).
+void plan_blocks(const std::vector<int> &ncru, int slots, std::vector<int> &bc, std::vector<int> &bl,
+                 std::vector<int> &bh) {
+    int64_t total = 0;
+    for (int n : ncru) total += n;
+    bc.clear();
+    bl.clear();
+    bh.clear();
+    for (size_t c = 0; c < ncru.size(); ++c) {
+        const int64_t n = ncru[c];
+        int64_t bpc = (int64_t)((double)slots * (double)n / (double)total);
+        bpc = std::max<int64_t>(1, std::min<int64_t>(bpc, (n + 31) / 32));
+        for (int64_t r = 0; r < bpc; ++r) {
+            bc.push_back((int)c);
+            bl.push_back((int)(n * r / bpc));
+            bh.push_back((int)(n * (r + 1) / bpc));
+        }
+    }
+}
+
 }  // namespace
 
 struct gw_grad {
@@ -513,7 +645,8 @@ struct gw_grad {
     int n_cells = 0;
     int64_t n_crus = 0;
     int n_blocks = 0;
-    std::vector<int> ncru, blk_cell, blk_lo, blk0;
+    int sm_count = 1, slots = 1;  // SMs, and resident k_ssa blocks on the device
+    std::vector<int> ncru, blk_cell, blk_lo, blk_hi, cru_cell;
     std::vector<int64_t> cru0;
     std::vector<CellStatic> cs;
     std::vector<double> stim;
@@ -529,16 +662,16 @@ struct gw_grad {
     gw_grad_stats stats{};
     std::vector<double> G_final;
     // tables
-    Buf d_cs, d_blk_cell, d_blk_lo, d_blk0, d_cru0, d_ncru, d_rng_cell, d_stim;
+    Buf d_cs, d_blk_cell, d_blk_lo, d_blk_hi, d_cru_cell, d_cru0, d_ncru, d_rng_cell, d_stim, d_cc;
     // initial state
     Buf x_init, G_init, carry_init, sv_init;
     // state
     Buf x, out, G, carry, t, sv, status, events, V, regime;
     // checkpoints and segment
     Buf ck_x, ck_G, ck_carry, ck_t, ck_sv;
-    Buf seg_x, seg_G, seg_carry, seg_sv;
+    Buf seg_x, seg_G, seg_carry, seg_sv, quiet, busy, busy_n;
     // adjoint
-    Buf lam_x, lam_G, lam_cy, lam_th, part, dLdV;
+    Buf lam_x, lam_G, lam_cy, lam_th, ai_row, dLdV;
 
     ~gw_grad() {
         if (ev0) cudaEventDestroy(ev0);
@@ -560,6 +693,8 @@ struct gw_grad {
         a.cs = d_cs.as<CellStatic>();
         a.blk_cell = d_blk_cell.as<int>();
         a.blk_lo = d_blk_lo.as<int>();
+        a.blk_hi = d_blk_hi.as<int>();
+        a.cru_cell = d_cru_cell.as<int>();
         a.cru0 = d_cru0.as<int64_t>();
         a.ncru = d_ncru.as<int>();
         a.rng_cell = d_rng_cell.as<int>();
@@ -589,8 +724,8 @@ struct gw_grad {
         b.lam_G = lam_G.as<double>();
         b.lam_cy = lam_cy.as<double>();
         b.lam_th = lam_th.as<double>();
-        b.part = part.as<double>();
-        b.blk0 = d_blk0.as<int>();
+        b.ai_row = ai_row.as<double>();
+        b.cc = d_cc.as<dev::SsaConsts<double>>();
         b.dLdV = dLdV.as<double>();
         return b;
     }
@@ -696,7 +831,6 @@ int gw_grad_create(const gw_grad_desc *d, gw_grad **out) {
     g->cs.resize(d->n_cells);
     g->ncru.resize(d->n_cells);
     g->cru0.resize(d->n_cells);
-    g->blk0.resize(d->n_cells + 1);
     for (int c = 0; c < d->n_cells; ++c) {
         const int n = d->ncru[c];
         if (n < 1) {
@@ -707,13 +841,18 @@ int gw_grad_create(const gw_grad_desc *d, gw_grad **out) {
         g->cru0[c] = g->n_crus;
         g->n_crus += n;
         make_cell_static(d->params[d->params_per_cell ? c : 0], n, g->cs[c]);
-        g->blk0[c] = (int)g->blk_cell.size();
-        for (int lo = 0; lo < n; lo += kBlk) {
-            g->blk_cell.push_back(c);
-            g->blk_lo.push_back(lo);
-        }
+        g->cru_cell.insert(g->cru_cell.end(), (size_t)n, c);
     }
-    g->blk0[d->n_cells] = (int)g->blk_cell.size();
+    {
+        int per_sm = 1;
+        cudaDeviceGetAttribute(&g->sm_count, cudaDevAttrMultiProcessorCount, d->device);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ssa, kBlk, 0) != cudaSuccess) {
+            cudaGetLastError();
+            per_sm = 1;
+        }
+        g->slots = std::max(1, g->sm_count * std::max(1, per_sm));
+    }
+    plan_blocks(g->ncru, g->slots, g->blk_cell, g->blk_lo, g->blk_hi);
     g->n_blocks = (int)g->blk_cell.size();
     std::vector<int> rng_cell(d->n_cells);
     for (int c = 0; c < d->n_cells; ++c) rng_cell[c] = d->cell_base + c;
@@ -727,7 +866,9 @@ int gw_grad_create(const gw_grad_desc *d, gw_grad **out) {
     up(g->d_cs, g->cs.data(), sizeof(CellStatic) * C);
     up(g->d_blk_cell, g->blk_cell.data(), sizeof(int) * g->n_blocks);
     up(g->d_blk_lo, g->blk_lo.data(), sizeof(int) * g->n_blocks);
-    up(g->d_blk0, g->blk0.data(), sizeof(int) * (C + 1));
+    up(g->d_blk_hi, g->blk_hi.data(), sizeof(int) * g->n_blocks);
+    up(g->d_cru_cell, g->cru_cell.data(), sizeof(int) * N);
+    up(g->d_cc, nullptr, sizeof(dev::SsaConsts<double>) * C);
     up(g->d_cru0, g->cru0.data(), sizeof(int64_t) * C);
     up(g->d_ncru, g->ncru.data(), sizeof(int) * C);
     up(g->d_rng_cell, rng_cell.data(), sizeof(int) * C);
@@ -755,22 +896,32 @@ int gw_grad_create(const gw_grad_desc *d, gw_grad **out) {
     up(g->seg_G, nullptr, sizeof(double) * kNumGlobals * C * S);
     up(g->seg_carry, nullptr, sizeof(double) * 4 * C * S);
     up(g->seg_sv, nullptr, sizeof(double) * kSvCount * C * S);
+    up(g->quiet, nullptr, sizeof(uint8_t) * N * S);
+    up(g->busy, nullptr, sizeof(int) * N * S);
+    up(g->busy_n, nullptr, sizeof(int) * S);
     up(g->lam_x, nullptr, sizeof(double) * kLamX * N);
     up(g->lam_G, nullptr, sizeof(double) * kNumGlobals * C);
     up(g->lam_cy, nullptr, sizeof(double) * 3 * C);
     up(g->lam_th, nullptr, sizeof(double) * kTheta * C);
-    up(g->part, nullptr, sizeof(double) * kAdjIn * g->n_blocks);
+    up(g->ai_row, nullptr, sizeof(double) * kAdjIn * N);
     up(g->dLdV, nullptr, sizeof(double) * std::max<int64_t>(1, g->n_samples) * C);
     if (!rc) rc = g->cuda(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking), "gw_grad_create");
     if (!rc) rc = g->cuda(cudaEventCreate(&g->ev0), "gw_grad_create");
     if (!rc) rc = g->cuda(cudaEventCreate(&g->ev1), "gw_grad_create");
+    if (!rc) {
+        k_init_consts<<<(d->n_cells + 127) / 128, 128, 0, g->stream>>>(g->d_cs.as<CellStatic>(),
+                                                                      g->d_cc.as<dev::SsaConsts<double>>(), d->n_cells);
+        rc = g->cuda(cudaGetLastError(), "gw_grad_create");
+        if (!rc) rc = g->cuda(cudaStreamSynchronize(g->stream), "gw_grad_create");
+    }
     if (rc) {
         g_grad_create_error = g->err;
         delete g;
         return rc;
     }
     g->stats.checkpoint_bytes = (int64_t)(g->ck_x.n + g->ck_G.n + g->ck_carry.n + g->ck_t.n + g->ck_sv.n);
-    g->stats.segment_bytes = (int64_t)(g->seg_x.n + g->seg_G.n + g->seg_carry.n + g->seg_sv.n);
+    g->stats.segment_bytes =
+        (int64_t)(g->seg_x.n + g->seg_G.n + g->seg_carry.n + g->seg_sv.n + g->quiet.n + g->busy.n + g->busy_n.n);
     *out = g;
     return GW_OK;
 }
@@ -880,20 +1031,25 @@ int gw_grad_backward(gw_grad *g, const double *dL_dV, double *sens) {
     a.seg_G = g->seg_G.as<double>();
     a.seg_carry = g->seg_carry.as<double>();
     a.seg_sv = g->seg_sv.as<double>();
+    a.quiet = g->quiet.as<uint8_t>();
+    a.busy = g->busy.as<int>();
+    a.busy_n = g->busy_n.as<int>();
     const AdjArgs b = g->adj_args();
-    const int cb = std::min(128, ((g->n_cells + 31) / 32) * 32);
-    const int cg = (g->n_cells + cb - 1) / cb;
+    const int qgrid = (int)((g->n_crus + kBlk - 1) / kBlk);
+    const int bgrid = 2 * g->sm_count;
     cudaEventRecord(g->ev0, g->stream);
     for (int64_t k = g->n_ck - 1; k >= 0; --k) {
         const int64_t s0 = k * g->ck_every, s1 = std::min(s0 + g->ck_every, g->n_steps);
         if ((rc = g->restore(k))) return rc;
+        if ((rc = g->cuda(cudaMemsetAsync(g->busy_n.p, 0, g->busy_n.n, g->stream), "gw_grad_backward"))) return rc;
         for (int64_t s = s0; s < s1; ++s) {
             k_ssa<<<g->n_blocks, kBlk, 0, g->stream>>>(a, s, (int)(s - s0));
             k_global<<<g->n_cells, kBlk, 0, g->stream>>>(a, s, (int)(s - s0), 0);
         }
         for (int64_t s = s1 - 1; s >= s0; --s) {
-            k_cru_adj<<<g->n_blocks, kBlk, 0, g->stream>>>(a, b, s, (int)(s - s0));
-            k_global_adj<<<cg, cb, 0, g->stream>>>(a, b, s, (int)(s - s0));
+            k_cru_busy<<<bgrid, kBlk, 0, g->stream>>>(a, b, s, (int)(s - s0));
+            k_cru_quiet<<<qgrid, kBlk, 0, g->stream>>>(a, b, (int)(s - s0));
+            k_global_adj<<<g->n_cells, kBlk, 0, g->stream>>>(a, b, s, (int)(s - s0));
         }
     }
     cudaEventRecord(g->ev1, g->stream);
@@ -919,7 +1075,7 @@ int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_para
     }
     cudaSetDevice(g->device);
     // tables of the source copies (cell v = a copy of src_cell[v]) and the variants
-    std::vector<int> ncru(n_var), bc, bl, rngc(n_var);
+    std::vector<int> ncru(n_var), bc, bl, bh, rngc(n_var);
     std::vector<int64_t> c0(n_var);
     std::vector<CellStatic> vcs(n_var);
     std::vector<double> stim(4 * (size_t)n_var), vsv(kSvCount * (size_t)n_var);
@@ -932,11 +1088,8 @@ int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_para
         rngc[v] = g->cell_base + s;
         for (int k = 0; k < 4; ++k) stim[4 * v + k] = g->stim[4 * s + k];
         make_cell_static(params[v], ncru[v], vcs[v]);
-        for (int lo = 0; lo < ncru[v]; lo += kBlk) {
-            bc.push_back(v);
-            bl.push_back(lo);
-        }
     }
+    plan_blocks(ncru, g->slots, bc, bl, bh);
     const int nb = (int)bc.size();
     std::vector<CellStatic> scs(n_var);
     for (int v = 0; v < n_var; ++v) scs[v] = g->cs[src_cell[v]];
@@ -958,7 +1111,7 @@ int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_para
         std::memcpy(&sv[kSvCount * (size_t)v], &sv0[kSvCount * (size_t)s], sizeof(double) * kSvCount);
         step_values(vcs[v], &G0[kNumGlobals * (size_t)s], &vsv[kSvCount * (size_t)v]);
     }
-    Buf d_cs, d_vcs, d_bc, d_bl, d_c0, d_n, d_rng, d_stim, x, out, vx, vout, dG, dvG, dcy, dvcy, dt_, dvt, dsv, dvsv,
+    Buf d_cs, d_vcs, d_bc, d_bl, d_bh, d_c0, d_n, d_rng, d_stim, x, out, vx, vout, dG, dvG, dcy, dvcy, dt_, dvt, dsv, dvsv,
         dst, dvst, dV, dreg;
     auto up = [&](Buf &b, const void *src, size_t bytes) {
         if (rc) return;
@@ -969,6 +1122,7 @@ int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_para
     up(d_vcs, vcs.data(), sizeof(CellStatic) * n_var);
     up(d_bc, bc.data(), sizeof(int) * nb);
     up(d_bl, bl.data(), sizeof(int) * nb);
+    up(d_bh, bh.data(), sizeof(int) * nb);
     up(d_c0, c0.data(), sizeof(int64_t) * n_var);
     up(d_n, ncru.data(), sizeof(int) * n_var);
     up(d_rng, rngc.data(), sizeof(int) * n_var);
@@ -1014,6 +1168,7 @@ int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_para
     a.cs = d_cs.as<CellStatic>();
     a.blk_cell = d_bc.as<int>();
     a.blk_lo = d_bl.as<int>();
+    a.blk_hi = d_bh.as<int>();
     a.cru0 = d_c0.as<int64_t>();
     a.ncru = d_n.as<int>();
     a.rng_cell = d_rng.as<int>();

@@ -44,6 +44,103 @@ struct Carry {
 GW_HD double sqd(double x) { return x * x; }
 GW_HD double cubed(double x) { return x * x * x; }
 
+// The transcendental terms of one global increment, each a function of the globals alone.  The
+// increment and its adjoint read them from T[]; a block may evaluate them on kNT threads at once
+// (on GB300 an FP64 instruction costs a sub-partition the same time for 1 or 32 active lanes) and
+// pass them in: the values are the same bit for bit as one thread's.
+enum Term {
+    T_E = 0,    // exp(-V F/RT)
+    T_LNA,      // log(Nao / Nai)
+    T_LK,       // log(Ko / Ki)
+    T_E1,       // exp(eta V F/RT)
+    T_ENAK,     // exp(-0.1 V F/RT)
+    T_PNAK,     // pow(KmNai / Nai, 1.5)
+    T_RKR,      // exp(0.0446 V)
+    T_LKS,      // log((Ko + 0.01833 Nao) / (Ki + 0.01833 Nai))
+    T_K1,       // exp(1.5 (V - EK) F/RT)
+    T_KP,       // exp((7.488 - V) / 5.98)
+    T_FU,       // pow(Cai / Kmf, Hf)
+    T_RU,       // pow(CaNSR / Kmr, Hr)
+    T_AM,       // exp(-0.1 (V + 47.13))
+    T_BM,       // exp(-V / 11)
+    T_BH_HI,    // V >= -40: exp(-(V + 10.66) / 11.1)
+    T_BJ_HI_Z,  //           exp(-0.1 (V + 32))
+    T_BJ_HI_Y,  //           exp(-2.535e-7 V)
+    T_AH_LO,    // V < -40:  exp(-(V + 80) / 6.8)
+    T_BH_LO_1,  //           exp(0.079 V)
+    T_BH_LO_2,  //           exp(0.35 V)
+    T_AJ_A,     //           exp(0.2444 V)
+    T_AJ_B,     //           exp(-0.04391 V)
+    T_AJ_D,     //           exp(0.311 (V + 79.23))
+    T_BJ_LO_Z,  //           exp(-0.1378 (V + 40.14))
+    T_BJ_LO_Y,  //           exp(-0.01052 V)
+    T_XINF,     // exp(-(V - 24.7) / 13.6)
+    T_TAU1,     // exp(-0.148 (V - 10))
+    T_TAU2,     // exp(0.0687 (V - 10))
+    T_KR,       // 7 terms of the IKr chain: q01 q10 q23 q24 q32 q34 q43 without their prefactors
+    T_KV14 = T_KR + 7,   // aa, ai, ba, bi of Kv1.4 without their prefactors
+    T_KV43 = T_KV14 + 4,  // the same for Kv4.3
+    kNT = T_KV43 + 4
+};
+
+GW_HD double glob_term(const CellStatic &C, const double *g, int k) {
+    const gw_params &p = C.p;
+    const double V = g[0];
+    switch (k) {
+    case T_E: return exp(-(V * C.F_RT));
+    case T_LNA: return log(p.Nao / g[1]);
+    case T_LK: return log(p.Ko / g[2]);
+    case T_E1: return exp(p.eta * (V * C.F_RT));
+    case T_ENAK: return exp(-0.1 * (V * C.F_RT));
+    case T_PNAK: return pow(p.KmNai / g[1], 1.5);
+    case T_RKR: return exp(0.0446 * V);
+    case T_LKS: return log((p.Ko + 0.01833 * p.Nao) / (g[2] + 0.01833 * g[1]));
+    case T_K1: {
+        const double EK = log(p.Ko / g[2]) * C.RT_F / 1.0;
+        return exp(1.5 * (V - EK) * C.F_RT);
+    }
+    case T_KP: return exp((7.488 - V) / 5.98);
+    case T_FU: return pow(g[3] / p.Kmf, p.Hf);
+    case T_RU: return pow(g[4] / p.Kmr, p.Hr);
+    case T_AM: return exp(-0.1 * (V + 47.13));
+    case T_BM: return exp(-V / 11.0);
+    case T_BH_HI: return exp(-(V + 10.66) / 11.1);
+    case T_BJ_HI_Z: return exp(-0.1 * (V + 32.0));
+    case T_BJ_HI_Y: return exp(-2.535e-7 * V);
+    case T_AH_LO: return exp(-(V + 80.0) / 6.8);
+    case T_BH_LO_1: return exp(0.079 * V);
+    case T_BH_LO_2: return exp(0.35 * V);
+    case T_AJ_A: return exp(0.2444 * V);
+    case T_AJ_B: return exp(-0.04391 * V);
+    case T_AJ_D: return exp(0.311 * (V + 79.23));
+    case T_BJ_LO_Z: return exp(-0.1378 * (V + 40.14));
+    case T_BJ_LO_Y: return exp(-0.01052 * V);
+    case T_XINF: return exp(-(V - 24.7) / 13.6);
+    case T_TAU1: return exp(-0.148 * (V - 10.0));
+    case T_TAU2: return exp(0.0687 * (V - 10.0));
+    case T_KR + 0: return exp(0.0272 * V);
+    case T_KR + 1: return exp(-0.0431 * V);
+    case T_KR + 2: return exp(0.0262 * V);
+    case T_KR + 3: return exp(2.71e-6 * V);
+    case T_KR + 4: return exp(-0.0269 * V);
+    case T_KR + 5: return exp(0.0120 * V);
+    case T_KR + 6: return exp(-0.0443 * V);
+    case T_KV14 + 0: return exp(p.aaKv14 * V);
+    case T_KV14 + 1: return exp(-p.aiKv14 * V);
+    case T_KV14 + 2: return exp(-p.baKv14 * V);
+    case T_KV14 + 3: return exp(p.biKv14 * V);
+    case T_KV43 + 0: return exp(p.aaKv43 * V);
+    case T_KV43 + 1: return exp(-p.aiKv43 * V);
+    case T_KV43 + 2: return exp(-p.baKv43 * V);
+    case T_KV43 + 3: return exp(p.biKv43 * V);
+    default: return 0.0;
+    }
+}
+
+GW_HD void glob_terms(const CellStatic &C, const double *g, double *T) {
+    for (int k = 0; k < kNT; ++k) T[k] = glob_term(C, g, k);
+}
+
 // ---------------------------------------------------------------------------------------------
 // The global increment d = G[s+1] - G[s] (update_V_and_concentration_derivatives GW.tpp:171-212,
 // update_gate_derivatives :163-168, update_Kr/Kv_derivatives :127-160 with update_QKr/QKv
@@ -51,17 +148,17 @@ GW_HD double cubed(double x) { return x * x * x; }
 // ---------------------------------------------------------------------------------------------
 
 // Rates of the Kv1.4 / Kv4.3 chains (update_QKv, GW.tpp:65-123): aa, ai, ba, bi.
-GW_HD void kv_rates(const gw_params &p, int ch, double V, double r[4]) {
+GW_HD void kv_rates(const gw_params &p, int ch, const double *T, double r[4]) {
     if (ch == 0) {
-        r[0] = p.alphaa0Kv14 * exp(p.aaKv14 * V);
-        r[1] = p.alphai0Kv14 * exp(-p.aiKv14 * V);
-        r[2] = p.betaa0Kv14 * exp(-p.baKv14 * V);
-        r[3] = p.betai0Kv14 * exp(p.biKv14 * V);
+        r[0] = p.alphaa0Kv14 * T[T_KV14 + 0];
+        r[1] = p.alphai0Kv14 * T[T_KV14 + 1];
+        r[2] = p.betaa0Kv14 * T[T_KV14 + 2];
+        r[3] = p.betai0Kv14 * T[T_KV14 + 3];
     } else {
-        r[0] = p.alphaa0Kv43 * exp(p.aaKv43 * V);
-        r[1] = p.alphai0Kv43 * exp(-p.aiKv43 * V);
-        r[2] = p.betaa0Kv43 * exp(-p.baKv43 * V);
-        r[3] = p.betai0Kv43 * exp(p.biKv43 * V);
+        r[0] = p.alphaa0Kv43 * T[T_KV43 + 0];
+        r[1] = p.alphai0Kv43 * T[T_KV43 + 1];
+        r[2] = p.betaa0Kv43 * T[T_KV43 + 2];
+        r[3] = p.betai0Kv43 * T[T_KV43 + 3];
     }
 }
 
@@ -92,9 +189,9 @@ GW_HD void kv_edges(const gw_params &p, int ch, KvEdge e[26]) {
 }
 
 // Q matrix of one Kv chain in the reference's arithmetic (fill order of update_QKv).
-GW_HD void kv_matrix(const gw_params &p, int ch, double V, double Q[10][10]) {
+GW_HD void kv_matrix(const gw_params &p, int ch, const double *T, double Q[10][10]) {
     double r[4];
-    kv_rates(p, ch, V, r);
+    kv_rates(p, ch, T, r);
     const double aa = r[0], ai = r[1], ba = r[2], bi = r[3];
     const double f1 = ch == 0 ? p.f1Kv14 : p.f1Kv43, f2 = ch == 0 ? p.f2Kv14 : p.f2Kv43;
     const double f3 = ch == 0 ? p.f3Kv14 : p.f3Kv43, f4 = ch == 0 ? p.f4Kv14 : p.f4Kv43;
@@ -134,15 +231,15 @@ GW_HD void kv_deriv(const double Q[10][10], const double *x, double *d, double d
 struct KrQ {
     double q01, q10, q23, q24, q32, q34, q43, q42;
 };
-GW_HD KrQ kr_q(double V) {
+GW_HD KrQ kr_q(const double *T) {
     KrQ q;
-    q.q01 = 0.0069 * exp(0.0272 * V);
-    q.q10 = 0.0227 * exp(-0.0431 * V);
-    q.q23 = 0.0218 * exp(0.0262 * V);
-    q.q24 = 1.29e-5 * exp(2.71e-6 * V);
-    q.q32 = 0.0009 * exp(-0.0269 * V);
-    q.q34 = 0.0622 * exp(0.0120 * V);
-    q.q43 = 0.0059 * exp(-0.0443 * V);
+    q.q01 = 0.0069 * T[T_KR + 0];
+    q.q10 = 0.0227 * T[T_KR + 1];
+    q.q23 = 0.0218 * T[T_KR + 2];
+    q.q24 = 1.29e-5 * T[T_KR + 3];
+    q.q32 = 0.0009 * T[T_KR + 4];
+    q.q34 = 0.0622 * T[T_KR + 5];
+    q.q43 = 0.0059 * T[T_KR + 6];
     q.q42 = q.q32 * q.q43 * q.q24 / (q.q23 * q.q34);
     return q;
 }
@@ -154,48 +251,48 @@ struct Gates {
     double am, bm, ah, bh, aj, bj, xinf, tinv;
     double dam, dbm, dah, dbh, daj, dbj, dxinf, dtinv;
 };
-GW_HD Gates gate_rates(double V, bool derivs) {
+GW_HD Gates gate_rates(double V, bool derivs, const double *T) {
     Gates r{};
     const bool hi = V >= -40.0;
     {
-        const double w = V + 47.13, E = exp(-0.1 * w);
+        const double w = V + 47.13, E = T[T_AM];
         r.am = (V == -47.13) ? 3.2 : 0.32 * w / (1.0 - E);
         if (derivs) r.dam = (V == -47.13) ? 0.16 : 0.32 * ((1.0 - E) - w * 0.1 * E) / sqd(1.0 - E);
     }
-    r.bm = 0.08 * exp(-V / 11.0);
+    r.bm = 0.08 * T[T_BM];
     r.dbm = -r.bm / 11.0;
     if (hi) {
         r.ah = 0.0;
-        const double X = exp(-(V + 10.66) / 11.1);
+        const double X = T[T_BH_HI];
         r.bh = 1.0 / (0.13 * (1.0 + X));
         r.dbh = r.bh * X / (11.1 * (1.0 + X));
         r.aj = 0.0;
-        const double Z = exp(-0.1 * (V + 32.0)), y0 = 0.3 * exp(-2.535e-7 * V);
+        const double Z = T[T_BJ_HI_Z], y0 = 0.3 * T[T_BJ_HI_Y];
         r.bj = y0 / (1.0 + Z);
         r.dbj = r.bj * (-2.535e-7 + 0.1 * Z / (1.0 + Z));
     } else {
-        r.ah = 0.135 * exp(-(V + 80.0) / 6.8);
+        r.ah = 0.135 * T[T_AH_LO];
         r.dah = -r.ah / 6.8;
-        const double e1 = exp(0.079 * V), e2 = exp(0.35 * V);
+        const double e1 = T[T_BH_LO_1], e2 = T[T_BH_LO_2];
         r.bh = 3.56 * e1 + 3.1e5 * e2;
         r.dbh = 3.56 * 0.079 * e1 + 3.1e5 * 0.35 * e2;
-        const double ea = exp(0.2444 * V), eb = exp(-0.04391 * V);
+        const double ea = T[T_AJ_A], eb = T[T_AJ_B];
         const double P = -127140.0 * ea - 3.474e-5 * eb, Qv = V + 37.78;
-        const double D = 1.0 + exp(0.311 * (V + 79.23));
+        const double D = 1.0 + T[T_AJ_D];
         r.aj = P * Qv / D;
         const double dP = -127140.0 * 0.2444 * ea + 3.474e-5 * 0.04391 * eb, dD = 0.311 * (D - 1.0);
         r.daj = (dP * Qv + P) / D - P * Qv * dD / sqd(D);
-        const double Z = exp(-0.1378 * (V + 40.14)), y0 = 0.1212 * exp(-0.01052 * V);
+        const double Z = T[T_BJ_LO_Z], y0 = 0.1212 * T[T_BJ_LO_Y];
         r.bj = y0 / (1.0 + Z);
         r.dbj = r.bj * (-0.01052 + 0.1378 * Z / (1.0 + Z));
     }
     {
-        const double X = exp(-(V - 24.7) / 13.6);
+        const double X = T[T_XINF];
         r.xinf = 1.0 / (1.0 + X);
         r.dxinf = r.xinf * r.xinf * X / 13.6;
     }
     {
-        const double u = V - 10.0, E1 = exp(-0.148 * u), E2 = exp(0.0687 * u);
+        const double u = V - 10.0, E1 = T[T_TAU1], E2 = T[T_TAU2];
         r.tinv = 0.0000719 * u / (1.0 - E1) + 0.000131 * u / (E2 - 1.0);
         r.dtinv = 0.0000719 * ((1.0 - E1) - u * 0.148 * E1) / sqd(1.0 - E1) +
                   0.000131 * ((E2 - 1.0) - u * 0.0687 * E2) / sqd(E2 - 1.0);
@@ -203,42 +300,43 @@ GW_HD Gates gate_rates(double V, bool derivs) {
     return r;
 }
 
-// The global increment (the same formulas and order as the reference).  Returns false for a
-// non-positive Nernst argument, where the reference exits (common.hpp:72-75).
+// The global increment (the same formulas and order as the reference), from the globals g and
+// their terms T (glob_terms).  Returns false for a non-positive Nernst argument, where the
+// reference exits (common.hpp:72-75).
 GW_HD bool glob_increment(const CellStatic &C, const double *g, const Carry &cy, double Istim, double dt,
-                          double *d) {
+                          const double *T, double *d) {
     const gw_params &p = C.p;
     const double V = g[0], Nai = g[1], Ki = g[2], Cai = g[3], CaNSR = g[4], CaLT = g[5], CaHT = g[6];
     const double m = g[7], h = g[8], jg = g[9], xKs = g[10];
     const double *Kr = g + 11, *Kv43 = g + 16, *Kv14 = g + 26;
     if (!(Nai > 0.0) || !(Ki > 0.0)) return false;
-    const double VF_RT = V * C.F_RT, e = exp(-VF_RT);
-    const double ENa = log(p.Nao / Nai) * C.RT_F / 1.0;
-    const double EK = log(p.Ko / Ki) * C.RT_F / 1.0;
-    const double ECa = log(p.Ko / Ki) * C.RT_F / 2.0;
+    const double VF_RT = V * C.F_RT, e = T[T_E];
+    const double ENa = T[T_LNA] * C.RT_F / 1.0;
+    const double EK = T[T_LK] * C.RT_F / 1.0;
+    const double ECa = T[T_LK] * C.RT_F / 2.0;
     const double INa = p.GNa * cubed(m) * h * jg * (V - ENa);
     const double INab = p.GNab * (V - ENa);
-    const double e1 = exp(p.eta * VF_RT), e2 = e1 * e;
+    const double e1 = T[T_E1], e2 = e1 * e;
     const double INaCa = C.INaCa_const * (e1 * cubed(Nai) * p.Cao - e2 * C.Nao3 * Cai) / (1.0 + p.ksat * e2);
-    const double fNaK = 1.0 / (1.0 + 0.1245 * exp(-0.1 * VF_RT) + 0.0365 * C.sigma * e);
-    const double INaK = C.INaK_const * fNaK / (1.0 + pow(p.KmNai / Nai, 1.5));
-    const double RKr = 1.0 / (1.0 + 1.4945 * exp(0.0446 * V));
+    const double fNaK = 1.0 / (1.0 + 0.1245 * T[T_ENAK] + 0.0365 * C.sigma * e);
+    const double INaK = C.INaK_const * fNaK / (1.0 + T[T_PNAK]);
+    const double RKr = 1.0 / (1.0 + 1.4945 * T[T_RKR]);
     const double IKr = p.GKr * C.sqrtKo * RKr * Kr[3] * (V - EK) * 0.5;
-    const double EKs = log((p.Ko + 0.01833 * p.Nao) / (Ki + 0.01833 * Nai)) * C.RT_F;
+    const double EKs = T[T_LKS] * C.RT_F;
     const double IKs = p.GKs * sqd(xKs) * (V - EKs);
     const double mm = C.PKv14_Csc * (kFaradayA * VF_RT) * Kv14[4] / (1 - e);
     const double IKv14 = mm * ((Ki - p.Ko * e) + 0.02 * (Nai - p.Nao * e)) * 1.0e9;
     const double IKv43 = p.GKv43 * Kv43[4] * (V - EK);
     const double Ito1 = IKv14 + IKv43;
     const double Ito2 = cy.clch * C.Ito2_const * VF_RT * (p.Clcyto * e - p.Clo) / (e - 1.0);
-    const double K1inf = 1.0 / (2.0 + exp(1.5 * (V - EK) * C.F_RT));
+    const double K1inf = 1.0 / (2.0 + T[T_K1]);
     const double IK1 = p.GK1 * K1inf * C.IK1_const * (V - EK);
-    const double Kp = 1. / (1. + exp((7.488 - V) / 5.98));
+    const double Kp = 1. / (1. + T[T_KP]);
     const double IKp = p.GKp * Kp * (V - EK);
     const double ICaL = cy.jlcc * C.ICaL_const;
     const double ICab = p.GCab * (V - ECa);
     const double IpCa = p.IpCamax * (Cai / (p.KmpCa + Cai));
-    const double fu = pow(Cai / p.Kmf, p.Hf), ru = pow(CaNSR / p.Kmr, p.Hr);
+    const double fu = T[T_FU], ru = T[T_RU];
     const double Jup = (p.Vmaxf * fu - p.Vmaxr * ru) / (1.0 + fu + ru);
     const double Jtr_tot = cy.jtr * C.CRU_factor, Jxfer_tot = cy.jxfer * C.CRU_factor;
     const double beta_cyto = 1.0 / (1.0 + C.CMDN_const / sqd(p.KCMDN + Cai));
@@ -252,12 +350,12 @@ GW_HD bool glob_increment(const CellStatic &C, const double *g, const Carry &cy,
     d[5] = dLT * dt;
     d[6] = dHT * dt;
     d[0] = dt * (Istim - (INa + ICaL + IKr + IKs + Ito1 + IK1 + IKp + Ito2 + INaK + INaCa + IpCa + ICab + INab));
-    const Gates gr = gate_rates(V, false);
+    const Gates gr = gate_rates(V, false, T);
     d[7] = dt * (gr.am * (1.0 - m) - gr.bm * m);
     d[8] = dt * (gr.ah * (1.0 - h) - gr.bh * h);
     d[9] = dt * (gr.aj * (1.0 - jg) - gr.bj * jg);
     d[10] = dt * (gr.xinf - xKs) * gr.tinv;
-    const KrQ q = kr_q(V);
+    const KrQ q = kr_q(T);
     const double Q00 = -q.q01, Q11 = -(q.q10 + p.Kf), Q22 = -(p.Kb + q.q23 + q.q24), Q33 = -(q.q32 + q.q34);
     const double Q44 = -(q.q42 + q.q43);
     d[11] = dt * (q.q10 * Kr[1] + Q00 * Kr[0]);
@@ -266,9 +364,9 @@ GW_HD bool glob_increment(const CellStatic &C, const double *g, const Carry &cy,
     d[14] = dt * (q.q23 * Kr[2] + q.q43 * Kr[4] + Q33 * Kr[3]);
     d[15] = dt * (q.q24 * Kr[2] + q.q34 * Kr[3] + Q44 * Kr[4]);
     double Q[10][10];
-    kv_matrix(p, 1, V, Q);
+    kv_matrix(p, 1, T, Q);
     kv_deriv(Q, Kv43, d + 16, dt);
-    kv_matrix(p, 0, V, Q);
+    kv_matrix(p, 0, T, Q);
     kv_deriv(Q, Kv14, d + 26, dt);
     return true;
 }
@@ -276,13 +374,25 @@ GW_HD bool glob_increment(const CellStatic &C, const double *g, const Carry &cy,
 // Per-step SSA values of a state (the lane's sv[], gw_internal.h SvIndex) in the reference's
 // arithmetic: update_LCC_rates (GW_utils.tpp:118-186), update_LCC_inactivation_rates
 // (GW_utils.hpp:378-383) and the JLCC factors (GW.tpp:216-221).
-GW_HD void step_values(const CellStatic &C, const double *g, double *sv) {
+// Their transcendental terms, by index (as glob_term).
+enum SvTerm { S_E = 0, S_AL, S_BE, S_Y, S_TAU, kNS };
+GW_HD double sv_term(const CellStatic &C, const double *g, int k) {
     const double V = g[0];
-    const double e = exp(-(V * C.F_RT));
-    const double al = 2.0 * exp(0.012 * (V - 35.0));
-    const double be = 0.0882 * exp(-0.05 * (V - 35.0));
-    const double yinf = 0.4 / (1.0 + exp((V + 12.5) / 5.0)) + 0.6;
-    const double tau = 340.0 / (1.0 + exp((V + 30.0) / 12.0)) + 60.0;
+    switch (k) {
+    case S_E: return exp(-(V * C.F_RT));
+    case S_AL: return exp(0.012 * (V - 35.0));
+    case S_BE: return exp(-0.05 * (V - 35.0));
+    case S_Y: return exp((V + 12.5) / 5.0);
+    default: return exp((V + 30.0) / 12.0);
+    }
+}
+GW_HD void step_values(const CellStatic &C, const double *g, const double *S, double *sv) {
+    const double V = g[0];
+    const double e = S[S_E];
+    const double al = 2.0 * S[S_AL];
+    const double be = 0.0882 * S[S_BE];
+    const double yinf = 0.4 / (1.0 + S[S_Y]) + 0.6;
+    const double tau = 340.0 / (1.0 + S[S_TAU]) + 60.0;
     const double JE = sqd(1.0 / e);
     for (int i = 0; i < kSvCount; ++i) sv[i] = 0.0;
     sv[SV_A4] = 4 * al; sv[SV_A3] = 3 * al; sv[SV_A2] = 2 * al; sv[SV_A1] = al;
@@ -301,6 +411,18 @@ GW_HD void step_values(const CellStatic &C, const double *g, double *sv) {
     sv[SV_CANSR] = g[4];
 }
 
+// The same with the terms evaluated here, one after the other.
+GW_HD bool glob_increment(const CellStatic &C, const double *g, const Carry &cy, double Istim, double dt, double *d) {
+    double T[kNT];
+    glob_terms(C, g, T);
+    return glob_increment(C, g, cy, Istim, dt, T, d);
+}
+GW_HD void step_values(const CellStatic &C, const double *g, double *sv) {
+    double S[kNS];
+    for (int k = 0; k < kNS; ++k) S[k] = sv_term(C, g, k);
+    step_values(C, g, S, sv);
+}
+
 // dJM/dV and dJE/dV of the JLCC factors: JE = exp(2 V F/RT), JM = JLCC_const V F/RT / (JE - 1).
 GW_HD void jlcc_factor_derivs(const CellStatic &C, double V, double JE, double &dJM, double &dJE) {
     dJE = 2.0 * C.F_RT * JE;
@@ -310,8 +432,8 @@ GW_HD void jlcc_factor_derivs(const CellStatic &C, double V, double JE, double &
 // The adjoint of one global increment: with lam = dL/dG[s+1] and G[s+1] = G[s] + d, adds
 // dL/dG[s] (the identity included) to lam_g, dL/d(carry jlcc, jtr, jxfer) to lam_cy[0..2] and the
 // relative sensitivities of GKr, GKs, GK1, INaKmax and Vmax to lam_th.
-GW_HD void glob_increment_adj(const CellStatic &C, const double *g, const Carry &cy, double dt, const double *lam,
-                              double *lam_g, double *lam_cy, double *lam_th) {
+GW_HD void glob_increment_adj(const CellStatic &C, const double *g, const Carry &cy, double dt, const double *T,
+                              const double *lam, double *lam_g, double *lam_cy, double *lam_th) {
     const gw_params &p = C.p;
     const double V = g[0], Nai = g[1], Ki = g[2], Cai = g[3], CaNSR = g[4], CaLT = g[5], CaHT = g[6];
     const double m = g[7], h = g[8], jg = g[9], xKs = g[10];
@@ -319,28 +441,28 @@ GW_HD void glob_increment_adj(const CellStatic &C, const double *g, const Carry 
     for (int i = 0; i < kNumGlobals; ++i) lam_g[i] += lam[i];
     // forward values
     const double F_RT = C.F_RT, RT_F = C.RT_F;
-    const double VF_RT = V * F_RT, e = exp(-VF_RT);
-    const double ENa = log(p.Nao / Nai) * RT_F, EK = log(p.Ko / Ki) * RT_F, ECa = log(p.Ko / Ki) * RT_F / 2.0;
+    const double VF_RT = V * F_RT, e = T[T_E];
+    const double ENa = T[T_LNA] * RT_F, EK = T[T_LK] * RT_F, ECa = T[T_LK] * RT_F / 2.0;
     const double m3hj = cubed(m) * h * jg;
-    const double e1 = exp(p.eta * VF_RT), e2 = e1 * e;
+    const double e1 = T[T_E1], e2 = e1 * e;
     const double numNC = e1 * cubed(Nai) * p.Cao - e2 * C.Nao3 * Cai, denNC = 1.0 + p.ksat * e2;
     const double INaCa = C.INaCa_const * numNC / denNC;
-    const double E1k = exp(-0.1 * VF_RT);
+    const double E1k = T[T_ENAK];
     const double fNaK = 1.0 / (1.0 + 0.1245 * E1k + 0.0365 * C.sigma * e);
-    const double qNaK = 1.0 + pow(p.KmNai / Nai, 1.5);
+    const double qNaK = 1.0 + T[T_PNAK];
     const double INaK = C.INaK_const * fNaK / qNaK;
-    const double ERk = exp(0.0446 * V), RKr = 1.0 / (1.0 + 1.4945 * ERk);
+    const double ERk = T[T_RKR], RKr = 1.0 / (1.0 + 1.4945 * ERk);
     const double IKr = p.GKr * C.sqrtKo * RKr * Kr[3] * (V - EK) * 0.5;
     const double sKs = Ki + 0.01833 * Nai;
-    const double EKs = log((p.Ko + 0.01833 * p.Nao) / sKs) * RT_F;
+    const double EKs = T[T_LKS] * RT_F;
     const double IKs = p.GKs * sqd(xKs) * (V - EKs);
     const double P14 = C.PKv14_Csc * kFaradayA;
     const double A14 = (Ki - p.Ko * e) + 0.02 * (Nai - p.Nao * e);
     const double mm = P14 * VF_RT * Kv14[4] / (1 - e);
-    const double uK1 = V - EK, EK1 = exp(1.5 * uK1 * F_RT), K1inf = 1.0 / (2.0 + EK1);
+    const double uK1 = V - EK, EK1 = T[T_K1], K1inf = 1.0 / (2.0 + EK1);
     const double IK1 = p.GK1 * K1inf * C.IK1_const * uK1;
-    const double EKp = exp((7.488 - V) / 5.98), Kp = 1. / (1. + EKp);
-    const double fu = pow(Cai / p.Kmf, p.Hf), ru = pow(CaNSR / p.Kmr, p.Hr), den = 1.0 + fu + ru;
+    const double EKp = T[T_KP], Kp = 1. / (1. + EKp);
+    const double fu = T[T_FU], ru = T[T_RU], den = 1.0 + fu + ru;
     const double Jup = (p.Vmaxf * fu - p.Vmaxr * ru) / den;
     const double Jxfer_tot = cy.jxfer * C.CRU_factor;
     const double beta = 1.0 / (1.0 + C.CMDN_const / sqd(p.KCMDN + Cai));
@@ -402,7 +524,7 @@ GW_HD void glob_increment_adj(const CellStatic &C, const double *g, const Carry 
     {
         const double lf = lINaK * C.INaK_const / qNaK;
         const double lq = -lINaK * INaK / qNaK;
-        lNai += lq * (-1.5 * pow(p.KmNai / Nai, 1.5) / Nai);
+        lNai += lq * (-1.5 * T[T_PNAK] / Nai);
         const double lD = -lf * sqd(fNaK);
         lVF += lD * 0.1245 * (-0.1) * E1k;
         le += lD * 0.0365 * C.sigma;
@@ -486,7 +608,7 @@ GW_HD void glob_increment_adj(const CellStatic &C, const double *g, const Carry 
     lKi += lEK * (-RT_F / Ki) + lECa * (-RT_F / (2.0 * Ki));
     // gates
     {
-        const Gates gr = gate_rates(V, true);
+        const Gates gr = gate_rates(V, true, T);
         lam_g[7] += lam[7] * dt * (-gr.am - gr.bm);
         lam_g[8] += lam[8] * dt * (-gr.ah - gr.bh);
         lam_g[9] += lam[9] * dt * (-gr.aj - gr.bj);
@@ -498,7 +620,7 @@ GW_HD void glob_increment_adj(const CellStatic &C, const double *g, const Carry 
     }
     // IKr chain: d_k = dt (sum over edges a->b of q x_a into b, minus out of a)
     {
-        const KrQ q = kr_q(V);
+        const KrQ q = kr_q(T);
         const double *l = lam + 11;
         double *lx = lam_g + 11;
         double lq01 = 0, lq10 = 0, lq23 = 0, lq24 = 0, lq32 = 0, lq34 = 0, lq43 = 0, lq42 = 0;
@@ -532,7 +654,7 @@ GW_HD void glob_increment_adj(const CellStatic &C, const double *g, const Carry 
         const double *l = lam + (ch == 0 ? 26 : 16);
         double *lx = lam_g + (ch == 0 ? 26 : 16);
         double r[4], lr[4] = {0, 0, 0, 0};
-        kv_rates(p, ch, V, r);
+        kv_rates(p, ch, T, r);
         KvEdge E[26];
         kv_edges(p, ch, E);
         for (int k = 0; k < 26; ++k) {
@@ -711,6 +833,14 @@ GW_HD void cru_begin_adj(const CruCont &s0, const int o[4], const CruPar &P, Cru
         la.c[j] -= l * k;
         la.rel[j] = 0.0;
     }
+}
+
+// glob_increment_adj with the terms evaluated here.
+GW_HD void glob_increment_adj(const CellStatic &C, const double *g, const Carry &cy, double dt, const double *lam,
+                              double *lam_g, double *lam_cy, double *lam_th) {
+    double T[kNT];
+    glob_terms(C, g, T);
+    glob_increment_adj(C, g, cy, dt, T, lam, lam_g, lam_cy, lam_th);
 }
 
 }  // namespace adj
