@@ -66,10 +66,14 @@ METRIC = "CRU-steps/s and sim-ms/wall-s: batched vs plain GPU vs CPU, at KS/FP64
 # JLCC 16 B, CaJSR 4 B, CaJSR compensation 4 B = 72 B, read and written once per CRU-step.
 BYTES_PER_CRU_STEP = 2 * 72
 # From the ncu captures of the engine kernel on this workload (profiles/engine_kernel_cell12500.txt
-# and profiles/engine_kernel_cell12500_instmix.txt): DRAM bytes (read + write) of one 1000-step
-# launch, and warp instructions issued per CRU-step.
-TRAFFIC_PER_LAUNCH = 1.047296e6
-WARP_INST_PER_CRU_STEP = 28.4
+# and profiles/engine_kernel_cell12500_instmix.txt, the launch at 0-1 ms of the beat): DRAM bytes
+# (read + write) of one 1000-step launch, and warp instructions issued per CRU-step.
+TRAFFIC_PER_LAUNCH = 1.05472e6
+WARP_INST_PER_CRU_STEP = 31.25
+# The same for config 3's ensemble kernel (profiles/engine_kernel_batched256.txt, one 100-step launch
+# at 20 ms): DRAM bytes per launch and CRU, and warp instructions per CRU-step.
+BATCHED_TRAFFIC_PER_LAUNCH_CRU = 213.9e6 / 1870540
+BATCHED_WARP_INST_PER_CRU_STEP = 38.8
 CPU_PRE_NCRU = 1250   # the CPU's beat run, tiled x10 to 12,500 CRUs at each window start
 
 
@@ -87,9 +91,13 @@ def parse():
                     help="only run config 4 (32 cells x 5,000 CRUs, adjoint of a V-trace MSE) over MS ms after "
                          "one stimulus and print its timing as one JSON line")
     ap.add_argument("--config4-cells", type=int, default=32)
+    ap.add_argument("--config4-checkpoint", type=int, default=200, help="global steps between adjoint checkpoints")
     ap.add_argument("--profile-batched", type=int, default=0, metavar="LAUNCHES",
                     help="only run config 3's ensemble with 100 steps per launch: 200 launches (0-20 ms), then "
                          "LAUNCHES more (the launches an ncu capture takes)")
+    ap.add_argument("--ks-full-cells", type=float, default=0.0, metavar="MS",
+                    help="only run the FP32 vs FP64 KS comparison of 200 replicate 12,500-CRU cells over the "
+                         "first MS ms after a stimulus and print it as one JSON line")
     ap.add_argument("--config5-accuracy", type=int, default=0, metavar="BEATS",
                     help="only run config 5's FP32 vs FP64 APD90 / peak-Cai comparison over BEATS beats at 2 Hz "
                          "(64 cells) and print it as one JSON line")
@@ -298,10 +306,14 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     if args.config4:
-        print(json.dumps({"config4": config4_measure(0, args.config4, args.config4_cells)}), flush=True)
+        print(json.dumps({"config4": config4_measure(0, args.config4, args.config4_cells,
+                                                     checkpoint_every=args.config4_checkpoint)}), flush=True)
         return 0
     if args.profile_batched:
         profile_batched(0, args.profile_batched)
+        return 0
+    if args.ks_full_cells:
+        print(json.dumps({"ks_full_cells": ks_full_cells(0, t_ms=args.ks_full_cells)}), flush=True)
         return 0
     if args.config5_accuracy:
         print(json.dumps({"config5_accuracy": config5_accuracy(0, beats=args.config5_accuracy)}), flush=True)
@@ -481,6 +493,12 @@ def batched_measure(device, window_ms=400.0, cluster_ctas="auto"):
             "wall_cru_steps_per_s": total / wall, "cells": len(ncru), "crus": int(ncru.sum()),
             "algorithmic_GBps": total * BYTES_PER_CRU_STEP / kern / 1e9,
             "autotuned": cluster_ctas == "auto", "tuned_us_per_step": e.tuned_us_per_step,
+            "issue_roofline": {"warp_inst_per_cru_step": BATCHED_WARP_INST_PER_CRU_STEP,
+                               "frac_gpu": BATCHED_WARP_INST_PER_CRU_STEP * total / kern / (152 * 4 * 2.07e9),
+                               "note": "warp instructions per CRU-step from the ncu capture of one launch at "
+                                       "20 ms; 152 SMs x 4 schedulers x 2.07 GHz"},
+            "dram_bytes_per_cru_step": BATCHED_TRAFFIC_PER_LAUNCH_CRU * (st1["launches"] - st0["launches"])
+                                       * int(ncru.sum()) / total,
             "launch_shape": {k: st1[k] for k in ("cluster_ctas", "cta_crus", "threads_per_cta", "n_clusters")},
             "workload": f"{len(ncru)} cells, 2,000-12,500 CRUs, log-normal(0.1) PCaL/GKr/GKs/Vmax/rRyR, "
                         f"CL 400-1000 ms, 0-{window_ms:g} ms of the beat ({steps} steps)"}
@@ -609,6 +627,47 @@ def profile_batched(device, launches):
                                           "cru_steps_per_s": total / ((st1["kernel_ms"] - st0["kernel_ms"]) / 1e3),
                                           "events_per_cru_step": (st1["events"] - st0["events"]) / total}}),
           flush=True)
+
+
+def ks_full_cells(device, cells=200, ncru=12500, t_ms=50.0, every=500):
+    """Ensemble statistics at the headline cell size: 200 replicate 12,500-CRU cells (one stream
+    each), FP32 engine vs FP64 engine (reference arithmetic), the first t_ms ms after a +100 pA/pF
+    0.5 ms stimulus, recorded every 0.5 ms with the device's record-time CRU sums.  Two-sample KS
+    p-values (alpha = 0.01) of peak Cai, its time, V at the end of the window, and the peak LCC and
+    RyR open fractions and their times."""
+    import numpy as np
+    from scipy.stats import ks_2samp
+
+    from gwgb300 import Ensemble
+
+    steps = int(round(t_ms / DT))
+    out, secs = {}, {}
+    for prec, seed in (("fp32", 41), ("fp64", 42)):
+        e = Ensemble([ncru] * cells, precision=prec, seed=seed, device=device)
+        for c in range(cells):
+            e.sample_initial_crus(c)
+        e.set_pulse(0.0, PERIOD, STIM_DUR, STIM_AMP)
+        st0 = e.stats()
+        tr = e.run(DT, steps, record_every=every, sums=True)
+        secs[prec] = (e.stats()["kernel_ms"] - st0["kernel_ms"]) / 1e3
+        e.close()
+        t = (np.arange(tr.globals.shape[1]) + 1) * every * DT
+        Cai = tr.var("Cai")
+        lcc = tr.sum("LCC_open") / (4 * ncru)
+        ryr = tr.sum("RyR_open") / (20 * ncru)
+        out[prec] = {"peak_Cai": Cai.max(axis=1), "t_peak_Cai": t[Cai.argmax(axis=1)], "V_end": tr.var("V")[:, -1],
+                     "peak_LCC_open": lcc.max(axis=1), "t_peak_LCC_open": t[lcc.argmax(axis=1)],
+                     "peak_RyR_open": ryr.max(axis=1), "t_peak_RyR_open": t[ryr.argmax(axis=1)]}
+    res = {"reference": "FP64 engine (reference arithmetic, bit-exact channel sequences vs the oracle)",
+           "cells": cells, "ncru": ncru, "window_ms": t_ms, "alpha": 0.01, "kernel_s": secs, "ks_pvalue": {},
+           "rel_diff_of_means": {}, "fp64_mean": {}}
+    for k in out["fp32"]:
+        a, b = out["fp32"][k], out["fp64"][k]
+        res["ks_pvalue"][k] = float(ks_2samp(a, b).pvalue)
+        res["rel_diff_of_means"][k] = float(abs(a.mean() - b.mean()) / max(abs(b.mean()), 1e-30))
+        res["fp64_mean"][k] = float(b.mean())
+    res["all_pass"] = bool(min(res["ks_pvalue"].values()) > 0.01)
+    return res
 
 
 def _lib_globals():

@@ -160,6 +160,15 @@ __device__ __forceinline__ void block_sum(double (&v)[N], double *sh) {
         }
 }
 
+// The cell's constant block into shared memory by the whole block (16-byte words): the serial
+// global step reads ~100 of its fields, each from shared memory then instead of L2.
+__device__ __forceinline__ void stage_cell(CellStatic &dst, const CellStatic &src) {
+    static_assert(sizeof(CellStatic) % 16 == 0, "CellStatic is copied in 16-byte words");
+    const uint4 *s = reinterpret_cast<const uint4 *>(&src);
+    uint4 *d = reinterpret_cast<uint4 *>(&dst);
+    for (int i = (int)threadIdx.x; i < (int)(sizeof(CellStatic) / 16); i += (int)blockDim.x) d[i] = s[i];
+}
+
 __device__ __forceinline__ void open_counts(const CruD &c, int o[4]) {
 #pragma unroll
     for (int j = 0; j < 4; ++j) o[j] = dev::byte_s(c.ryr[2], j) + dev::byte_s(c.ryr[3], j);
@@ -319,15 +328,16 @@ __global__ void __launch_bounds__(kBlk) k_global(const GradArgs a, int64_t step,
     __shared__ double gn[kNumGlobals];
     __shared__ double S[kNS];
     __shared__ int ok;
+    __shared__ __align__(16) CellStatic C;
     const int cell = blockIdx.x;
     if (a.status[cell] != 0) return;  // the same for the whole block
+    stage_cell(C, use_var ? a.var_cs[cell] : a.cs[cell]);
     const int n = a.ncru[cell];
     const double *o = (use_var ? a.var_out : a.out) + 4 * a.cru0[cell];
     double s[4] = {0.0, 0.0, 0.0, 0.0};
     for (int m = (int)threadIdx.x; m < n; m += kBlk)
         for (int q = 0; q < 4; ++q) s[q] += o[4 * m + q];
-    block_sum<4>(s, sh);
-    const CellStatic &C = use_var ? a.var_cs[cell] : a.cs[cell];
+    block_sum<4>(s, sh);  // its barrier also publishes C
     double *g = a.G + (int64_t)kNumGlobals * cell;
     if (threadIdx.x < kNT) T[threadIdx.x] = glob_term(C, g, (int)threadIdx.x);
     __syncthreads();
@@ -530,14 +540,15 @@ __global__ void __launch_bounds__(kBlk) k_cru_busy(const GradArgs a, const AdjAr
 __global__ void __launch_bounds__(kBlk) k_global_adj(const GradArgs a, const AdjArgs b, int64_t step, int slot) {
     __shared__ double sh[(kBlk / 32) * kAdjIn];
     __shared__ double T[kNT];
+    __shared__ __align__(16) CellStatic C;
     const int cell = blockIdx.x;
+    stage_cell(C, a.cs[cell]);
     const int n = a.ncru[cell];
     const double *rows = b.ai_row + (int64_t)kAdjIn * a.cru0[cell];
     double ai[kAdjIn] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int m = (int)threadIdx.x; m < n; m += kBlk)
         for (int q = 0; q < kAdjIn; ++q) ai[q] += rows[(int64_t)kAdjIn * m + q];
-    block_sum<kAdjIn>(ai, sh);
-    const CellStatic &C = a.cs[cell];
+    block_sum<kAdjIn>(ai, sh);  // its barrier also publishes C
     const int64_t r = (int64_t)slot * a.n_cells + cell;
     const double *g = a.seg_G + r * kNumGlobals;
     if (threadIdx.x < kNT) T[threadIdx.x] = glob_term(C, g, (int)threadIdx.x);

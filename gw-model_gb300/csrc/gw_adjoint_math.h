@@ -786,10 +786,13 @@ GW_HD void cru_substep_adj(const CruCont &s0, double h, const CruIn &in, const C
     for (int j = 0; j < 4; ++j) jxf[j] = P.rxfer * (s0.c[j] - in.Cai);
     double lc[4], liss[4], lxf[4];
     for (int j = 0; j < 4; ++j) {
+        // beta = 1 / (1 + BSR/uR^2 + BSL/uL^2) and its x derivative 2 beta^2 (BSR/uR^3 + BSL/uL^3),
+        // over the common denominator (one division; the adjoint need not round as the forward)
         const double x = s0.c[j];
-        const double uR = P.KBSR + x, uL = P.KBSL + x;
-        const double beta = 1.0 / (1.0 + P.BSR_const / (uR * uR) + P.BSL_const / (uL * uL));
-        const double dbeta = 2.0 * beta * beta * (P.BSR_const / (uR * uR * uR) + P.BSL_const / (uL * uL * uL));
+        const double uR = P.KBSR + x, uL = P.KBSL + x, A2 = uR * uR, B2 = uL * uL;
+        const double r = 1.0 / (A2 * B2 + P.BSR_const * B2 + P.BSL_const * A2);
+        const double beta = A2 * B2 * r;
+        const double dbeta = 2.0 * uR * uL * (P.BSR_const * uL * B2 + P.BSL_const * uR * A2) * r * r;
         const double A = s0.L[j] + s0.rel[j] - jxf[j] + jiss[j];
         const double lcn = la.c[j];
         const double lA = lcn * h * beta;
@@ -801,14 +804,17 @@ GW_HD void cru_substep_adj(const CruCont &s0, double h, const CruIn &in, const C
     }
     double lJ, ljtr = l_jtr;
     {
-        const double x = s0.J, u = P.KCSQN + x;
-        const double beta = 1.0 / (1.0 + P.CSQN_const / (u * u));
+        // beta = u^2 / (u^2 + CSQN), d beta/dx = 2 u CSQN / (u^2 + CSQN)^2,
+        // d beta/dCSQN = -u^2 / (u^2 + CSQN)^2
+        const double x = s0.J, u = P.KCSQN + x, U2 = u * u;
+        const double r = 1.0 / (U2 + P.CSQN_const);
+        const double beta = U2 * r;
         const double G = jtr - P.VSS_VJSR * (s0.rel[0] + s0.rel[1] + s0.rel[2] + s0.rel[3]);
         const double lJn = la.J;
-        lJ = lJn + lJn * h * G * (2.0 * beta * beta * P.CSQN_const / (u * u * u));
+        lJ = lJn + lJn * h * G * (2.0 * u * P.CSQN_const * r * r);
         ljtr += lJn * h * beta;
         for (int j = 0; j < 4; ++j) la.rel[j] -= lJn * h * beta * P.VSS_VJSR;
-        ai.CSQN += lJn * h * G * (-beta * beta / (u * u));
+        ai.CSQN += lJn * h * G * (-U2 * r * r);
     }
     for (int j = 0; j < 4; ++j) {
         lc[j] += P.rxfer * lxf[j];

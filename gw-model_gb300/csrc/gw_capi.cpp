@@ -400,6 +400,66 @@ __global__ void unpack_trace_kernel(int nr, int ncr, int64_t stride, bool fp64, 
     }
 }
 
+// The reference's Python currents (GWSolution, src/model.py:46-549 and :771-899) of every record of a
+// launch, one thread per (cell, record), from the staged globals [cell][rec_cap][36] and CRU sums
+// [cell][rec_cap][8] (int64, Ca in 2^-40 mM).  Formulas as written there (they differ from the C++
+// step in places: ECa from Cai/Cao, IKv14 with Nai - Nao, ICaL with exp(2VF/RT) and the conducting
+// subunits' CaSS); NCaRU / (simulated CRUs) scales the CRU-dependent currents.
+__global__ void currents_kernel(const CellStatic *cs, const double *glob, const unsigned long long *sums, int rec_cap,
+                                int nr, int n_cells, double *out) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n_cells * nr) return;
+    const int cell = (int)(idx / nr), r = (int)(idx % nr);
+    const double *g = glob + ((int64_t)cell * rec_cap + r) * kNumGlobals;
+    const unsigned long long *sm = sums + ((int64_t)cell * rec_cap + r) * kSumFields;
+    const gw_params &p = cs[cell].p;
+    const double F = kFaraday, F_R = kFaraday / kGasConst, F_RT = F_R / p.T;
+    const double V = g[0], Nai = g[1], Ki = g[2], Cai = g[3], CaNSR = g[4];
+    const double m = g[7], h = g[8], jg = g[9], xKs = g[10], XKr = g[11 + 3], XKv43 = g[16 + 4], XKv14 = g[26 + 4];
+    const double Ko = p.Ko, Nao = p.Nao, Cao = p.Cao;
+    const double ENa = log(Nao / Nai) / F_RT, EK = log(Ko / Ki) / F_RT;
+    const double EKs = log((Ko + 0.01833 * Nao) / (Ki + 0.01833 * Nai)) / F_RT, ECa = 0.5 * log(Cao / Cai) / F_RT;
+    double *o = out + ((int64_t)cell * rec_cap + r) * GW_CURRENTS;
+    o[GW_CUR_INA] = p.GNa * (m * m * m) * h * jg * (V - ENa);
+    o[GW_CUR_INAB] = p.GNab * (V - ENa);
+    o[GW_CUR_IKR] = 0.5 * p.GKr * sqrt(Ko) * (1.0 / (1.0 + 1.4945 * exp(0.0446 * V))) * XKr * (V - EK);
+    o[GW_CUR_IKS] = p.GKs * (xKs * xKs) * (V - EKs);
+    o[GW_CUR_IKV43] = p.GKv43 * XKv43 * (V - EK);
+    const double VF_RT = V * F_R / p.T, eVF = exp(VF_RT);
+    const double mult14 = (p.PKv14 / p.Csc) * F * VF_RT * XKv14 / (1.0 - eVF);
+    o[GW_CUR_IKV14] = mult14 * ((Ki - Ko * eVF) + 0.02 * (Nai - Nao)) * 1e9;
+    o[GW_CUR_ITO1] = o[GW_CUR_IKV14] + o[GW_CUR_IKV43];
+    const double K1inf = 1.0 / (2.0 + exp(1.5 * (V - EK) * F_R / p.T));
+    o[GW_CUR_IK1] = p.GK1 * K1inf * (Ko / (Ko + p.KmK1)) * (V - EK);
+    o[GW_CUR_IKP] = p.GKp * (1.0 / (1.0 + exp((7.488 - V) / 5.98))) * (V - EK);
+    const double sigma = (exp(Nao / 67.3) - 1.0) / 7.0;
+    const double fNaK = 1.0 / (1.0 + 0.1245 * exp(-0.1 * V * F_R / p.T) + 0.0365 * sigma * exp(-V * F_R / p.T));
+    o[GW_CUR_INAK] = p.INaKmax * Ko / (Ko + p.KmKo) * fNaK / (1.0 + pow(p.KmNai / Nai, 1.5));
+    const double e1 = exp(p.eta * V * F_R / p.T), e2 = exp((p.eta - 1.0) * V * F_R / p.T);
+    const double multNaCa = 5000.0 * p.kNaCa / ((p.KmNa * p.KmNa * p.KmNa + Nao * Nao * Nao) * (p.KmCa + Cao));
+    o[GW_CUR_INACA] = multNaCa * (e1 * (Nai * Nai * Nai) * Cao - e2 * (Nao * Nao * Nao) * Cai) / (1.0 + p.ksat * e2);
+    o[GW_CUR_IPCA] = p.IpCamax * (Cai / (p.KmpCa + Cai));
+    o[GW_CUR_ICAB] = p.GCab * (V - ECa);
+    const double fu = pow(Cai / p.Kmf, p.Hf), ru = pow(CaNSR / p.Kmr, p.Hr);
+    o[GW_CUR_JUP] = (p.Vmaxf * fu - p.Vmaxr * ru) / (1.0 + fu + ru);
+    auto S = [&](int f) {
+        const long long v = (long long)sm[f];
+        const bool ca = f == GW_SUM_CASS_CONDUCTING || f == GW_SUM_CASS || f == GW_SUM_CAJSR;
+        return ca ? ldexp((double)v, -40) : (double)v;
+    };
+    const double n = S(GW_SUM_CRUS), scale = (double)p.NCaRU / n;
+    const double e2VF = exp(2.0 * VF_RT);
+    const double multL = scale * (p.PCaL / p.CSA) * (4.0 * F * VF_RT) / (e2VF - 1.0);
+    o[GW_CUR_ICAL] = multL * (e2VF * S(GW_SUM_CASS_CONDUCTING) - 0.341 * Cao * S(GW_SUM_LCC_CONDUCTING)) * 1e9;
+    const double emVF = exp(-VF_RT);
+    const double multT = scale * (p.Pto2 / p.CSA) * (F * VF_RT) / (emVF - 1.0);
+    o[GW_CUR_ITO2] = multT * S(GW_SUM_CLCH_OPEN) * (p.Clcyto * emVF - p.Clo) * 1e9;
+    o[GW_CUR_JTR] = p.rtr * (n * CaNSR - S(GW_SUM_CAJSR));
+    o[GW_CUR_JXFER] = p.rxfer * (S(GW_SUM_CASS) - 4.0 * n * Cai);
+    o[GW_CUR_LCC_OPEN_FRACTION] = S(GW_SUM_LCC_OPEN) / (4.0 * n);
+    o[GW_CUR_RYR_OPEN_FRACTION] = S(GW_SUM_RYR_OPEN) / (20.0 * n);
+}
+
 // Bump allocator over the scratch (256-byte aligned regions).
 struct ScratchCursor {
     unsigned char *base;
@@ -906,7 +966,8 @@ int gw_run(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_trace *tr
     const bool planes = recording && (tr->CaSS || tr->CaJSR || tr->LCC || tr->LCC_inactivation || tr->RyR || tr->ClCh);
     const bool codec = recording && (tr->LCC_i8 || tr->LCC_inactivation_u8 || tr->ClCh_u8 || tr->RyR_i16 ||
                                      tr->CaSS_f32 || tr->CaJSR_f32);
-    const bool sums = recording && tr->cru_sums;
+    const bool currents = recording && tr->currents;
+    const bool sums = recording && (tr->cru_sums || currents);
     if (planes && codec)
         return fail(c, GW_ERR_INVALID_ARGUMENT,
                     "trace: request either the int32/double CRU arrays or the reduced-memory ones, not both");
@@ -923,7 +984,8 @@ int gw_run(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_trace *tr
     const int chunk = c->steps_per_launch;
     // Device trace buffers for the records of one launch.
     const int rec_cap = recording ? (int)std::min<int64_t>(tr->max_records, chunk / record_every + 2) : 0;
-    DevBuf d_t, d_glob, d_tlcc, d_tflags, d_tryr, d_tcass, d_tcajsr, d_gate, d_clch, d_ryrc, d_cassf, d_cajsrf, d_sums;
+    DevBuf d_t, d_glob, d_tlcc, d_tflags, d_tryr, d_tcass, d_tcajsr, d_gate, d_clch, d_ryrc, d_cassf, d_cajsrf, d_sums,
+        d_cur;
     int64_t stride = 0;
     const int64_t ncr = tr_cell >= 0 ? c->ncru[tr_cell] : 0;
     if (recording) {
@@ -946,6 +1008,7 @@ int gw_run(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_trace *tr
             CK(c, d_cajsrf.alloc(4 * ncr * rec_cap));
         }
         if (sums) CK(c, d_sums.alloc(sizeof(unsigned long long) * kSumFields * (size_t)rec_cap * c->n_cells));
+        if (currents) CK(c, d_cur.alloc(sizeof(double) * GW_CURRENTS * (size_t)rec_cap * c->n_cells));
     }
     KernelArgs a = base_args(c);
     a.dt = dt;
@@ -970,7 +1033,7 @@ int gw_run(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_trace *tr
     a.tr_sums = d_sums.as<unsigned long long>();
     CK(c, cudaMemsetAsync(c->d_status.p, 0, sizeof(int) * c->n_cells, c->stream));
     std::vector<unsigned long long> h_sums;
-    std::vector<double> h_t, h_glob;
+    std::vector<double> h_t, h_glob, h_cur;
     std::vector<uint32_t> h_lcc, h_flags, h_ryr;
     std::vector<unsigned char> h_cass, h_cajsr;
     float total_ms = 0.f;
@@ -996,8 +1059,23 @@ int gw_run(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_trace *tr
         c->stats.launches++;
         if (recording && r_hi >= r_lo) {
             const int64_t nr = r_hi - r_lo + 1;
+            if (currents) {
+                const int64_t nt = (int64_t)c->n_cells * nr;
+                currents_kernel<<<(unsigned)((nt + 127) / 128), 128, 0, c->stream>>>(
+                    c->d_cs.as<CellStatic>(), d_glob.as<double>(), d_sums.as<unsigned long long>(), rec_cap, (int)nr,
+                    c->n_cells, d_cur.as<double>());
+                CK(c, cudaGetLastError());
+            }
             CK(c, cudaStreamSynchronize(c->stream));
-            if (sums) {
+            if (currents) {
+                h_cur.resize((size_t)GW_CURRENTS * rec_cap * c->n_cells);
+                CK(c, cudaMemcpy(h_cur.data(), d_cur.p, d_cur.n, cudaMemcpyDeviceToHost));
+                for (int cell = 0; cell < c->n_cells; ++cell)
+                    std::memcpy(tr->currents + ((int64_t)cell * tr->max_records + r_lo) * GW_CURRENTS,
+                                h_cur.data() + (int64_t)cell * rec_cap * GW_CURRENTS,
+                                sizeof(double) * GW_CURRENTS * nr);
+            }
+            if (tr->cru_sums) {
                 h_sums.resize((size_t)kSumFields * rec_cap * c->n_cells);
                 CK(c, cudaMemcpy(h_sums.data(), d_sums.p, d_sums.n, cudaMemcpyDeviceToHost));
                 for (int cell = 0; cell < c->n_cells; ++cell)
@@ -1108,7 +1186,7 @@ int gw_run_noalloc(gw_ctx *c, double dt, int64_t n_steps, int record_every, gw_t
     if (tr) tr->n_written = 0;
     const bool recording = tr && record_every > 0 && tr->max_records > 0;
     if (recording && (tr->cru_sums || tr->LCC_i8 || tr->LCC_inactivation_u8 || tr->ClCh_u8 || tr->RyR_i16 ||
-                      tr->CaSS_f32 || tr->CaJSR_f32))
+                      tr->CaSS_f32 || tr->CaJSR_f32 || tr->currents))
         return fail(c, GW_ERR_INVALID_ARGUMENT, "gw_run_noalloc records the int32/double trace arrays only");
     const bool cru_fields = recording && (tr->CaSS || tr->CaJSR || tr->LCC || tr->LCC_inactivation || tr->RyR || tr->ClCh);
     const int tr_cell = cru_fields ? tr->cru_cell : -1;

@@ -64,10 +64,14 @@ class GwTrace(C.Structure):
                 ("n_written", C.c_int64), ("cru_sums", C.POINTER(C.c_double)),
                 ("LCC_i8", C.POINTER(C.c_int8)), ("LCC_inactivation_u8", C.POINTER(C.c_uint8)),
                 ("ClCh_u8", C.POINTER(C.c_uint8)), ("RyR_i16", C.POINTER(C.c_int16)),
-                ("CaSS_f32", C.POINTER(C.c_float)), ("CaJSR_f32", C.POINTER(C.c_float))]
+                ("CaSS_f32", C.POINTER(C.c_float)), ("CaJSR_f32", C.POINTER(C.c_float)),
+                ("currents", C.POINTER(C.c_double))]
 
 
 CRU_SUMS = 8
+# Last axis of gw_trace.currents (GW_CUR_* order): the reference's GWSolution currents, evaluated on the device.
+CURRENT_FIELDS = ["INa", "INab", "IKr", "IKs", "IKv43", "IKv14", "Ito1", "IK1", "IKp", "INaK", "INaCa", "IpCa",
+                  "ICab", "Jup", "ICaL", "Ito2", "Jtr", "Jxfer", "LCC_open_fraction", "RyR_open_fraction"]
 SUM_FIELDS = ["LCC_open", "LCC_conducting", "CaSS_conducting", "RyR_open", "ClCh_open", "CaSS", "CaJSR", "CRUs"]
 
 

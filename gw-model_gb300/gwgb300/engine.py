@@ -79,12 +79,16 @@ class Trace:
     crus: Optional[Dict[str, np.ndarray]] = None
     cru_sums: Optional[np.ndarray] = None   # [n_cells, n_records, 8], fields _lib.SUM_FIELDS
     codec: Optional[Dict[str, np.ndarray]] = None  # reduced-memory CRU records of cru_cell
+    currents: Optional[np.ndarray] = None  # [n_cells, n_records, 20], fields _lib.CURRENT_FIELDS
 
     def var(self, name: str) -> np.ndarray:
         return self.globals[..., GLOBAL_NAMES.index(name)]
 
     def sum(self, name: str) -> np.ndarray:
         return self.cru_sums[..., _lib.SUM_FIELDS.index(name)]
+
+    def current(self, name: str) -> np.ndarray:
+        return self.currents[..., _lib.CURRENT_FIELDS.index(name)]
 
 
 class Ensemble:
@@ -270,10 +274,12 @@ class Ensemble:
 
     # ---- stepping ----
     def run(self, dt: float, n_steps: int, record_every: int = 0, cru_cell: Optional[int] = None,
-            max_records: Optional[int] = None, sums: bool = False, codec: bool = False) -> Optional[Trace]:
+            max_records: Optional[int] = None, sums: bool = False, codec: bool = False,
+            currents: bool = False) -> Optional[Trace]:
         """Advance every cell by n_steps.  With record_every > 0, returns the globals of every cell
         at each record; cru_cell adds that cell's CRU arrays (codec=True: in the reduced-memory
-        layout, written by the device); sums=True adds every cell's record-time CRU sums."""
+        layout, written by the device); sums=True adds every cell's record-time CRU sums;
+        currents=True the reference's GWSolution currents of every record, evaluated on the device."""
         if record_every <= 0:
             check(self.L.gw_run(self.h, dt, int(n_steps), 0, None), self.h)
             return None
@@ -291,6 +297,10 @@ class Ensemble:
         if sums:
             cs = np.zeros((self.n_cells, max(nrec, 1), _lib.CRU_SUMS))
             tr.cru_sums = _dp(cs)
+        cur = None
+        if currents:
+            cur = np.zeros((self.n_cells, max(nrec, 1), len(_lib.CURRENT_FIELDS)))
+            tr.currents = _dp(cur)
         if cru_cell is not None and codec:
             n = int(self.ncru[cru_cell])
             cod = {"LCC": np.zeros((nrec, n, 4), np.int8), "LCC_inactivation": np.zeros((nrec, n, 4), np.bool_),
@@ -319,7 +329,8 @@ class Ensemble:
             crus = {a: b[:k] for a, b in crus.items()}
         if cod is not None:
             cod = {a: b[:k] for a, b in cod.items()}
-        return Trace(t=t[:k], globals=G[:, :k], crus=crus, cru_sums=None if cs is None else cs[:, :k], codec=cod)
+        return Trace(t=t[:k], globals=G[:, :k], crus=crus, cru_sums=None if cs is None else cs[:, :k], codec=cod,
+                     currents=None if cur is None else cur[:, :k])
 
     def stats(self) -> dict:
         s = GwStats()

@@ -129,7 +129,21 @@ typedef struct gw_trace {
     int16_t *RyR_i16;
     float *CaSS_f32;
     float *CaJSR_f32;
+    /* The reference's Python current post-processing (GWSolution properties, src/model.py:771-899,
+     * with the currents of :46-549) evaluated on the device at every record of every cell from the
+     * record's globals and CRU sums, so no CRU array leaves the device:
+     * [n_cells][max_records][GW_CURRENTS], fields GW_CUR_*, or NULL.  Not with gw_run_noalloc. */
+    double *currents;
 } gw_trace;
+
+/* Last axis of gw_trace.currents: pA/pF for the currents, mM/ms for the fluxes. */
+#define GW_CURRENTS 20
+enum {
+    GW_CUR_INA = 0, GW_CUR_INAB = 1, GW_CUR_IKR = 2, GW_CUR_IKS = 3, GW_CUR_IKV43 = 4, GW_CUR_IKV14 = 5,
+    GW_CUR_ITO1 = 6, GW_CUR_IK1 = 7, GW_CUR_IKP = 8, GW_CUR_INAK = 9, GW_CUR_INACA = 10, GW_CUR_IPCA = 11,
+    GW_CUR_ICAB = 12, GW_CUR_JUP = 13, GW_CUR_ICAL = 14, GW_CUR_ITO2 = 15, GW_CUR_JTR = 16, GW_CUR_JXFER = 17,
+    GW_CUR_LCC_OPEN_FRACTION = 18, GW_CUR_RYR_OPEN_FRACTION = 19
+};
 
 /* Last axis of gw_trace.cru_sums.  Counts are exact; the Ca sums carry 2^-40 mM resolution. */
 #define GW_CRU_SUMS 8

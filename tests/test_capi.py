@@ -58,6 +58,7 @@ int main(void) {
   O(gw_params, NCaRU) O(gw_params, Ko) O(gw_params, Hr) O(gw_globals, Kr) O(gw_globals, Kv43)
   O(gw_globals, Kv14) O(gw_ensemble_desc, seed) O(gw_ensemble_desc, ode_fp32_rhs)
   O(gw_trace, cru_cell) O(gw_trace, n_written) O(gw_trace, cru_sums) O(gw_trace, CaJSR_f32)
+  O(gw_trace, currents)
   O(gw_stats, kernel_ms) O(gw_stats, ctas) O(gw_stats, device_allocs)
   O(gw_grad_desc, seed) O(gw_grad_desc, dt) O(gw_grad_desc, n_steps) O(gw_grad_desc, stim)
   O(gw_grad_desc, event_cap) O(gw_grad_stats, events) O(gw_grad_stats, segment_bytes)
@@ -127,6 +128,16 @@ def test_invalid_arguments_without_device(enginelib):
     assert b"n_cells" in buf.value
     assert enginelib.gw_grad_forward(None, None) == _lib.GW_ERR_INVALID_ARGUMENT
     assert enginelib.gw_grad_backward(None, None, None) == _lib.GW_ERR_INVALID_ARGUMENT
+
+
+def test_current_fields_match_bindings():
+    from gwgb300 import _lib
+
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    codes = dict((n, int(v)) for n, v in re.findall(r"(GW_CUR_\w+)\s*=\s*(\d+)", src))
+    assert int(re.search(r"#define GW_CURRENTS (\d+)", src).group(1)) == len(_lib.CURRENT_FIELDS) == len(codes)
+    for n, v in codes.items():
+        assert _lib.CURRENT_FIELDS[v].upper() == n[len("GW_CUR_"):]
 
 
 def test_grad_theta_enum_matches_bindings():

@@ -100,6 +100,34 @@ def test_currents_from_device_sums():
     assert np.all(c_sums["ICaL"] <= 0)  # inward
 
 
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_currents_on_device_match_host_formulas(precision):
+    """gw_trace.currents (the reference's GWSolution currents evaluated by the device at every record
+    of every cell) against gwgb300.analysis.currents (the same formulas on the host, checked against
+    the reference's own Python in tests/test_analysis.py) on the same records, for two cells with
+    their own parameters and CRU counts, over the upstroke and Ca release."""
+    from gwgb300 import Ensemble, _lib, analysis, engine
+
+    d = _lib.default_params()
+    params = [engine.params_from(None, GKr=d.GKr * 1.2, PCaL=d.PCaL * 0.8, NCaRU=7000),
+              engine.params_from(None, GK1=d.GK1 * 0.9, Vmaxf=d.Vmaxf * 1.1, Vmaxr=d.Vmaxr * 1.1, NCaRU=12500)]
+    e = Ensemble(NCRU, params, precision=precision, seed=17)
+    for c in range(len(NCRU)):
+        e.sample_initial_crus(c)
+    e.set_pulse(0.0, 1000.0, 0.5, 100.0)
+    tr = e.run(1e-3, 30_000, record_every=250, sums=True, currents=True)
+    e.close()
+    R = 30_000 // 250
+    assert tr.currents.shape == (2, R, len(_lib.CURRENT_FIELDS))
+    for c in range(2):
+        host = analysis.currents(tr.globals[c], params[c], cru_sums=tr.cru_sums[c])
+        for k, name in enumerate(_lib.CURRENT_FIELDS):
+            dev, ref = tr.currents[c, :, k], host[name]
+            scale = max(float(np.max(np.abs(ref))), 1e-300)
+            np.testing.assert_allclose(dev, ref, rtol=1e-10, atol=1e-12 * scale, err_msg=f"cell {c} {name}")
+    assert tr.current("ICaL").min() < 0 and tr.var("V").max() > 0  # an upstroke with an inward ICaL
+
+
 def test_noalloc_rejects_sums_and_codec():
     import ctypes as C
 
@@ -110,5 +138,9 @@ def test_noalloc_rejects_sums_and_codec():
     tr.max_records = 2
     s = np.zeros((2, 2, 8))
     tr.cru_sums = s.ctypes.data_as(C.POINTER(C.c_double))
+    assert e.L.gw_run_noalloc(e.h, 1e-3, 20, 10, C.byref(tr)) == _lib.GW_ERR_INVALID_ARGUMENT
+    tr.cru_sums = None
+    cur = np.zeros((2, 2, len(_lib.CURRENT_FIELDS)))
+    tr.currents = cur.ctypes.data_as(C.POINTER(C.c_double))
     assert e.L.gw_run_noalloc(e.h, 1e-3, 20, 10, C.byref(tr)) == _lib.GW_ERR_INVALID_ARGUMENT
     e.close()
