@@ -86,6 +86,8 @@ struct GradArgs {
     const int *blk_lo;          // [blocks] first CRU (within the cell) of each block
     const int *blk_hi;          // [blocks] end of the block's CRU range (within the cell)
     const int *cru_cell;        // [n_crus] cell of each CRU (backward kernels)
+    const int *blk0;            // [n_cells + 1] first block of each cell
+    double *part;               // [blocks][4] each block's sums of its CRUs' fluxes of the step
     const int64_t *cru0;        // [n_cells] first CRU of each cell in the CRU arrays
     const int *ncru;            // [n_cells]
     const int *rng_cell;        // [n_cells] cell index that keys the cell's random streams
@@ -119,6 +121,7 @@ struct GradArgs {
     const CellStatic *var_cs;   // [n_cells]
     double *var_x;              // [n_crus][9] CaSS[4], CaJSR, JLCC[4]
     double *var_out;            // [n_crus][4]
+    double *var_part;           // [blocks][4]
     const double *var_sv;       // [n_cells][kSvCount]
 };
 
@@ -129,6 +132,7 @@ struct AdjArgs {
     double *lam_cy;     // [n_cells][3] adjoints of the carry sums JLCC, Jtr, Jxfer
     double *lam_th;     // [n_cells][8] relative sensitivities
     double *ai_row;     // [n_crus][kAdjIn] each CRU's adjoints of its step inputs and parameters
+    double *ai_part;    // [blocks][kAdjIn] each block's sums of its CRUs' rows
     const dev::SsaConsts<double> *cc;  // [n_cells] SSA constants (k_cru_busy)
     const double *dLdV; // [n_cells][n_samples]
 };
@@ -213,6 +217,7 @@ __global__ void __launch_bounds__(kBlk) k_ssa(const GradArgs a, int64_t step, in
     __shared__ dev::SsaConsts<double> cc;
     __shared__ double sv[kSvCount];
     __shared__ double vsv[kSvCount];
+    __shared__ double shp[(kBlk / 32) * 4];
     const int cell = a.blk_cell[blockIdx.x];
     const bool var = a.var_x != nullptr;
     if (threadIdx.x == 0) dev::load_ssa_consts<double>(cc, a.cs[cell]);
@@ -317,72 +322,91 @@ __global__ void __launch_bounds__(kBlk) k_ssa(const GradArgs a, int64_t step, in
     const unsigned int wev = __reduce_add_sync(0xffffffffu, ev);
     if (a.events && lane == 0 && wev) atomicAdd(&a.events[cell], (unsigned long long)wev);
     if (err) atomicExch(&a.status[cell], (int)GW_ERR_EVENT_CAP);
+    // The block's flux sums over its CRU range, in a fixed order (the lanes took the CRUs in the
+    // order they finished, so per-lane sums would not be reproducible).
+    __syncthreads();
+    for (int w = 0; w < (var ? 2 : 1); ++w) {
+        const double *rows = (w ? a.var_out : a.out) + 4 * c0;
+        double s4[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int m = lo + (int)threadIdx.x; m < lo + span; m += kBlk)
+            for (int q = 0; q < 4; ++q) s4[q] += rows[4 * (int64_t)m + q];
+        block_sum<4>(s4, shp);
+        if (threadIdx.x == 0)
+            for (int q = 0; q < 4; ++q) (w ? a.var_part : a.part)[4 * (int64_t)blockIdx.x + q] = s4[q];
+        __syncthreads();
+    }
 }
 
-// The cell's flux sums of the step and its global step (one block per cell): the transcendental
-// terms of the increment, then of the new state's SSA values, on one thread each; the rest on
-// thread 0.
+// The cell's flux sums of the step (its blocks' partial sums, in block order) and its global step
+// (one block per cell), the increment's dependency levels one item per thread (on GB300 an FP64
+// instruction costs a sub-partition the same time for 1 or 32 active lanes, so a level costs about
+// one item): the transcendental terms, the Kv generator entries, the currents and derivative
+// components, then d[0..6] and the update; then the new state's SSA values.
 __global__ void __launch_bounds__(kBlk) k_global(const GradArgs a, int64_t step, int slot, int use_var) {
-    __shared__ double sh[(kBlk / 32) * 4];
     __shared__ double T[kNT];
-    __shared__ double gn[kNumGlobals];
+    __shared__ double E[2 * kKvE];
+    __shared__ double Qv[kNQ];
+    __shared__ double gs[kNumGlobals], gn[kNumGlobals];
     __shared__ double S[kNS];
+    __shared__ double sums[4];
     __shared__ int ok;
     __shared__ __align__(16) CellStatic C;
     const int cell = blockIdx.x;
     if (a.status[cell] != 0) return;  // the same for the whole block
+    const int t = (int)threadIdx.x;
     stage_cell(C, use_var ? a.var_cs[cell] : a.cs[cell]);
-    const int n = a.ncru[cell];
-    const double *o = (use_var ? a.var_out : a.out) + 4 * a.cru0[cell];
-    double s[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int m = (int)threadIdx.x; m < n; m += kBlk)
-        for (int q = 0; q < 4; ++q) s[q] += o[4 * m + q];
-    block_sum<4>(s, sh);  // its barrier also publishes C
     double *g = a.G + (int64_t)kNumGlobals * cell;
-    if (threadIdx.x < kNT) T[threadIdx.x] = glob_term(C, g, (int)threadIdx.x);
+    double *cy = a.carry + 4 * (int64_t)cell;
+    if (t < kNumGlobals) gs[t] = g[t];
+    if (t < 4) {
+        const double *pp = use_var ? a.var_part : a.part;
+        double v = 0.0;
+        for (int b = a.blk0[cell]; b < a.blk0[cell + 1]; ++b) v += pp[4 * (int64_t)b + t];
+        sums[t] = v;
+    }
+    const Carry c0{cy[0], cy[1], cy[2], cy[3]};
+    const double istim = pulse_at(a.t[cell], a.stim + 4 * (int64_t)cell);
+    __syncthreads();
+    if (t < kNT) T[t] = glob_term(C, gs, t);
+    __syncthreads();
+    if (t < 2 * kKvE) E[t] = kv_entry(C.p, T, t);
+    __syncthreads();
+    if (t < kNQ) Qv[t] = glob_qty(C, gs, c0, a.dt, T, E, t);
+    __syncthreads();
+    if (t < kNumGlobals) gn[t] = gs[t] + (t < 7 ? glob_dconc(C, c0, istim, a.dt, Qv, t) : Qv[Q_D + t - 7]);
     __syncthreads();
     double *svo = (use_var ? const_cast<double *>(a.var_sv) : a.sv) + (int64_t)kSvCount * cell;
-    if (threadIdx.x == 0) {
+    if (t == 0) {
         ok = 0;
-        double *cy = a.carry + 4 * (int64_t)cell;
-        double gl[kNumGlobals], d[kNumGlobals];
-        for (int k = 0; k < kNumGlobals; ++k) gl[k] = g[k];
-        const Carry c0{cy[0], cy[1], cy[2], cy[3]};
-        const double istim = pulse_at(a.t[cell], a.stim + 4 * (int64_t)cell);
         if (a.seg_G) {
             const int64_t r = (int64_t)slot * a.n_cells + cell;
-            for (int k = 0; k < kNumGlobals; ++k) a.seg_G[r * kNumGlobals + k] = gl[k];
+            for (int k = 0; k < kNumGlobals; ++k) a.seg_G[r * kNumGlobals + k] = gs[k];
             for (int k = 0; k < 4; ++k) a.seg_carry[r * 4 + k] = cy[k];
             for (int k = 0; k < kSvCount; ++k) a.seg_sv[r * kSvCount + k] = svo[k];
         }
-        if (a.regime && gl[0] >= -40.0) a.regime[cell] += 1ull;
-        if (!glob_increment(C, gl, c0, istim, a.dt, T, d)) {
+        if (a.regime && gs[0] >= -40.0) a.regime[cell] += 1ull;
+        bool fin = true;
+        for (int k = 0; k < kNumGlobals; ++k) fin = fin && isfinite(gn[k]);
+        if (!(gs[1] > 0.0) || !(gs[2] > 0.0)) {
             a.status[cell] = GW_ERR_NERNST;
+        } else if (!fin) {
+            a.status[cell] = GW_ERR_NONFINITE;
         } else {
-            bool fin = true;
-            for (int k = 0; k < kNumGlobals; ++k) {
-                gl[k] += d[k];
-                fin = fin && isfinite(gl[k]);
-            }
-            if (!fin) {
-                a.status[cell] = GW_ERR_NONFINITE;
-            } else {
-                for (int k = 0; k < kNumGlobals; ++k) g[k] = gn[k] = gl[k];
-                // carry order {JLCC, ClCh, Jtr, Jxfer} from the per-CRU {JLCC, Jxfer, Jtr, ClCh}
-                cy[0] = s[0];
-                cy[1] = s[3];
-                cy[2] = s[2];
-                cy[3] = s[1];
-                a.t[cell] += a.dt;
-                ok = 1;
-            }
+            for (int k = 0; k < kNumGlobals; ++k) g[k] = gn[k];
+            // carry order {JLCC, ClCh, Jtr, Jxfer} from the per-CRU {JLCC, Jxfer, Jtr, ClCh}
+            cy[0] = sums[0];
+            cy[1] = sums[3];
+            cy[2] = sums[2];
+            cy[3] = sums[1];
+            a.t[cell] += a.dt;
+            ok = 1;
         }
     }
     __syncthreads();
     if (!ok) return;
-    if (threadIdx.x < kNS) S[threadIdx.x] = sv_term(C, gn, (int)threadIdx.x);
+    if (t < kNS) S[t] = sv_term(C, gn, t);
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (t == 0) {
         step_values(C, gn, S, svo);
         if (a.V && (step + 1) % a.sample_every == 0) {
             const int64_t si = (step + 1) / a.sample_every - 1;
@@ -430,25 +454,39 @@ __device__ __forceinline__ void store_adj(const CruCont &la, const CruAdjIn &ai,
 }
 
 // Reverse of step `slot` for the CRUs whose step had no jump: one sub-step of length dt (the
-// iteration's h = dt - 0) and no transition.
+// iteration's h = dt - 0) and no transition.  Block b takes the CRU range of the forward block
+// tables; after its CRUs it sums all its range's rows (the listed CRUs' rows come from k_cru_busy,
+// launched before it) in a fixed order into ai_part[b].
 __global__ void __launch_bounds__(kBlk) k_cru_quiet(const GradArgs a, const AdjArgs b, int slot) {
-    const int64_t i = (int64_t)blockIdx.x * kBlk + threadIdx.x;
-    if (i >= a.n_crus || !a.quiet[(int64_t)slot * a.n_crus + i]) return;
-    const int cell = a.cru_cell[i];
-    const CruD x0 = a.seg_x[(int64_t)slot * a.n_crus + i];
+    __shared__ double shp[(kBlk / 32) * kAdjIn];
+    const int cell = a.blk_cell[blockIdx.x];
+    const int lo = a.blk_lo[blockIdx.x], hi = a.blk_hi[blockIdx.x];
+    const int64_t c0 = a.cru0[cell];
     const CruPar P = cru_par(a.cs[cell]);
     const CruIn in = cru_in(a.seg_sv + ((int64_t)slot * a.n_cells + cell) * kSvCount);
     const double *lc = b.lam_cy + 3 * (int64_t)cell;
-    double *lx = b.lam_x + (int64_t)kLamX * i;
-    CruCont la = lam_after(lx, lc);
-    CruAdjIn ai{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    int o[4];
-    open_counts(x0, o);
-    CruCont s0 = cont_of(x0);
-    cru_begin(s0, o, P);
-    cru_substep_adj(s0, a.dt, in, P, lc[1], lc[2], la, ai);
-    cru_begin_adj(s0, o, P, la, ai);
-    store_adj(la, ai, lx, b.ai_row + (int64_t)kAdjIn * i);
+    for (int m = lo + (int)threadIdx.x; m < hi; m += kBlk) {
+        const int64_t i = c0 + m;
+        if (!a.quiet[(int64_t)slot * a.n_crus + i]) continue;
+        const CruD x0 = a.seg_x[(int64_t)slot * a.n_crus + i];
+        double *lx = b.lam_x + (int64_t)kLamX * i;
+        CruCont la = lam_after(lx, lc);
+        CruAdjIn ai{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        int o[4];
+        open_counts(x0, o);
+        CruCont s0 = cont_of(x0);
+        cru_begin(s0, o, P);
+        cru_substep_adj(s0, a.dt, in, P, lc[1], lc[2], la, ai);
+        cru_begin_adj(s0, o, P, la, ai);
+        store_adj(la, ai, lx, b.ai_row + (int64_t)kAdjIn * i);
+    }
+    __syncthreads();
+    double s6[kAdjIn] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int m = lo + (int)threadIdx.x; m < hi; m += kBlk)
+        for (int q = 0; q < kAdjIn; ++q) s6[q] += b.ai_row[(int64_t)kAdjIn * (c0 + m) + q];
+    block_sum<kAdjIn>(s6, shp);
+    if (threadIdx.x == 0)
+        for (int q = 0; q < kAdjIn; ++q) b.ai_part[(int64_t)kAdjIn * blockIdx.x + q] = s6[q];
 }
 
 // One recorded sub-step of a CRU's step: the state at its start and what ended it.
@@ -538,22 +576,24 @@ __global__ void __launch_bounds__(kBlk) k_cru_busy(const GradArgs a, const AdjAr
 // Reverse of the global step `step` (one block per cell): the cell's CRU rows summed in a fixed
 // order, then the adjoint of the global increment by thread 0.
 __global__ void __launch_bounds__(kBlk) k_global_adj(const GradArgs a, const AdjArgs b, int64_t step, int slot) {
-    __shared__ double sh[(kBlk / 32) * kAdjIn];
     __shared__ double T[kNT];
+    __shared__ double sai[kAdjIn];
     __shared__ __align__(16) CellStatic C;
     const int cell = blockIdx.x;
     stage_cell(C, a.cs[cell]);
-    const int n = a.ncru[cell];
-    const double *rows = b.ai_row + (int64_t)kAdjIn * a.cru0[cell];
-    double ai[kAdjIn] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int m = (int)threadIdx.x; m < n; m += kBlk)
-        for (int q = 0; q < kAdjIn; ++q) ai[q] += rows[(int64_t)kAdjIn * m + q];
-    block_sum<kAdjIn>(ai, sh);  // its barrier also publishes C
+    if (threadIdx.x < kAdjIn) {
+        double v = 0.0;
+        for (int k = a.blk0[cell]; k < a.blk0[cell + 1]; ++k) v += b.ai_part[(int64_t)kAdjIn * k + threadIdx.x];
+        sai[threadIdx.x] = v;
+    }
     const int64_t r = (int64_t)slot * a.n_cells + cell;
     const double *g = a.seg_G + r * kNumGlobals;
+    __syncthreads();
     if (threadIdx.x < kNT) T[threadIdx.x] = glob_term(C, g, (int)threadIdx.x);
     __syncthreads();
     if (threadIdx.x != 0) return;
+    double ai[kAdjIn];
+    for (int q = 0; q < kAdjIn; ++q) ai[q] = sai[q];
     const double *cyv = a.seg_carry + r * 4;
     const double *sv = a.seg_sv + r * kSvCount;
     const Carry cy{cyv[0], cyv[1], cyv[2], cyv[3]};
@@ -631,13 +671,15 @@ int pack_cru(const double *CaSS, const double *CaJSR, const int32_t *LCC, const 
 // down so that all of them fit the device's `slots` resident blocks in one wave (at least one, at
 // most one per 32 CRUs); block r of bpc takes CRUs [ncru r / bpc, ncru (r + 1) / bpc).
 void plan_blocks(const std::vector<int> &ncru, int slots, std::vector<int> &bc, std::vector<int> &bl,
-                 std::vector<int> &bh) {
+                 std::vector<int> &bh, std::vector<int> &b0) {
     int64_t total = 0;
     for (int n : ncru) total += n;
     bc.clear();
     bl.clear();
     bh.clear();
+    b0.assign(ncru.size() + 1, 0);
     for (size_t c = 0; c < ncru.size(); ++c) {
+        b0[c] = (int)bc.size();
         const int64_t n = ncru[c];
         int64_t bpc = (int64_t)((double)slots * (double)n / (double)total);
         bpc = std::max<int64_t>(1, std::min<int64_t>(bpc, (n + 31) / 32));
@@ -647,6 +689,7 @@ void plan_blocks(const std::vector<int> &ncru, int slots, std::vector<int> &bc, 
             bh.push_back((int)(n * (r + 1) / bpc));
         }
     }
+    b0[ncru.size()] = (int)bc.size();
 }
 
 }  // namespace
@@ -657,7 +700,7 @@ struct gw_grad {
     int64_t n_crus = 0;
     int n_blocks = 0;
     int sm_count = 1, slots = 1;  // SMs, and resident k_ssa blocks on the device
-    std::vector<int> ncru, blk_cell, blk_lo, blk_hi, cru_cell;
+    std::vector<int> ncru, blk_cell, blk_lo, blk_hi, blk0, cru_cell;
     std::vector<int64_t> cru0;
     std::vector<CellStatic> cs;
     std::vector<double> stim;
@@ -673,16 +716,16 @@ struct gw_grad {
     gw_grad_stats stats{};
     std::vector<double> G_final;
     // tables
-    Buf d_cs, d_blk_cell, d_blk_lo, d_blk_hi, d_cru_cell, d_cru0, d_ncru, d_rng_cell, d_stim, d_cc;
+    Buf d_cs, d_blk_cell, d_blk_lo, d_blk_hi, d_blk0, d_cru_cell, d_cru0, d_ncru, d_rng_cell, d_stim, d_cc;
     // initial state
     Buf x_init, G_init, carry_init, sv_init;
     // state
-    Buf x, out, G, carry, t, sv, status, events, V, regime;
+    Buf x, out, part, G, carry, t, sv, status, events, V, regime;
     // checkpoints and segment
     Buf ck_x, ck_G, ck_carry, ck_t, ck_sv;
     Buf seg_x, seg_G, seg_carry, seg_sv, quiet, busy, busy_n;
     // adjoint
-    Buf lam_x, lam_G, lam_cy, lam_th, ai_row, dLdV;
+    Buf lam_x, lam_G, lam_cy, lam_th, ai_row, ai_part, dLdV;
 
     ~gw_grad() {
         if (ev0) cudaEventDestroy(ev0);
@@ -706,6 +749,8 @@ struct gw_grad {
         a.blk_lo = d_blk_lo.as<int>();
         a.blk_hi = d_blk_hi.as<int>();
         a.cru_cell = d_cru_cell.as<int>();
+        a.blk0 = d_blk0.as<int>();
+        a.part = part.as<double>();
         a.cru0 = d_cru0.as<int64_t>();
         a.ncru = d_ncru.as<int>();
         a.rng_cell = d_rng_cell.as<int>();
@@ -736,6 +781,7 @@ struct gw_grad {
         b.lam_cy = lam_cy.as<double>();
         b.lam_th = lam_th.as<double>();
         b.ai_row = ai_row.as<double>();
+        b.ai_part = ai_part.as<double>();
         b.cc = d_cc.as<dev::SsaConsts<double>>();
         b.dLdV = dLdV.as<double>();
         return b;
@@ -863,7 +909,7 @@ int gw_grad_create(const gw_grad_desc *d, gw_grad **out) {
         }
         g->slots = std::max(1, g->sm_count * std::max(1, per_sm));
     }
-    plan_blocks(g->ncru, g->slots, g->blk_cell, g->blk_lo, g->blk_hi);
+    plan_blocks(g->ncru, g->slots, g->blk_cell, g->blk_lo, g->blk_hi, g->blk0);
     g->n_blocks = (int)g->blk_cell.size();
     std::vector<int> rng_cell(d->n_cells);
     for (int c = 0; c < d->n_cells; ++c) rng_cell[c] = d->cell_base + c;
@@ -878,6 +924,9 @@ int gw_grad_create(const gw_grad_desc *d, gw_grad **out) {
     up(g->d_blk_cell, g->blk_cell.data(), sizeof(int) * g->n_blocks);
     up(g->d_blk_lo, g->blk_lo.data(), sizeof(int) * g->n_blocks);
     up(g->d_blk_hi, g->blk_hi.data(), sizeof(int) * g->n_blocks);
+    up(g->d_blk0, g->blk0.data(), sizeof(int) * (C + 1));
+    up(g->part, nullptr, sizeof(double) * 4 * g->n_blocks);
+    up(g->ai_part, nullptr, sizeof(double) * kAdjIn * g->n_blocks);
     up(g->d_cru_cell, g->cru_cell.data(), sizeof(int) * N);
     up(g->d_cc, nullptr, sizeof(dev::SsaConsts<double>) * C);
     up(g->d_cru0, g->cru0.data(), sizeof(int64_t) * C);
@@ -1046,7 +1095,6 @@ int gw_grad_backward(gw_grad *g, const double *dL_dV, double *sens) {
     a.busy = g->busy.as<int>();
     a.busy_n = g->busy_n.as<int>();
     const AdjArgs b = g->adj_args();
-    const int qgrid = (int)((g->n_crus + kBlk - 1) / kBlk);
     const int bgrid = 2 * g->sm_count;
     cudaEventRecord(g->ev0, g->stream);
     for (int64_t k = g->n_ck - 1; k >= 0; --k) {
@@ -1059,7 +1107,7 @@ int gw_grad_backward(gw_grad *g, const double *dL_dV, double *sens) {
         }
         for (int64_t s = s1 - 1; s >= s0; --s) {
             k_cru_busy<<<bgrid, kBlk, 0, g->stream>>>(a, b, s, (int)(s - s0));
-            k_cru_quiet<<<qgrid, kBlk, 0, g->stream>>>(a, b, (int)(s - s0));
+            k_cru_quiet<<<g->n_blocks, kBlk, 0, g->stream>>>(a, b, (int)(s - s0));
             k_global_adj<<<g->n_cells, kBlk, 0, g->stream>>>(a, b, s, (int)(s - s0));
         }
     }
@@ -1086,7 +1134,7 @@ int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_para
     }
     cudaSetDevice(g->device);
     // tables of the source copies (cell v = a copy of src_cell[v]) and the variants
-    std::vector<int> ncru(n_var), bc, bl, bh, rngc(n_var);
+    std::vector<int> ncru(n_var), bc, bl, bh, b0, rngc(n_var);
     std::vector<int64_t> c0(n_var);
     std::vector<CellStatic> vcs(n_var);
     std::vector<double> stim(4 * (size_t)n_var), vsv(kSvCount * (size_t)n_var);
@@ -1100,7 +1148,7 @@ int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_para
         for (int k = 0; k < 4; ++k) stim[4 * v + k] = g->stim[4 * s + k];
         make_cell_static(params[v], ncru[v], vcs[v]);
     }
-    plan_blocks(ncru, g->slots, bc, bl, bh);
+    plan_blocks(ncru, g->slots, bc, bl, bh, b0);
     const int nb = (int)bc.size();
     std::vector<CellStatic> scs(n_var);
     for (int v = 0; v < n_var; ++v) scs[v] = g->cs[src_cell[v]];
@@ -1122,7 +1170,7 @@ int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_para
         std::memcpy(&sv[kSvCount * (size_t)v], &sv0[kSvCount * (size_t)s], sizeof(double) * kSvCount);
         step_values(vcs[v], &G0[kNumGlobals * (size_t)s], &vsv[kSvCount * (size_t)v]);
     }
-    Buf d_cs, d_vcs, d_bc, d_bl, d_bh, d_c0, d_n, d_rng, d_stim, x, out, vx, vout, dG, dvG, dcy, dvcy, dt_, dvt, dsv, dvsv,
+    Buf d_cs, d_vcs, d_bc, d_bl, d_bh, d_b0, d_part, d_vpart, d_c0, d_n, d_rng, d_stim, x, out, vx, vout, dG, dvG, dcy, dvcy, dt_, dvt, dsv, dvsv,
         dst, dvst, dV, dreg;
     auto up = [&](Buf &b, const void *src, size_t bytes) {
         if (rc) return;
@@ -1134,6 +1182,9 @@ int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_para
     up(d_bc, bc.data(), sizeof(int) * nb);
     up(d_bl, bl.data(), sizeof(int) * nb);
     up(d_bh, bh.data(), sizeof(int) * nb);
+    up(d_b0, b0.data(), sizeof(int) * (n_var + 1));
+    up(d_part, nullptr, sizeof(double) * 4 * nb);
+    up(d_vpart, nullptr, sizeof(double) * 4 * nb);
     up(d_c0, c0.data(), sizeof(int64_t) * n_var);
     up(d_n, ncru.data(), sizeof(int) * n_var);
     up(d_rng, rngc.data(), sizeof(int) * n_var);
@@ -1180,6 +1231,9 @@ int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_para
     a.blk_cell = d_bc.as<int>();
     a.blk_lo = d_bl.as<int>();
     a.blk_hi = d_bh.as<int>();
+    a.blk0 = d_b0.as<int>();
+    a.part = d_part.as<double>();
+    a.var_part = d_vpart.as<double>();
     a.cru0 = d_c0.as<int64_t>();
     a.ncru = d_n.as<int>();
     a.rng_cell = d_rng.as<int>();

@@ -300,74 +300,200 @@ GW_HD Gates gate_rates(double V, bool derivs, const double *T) {
     return r;
 }
 
-// The global increment (the same formulas and order as the reference), from the globals g and
-// their terms T (glob_terms).  Returns false for a non-positive Nernst argument, where the
-// reference exits (common.hpp:72-75).
-GW_HD bool glob_increment(const CellStatic &C, const double *g, const Carry &cy, double Istim, double dt,
-                          const double *T, double *d) {
+// The global increment (the same formulas and order as the reference) in three dependency levels,
+// so that a block can evaluate each level's items one per thread:
+//   glob_term   (level 1) the transcendental terms T, functions of the globals alone;
+//   kv_entry    (level 2) the off-diagonal Kv generator entries, functions of T;
+//   glob_qty    (level 3) the currents, fluxes and buffer factors, and the derivative components
+//               d[7..35] of the gates and Markov chains, functions of the globals, T, the carry and
+//               the Kv entries;
+//   glob_dconc  (level 4) d[0..6], linear combinations of the level-3 currents.
+// glob_increment runs the levels one item after the other; the values are the same either way.
+
+// Off-diagonal entries of the Kv4.3 (channel 1) and Kv1.4 (channel 0) generators, in the fill order
+// of update_QKv (GW.tpp:65-123): entry e < 26 of channel ch is kv_edges' edge e.
+constexpr int kKvE = 26;
+GW_HD double kv_entry(const gw_params &p, const double *T, int k) {
+    const int ch = k < kKvE ? 1 : 0, e = k % kKvE;
+    double r[4];
+    kv_rates(p, ch, T, r);
+    const double aa = r[0], ai = r[1], ba = r[2], bi = r[3];
+    const double f1 = ch == 0 ? p.f1Kv14 : p.f1Kv43, f2 = ch == 0 ? p.f2Kv14 : p.f2Kv43;
+    const double f3 = ch == 0 ? p.f3Kv14 : p.f3Kv43, f4 = ch == 0 ? p.f4Kv14 : p.f4Kv43;
+    const double b1 = ch == 0 ? p.b1Kv14 : p.b1Kv43, b2 = ch == 0 ? p.b2Kv14 : p.b2Kv43;
+    const double b3 = ch == 0 ? p.b3Kv14 : p.b3Kv43, b4 = ch == 0 ? p.b4Kv14 : p.b4Kv43;
+    switch (e) {
+    case 0: return 4 * aa;          // Q01
+    case 1: return bi;              // Q05
+    case 2: return ba;              // Q10
+    case 3: return 3 * aa;          // Q12
+    case 4: return f1 * bi;         // Q16
+    case 5: return 2 * ba;          // Q21
+    case 6: return 2 * aa;          // Q23
+    case 7: return f2 * bi;         // Q27
+    case 8: return 3 * ba;          // Q32
+    case 9: return aa;              // Q34
+    case 10: return f3 * bi;        // Q38
+    case 11: return 4 * ba;         // Q43
+    case 12: return f4 * bi;        // Q49
+    case 13: return 4 * aa * b1;    // Q56
+    case 14: return ai;             // Q50
+    case 15: return ba / f1;        // Q65
+    case 16: return 3 * aa * b2 / b1;  // Q67
+    case 17: return ai / b1;        // Q61
+    case 18: return 2 * ba * f1 / f2;  // Q76
+    case 19: return 2 * aa * b3 / b2;  // Q78
+    case 20: return ai / b2;        // Q72
+    case 21: return 3 * ba * f2 / f3;  // Q87
+    case 22: return aa * b4 / b3;   // Q89
+    case 23: return ai / b3;        // Q83
+    case 24: return 4 * ba * f3 / f4;  // Q98
+    default: return ai / b4;        // Q94
+    }
+}
+
+// The Q matrix of a channel from its entries E[26] (the diagonal as update_QKv forms it).
+GW_HD void kv_fill(const double *E, double Q[10][10]) {
+    Q[0][1] = E[0]; Q[0][5] = E[1]; Q[0][0] = -(Q[0][1] + Q[0][5]);
+    Q[1][0] = E[2]; Q[1][2] = E[3]; Q[1][6] = E[4]; Q[1][1] = -(Q[1][0] + Q[1][2] + Q[1][6]);
+    Q[2][1] = E[5]; Q[2][3] = E[6]; Q[2][7] = E[7]; Q[2][2] = -(Q[2][1] + Q[2][3] + Q[2][7]);
+    Q[3][2] = E[8]; Q[3][4] = E[9]; Q[3][8] = E[10]; Q[3][3] = -(Q[3][2] + Q[3][4] + Q[3][8]);
+    Q[4][3] = E[11]; Q[4][9] = E[12]; Q[4][4] = -(Q[4][3] + Q[4][9]);
+    Q[5][6] = E[13]; Q[5][0] = E[14]; Q[5][5] = -(Q[5][6] + Q[5][0]);
+    Q[6][5] = E[15]; Q[6][7] = E[16]; Q[6][1] = E[17]; Q[6][6] = -(Q[6][5] + Q[6][7] + Q[6][1]);
+    Q[7][6] = E[18]; Q[7][8] = E[19]; Q[7][2] = E[20]; Q[7][7] = -(Q[7][6] + Q[7][8] + Q[7][2]);
+    Q[8][7] = E[21]; Q[8][9] = E[22]; Q[8][3] = E[23]; Q[8][8] = -(Q[8][7] + Q[8][9] + Q[8][3]);
+    Q[9][8] = E[24]; Q[9][4] = E[25]; Q[9][9] = -(Q[9][8] + Q[9][4]);
+}
+
+// Component i of update_Kv_derivatives (GW.tpp:136-160) from the channel's entries E[26].
+GW_HD double kv_component(const double *E, const double *x, int i, double dt) {
+    double Q[10][10];
+    kv_fill(E, Q);
+    switch (i) {
+    case 0: return dt * (Q[1][0] * x[1] + Q[5][0] * x[5] + Q[0][0] * x[0]);
+    case 1: return dt * (Q[0][1] * x[0] + Q[2][1] * x[2] + Q[6][1] * x[6] + Q[1][1] * x[1]);
+    case 2: return dt * (Q[1][2] * x[1] + Q[3][2] * x[3] + Q[7][2] * x[7] + Q[2][2] * x[2]);
+    case 3: return dt * (Q[2][3] * x[2] + Q[4][3] * x[4] + Q[8][3] * x[8] + Q[3][3] * x[3]);
+    case 4: return dt * (Q[3][4] * x[3] + Q[9][4] * x[9] + Q[4][4] * x[4]);
+    case 5: return dt * (Q[6][5] * x[6] + Q[0][5] * x[0] + Q[5][5] * x[5]);
+    case 6: return dt * (Q[5][6] * x[5] + Q[7][6] * x[7] + Q[1][6] * x[1] + Q[6][6] * x[6]);
+    case 7: return dt * (Q[6][7] * x[6] + Q[8][7] * x[8] + Q[2][7] * x[2] + Q[7][7] * x[7]);
+    case 8: return dt * (Q[7][8] * x[7] + Q[9][8] * x[9] + Q[3][8] * x[3] + Q[8][8] * x[8]);
+    default: return dt * (Q[8][9] * x[8] + Q[4][9] * x[4] + Q[9][9] * x[9]);
+    }
+}
+
+// Level-3 quantities.
+enum Qty {
+    Q_INA = 0, Q_INAB, Q_INACA, Q_INAK, Q_IKR, Q_IKS, Q_IKV14, Q_IKV43, Q_ITO2, Q_IK1, Q_IKP, Q_ICAL, Q_ICAB,
+    Q_IPCA, Q_JUP, Q_BETA, Q_DLT, Q_DHT,
+    Q_D,              // d[7 + i], i = 0 .. 28: gates m h j xKs, IKr chain, Kv4.3, Kv1.4
+    kNQ = Q_D + 29
+};
+
+GW_HD double glob_qty(const CellStatic &C, const double *g, const Carry &cy, double dt, const double *T,
+                      const double *KvE, int k) {
     const gw_params &p = C.p;
     const double V = g[0], Nai = g[1], Ki = g[2], Cai = g[3], CaNSR = g[4], CaLT = g[5], CaHT = g[6];
     const double m = g[7], h = g[8], jg = g[9], xKs = g[10];
     const double *Kr = g + 11, *Kv43 = g + 16, *Kv14 = g + 26;
-    if (!(Nai > 0.0) || !(Ki > 0.0)) return false;
     const double VF_RT = V * C.F_RT, e = T[T_E];
     const double ENa = T[T_LNA] * C.RT_F / 1.0;
     const double EK = T[T_LK] * C.RT_F / 1.0;
     const double ECa = T[T_LK] * C.RT_F / 2.0;
-    const double INa = p.GNa * cubed(m) * h * jg * (V - ENa);
-    const double INab = p.GNab * (V - ENa);
-    const double e1 = T[T_E1], e2 = e1 * e;
-    const double INaCa = C.INaCa_const * (e1 * cubed(Nai) * p.Cao - e2 * C.Nao3 * Cai) / (1.0 + p.ksat * e2);
-    const double fNaK = 1.0 / (1.0 + 0.1245 * T[T_ENAK] + 0.0365 * C.sigma * e);
-    const double INaK = C.INaK_const * fNaK / (1.0 + T[T_PNAK]);
-    const double RKr = 1.0 / (1.0 + 1.4945 * T[T_RKR]);
-    const double IKr = p.GKr * C.sqrtKo * RKr * Kr[3] * (V - EK) * 0.5;
-    const double EKs = T[T_LKS] * C.RT_F;
-    const double IKs = p.GKs * sqd(xKs) * (V - EKs);
-    const double mm = C.PKv14_Csc * (kFaradayA * VF_RT) * Kv14[4] / (1 - e);
-    const double IKv14 = mm * ((Ki - p.Ko * e) + 0.02 * (Nai - p.Nao * e)) * 1.0e9;
-    const double IKv43 = p.GKv43 * Kv43[4] * (V - EK);
-    const double Ito1 = IKv14 + IKv43;
-    const double Ito2 = cy.clch * C.Ito2_const * VF_RT * (p.Clcyto * e - p.Clo) / (e - 1.0);
-    const double K1inf = 1.0 / (2.0 + T[T_K1]);
-    const double IK1 = p.GK1 * K1inf * C.IK1_const * (V - EK);
-    const double Kp = 1. / (1. + T[T_KP]);
-    const double IKp = p.GKp * Kp * (V - EK);
-    const double ICaL = cy.jlcc * C.ICaL_const;
-    const double ICab = p.GCab * (V - ECa);
-    const double IpCa = p.IpCamax * (Cai / (p.KmpCa + Cai));
-    const double fu = T[T_FU], ru = T[T_RU];
-    const double Jup = (p.Vmaxf * fu - p.Vmaxr * ru) / (1.0 + fu + ru);
-    const double Jtr_tot = cy.jtr * C.CRU_factor, Jxfer_tot = cy.jxfer * C.CRU_factor;
-    const double beta_cyto = 1.0 / (1.0 + C.CMDN_const / sqd(p.KCMDN + Cai));
-    double dLT = p.kLTRPNp * Cai * (p.LTRPNtot - CaLT) - p.kLTRPNm * CaLT;
-    double dHT = p.kHTRPNp * Cai * (p.HTRPNtot - CaHT) - p.kHTRPNm * CaHT;
-    d[1] = -dt * C.CSA_FVcyto * (INa + INab + 3 * INaCa + 3 * INaK);
-    d[2] = -dt * C.CSA_FVcyto * (IKr + IKs + Ito1 + IK1 + IKp - 2 * INaK);
-    d[3] = dt * beta_cyto *
-           (-0.5 * C.CSA_FVcyto * (ICab + IpCa - 2 * INaCa) + C.VSS_Vcyto * Jxfer_tot - Jup - (dLT + dHT));
-    d[4] = dt * (C.Vcyto_VNSR * Jup - C.VJSR_VNSR * Jtr_tot);
-    d[5] = dLT * dt;
-    d[6] = dHT * dt;
-    d[0] = dt * (Istim - (INa + ICaL + IKr + IKs + Ito1 + IK1 + IKp + Ito2 + INaK + INaCa + IpCa + ICab + INab));
-    const Gates gr = gate_rates(V, false, T);
-    d[7] = dt * (gr.am * (1.0 - m) - gr.bm * m);
-    d[8] = dt * (gr.ah * (1.0 - h) - gr.bh * h);
-    d[9] = dt * (gr.aj * (1.0 - jg) - gr.bj * jg);
-    d[10] = dt * (gr.xinf - xKs) * gr.tinv;
-    const KrQ q = kr_q(T);
-    const double Q00 = -q.q01, Q11 = -(q.q10 + p.Kf), Q22 = -(p.Kb + q.q23 + q.q24), Q33 = -(q.q32 + q.q34);
-    const double Q44 = -(q.q42 + q.q43);
-    d[11] = dt * (q.q10 * Kr[1] + Q00 * Kr[0]);
-    d[12] = dt * (q.q01 * Kr[0] + p.Kb * Kr[2] + Q11 * Kr[1]);
-    d[13] = dt * (p.Kf * Kr[1] + q.q32 * Kr[3] + q.q42 * Kr[4] + Q22 * Kr[2]);
-    d[14] = dt * (q.q23 * Kr[2] + q.q43 * Kr[4] + Q33 * Kr[3]);
-    d[15] = dt * (q.q24 * Kr[2] + q.q34 * Kr[3] + Q44 * Kr[4]);
-    double Q[10][10];
-    kv_matrix(p, 1, T, Q);
-    kv_deriv(Q, Kv43, d + 16, dt);
-    kv_matrix(p, 0, T, Q);
-    kv_deriv(Q, Kv14, d + 26, dt);
+    (void)CaNSR;
+    switch (k) {
+    case Q_INA: return p.GNa * cubed(m) * h * jg * (V - ENa);
+    case Q_INAB: return p.GNab * (V - ENa);
+    case Q_INACA: {
+        const double e1 = T[T_E1], e2 = e1 * e;
+        return C.INaCa_const * (e1 * cubed(Nai) * p.Cao - e2 * C.Nao3 * Cai) / (1.0 + p.ksat * e2);
+    }
+    case Q_INAK: {
+        const double fNaK = 1.0 / (1.0 + 0.1245 * T[T_ENAK] + 0.0365 * C.sigma * e);
+        return C.INaK_const * fNaK / (1.0 + T[T_PNAK]);
+    }
+    case Q_IKR: {
+        const double RKr = 1.0 / (1.0 + 1.4945 * T[T_RKR]);
+        return p.GKr * C.sqrtKo * RKr * Kr[3] * (V - EK) * 0.5;
+    }
+    case Q_IKS: return p.GKs * sqd(xKs) * (V - T[T_LKS] * C.RT_F);
+    case Q_IKV14: {
+        const double mm = C.PKv14_Csc * (kFaradayA * VF_RT) * Kv14[4] / (1 - e);
+        return mm * ((Ki - p.Ko * e) + 0.02 * (Nai - p.Nao * e)) * 1.0e9;
+    }
+    case Q_IKV43: return p.GKv43 * Kv43[4] * (V - EK);
+    case Q_ITO2: return cy.clch * C.Ito2_const * VF_RT * (p.Clcyto * e - p.Clo) / (e - 1.0);
+    case Q_IK1: return p.GK1 * (1.0 / (2.0 + T[T_K1])) * C.IK1_const * (V - EK);
+    case Q_IKP: return p.GKp * (1. / (1. + T[T_KP])) * (V - EK);
+    case Q_ICAL: return cy.jlcc * C.ICaL_const;
+    case Q_ICAB: return p.GCab * (V - ECa);
+    case Q_IPCA: return p.IpCamax * (Cai / (p.KmpCa + Cai));
+    case Q_JUP: {
+        const double fu = T[T_FU], ru = T[T_RU];
+        return (p.Vmaxf * fu - p.Vmaxr * ru) / (1.0 + fu + ru);
+    }
+    case Q_BETA: return 1.0 / (1.0 + C.CMDN_const / sqd(p.KCMDN + Cai));
+    case Q_DLT: return p.kLTRPNp * Cai * (p.LTRPNtot - CaLT) - p.kLTRPNm * CaLT;
+    case Q_DHT: return p.kHTRPNp * Cai * (p.HTRPNtot - CaHT) - p.kHTRPNm * CaHT;
+    default: break;
+    }
+    const int i = k - Q_D;
+    if (i < 4) {
+        const Gates gr = gate_rates(V, false, T);
+        switch (i) {
+        case 0: return dt * (gr.am * (1.0 - m) - gr.bm * m);
+        case 1: return dt * (gr.ah * (1.0 - h) - gr.bh * h);
+        case 2: return dt * (gr.aj * (1.0 - jg) - gr.bj * jg);
+        default: return dt * (gr.xinf - xKs) * gr.tinv;
+        }
+    }
+    if (i < 9) {
+        const KrQ q = kr_q(T);
+        switch (i - 4) {
+        case 0: return dt * (q.q10 * Kr[1] + (-q.q01) * Kr[0]);
+        case 1: return dt * (q.q01 * Kr[0] + p.Kb * Kr[2] + (-(q.q10 + p.Kf)) * Kr[1]);
+        case 2: return dt * (p.Kf * Kr[1] + q.q32 * Kr[3] + q.q42 * Kr[4] + (-(p.Kb + q.q23 + q.q24)) * Kr[2]);
+        case 3: return dt * (q.q23 * Kr[2] + q.q43 * Kr[4] + (-(q.q32 + q.q34)) * Kr[3]);
+        default: return dt * (q.q24 * Kr[2] + q.q34 * Kr[3] + (-(q.q42 + q.q43)) * Kr[4]);
+        }
+    }
+    if (i < 19) return kv_component(KvE, Kv43, i - 9, dt);
+    return kv_component(KvE + kKvE, Kv14, i - 19, dt);
+}
+
+// d[k], k < 7, from the level-3 quantities Qv.
+GW_HD double glob_dconc(const CellStatic &C, const Carry &cy, double Istim, double dt, const double *Qv, int k) {
+    const double INa = Qv[Q_INA], INab = Qv[Q_INAB], INaCa = Qv[Q_INACA], INaK = Qv[Q_INAK];
+    const double IKr = Qv[Q_IKR], IKs = Qv[Q_IKS], Ito1 = Qv[Q_IKV14] + Qv[Q_IKV43], IK1 = Qv[Q_IK1];
+    const double IKp = Qv[Q_IKP];
+    switch (k) {
+    case 0:
+        return dt * (Istim - (INa + Qv[Q_ICAL] + IKr + IKs + Ito1 + IK1 + IKp + Qv[Q_ITO2] + INaK + INaCa +
+                              Qv[Q_IPCA] + Qv[Q_ICAB] + INab));
+    case 1: return -dt * C.CSA_FVcyto * (INa + INab + 3 * INaCa + 3 * INaK);
+    case 2: return -dt * C.CSA_FVcyto * (IKr + IKs + Ito1 + IK1 + IKp - 2 * INaK);
+    case 3:
+        return dt * Qv[Q_BETA] *
+               (-0.5 * C.CSA_FVcyto * (Qv[Q_ICAB] + Qv[Q_IPCA] - 2 * INaCa) + C.VSS_Vcyto * (cy.jxfer * C.CRU_factor) -
+                Qv[Q_JUP] - (Qv[Q_DLT] + Qv[Q_DHT]));
+    case 4: return dt * (C.Vcyto_VNSR * Qv[Q_JUP] - C.VJSR_VNSR * (cy.jtr * C.CRU_factor));
+    case 5: return Qv[Q_DLT] * dt;
+    default: return Qv[Q_DHT] * dt;
+    }
+}
+
+// The global increment d = G[s+1] - G[s] from the globals g and their terms T.  Returns false for a
+// non-positive Nernst argument, where the reference exits (common.hpp:72-75).
+GW_HD bool glob_increment(const CellStatic &C, const double *g, const Carry &cy, double Istim, double dt,
+                          const double *T, double *d) {
+    if (!(g[1] > 0.0) || !(g[2] > 0.0)) return false;
+    double E[2 * kKvE], Qv[kNQ];
+    for (int k = 0; k < 2 * kKvE; ++k) E[k] = kv_entry(C.p, T, k);
+    for (int k = 0; k < kNQ; ++k) Qv[k] = glob_qty(C, g, cy, dt, T, E, k);
+    for (int k = 0; k < 7; ++k) d[k] = glob_dconc(C, cy, Istim, dt, Qv, k);
+    for (int k = 0; k < 29; ++k) d[7 + k] = Qv[Q_D + k];
     return true;
 }
 
