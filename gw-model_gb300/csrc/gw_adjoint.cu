@@ -173,6 +173,12 @@ __device__ __forceinline__ void stage_cell(CellStatic &dst, const CellStatic &sr
     for (int i = (int)threadIdx.x; i < (int)(sizeof(CellStatic) / 16); i += (int)blockDim.x) d[i] = s[i];
 }
 
+// The item of thread t when a level's items are dealt round-robin over the block's warps: each item
+// takes its own code path, and a warp runs the paths of its lanes one after the other, so items
+// spread over the four warps (four sub-partitions, four FP64 units) finish about 4x sooner than
+// items packed into the lanes of one or two warps.
+__device__ __forceinline__ int item_of(int t) { return (t & 31) * (kBlk / 32) + (t >> 5); }
+
 __device__ __forceinline__ void open_counts(const CruD &c, int o[4]) {
 #pragma unroll
     for (int j = 0; j < 4; ++j) o[j] = dev::byte_s(c.ryr[2], j) + dev::byte_s(c.ryr[3], j);
@@ -367,11 +373,12 @@ __global__ void __launch_bounds__(kBlk) k_global(const GradArgs a, int64_t step,
     const Carry c0{cy[0], cy[1], cy[2], cy[3]};
     const double istim = pulse_at(a.t[cell], a.stim + 4 * (int64_t)cell);
     __syncthreads();
-    if (t < kNT) T[t] = glob_term(C, gs, t);
+    const int it = item_of(t);
+    if (it < kNT) T[it] = glob_term(C, gs, it);
     __syncthreads();
-    if (t < 2 * kKvE) E[t] = kv_entry(C.p, T, t);
+    if (it < 2 * kKvE) E[it] = kv_entry(C.p, T, it);
     __syncthreads();
-    if (t < kNQ) Qv[t] = glob_qty(C, gs, c0, a.dt, T, E, t);
+    if (it < kNQ) Qv[it] = glob_qty(C, gs, c0, a.dt, T, E, it);
     __syncthreads();
     if (t < kNumGlobals) gn[t] = gs[t] + (t < 7 ? glob_dconc(C, c0, istim, a.dt, Qv, t) : Qv[Q_D + t - 7]);
     __syncthreads();
@@ -404,7 +411,7 @@ __global__ void __launch_bounds__(kBlk) k_global(const GradArgs a, int64_t step,
     }
     __syncthreads();
     if (!ok) return;
-    if (t < kNS) S[t] = sv_term(C, gn, t);
+    if (it < kNS) S[it] = sv_term(C, gn, it);
     __syncthreads();
     if (t == 0) {
         step_values(C, gn, S, svo);
@@ -573,56 +580,72 @@ __global__ void __launch_bounds__(kBlk) k_cru_busy(const GradArgs a, const AdjAr
     }
 }
 
-// Reverse of the global step `step` (one block per cell): the cell's CRU rows summed in a fixed
-// order, then the adjoint of the global increment by thread 0.
+// Reverse of the global step `step` (one block per cell): the cell's block sums of the CRU rows, the
+// increment's transcendental terms one per thread, the kAdjParts parts of the increment's adjoint
+// one per thread into rows summed in a fixed order, then the CRU inputs' contributions.
+constexpr int kAdjOut = kNumGlobals + 3 + kTheta;  // lam_g, lam_cy, lam_th of one part
 __global__ void __launch_bounds__(kBlk) k_global_adj(const GradArgs a, const AdjArgs b, int64_t step, int slot) {
     __shared__ double T[kNT];
     __shared__ double sai[kAdjIn];
+    __shared__ double lam[kNumGlobals];
+    __shared__ double rows[kAdjParts][kAdjOut];
+    __shared__ double tot[kAdjOut];
     __shared__ __align__(16) CellStatic C;
     const int cell = blockIdx.x;
+    const int t = (int)threadIdx.x;
     stage_cell(C, a.cs[cell]);
-    if (threadIdx.x < kAdjIn) {
+    if (t < kAdjIn) {
         double v = 0.0;
-        for (int k = a.blk0[cell]; k < a.blk0[cell + 1]; ++k) v += b.ai_part[(int64_t)kAdjIn * k + threadIdx.x];
-        sai[threadIdx.x] = v;
+        for (int k = a.blk0[cell]; k < a.blk0[cell + 1]; ++k) v += b.ai_part[(int64_t)kAdjIn * k + t];
+        sai[t] = v;
     }
     const int64_t r = (int64_t)slot * a.n_cells + cell;
     const double *g = a.seg_G + r * kNumGlobals;
-    __syncthreads();
-    if (threadIdx.x < kNT) T[threadIdx.x] = glob_term(C, g, (int)threadIdx.x);
-    __syncthreads();
-    if (threadIdx.x != 0) return;
-    double ai[kAdjIn];
-    for (int q = 0; q < kAdjIn; ++q) ai[q] = sai[q];
     const double *cyv = a.seg_carry + r * 4;
-    const double *sv = a.seg_sv + r * kSvCount;
     const Carry cy{cyv[0], cyv[1], cyv[2], cyv[3]};
     double *lgp = b.lam_G + (int64_t)kNumGlobals * cell;
-    double lam[kNumGlobals], lg[kNumGlobals];
-    for (int k = 0; k < kNumGlobals; ++k) {
-        lam[k] = lgp[k];
-        lg[k] = 0.0;
+    if (t < kNumGlobals) {
+        double v = lgp[t];
+        if (t == 0 && (step + 1) % a.sample_every == 0) {
+            const int64_t si = (step + 1) / a.sample_every - 1;
+            if (si < a.n_samples) v += b.dLdV[(int64_t)cell * a.n_samples + si];
+        }
+        lam[t] = v;
     }
-    if ((step + 1) % a.sample_every == 0) {
-        const int64_t si = (step + 1) / a.sample_every - 1;
-        if (si < a.n_samples) lam[0] += b.dLdV[(int64_t)cell * a.n_samples + si];
+    __syncthreads();
+    const int it = item_of(t);
+    if (it < kNT) T[it] = glob_term(C, g, it);
+    __syncthreads();
+    if (it < kAdjParts) {
+        double *row = rows[it];
+        for (int k = 0; k < kAdjOut; ++k) row[k] = 0.0;
+        glob_increment_adj(C, g, cy, a.dt, T, lam, it, row, row + kNumGlobals, row + kNumGlobals + 3);
     }
-    double lcy[3] = {0.0, 0.0, 0.0};
+    __syncthreads();
+    if (t < kAdjOut) {
+        double v = 0.0;
+        for (int q = 0; q < kAdjParts; ++q) v += rows[q][t];
+        tot[t] = v;
+    }
+    __syncthreads();
+    if (t != 0) return;
+    const double *sv = a.seg_sv + r * kSvCount;
+    double lg[kNumGlobals];
+    for (int k = 0; k < kNumGlobals; ++k) lg[k] = tot[k];
     double *th = b.lam_th + (int64_t)kTheta * cell;
     double lth[kTheta];
-    for (int k = 0; k < kTheta; ++k) lth[k] = th[k];
-    glob_increment_adj(C, g, cy, a.dt, T, lam, lg, lcy, lth);
+    for (int k = 0; k < kTheta; ++k) lth[k] = th[k] + tot[kNumGlobals + 3 + k];
     // the CRUs' step inputs: Cai, CaNSR and the JLCC factors of V
-    lg[3] += ai[0];
-    lg[4] += ai[1];
+    lg[3] += sai[0];
+    lg[4] += sai[1];
     double dJM, dJE;
     jlcc_factor_derivs(C, g[0], sv[SV_JEXP], dJM, dJE);
-    lg[0] += ai[2] * dJM + ai[3] * dJE;
-    lth[TH_PCAL] += ai[2] * sv[SV_JMUL];
-    lth[TH_RRYR] += ai[4];
-    lth[TH_CSQNT] += ai[5] * C.CSQN_const;
+    lg[0] += sai[2] * dJM + sai[3] * dJE;
+    lth[TH_PCAL] += sai[2] * sv[SV_JMUL];
+    lth[TH_RRYR] += sai[4];
+    lth[TH_CSQNT] += sai[5] * C.CSQN_const;
     for (int k = 0; k < kNumGlobals; ++k) lgp[k] = lg[k];
-    for (int k = 0; k < 3; ++k) b.lam_cy[3 * (int64_t)cell + k] = lcy[k];
+    for (int k = 0; k < 3; ++k) b.lam_cy[3 * (int64_t)cell + k] = tot[kNumGlobals + k];
     for (int k = 0; k < kTheta; ++k) th[k] = lth[k];
 }
 

@@ -555,197 +555,168 @@ GW_HD void jlcc_factor_derivs(const CellStatic &C, double V, double JE, double &
     dJM = C.JLCC_const * C.F_RT * ((JE - 1.0) - V * dJE) / sqd(JE - 1.0);
 }
 
-// The adjoint of one global increment: with lam = dL/dG[s+1] and G[s+1] = G[s] + d, adds
-// dL/dG[s] (the identity included) to lam_g, dL/d(carry jlcc, jtr, jxfer) to lam_cy[0..2] and the
-// relative sensitivities of GKr, GKs, GK1, INaKmax and Vmax to lam_th.
+// The adjoint of one global increment, in kAdjParts independent parts: with lam = dL/dG[s+1] and
+// G[s+1] = G[s] + d, part q adds its share of dL/dG[s] to lam_g, of dL/d(carry JLCC, Jtr, Jxfer) to
+// lam_cy and of the relative sensitivities of GKr, GKs, GK1, INaKmax and Vmax to lam_th.  The sum of
+// the parts is the whole adjoint (part 0 carries the identity); each part converts its own V, exp(-VF/RT)
+// and Nernst-potential accumulators at its end, so that a block can run the parts one per thread.
+enum AdjPart { AP_NA = 0, AP_NAK, AP_TO, AP_K1, AP_CA, AP_GATE_MH, AP_GATE_JX, AP_KR, AP_KV43, AP_KV14, kAdjParts };
+
 GW_HD void glob_increment_adj(const CellStatic &C, const double *g, const Carry &cy, double dt, const double *T,
-                              const double *lam, double *lam_g, double *lam_cy, double *lam_th) {
+                              const double *lam, int part, double *lam_g, double *lam_cy, double *lam_th) {
     const gw_params &p = C.p;
     const double V = g[0], Nai = g[1], Ki = g[2], Cai = g[3], CaNSR = g[4], CaLT = g[5], CaHT = g[6];
     const double m = g[7], h = g[8], jg = g[9], xKs = g[10];
     const double *Kr = g + 11, *Kv43 = g + 16, *Kv14 = g + 26;
-    for (int i = 0; i < kNumGlobals; ++i) lam_g[i] += lam[i];
-    // forward values
-    const double F_RT = C.F_RT, RT_F = C.RT_F;
+    const double F_RT = C.F_RT, RT_F = C.RT_F, CSA = C.CSA_FVcyto;
     const double VF_RT = V * F_RT, e = T[T_E];
     const double ENa = T[T_LNA] * RT_F, EK = T[T_LK] * RT_F, ECa = T[T_LK] * RT_F / 2.0;
-    const double m3hj = cubed(m) * h * jg;
-    const double e1 = T[T_E1], e2 = e1 * e;
-    const double numNC = e1 * cubed(Nai) * p.Cao - e2 * C.Nao3 * Cai, denNC = 1.0 + p.ksat * e2;
-    const double INaCa = C.INaCa_const * numNC / denNC;
-    const double E1k = T[T_ENAK];
-    const double fNaK = 1.0 / (1.0 + 0.1245 * E1k + 0.0365 * C.sigma * e);
-    const double qNaK = 1.0 + T[T_PNAK];
-    const double INaK = C.INaK_const * fNaK / qNaK;
-    const double ERk = T[T_RKR], RKr = 1.0 / (1.0 + 1.4945 * ERk);
-    const double IKr = p.GKr * C.sqrtKo * RKr * Kr[3] * (V - EK) * 0.5;
-    const double sKs = Ki + 0.01833 * Nai;
-    const double EKs = T[T_LKS] * RT_F;
-    const double IKs = p.GKs * sqd(xKs) * (V - EKs);
-    const double P14 = C.PKv14_Csc * kFaradayA;
-    const double A14 = (Ki - p.Ko * e) + 0.02 * (Nai - p.Nao * e);
-    const double mm = P14 * VF_RT * Kv14[4] / (1 - e);
-    const double uK1 = V - EK, EK1 = T[T_K1], K1inf = 1.0 / (2.0 + EK1);
-    const double IK1 = p.GK1 * K1inf * C.IK1_const * uK1;
-    const double EKp = T[T_KP], Kp = 1. / (1. + EKp);
-    const double fu = T[T_FU], ru = T[T_RU], den = 1.0 + fu + ru;
-    const double Jup = (p.Vmaxf * fu - p.Vmaxr * ru) / den;
-    const double Jxfer_tot = cy.jxfer * C.CRU_factor;
-    const double beta = 1.0 / (1.0 + C.CMDN_const / sqd(p.KCMDN + Cai));
-    const double dLT = p.kLTRPNp * Cai * (p.LTRPNtot - CaLT) - p.kLTRPNm * CaLT;
-    const double dHT = p.kHTRPNp * Cai * (p.HTRPNtot - CaHT) - p.kHTRPNm * CaHT;
-    const double ICab = p.GCab * (V - ECa), IpCa = p.IpCamax * (Cai / (p.KmpCa + Cai));
-    const double Q3 = -0.5 * C.CSA_FVcyto * (ICab + IpCa - 2 * INaCa) + C.VSS_Vcyto * Jxfer_tot - Jup - (dLT + dHT);
-    const double CSA = C.CSA_FVcyto;
-
-    // adjoints of the currents
-    double lINa = 0, lINab = 0, lINaCa = 0, lINaK = 0, lIKr = 0, lIKs = 0, lIto1 = 0, lIK1 = 0, lIKp = 0;
-    double lIto2 = 0, lICaL = 0, lICab = 0, lIpCa = 0, lJup = 0, lJtr = 0, lJxfer = 0, lbeta = 0, ldLT = 0, ldHT = 0;
-    // d[1], d[2]
-    lINa += -dt * CSA * lam[1]; lINab += -dt * CSA * lam[1]; lINaCa += -3 * dt * CSA * lam[1];
-    lINaK += -3 * dt * CSA * lam[1];
-    lIKr += -dt * CSA * lam[2]; lIKs += -dt * CSA * lam[2]; lIto1 += -dt * CSA * lam[2];
-    lIK1 += -dt * CSA * lam[2]; lIKp += -dt * CSA * lam[2]; lINaK += 2 * dt * CSA * lam[2];
-    // d[3]
-    lbeta += lam[3] * dt * Q3;
-    {
-        const double lQ = lam[3] * dt * beta;
-        lICab += -0.5 * CSA * lQ; lIpCa += -0.5 * CSA * lQ; lINaCa += CSA * lQ;
-        lJxfer += C.VSS_Vcyto * lQ; lJup -= lQ; ldLT -= lQ; ldHT -= lQ;
-    }
-    // d[4], d[5], d[6]
-    lJup += dt * C.Vcyto_VNSR * lam[4];
-    lJtr += -dt * C.VJSR_VNSR * lam[4];
-    ldLT += dt * lam[5];
-    ldHT += dt * lam[6];
-    // d[0]
-    {
-        const double l0 = -dt * lam[0];
-        lINa += l0; lICaL += l0; lIKr += l0; lIKs += l0; lIto1 += l0; lIK1 += l0; lIKp += l0;
-        lIto2 += l0; lINaK += l0; lINaCa += l0; lIpCa += l0; lICab += l0; lINab += l0;
-    }
-    // state adjoints from the currents
+    // adjoints of the currents: d[0] = dt (Istim - sum I), d[1] and d[2] their Na and K shares, d[3] the
+    // buffered cytosolic Ca balance (lQ = lam3 dt beta), d[4] the NSR balance
+    const double l0 = -dt * lam[0], l1 = -dt * CSA * lam[1], l2 = -dt * CSA * lam[2];
+    auto beta_cyto = [&]() { return 1.0 / (1.0 + C.CMDN_const / sqd(p.KCMDN + Cai)); };
     double lV = 0, lNai = 0, lKi = 0, lCai = 0, lCaNSR = 0, lVF = 0, le = 0, lENa = 0, lEK = 0, lECa = 0;
-    // INa, INab
-    lam_g[7] += lINa * 3 * p.GNa * sqd(m) * h * jg * (V - ENa);
-    lam_g[8] += lINa * p.GNa * cubed(m) * jg * (V - ENa);
-    lam_g[9] += lINa * p.GNa * cubed(m) * h * (V - ENa);
-    lV += lINa * p.GNa * m3hj;
-    lENa -= lINa * p.GNa * m3hj;
-    lV += lINab * p.GNab;
-    lENa -= lINab * p.GNab;
-    // INaCa
-    {
-        const double lnum = lINaCa * C.INaCa_const / denNC;
-        const double lden = -lINaCa * INaCa / denNC;
+    switch (part) {
+    case AP_NA: {
+        for (int i = 0; i < kNumGlobals; ++i) lam_g[i] += lam[i];
+        const double lQ = lam[3] * dt * beta_cyto();
+        const double lINa = l0 + l1, lINab = l0 + l1, lINaCa = l0 + 3 * l1 + CSA * lQ;
+        const double m3hj = cubed(m) * h * jg;
+        lam_g[7] += lINa * 3 * p.GNa * sqd(m) * h * jg * (V - ENa);
+        lam_g[8] += lINa * p.GNa * cubed(m) * jg * (V - ENa);
+        lam_g[9] += lINa * p.GNa * cubed(m) * h * (V - ENa);
+        lV += lINa * p.GNa * m3hj + lINab * p.GNab;
+        lENa -= lINa * p.GNa * m3hj + lINab * p.GNab;
+        const double e1 = T[T_E1], e2 = e1 * e;
+        const double numNC = e1 * cubed(Nai) * p.Cao - e2 * C.Nao3 * Cai, denNC = 1.0 + p.ksat * e2;
+        const double rden = 1.0 / denNC;
+        const double INaCa = C.INaCa_const * numNC * rden;
+        const double lnum = lINaCa * C.INaCa_const * rden;
+        const double lden = -lINaCa * INaCa * rden;
         double le1 = lnum * cubed(Nai) * p.Cao;
         lNai += lnum * 3 * e1 * sqd(Nai) * p.Cao;
-        double le2 = -lnum * C.Nao3 * Cai + lden * p.ksat;
+        const double le2 = -lnum * C.Nao3 * Cai + lden * p.ksat;
         lCai += -lnum * e2 * C.Nao3;
         le1 += le2 * e;
         le += le2 * e1;
         lVF += le1 * p.eta * e1;
+        break;
     }
-    // INaK
-    {
-        const double lf = lINaK * C.INaK_const / qNaK;
-        const double lq = -lINaK * INaK / qNaK;
+    case AP_NAK: {
+        const double lINaK = l0 + 3 * l1 - 2 * l2, lIKr = l0 + l2, lIKs = l0 + l2;
+        const double E1k = T[T_ENAK];
+        const double fNaK = 1.0 / (1.0 + 0.1245 * E1k + 0.0365 * C.sigma * e);
+        const double rq = 1.0 / (1.0 + T[T_PNAK]);
+        const double INaK = C.INaK_const * fNaK * rq;
+        const double lf = lINaK * C.INaK_const * rq;
+        const double lq = -lINaK * INaK * rq;
         lNai += lq * (-1.5 * T[T_PNAK] / Nai);
         const double lD = -lf * sqd(fNaK);
         lVF += lD * 0.1245 * (-0.1) * E1k;
         le += lD * 0.0365 * C.sigma;
         lam_th[TH_INAK] += lINaK * INaK;
-    }
-    // IKr
-    {
+        const double ERk = T[T_RKR], RKr = 1.0 / (1.0 + 1.4945 * ERk);
         const double k = p.GKr * C.sqrtKo * 0.5;
         lam_g[14] += lIKr * k * RKr * (V - EK);
         const double dRKr = -sqd(RKr) * 1.4945 * 0.0446 * ERk;
         lV += lIKr * k * Kr[3] * (RKr + (V - EK) * dRKr);
         lEK -= lIKr * k * RKr * Kr[3];
-        lam_th[TH_GKR] += lIKr * IKr;
-    }
-    // IKs
-    {
+        lam_th[TH_GKR] += lIKr * (k * RKr * Kr[3] * (V - EK));
+        const double sKs = Ki + 0.01833 * Nai, EKs = T[T_LKS] * RT_F;
         lam_g[10] += lIKs * 2 * p.GKs * xKs * (V - EKs);
         lV += lIKs * p.GKs * sqd(xKs);
-        const double lEKs = -lIKs * p.GKs * sqd(xKs);
-        lKi += lEKs * (-RT_F / sKs);
-        lNai += lEKs * (-0.01833 * RT_F / sKs);
-        lam_th[TH_GKS] += lIKs * IKs;
+        const double lEKs = -lIKs * p.GKs * sqd(xKs), rs = RT_F / sKs;
+        lKi -= lEKs * rs;
+        lNai -= lEKs * 0.01833 * rs;
+        lam_th[TH_GKS] += lIKs * (p.GKs * sqd(xKs) * (V - EKs));
+        break;
     }
-    // Ito1 = IKv14 + IKv43
-    {
-        const double lI14 = lIto1, lI43 = lIto1;
-        const double lmm = lI14 * A14 * 1.0e9, lA = lI14 * mm * 1.0e9;
+    case AP_TO: {
+        const double lIto1 = l0 + l2, lIto2 = l0;
+        const double P14 = C.PKv14_Csc * kFaradayA, r1 = 1.0 / (1 - e);
+        const double A14 = (Ki - p.Ko * e) + 0.02 * (Nai - p.Nao * e);
+        const double mm = P14 * VF_RT * Kv14[4] * r1;
+        const double lmm = lIto1 * A14 * 1.0e9, lA = lIto1 * mm * 1.0e9;
         lKi += lA;
         lNai += 0.02 * lA;
         le += lA * (-p.Ko - 0.02 * p.Nao);
-        lam_g[30] += lmm * P14 * VF_RT / (1 - e);
-        lVF += lmm * P14 * Kv14[4] / (1 - e);
-        le += lmm * P14 * VF_RT * Kv14[4] / sqd(1 - e);
-        lam_g[20] += lI43 * p.GKv43 * (V - EK);
-        lV += lI43 * p.GKv43 * Kv43[4];
-        lEK -= lI43 * p.GKv43 * Kv43[4];
-    }
-    // Ito2 = clch Ito2_const VF (Clcyto e - Clo) / (e - 1)
-    {
-        const double B = (p.Clcyto * e - p.Clo) / (e - 1.0);
-        const double k = cy.clch * C.Ito2_const;
+        lam_g[30] += lmm * P14 * VF_RT * r1;
+        lVF += lmm * P14 * Kv14[4] * r1;
+        le += lmm * P14 * VF_RT * Kv14[4] * r1 * r1;
+        lam_g[20] += lIto1 * p.GKv43 * (V - EK);
+        lV += lIto1 * p.GKv43 * Kv43[4];
+        lEK -= lIto1 * p.GKv43 * Kv43[4];
+        const double r2 = 1.0 / (e - 1.0);
+        const double B = (p.Clcyto * e - p.Clo) * r2, k = cy.clch * C.Ito2_const;
         lVF += lIto2 * k * B;
-        le += lIto2 * k * VF_RT * (p.Clo - p.Clcyto) / sqd(e - 1.0);
+        le += lIto2 * k * VF_RT * (p.Clo - p.Clcyto) * r2 * r2;
+        break;
     }
-    // IK1
-    {
+    case AP_K1: {
+        const double lIK1 = l0 + l2, lIKp = l0 + l2;
+        const double lQ = lam[3] * dt * beta_cyto();
+        const double lICab = l0 - 0.5 * CSA * lQ, lIpCa = l0 - 0.5 * CSA * lQ;
+        const double uK1 = V - EK, EK1 = T[T_K1], K1inf = 1.0 / (2.0 + EK1);
         const double dK1 = -sqd(K1inf) * 1.5 * F_RT * EK1;
         const double dIdu = p.GK1 * C.IK1_const * (K1inf + uK1 * dK1);
         lV += lIK1 * dIdu;
         lEK -= lIK1 * dIdu;
-        lam_th[TH_GK1] += lIK1 * IK1;
-    }
-    // IKp
-    {
+        lam_th[TH_GK1] += lIK1 * (p.GK1 * K1inf * C.IK1_const * uK1);
+        const double EKp = T[T_KP], Kp = 1. / (1. + EKp);
         const double dKp = sqd(Kp) * EKp / 5.98;
         lV += lIKp * p.GKp * (Kp + (V - EK) * dKp);
         lEK -= lIKp * p.GKp * Kp;
+        lam_cy[0] += l0 * C.ICaL_const;  // ICaL = sum JLCC x ICaL_const
+        lV += lICab * p.GCab;
+        lECa -= lICab * p.GCab;
+        lCai += lIpCa * p.IpCamax * p.KmpCa / sqd(p.KmpCa + Cai);
+        break;
     }
-    // ICaL, ICab, IpCa
-    lam_cy[0] += lICaL * C.ICaL_const;
-    lV += lICab * p.GCab;
-    lECa -= lICab * p.GCab;
-    lCai += lIpCa * p.IpCamax * p.KmpCa / sqd(p.KmpCa + Cai);
-    // Jup
-    {
-        const double dJdf = (p.Vmaxf * (1.0 + ru) + p.Vmaxr * ru) / sqd(den);
-        const double dJdr = -(p.Vmaxr * (1.0 + fu) + p.Vmaxf * fu) / sqd(den);
+    case AP_CA: {
+        const double beta = beta_cyto(), lQ = lam[3] * dt * beta;
+        const double fu = T[T_FU], ru = T[T_RU], rd = 1.0 / (1.0 + fu + ru);
+        const double Jup = (p.Vmaxf * fu - p.Vmaxr * ru) * rd;
+        const double dLT = p.kLTRPNp * Cai * (p.LTRPNtot - CaLT) - p.kLTRPNm * CaLT;
+        const double dHT = p.kHTRPNp * Cai * (p.HTRPNtot - CaHT) - p.kHTRPNm * CaHT;
+        const double e1 = T[T_E1], e2 = e1 * e;
+        const double INaCa = C.INaCa_const * (e1 * cubed(Nai) * p.Cao - e2 * C.Nao3 * Cai) / (1.0 + p.ksat * e2);
+        const double ICab = p.GCab * (V - ECa), IpCa = p.IpCamax * (Cai / (p.KmpCa + Cai));
+        const double Q3 =
+            -0.5 * CSA * (ICab + IpCa - 2 * INaCa) + C.VSS_Vcyto * (cy.jxfer * C.CRU_factor) - Jup - (dLT + dHT);
+        const double lbeta = lam[3] * dt * Q3;
+        const double lJup = -lQ + dt * C.Vcyto_VNSR * lam[4];
+        const double ldLT = -lQ + dt * lam[5], ldHT = -lQ + dt * lam[6];
+        const double dJdf = (p.Vmaxf * (1.0 + ru) + p.Vmaxr * ru) * rd * rd;
+        const double dJdr = -(p.Vmaxr * (1.0 + fu) + p.Vmaxf * fu) * rd * rd;
         lCai += lJup * dJdf * p.Hf * fu / Cai;
         lCaNSR += lJup * dJdr * p.Hr * ru / CaNSR;
         lam_th[TH_VMAX] += lJup * Jup;
+        lam_cy[1] += -dt * C.VJSR_VNSR * lam[4] * C.CRU_factor;
+        lam_cy[2] += C.VSS_Vcyto * lQ * C.CRU_factor;
+        lCai += lbeta * sqd(beta) * 2.0 * C.CMDN_const / cubed(p.KCMDN + Cai);
+        lCai += ldLT * p.kLTRPNp * (p.LTRPNtot - CaLT) + ldHT * p.kHTRPNp * (p.HTRPNtot - CaHT);
+        lam_g[5] += ldLT * (-p.kLTRPNp * Cai - p.kLTRPNm);
+        lam_g[6] += ldHT * (-p.kHTRPNp * Cai - p.kHTRPNm);
+        break;
     }
-    lam_cy[1] += lJtr * C.CRU_factor;
-    lam_cy[2] += lJxfer * C.CRU_factor;
-    // beta_cyto, troponin
-    lCai += lbeta * sqd(beta) * 2.0 * C.CMDN_const / cubed(p.KCMDN + Cai);
-    lCai += ldLT * p.kLTRPNp * (p.LTRPNtot - CaLT) + ldHT * p.kHTRPNp * (p.HTRPNtot - CaHT);
-    lam_g[5] += ldLT * (-p.kLTRPNp * Cai - p.kLTRPNm);
-    lam_g[6] += ldHT * (-p.kHTRPNp * Cai - p.kHTRPNm);
-    // Nernst potentials
-    lNai += lENa * (-RT_F / Nai);
-    lKi += lEK * (-RT_F / Ki) + lECa * (-RT_F / (2.0 * Ki));
-    // gates
-    {
+    case AP_GATE_MH:
+    case AP_GATE_JX: {
         const Gates gr = gate_rates(V, true, T);
-        lam_g[7] += lam[7] * dt * (-gr.am - gr.bm);
-        lam_g[8] += lam[8] * dt * (-gr.ah - gr.bh);
-        lam_g[9] += lam[9] * dt * (-gr.aj - gr.bj);
-        lam_g[10] += -lam[10] * dt * gr.tinv;
-        lV += lam[7] * dt * (gr.dam * (1.0 - m) - gr.dbm * m);
-        lV += lam[8] * dt * (gr.dah * (1.0 - h) - gr.dbh * h);
-        lV += lam[9] * dt * (gr.daj * (1.0 - jg) - gr.dbj * jg);
-        lV += lam[10] * dt * (gr.dxinf * gr.tinv + (gr.xinf - xKs) * gr.dtinv);
+        if (part == AP_GATE_MH) {
+            lam_g[7] += lam[7] * dt * (-gr.am - gr.bm);
+            lam_g[8] += lam[8] * dt * (-gr.ah - gr.bh);
+            lV += lam[7] * dt * (gr.dam * (1.0 - m) - gr.dbm * m);
+            lV += lam[8] * dt * (gr.dah * (1.0 - h) - gr.dbh * h);
+        } else {
+            lam_g[9] += lam[9] * dt * (-gr.aj - gr.bj);
+            lam_g[10] += -lam[10] * dt * gr.tinv;
+            lV += lam[9] * dt * (gr.daj * (1.0 - jg) - gr.dbj * jg);
+            lV += lam[10] * dt * (gr.dxinf * gr.tinv + (gr.xinf - xKs) * gr.dtinv);
+        }
+        break;
     }
-    // IKr chain: d_k = dt (sum over edges a->b of q x_a into b, minus out of a)
-    {
+    case AP_KR: {
+        // IKr chain: d_k = dt (sum over edges a->b of q x_a into b, minus out of a)
         const KrQ q = kr_q(T);
         const double *l = lam + 11;
         double *lx = lam_g + 11;
@@ -773,9 +744,10 @@ GW_HD void glob_increment_adj(const CellStatic &C, const double *g, const Carry 
         lq34 -= lq42 * q.q42 / q.q34;
         lV += lq01 * 0.0272 * q.q01 + lq10 * (-0.0431) * q.q10 + lq23 * 0.0262 * q.q23 + lq24 * 2.71e-6 * q.q24 +
               lq32 * (-0.0269) * q.q32 + lq34 * 0.0120 * q.q34 + lq43 * (-0.0443) * q.q43;
+        break;
     }
-    // Kv chains
-    for (int ch = 0; ch < 2; ++ch) {
+    default: {  // AP_KV43, AP_KV14
+        const int ch = part == AP_KV14 ? 0 : 1;
         const double *x = ch == 0 ? Kv14 : Kv43;
         const double *l = lam + (ch == 0 ? 26 : 16);
         double *lx = lam_g + (ch == 0 ? 26 : 16);
@@ -792,14 +764,24 @@ GW_HD void glob_increment_adj(const CellStatic &C, const double *g, const Carry 
         const double ka = ch == 0 ? p.aaKv14 : p.aaKv43, ki = ch == 0 ? p.aiKv14 : p.aiKv43;
         const double kb = ch == 0 ? p.baKv14 : p.baKv43, kbi = ch == 0 ? p.biKv14 : p.biKv43;
         lV += lr[0] * ka * r[0] - lr[1] * ki * r[1] - lr[2] * kb * r[2] + lr[3] * kbi * r[3];
+        break;
     }
-    // VF_RT and e = exp(-VF_RT) back to V
+    }
+    // this part's Nernst potentials, VF_RT and e = exp(-VF_RT) back to the globals
+    if (lENa != 0.0) lNai += lENa * (-RT_F / Nai);
+    if (lEK != 0.0 || lECa != 0.0) lKi += lEK * (-RT_F / Ki) + lECa * (-RT_F / (2.0 * Ki));
     lV += F_RT * lVF - F_RT * e * le;
     lam_g[0] += lV;
     lam_g[1] += lNai;
     lam_g[2] += lKi;
     lam_g[3] += lCai;
     lam_g[4] += lCaNSR;
+}
+
+// All parts, one after the other.
+GW_HD void glob_increment_adj(const CellStatic &C, const double *g, const Carry &cy, double dt, const double *T,
+                              const double *lam, double *lam_g, double *lam_cy, double *lam_th) {
+    for (int q = 0; q < kAdjParts; ++q) glob_increment_adj(C, g, cy, dt, T, lam, q, lam_g, lam_cy, lam_th);
 }
 
 // ---------------------------------------------------------------------------------------------
