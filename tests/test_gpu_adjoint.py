@@ -16,6 +16,8 @@
                                     not
   checkpoint interval               1,000 instead of 200: identical V and sensitivities
   torch.autograd.Function           gradient of the scales = sensitivities / scales
+  heterogeneous cells               3 cells of 300, 180 and 420 CRUs, own parameter sets and stimulus
+                                    times, 12 ms: adjoint vs central differences as above
 """
 import numpy as np
 import pytest
@@ -168,3 +170,59 @@ def test_autograd_function(recorded):
     loss.backward()
     np.testing.assert_array_equal(V.detach().numpy(), recorded["V"])
     np.testing.assert_allclose(scales.grad.numpy(), recorded["sens"], rtol=1e-12, atol=0)
+
+
+def test_heterogeneous_cells_match_central_differences(enginelib):
+    """Cells of 300, 180 and 420 CRUs with their own parameter sets (the 8 parameters scaled by
+    1 + U(-0.15, 0.15)) and stimulus times (0, 1.5 and 3 ms), 12 ms: every relative sensitivity of
+    every cell against central differences of frozen-trajectory replays (h = 1e-4, smaller where a
+    +-h replay starts a different number of steps at V >= -40 mV), rtol 1e-4."""
+    from gwgb300 import _lib
+    from gwgb300.adjoint import THETA, GradEngine, initial_states, scaled_params
+
+    ncru, steps, se, seed = [300, 180, 420], 12_000, 250, 5
+    base = _lib.default_params()
+    rng = np.random.default_rng(8)
+    pscale = 1.0 + rng.uniform(-0.15, 0.15, (3, len(THETA)))
+    params = [scaled_params(base, pscale[c]) for c in range(3)]
+    stim = np.array([[0.0, 0.0, 0.5, 100.0], [1.5, 0.0, 0.5, 100.0], [3.0, 0.0, 0.5, 100.0]])
+    g0 = np.frombuffer(bytes(_lib.default_globals(py=True)), dtype=np.float64).copy()
+    states = initial_states(ncru, seed=seed)
+    kw = dict(n_steps=steps, seed=seed, checkpoint_every=300, sample_every=se, stim=stim)
+    tscale = 1.0 + rng.uniform(-0.2, 0.2, (3, len(THETA)))
+    with GradEngine(ncru, [scaled_params(params[c], tscale[c]) for c in range(3)], **kw) as t:
+        for c in range(3):
+            t.set_state(c, g0, states[c])
+        Vt = t.forward()
+    with GradEngine(ncru, params, **kw) as e:
+        for c in range(3):
+            e.set_state(c, g0, states[c])
+        V = e.forward()
+        sens = e.backward(2.0 * (V - Vt) / Vt.size)
+        R0 = e.regime_steps()
+        K = len(THETA)
+        fd = np.full((3, K), np.nan)
+        todo = [(c, k) for c in range(3) for k in range(K)]
+        for h in (1e-4, 1e-5, 1e-6):
+            src, pv = [], []
+            for c, k in todo:
+                for sgn in (1.0, -1.0):
+                    s = np.ones(K)
+                    s[k] += sgn * h
+                    src.append(c)
+                    pv.append(scaled_params(params[c], s))
+            Vr, R = e.replay(src, pv, regime=True)
+            L = np.sum((Vr - Vt[np.asarray(src)]) ** 2, axis=1) / Vt.size
+            again = []
+            for i, (c, k) in enumerate(todo):
+                if R[2 * i] != R0[c] or R[2 * i + 1] != R0[c]:
+                    again.append((c, k))
+                else:
+                    fd[c, k] = (L[2 * i] - L[2 * i + 1]) / (2 * h)
+            todo = again
+            if not todo:
+                break
+    assert not todo, todo
+    assert V.max() > 0.0 and np.all(V[:, -1] > V[:, 0])  # every cell fired
+    for c in range(3):
+        np.testing.assert_allclose(sens[c], fd[c], rtol=1e-4, atol=1e-6 * np.max(np.abs(sens[c])), err_msg=f"cell {c}")
