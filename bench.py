@@ -791,10 +791,10 @@ def phase_checkpoint(device, windows, span, t_ms):
 
 
 def accuracy_crn(device, windows, K, span, steps=200, points_ms=(0.0, 15.0, 150.0, 350.0)):
-    """North-star check (c) at the headline config: the FP32 engine against the FP64 oracle from
-    the same 12,500-CRU state with common random numbers (the oracle in 24-bit-uniform mode draws
-    the engine's FP32 uniforms), after 1 and `steps` global steps, at rest before the stimulus,
-    in the Ca release (15 ms), on the plateau (150 ms) and in repolarisation (350 ms)."""
+    """The FP32 path's error against the FP64 oracle at the headline config, from the same 12,500-CRU
+    state with common random numbers (the oracle in 24-bit-uniform mode draws the engine's FP32
+    uniforms), after 1 and `steps` global steps, at rest before the stimulus, in the Ca release
+    (15 ms), on the plateau (150 ms) and in repolarisation (350 ms)."""
     import numpy as np
 
     import pyoracle as po

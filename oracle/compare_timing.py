@@ -1,4 +1,4 @@
-"""CPU speed of the oracle port against the reference's own C++ on the same cores (TEST/BASELINE
+"""CPU speed of the oracle port against the reference's own C++ on the same cores (TEST AND CPU-BASELINE
 INFRASTRUCTURE ONLY; needs oracle/_ref, which exists only where the reference sources were built).
 
 Workload, the same for all three builds: one cell of --ncru CRUs with the reference's random
