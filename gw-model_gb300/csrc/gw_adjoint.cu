@@ -4,7 +4,9 @@
 // Forward.  Per global step s, two kernels: k_ssa runs every CRU's hybrid SSA of step s (the FP64
 // lane of the engine, SsaLane<double, true>, with the engine's counter-based draws keyed on (seed,
 // cell, CRU, step), so the jump trajectory is the one gw_run draws); k_global sums each cell's CRU
-// fluxes and takes the FP64 global step (gw_adjoint_math.h, the reference's formulas and order).
+// fluxes and takes the FP64 global step with the engine's lane program (gw_ode_program.h), as
+// gw_run does.  The backward pass differentiates the reference's formulas of that step
+// (gw_adjoint_math.h), which the program evaluates to a few ulp.
 // The state of every CRU and cell is checkpointed every `checkpoint_every` steps.
 //
 // Backward, one checkpoint segment at a time from the last: the segment is recomputed from its
@@ -42,9 +44,11 @@
 #include <vector>
 
 #include "gw_adjoint_math.h"
+#include "gw_engine.cuh"
 #include "gw_gb300.h"
 #include "gw_internal.h"
 #include "gw_kernel.cuh"
+#include "gw_ode_program.h"
 
 using namespace gw;
 using namespace gw::adj;
@@ -81,7 +85,8 @@ struct Buf {
 // Arguments of the forward kernels for one set of cells (the ensemble, or a replay's source copies
 // or variants).
 struct GradArgs {
-    const CellStatic *cs;       // [n_cells]
+    const OdeProgram *prog;     // the global step as the engine's lane program (shared by all cells)
+    const CellStatic *cs;       // [n_cells] (ode_consts: the program's per-cell constants)
     const int *blk_cell;        // [blocks] cell of each CRU block
     const int *blk_lo;          // [blocks] first CRU (within the cell) of each block
     const int *blk_hi;          // [blocks] end of the block's CRU range (within the cell)
@@ -343,83 +348,132 @@ __global__ void __launch_bounds__(kBlk) k_ssa(const GradArgs a, int64_t step, in
     }
 }
 
-// The cell's flux sums of the step (its blocks' partial sums, in block order) and its global step
-// (one block per cell), the increment's dependency levels one item per thread (on GB300 an FP64
-// instruction costs a sub-partition the same time for 1 or 32 active lanes, so a level costs about
-// one item): the transcendental terms, the Kv generator entries, the currents and derivative
-// components, then d[0..6] and the update; then the new state's SSA values.
-__global__ void __launch_bounds__(kBlk) k_global(const GradArgs a, int64_t step, int slot, int use_var) {
-    __shared__ double T[kNT];
-    __shared__ double E[2 * kKvE];
-    __shared__ double Qv[kNQ];
-    __shared__ double gs[kNumGlobals], gn[kNumGlobals];
-    __shared__ double S[kNS];
+// Shared-memory layout of k_global: the engine's global-step data (OdeShared, the lane program, its
+// slot array, the exp/log tables, the staging row of the SSA values), as ode_phase addresses them.
+struct GlobalLayout {
+    uint32_t ode, prog, x, math, stage, total;
+};
+__host__ __device__ inline GlobalLayout global_layout() {
+    auto a16 = [](size_t n) { return (uint32_t)((n + 15) & ~(size_t)15); };
+    GlobalLayout L;
+    uint32_t o = 0;
+    L.ode = o;
+    o += a16(sizeof(dev::OdeShared));
+    L.prog = o;
+    o += a16(sizeof(OdeProgram));
+    L.x = o;
+    o += a16(kOdeMaxSlots * sizeof(double));
+    L.math = o;
+    o += a16(sizeof(math64::Tables));
+    L.stage = o;
+    o += a16(kSvCount * sizeof(double));
+    L.total = o;
+    return L;
+}
+
+// The cell's flux sums of the step (its blocks' partial sums, in block order) and its global step,
+// one block of the engine's kOdeLanes threads per cell running the engine's lane program
+// (gw_ode_program.h): every warp holds one op kind per phase, so a phase costs about one op.  The
+// program's transcendental phases of the step's state run first (the engine keeps them from the
+// previous step; a block here starts from the recorded globals), then the increments with the
+// update, then the phases up to the SSA values of the new state, which are staged as the engine
+// pushes them.
+__global__ void __launch_bounds__(kOdeLanes) k_global(const GradArgs a, int64_t step, int slot, int use_var) {
+    extern __shared__ __align__(16) unsigned char smem[];
     __shared__ double sums[4];
-    __shared__ int ok;
-    __shared__ __align__(16) CellStatic C;
+    const GlobalLayout L = global_layout();
+    dev::OdeShared &os = *reinterpret_cast<dev::OdeShared *>(smem + L.ode);
+    OdeProgram &P = *reinterpret_cast<OdeProgram *>(smem + L.prog);
+    double *X = reinterpret_cast<double *>(smem + L.x);
+    double *stage = reinterpret_cast<double *>(smem + L.stage);
+    const dev::OdeOffsets off{L.prog, L.x, L.ode, L.math, L.stage};
     const int cell = blockIdx.x;
     if (a.status[cell] != 0) return;  // the same for the whole block
     const int t = (int)threadIdx.x;
-    stage_cell(C, use_var ? a.var_cs[cell] : a.cs[cell]);
+    const CellStatic &C = use_var ? a.var_cs[cell] : a.cs[cell];
     double *g = a.G + (int64_t)kNumGlobals * cell;
     double *cy = a.carry + 4 * (int64_t)cell;
-    if (t < kNumGlobals) gs[t] = g[t];
+    double *svo = (use_var ? const_cast<double *>(a.var_sv) : a.sv) + (int64_t)kSvCount * cell;
+    {
+        const int4 *src = reinterpret_cast<const int4 *>(a.prog);
+        int4 *dst = reinterpret_cast<int4 *>(&P);
+        for (int i = t; i < (int)(sizeof(OdeProgram) / 16); i += kOdeLanes) dst[i] = src[i];
+    }
+    math64::load_tables(*reinterpret_cast<math64::Tables *>(smem + L.math), t, kOdeLanes);
+    for (int i = t; i < kOdeMaxSlots; i += kOdeLanes) X[i] = 0.0;
     if (t < 4) {
         const double *pp = use_var ? a.var_part : a.part;
         double v = 0.0;
         for (int b = a.blk0[cell]; b < a.blk0[cell + 1]; ++b) v += pp[4 * (int64_t)b + t];
         sums[t] = v;
     }
-    const Carry c0{cy[0], cy[1], cy[2], cy[3]};
-    const double istim = pulse_at(a.t[cell], a.stim + 4 * (int64_t)cell);
+    // the step's record (before anything of it is overwritten)
+    if (a.seg_G) {
+        const int64_t r = (int64_t)slot * a.n_cells + cell;
+        if (t < kNumGlobals) a.seg_G[r * kNumGlobals + t] = g[t];
+        if (t < 4) a.seg_carry[r * 4 + t] = cy[t];
+        if (t < kSvCount) a.seg_sv[r * kSvCount + t] = svo[t];
+    }
     __syncthreads();
-    const int it = item_of(t);
-    if (it < kNT) T[it] = glob_term(C, gs, it);
-    __syncthreads();
-    if (it < 2 * kKvE) E[it] = kv_entry(C.p, T, it);
-    __syncthreads();
-    if (it < kNQ) Qv[it] = glob_qty(C, gs, c0, a.dt, T, E, it);
-    __syncthreads();
-    if (t < kNumGlobals) gn[t] = gs[t] + (t < 7 ? glob_dconc(C, c0, istim, a.dt, Qv, t) : Qv[Q_D + t - 7]);
-    __syncthreads();
-    double *svo = (use_var ? const_cast<double *>(a.var_sv) : a.sv) + (int64_t)kSvCount * cell;
     if (t == 0) {
-        ok = 0;
-        if (a.seg_G) {
-            const int64_t r = (int64_t)slot * a.n_cells + cell;
-            for (int k = 0; k < kNumGlobals; ++k) a.seg_G[r * kNumGlobals + k] = gs[k];
-            for (int k = 0; k < 4; ++k) a.seg_carry[r * 4 + k] = cy[k];
-            for (int k = 0; k < kSvCount; ++k) a.seg_sv[r * kSvCount + k] = svo[k];
-        }
-        if (a.regime && gs[0] >= -40.0) a.regime[cell] += 1ull;
-        bool fin = true;
-        for (int k = 0; k < kNumGlobals; ++k) fin = fin && isfinite(gn[k]);
-        if (!(gs[1] > 0.0) || !(gs[2] > 0.0)) {
+        X[XS_ONE] = 1.0;
+        X[XS_MONE] = -1.0;
+        X[XS_DT] = a.dt;
+        X[XS_ISTIM] = pulse_at(a.t[cell], a.stim + 4 * (int64_t)cell);
+        for (int q = 0; q < 4; ++q) X[XS_SUMS + q] = cy[q];
+        os.status = 0;
+        if (a.regime && g[0] >= -40.0) a.regime[cell] += 1ull;
+    }
+    if (t < kNumGlobals) {
+        os.g[t] = g[t];
+        X[XS_G + t] = X[XS_GN + t] = g[t];
+    }
+    for (int i = t; i < kOdeConstCap; i += kOdeLanes) X[XS_FIRST_FREE + i] = C.ode_consts[i];
+    __syncthreads();
+    const int reg = dev::v_regime(os.g[0]);
+    for (int q = P.upd_phase + 1; q < P.n_phases; ++q) {
+        dev::ode_phase<double, double>(off, q, reg, t);
+        __syncthreads();
+    }
+    const bool nernst = dev::not_positive(os.g[1]) || dev::not_positive(os.g[2]);
+    for (int q = 0; q <= P.upd_phase; ++q) {
+        dev::ode_phase<double, double>(off, q, reg, t);
+        __syncthreads();
+    }
+    // the SSA values of the new state: the constant ones from their slots, the others from the
+    // program's phases up to the push, Cai and CaNSR from the new globals
+    if (t < kSvCount && t != SV_CAI && t != SV_CANSR && t != SV_CAI_LO && t != SV_CANSR_LO &&
+        P.sv_src[t] < XS_FIRST_FREE + kOdeMaxConsts)
+        stage[t] = X[P.sv_src[t]];
+    const int reg2 = dev::v_regime(os.g[0]);
+    for (int q = P.upd_phase + 1; q <= P.push_phase; ++q) {
+        dev::ode_phase<double, double>(off, q, reg2, t);
+        __syncthreads();
+    }
+    if (t == 0) {
+        dev::stage_pair(stage, SV_CAI, SV_CAI_LO, os.g[3]);
+        dev::stage_pair(stage, SV_CANSR, SV_CANSR_LO, os.g[4]);
+        if (nernst) {
             a.status[cell] = GW_ERR_NERNST;
-        } else if (!fin) {
-            a.status[cell] = GW_ERR_NONFINITE;
+        } else if (os.status != 0) {
+            a.status[cell] = os.status;
         } else {
-            for (int k = 0; k < kNumGlobals; ++k) g[k] = gn[k];
             // carry order {JLCC, ClCh, Jtr, Jxfer} from the per-CRU {JLCC, Jxfer, Jtr, ClCh}
             cy[0] = sums[0];
             cy[1] = sums[3];
             cy[2] = sums[2];
             cy[3] = sums[1];
             a.t[cell] += a.dt;
-            ok = 1;
+            if (a.V && (step + 1) % a.sample_every == 0) {
+                const int64_t si = (step + 1) / a.sample_every - 1;
+                if (si < a.n_samples) a.V[(int64_t)cell * a.n_samples + si] = os.g[0];
+            }
         }
     }
     __syncthreads();
-    if (!ok) return;
-    if (it < kNS) S[it] = sv_term(C, gn, it);
-    __syncthreads();
-    if (t == 0) {
-        step_values(C, gn, S, svo);
-        if (a.V && (step + 1) % a.sample_every == 0) {
-            const int64_t si = (step + 1) / a.sample_every - 1;
-            if (si < a.n_samples) a.V[(int64_t)cell * a.n_samples + si] = gn[0];
-        }
-    }
+    if (nernst || os.status != 0) return;
+    if (t < kNumGlobals) g[t] = os.g[t];
+    if (t < kSvCount) svo[t] = stage[t];
 }
 
 // The adjoint state of CRU i after its step (its lam_x row, and the carry adjoints: the step's
@@ -735,11 +789,12 @@ struct gw_grad {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::string err;
     std::vector<char> have_state;
+    OdeProgram prog{};
     bool forwarded = false;
     gw_grad_stats stats{};
     std::vector<double> G_final;
     // tables
-    Buf d_cs, d_blk_cell, d_blk_lo, d_blk_hi, d_blk0, d_cru_cell, d_cru0, d_ncru, d_rng_cell, d_stim, d_cc;
+    Buf d_cs, d_prog, d_blk_cell, d_blk_lo, d_blk_hi, d_blk0, d_cru_cell, d_cru0, d_ncru, d_rng_cell, d_stim, d_cc;
     // initial state
     Buf x_init, G_init, carry_init, sv_init;
     // state
@@ -767,6 +822,7 @@ struct gw_grad {
     }
     GradArgs args() const {
         GradArgs a{};
+        a.prog = d_prog.as<OdeProgram>();
         a.cs = d_cs.as<CellStatic>();
         a.blk_cell = d_blk_cell.as<int>();
         a.blk_lo = d_blk_lo.as<int>();
@@ -933,6 +989,16 @@ int gw_grad_create(const gw_grad_desc *d, gw_grad **out) {
         g->slots = std::max(1, g->sm_count * std::max(1, per_sm));
     }
     plan_blocks(g->ncru, g->slots, g->blk_cell, g->blk_lo, g->blk_hi, g->blk0);
+    {
+        // the engine's global-step program (one for all cells) and its per-cell constants
+        bool pow_fast = true;
+        for (int c = 0; c < d->n_cells; ++c) pow_fast = pow_fast && g->cs[c].p.Hf == 0.75 && g->cs[c].p.Hr == 0.75;
+        for (int c = 0; c < d->n_cells; ++c)
+            if (!ode_program_build(g->cs[c], pow_fast, c == 0 ? &g->prog : nullptr, g->cs[c].ode_consts)) {
+                delete g;
+                return fail_to(g_grad_create_error, GW_ERR_UNSUPPORTED, "global-step program does not fit its tables");
+            }
+    }
     g->n_blocks = (int)g->blk_cell.size();
     std::vector<int> rng_cell(d->n_cells);
     for (int c = 0; c < d->n_cells; ++c) rng_cell[c] = d->cell_base + c;
@@ -944,6 +1010,7 @@ int gw_grad_create(const gw_grad_desc *d, gw_grad **out) {
         if (!rc && src) rc = g->cuda(cudaMemcpy(b.p, src, bytes, cudaMemcpyHostToDevice), "gw_grad_create");
     };
     up(g->d_cs, g->cs.data(), sizeof(CellStatic) * C);
+    up(g->d_prog, &g->prog, sizeof(OdeProgram));
     up(g->d_blk_cell, g->blk_cell.data(), sizeof(int) * g->n_blocks);
     up(g->d_blk_lo, g->blk_lo.data(), sizeof(int) * g->n_blocks);
     up(g->d_blk_hi, g->blk_hi.data(), sizeof(int) * g->n_blocks);
@@ -1070,7 +1137,7 @@ int gw_grad_forward(gw_grad *g, double *V_samples) {
     for (int64_t s = 0; s < g->n_steps; ++s) {
         if (s % g->ck_every == 0 && (rc = g->save(s / g->ck_every))) return rc;
         k_ssa<<<g->n_blocks, kBlk, 0, g->stream>>>(a, s, 0);
-        k_global<<<g->n_cells, kBlk, 0, g->stream>>>(a, s, 0, 0);
+        k_global<<<g->n_cells, kOdeLanes, global_layout().total, g->stream>>>(a, s, 0, 0);
     }
     cudaEventRecord(g->ev1, g->stream);
     if ((rc = g->cuda(cudaGetLastError(), "gw_grad_forward launch"))) return rc;
@@ -1126,7 +1193,7 @@ int gw_grad_backward(gw_grad *g, const double *dL_dV, double *sens) {
         if ((rc = g->cuda(cudaMemsetAsync(g->busy_n.p, 0, g->busy_n.n, g->stream), "gw_grad_backward"))) return rc;
         for (int64_t s = s0; s < s1; ++s) {
             k_ssa<<<g->n_blocks, kBlk, 0, g->stream>>>(a, s, (int)(s - s0));
-            k_global<<<g->n_cells, kBlk, 0, g->stream>>>(a, s, (int)(s - s0), 0);
+            k_global<<<g->n_cells, kOdeLanes, global_layout().total, g->stream>>>(a, s, (int)(s - s0), 0);
         }
         for (int64_t s = s1 - 1; s >= s0; --s) {
             k_cru_busy<<<bgrid, kBlk, 0, g->stream>>>(a, b, s, (int)(s - s0));
@@ -1171,10 +1238,23 @@ int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_para
         for (int k = 0; k < 4; ++k) stim[4 * v + k] = g->stim[4 * s + k];
         make_cell_static(params[v], ncru[v], vcs[v]);
     }
+    // the replay's global-step program: the sources' and the variants' constants under one program
+    OdeProgram rprog{};
+    std::vector<CellStatic> scs(n_var);
+    {
+        bool pow_fast = true;
+        for (int v = 0; v < n_var; ++v) {
+            scs[v] = g->cs[src_cell[v]];
+            pow_fast = pow_fast && scs[v].p.Hf == 0.75 && scs[v].p.Hr == 0.75 && vcs[v].p.Hf == 0.75 &&
+                       vcs[v].p.Hr == 0.75;
+        }
+        for (int v = 0; v < n_var; ++v)
+            if (!ode_program_build(scs[v], pow_fast, v == 0 ? &rprog : nullptr, scs[v].ode_consts) ||
+                !ode_program_build(vcs[v], pow_fast, nullptr, vcs[v].ode_consts))
+                return fail_to(g->err, GW_ERR_UNSUPPORTED, "global-step program does not fit its tables");
+    }
     plan_blocks(ncru, g->slots, bc, bl, bh, b0);
     const int nb = (int)bc.size();
-    std::vector<CellStatic> scs(n_var);
-    for (int v = 0; v < n_var; ++v) scs[v] = g->cs[src_cell[v]];
     // initial states: the source's
     std::vector<double> G0((size_t)kNumGlobals * g->n_cells), cy0(4 * (size_t)g->n_cells),
         sv0((size_t)kSvCount * g->n_cells);
@@ -1193,7 +1273,7 @@ int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_para
         std::memcpy(&sv[kSvCount * (size_t)v], &sv0[kSvCount * (size_t)s], sizeof(double) * kSvCount);
         step_values(vcs[v], &G0[kNumGlobals * (size_t)s], &vsv[kSvCount * (size_t)v]);
     }
-    Buf d_cs, d_vcs, d_bc, d_bl, d_bh, d_b0, d_part, d_vpart, d_c0, d_n, d_rng, d_stim, x, out, vx, vout, dG, dvG, dcy, dvcy, dt_, dvt, dsv, dvsv,
+    Buf d_cs, d_vcs, d_rprog, d_bc, d_bl, d_bh, d_b0, d_part, d_vpart, d_c0, d_n, d_rng, d_stim, x, out, vx, vout, dG, dvG, dcy, dvcy, dt_, dvt, dsv, dvsv,
         dst, dvst, dV, dreg;
     auto up = [&](Buf &b, const void *src, size_t bytes) {
         if (rc) return;
@@ -1202,6 +1282,7 @@ int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_para
     };
     up(d_cs, scs.data(), sizeof(CellStatic) * n_var);
     up(d_vcs, vcs.data(), sizeof(CellStatic) * n_var);
+    up(d_rprog, &rprog, sizeof(OdeProgram));
     up(d_bc, bc.data(), sizeof(int) * nb);
     up(d_bl, bl.data(), sizeof(int) * nb);
     up(d_bh, bh.data(), sizeof(int) * nb);
@@ -1250,6 +1331,7 @@ int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_para
         if ((rc = g->cuda(cudaMemcpy(vx.p, xv.data(), vx.n, cudaMemcpyHostToDevice), "gw_grad_replay"))) return rc;
     }
     GradArgs a{};
+    a.prog = d_rprog.as<OdeProgram>();
     a.cs = d_cs.as<CellStatic>();
     a.blk_cell = d_bc.as<int>();
     a.blk_lo = d_bl.as<int>();
@@ -1290,8 +1372,8 @@ int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_para
     cudaEventRecord(g->ev0, g->stream);
     for (int64_t s = 0; s < g->n_steps; ++s) {
         k_ssa<<<nb, kBlk, 0, g->stream>>>(a, s, 0);
-        k_global<<<n_var, kBlk, 0, g->stream>>>(a, s, 0, 0);
-        k_global<<<n_var, kBlk, 0, g->stream>>>(va, s, 0, 1);
+        k_global<<<n_var, kOdeLanes, global_layout().total, g->stream>>>(a, s, 0, 0);
+        k_global<<<n_var, kOdeLanes, global_layout().total, g->stream>>>(va, s, 0, 1);
     }
     cudaEventRecord(g->ev1, g->stream);
     if ((rc = g->cuda(cudaGetLastError(), "gw_grad_replay launch"))) return rc;
