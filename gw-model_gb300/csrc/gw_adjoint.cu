@@ -56,6 +56,8 @@ using namespace gw::adj;
 namespace {
 
 constexpr int kBlk = 128;     // threads per block of the CRU kernels (one cell per block)
+constexpr int kSsaBlocksPerSm = 3;  // k_ssa without variants: resident blocks per SM (register cap)
+constexpr int kQCap = 512;    // k_ssa: CRUs per block whose first iteration runs after the block's ranges
 constexpr int kRec = 16;      // sub-steps a CRU keeps per block of its reverse sweep
 constexpr int kAdjIn = 6;     // per-cell CRU adjoints: Cai, CaNSR, JM, JE, rRyR (relative), CSQN_const
 constexpr int kLamX = 9;      // CRU adjoint state: CaSS[4], CaJSR, JLCC[4]
@@ -223,17 +225,29 @@ __device__ __forceinline__ CruIn cru_in(const double *sv) {
 
 // Forward SSA of step `step`: block b takes CRUs [blk_lo, blk_hi) of cell blk_cell, split evenly
 // over its warps; each warp runs its range with lane refill (one SSA iteration per pass; a lane
-// whose CRU finished its step takes the warp's next CRU).
-__global__ void __launch_bounds__(kBlk) k_ssa(const GradArgs a, int64_t step, int slot) {
+// whose CRU finished its step takes the warp's next CRU).  CRUs whose first iteration the FP32
+// screen declines (an event in the step) run after the ranges, packed into as few warps as they
+// fill, so that the FP64 rate evaluations run with full lanes.
+template <bool VAR>
+__global__ void __launch_bounds__(kBlk, VAR ? 1 : kSsaBlocksPerSm) k_ssa(const GradArgs a, int64_t step, int slot) {
     __shared__ dev::SsaConsts<double> cc;
     __shared__ double sv[kSvCount];
     __shared__ double vsv[kSvCount];
     __shared__ double shp[(kBlk / 32) * 4];
+    __shared__ float svf[kSvCount];          // float copies for the screen (SsaLane::surely_last)
+    __shared__ float sk[dev::SK_COUNT];
+    __shared__ int q[kQCap];                 // CRUs whose first iteration the screen declined
+    __shared__ int qn;
     const int cell = a.blk_cell[blockIdx.x];
-    const bool var = a.var_x != nullptr;
+    constexpr bool var = VAR;  // the replay's variants (a.var_x and the var_* arrays set)
     if (threadIdx.x == 0) dev::load_ssa_consts<double>(cc, a.cs[cell]);
+    if (threadIdx.x == 32) {
+        dev::load_screen_consts(sk, a.cs[cell]);
+        qn = 0;
+    }
     if (threadIdx.x < kSvCount) {
         sv[threadIdx.x] = a.sv[(int64_t)cell * kSvCount + threadIdx.x];
+        svf[threadIdx.x] = (float)sv[threadIdx.x];
         if (var) vsv[threadIdx.x] = a.var_sv[(int64_t)cell * kSvCount + threadIdx.x];
     }
     __syncthreads();
@@ -255,9 +269,71 @@ __global__ void __launch_bounds__(kBlk) k_ssa(const GradArgs a, int64_t step, in
     dev::Stream rng;
     CruCont v;
     double vjtr = 0.0, vjx = 0.0;
-    int m = a.status[cell] == 0 ? -1 : -2;  // CRU of this lane; -1 none yet, -2 none left
     unsigned int ev = 0;
     int err = 0;
+    // CRU mm of the cell into the lane (state, stream, Jrel; the variant's state)
+    auto fetch = [&](int mm, bool first) {
+        const int64_t i = c0 + mm;
+        c = a.x[i];
+        if (first && a.seg_x) a.seg_x[(int64_t)slot * a.n_crus + i] = c;
+        rng.open(a.seed, rc, (uint32_t)mm, (uint64_t)step, 0);
+        L.begin(c, cc);
+        if (var) {
+            // the variant follows the same sub-steps and events with its own parameters
+            const double *vx = a.var_x + (int64_t)kLamX * i;
+            for (int j = 0; j < 4; ++j) {
+                v.c[j] = vx[j];
+                v.L[j] = vx[5 + j];
+            }
+            v.J = vx[4];
+            int o[4];
+            open_counts(c, o);
+            cru_begin(v, o, P);
+        }
+    };
+    // After an iteration of CRU mm (f: what it did; lcc0, fl0: the channel state before it): the
+    // variant follows it, and at the end of the step the CRU's results are written.
+    auto after = [&](int mm, const dev::IterInfo<double> &f, uint32_t lcc0, uint32_t fl0, bool done) {
+        if (var) {
+            cru_substep(v, f.h, in, P, vjtr, vjx);
+            int e, j, onew;
+            classify(f, lcc0, fl0, c, e, j, onew);
+            cru_event(v, e, j, onew, in, P);
+        }
+        if (!done) return;
+        const int64_t i = c0 + mm;
+        a.x[i] = c;
+        double *o = a.out + 4 * i;
+        o[0] = c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3];
+        o[1] = L.jxfer_sum;
+        o[2] = L.jtr;
+        o[3] = (double)__popc((c.flags >> 4) & 0xFu);
+        if (var) {
+            double *vx = a.var_x + (int64_t)kLamX * i;
+            for (int j = 0; j < 4; ++j) {
+                vx[j] = v.c[j];
+                vx[5 + j] = v.L[j];
+            }
+            vx[4] = v.J;
+            double *vo = a.var_out + 4 * i;
+            vo[0] = v.L[0] + v.L[1] + v.L[2] + v.L[3];
+            vo[1] = vjx;
+            vo[2] = vjtr;
+            vo[3] = o[3];
+        }
+        if (a.quiet) {
+            const bool q = L.ev == 0;
+            a.quiet[(int64_t)slot * a.n_crus + i] = q ? 1 : 0;
+            if (!q) a.busy[(int64_t)slot * a.n_crus + atomicAdd(&a.busy_n[slot], 1)] = (int)i;
+        }
+        ev += (unsigned int)L.ev;
+    };
+    // Pass 1: the warp's CRU range, one iteration per lane and pass.  An iteration that the FP32
+    // screen shows to be the step's last runs without the FP64 rates (finish).  A CRU whose first
+    // iteration the screen declines is handed, untouched, to the block's queue, and its lane takes
+    // the next CRU; so every pass of the range runs with full lanes.
+    int m = a.status[cell] == 0 ? -1 : -2;  // CRU of this lane; -1 none yet, -2 none left
+    bool fresh = false;                      // no iteration of the lane's CRU has run yet
     for (;;) {
         const unsigned need = __ballot_sync(0xffffffffu, m == -1);
         if (need) {
@@ -266,23 +342,8 @@ __global__ void __launch_bounds__(kBlk) k_ssa(const GradArgs a, int64_t step, in
             if (m == -1) {
                 if (nm < end) {
                     m = nm;
-                    const int64_t i = c0 + m;
-                    c = a.x[i];
-                    if (a.seg_x) a.seg_x[(int64_t)slot * a.n_crus + i] = c;
-                    rng.open(a.seed, rc, (uint32_t)m, (uint64_t)step, 0);
-                    L.begin(c, cc);
-                    if (var) {
-                        // the variant follows the same sub-steps and events with its own parameters
-                        const double *vx = a.var_x + (int64_t)kLamX * i;
-                        for (int j = 0; j < 4; ++j) {
-                            v.c[j] = vx[j];
-                            v.L[j] = vx[5 + j];
-                        }
-                        v.J = vx[4];
-                        int o[4];
-                        open_counts(c, o);
-                        cru_begin(v, o, P);
-                    }
+                    fetch(m, true);
+                    fresh = true;
                 } else {
                     m = -2;
                 }
@@ -292,41 +353,75 @@ __global__ void __launch_bounds__(kBlk) k_ssa(const GradArgs a, int64_t step, in
         if (m >= 0) {
             const uint32_t lcc0 = c.lcc, fl0 = c.flags;
             dev::IterInfo<double> f;
-            const bool done = L.iterate(c, cc, sv, nullptr, rng, a.dt, a.event_cap, err, var ? &f : nullptr);
-            if (var) {
-                cru_substep(v, f.h, in, P, vjtr, vjx);
-                int e, j, onew;
-                classify(f, lcc0, fl0, c, e, j, onew);
-                cru_event(v, e, j, onew, in, P);
+            bool ran = true, done = false;
+            if (L.surely_last(c, cc, sk, svf, rng, a.dt)) {
+                L.finish(c, cc, sv, rng, a.dt, var ? &f : nullptr);
+                done = true;
+            } else {
+                const int qs = fresh ? atomicAdd(&qn, 1) : kQCap;
+                if (qs < kQCap) {
+                    q[qs] = m;
+                    m = -1;
+                    ran = false;
+                } else {  // the queue is full, or the CRU is past its first iteration
+                    done = L.iterate(c, cc, sv, nullptr, rng, a.dt, a.event_cap, err, var ? &f : nullptr);
+                }
             }
-            if (done) {
-                const int64_t i = c0 + m;
-                a.x[i] = c;
-                double *o = a.out + 4 * i;
-                o[0] = c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3];
-                o[1] = L.jxfer_sum;
-                o[2] = L.jtr;
-                o[3] = (double)__popc((c.flags >> 4) & 0xFu);
-                if (var) {
-                    double *vx = a.var_x + (int64_t)kLamX * i;
-                    for (int j = 0; j < 4; ++j) {
-                        vx[j] = v.c[j];
-                        vx[5 + j] = v.L[j];
+            fresh = false;
+            if (ran) {
+                after(m, f, lcc0, fl0, done);
+                if (done) m = -1;
+            }
+        }
+    }
+    // Pass 2: the queued CRUs (those with an event, and the few the screen's margins declined), on
+    // as few warps as they fill.  Their first iteration runs in FP64; later ones are screened, and
+    // a declined one waits (pend) until kDefer lanes of the warp wait or the warp has no queued
+    // CRUs left, then they run the FP64 iteration together.
+    __syncthreads();
+    const int nq = min(qn, kQCap);
+    const int nwu = min(nw, (nq + 31) >> 5);
+    if (warp < nwu) {
+        int qc = (int)((int64_t)nq * warp / nwu);
+        const int qe = (int)((int64_t)nq * (warp + 1) / nwu);
+        m = -1;
+        bool pend = false;  // the lane's next iteration needs the FP64 rates
+        for (;;) {
+            const unsigned need = __ballot_sync(0xffffffffu, m == -1);
+            if (need) {
+                const int nm = qc + __popc(need & ((1u << lane) - 1u));
+                qc += __popc(need);
+                if (m == -1) {
+                    if (nm < qe) {
+                        m = q[nm];
+                        fetch(m, false);
+                        pend = true;
+                    } else {
+                        m = -2;
                     }
-                    vx[4] = v.J;
-                    double *vo = a.var_out + 4 * i;
-                    vo[0] = v.L[0] + v.L[1] + v.L[2] + v.L[3];
-                    vo[1] = vjx;
-                    vo[2] = vjtr;
-                    vo[3] = o[3];
                 }
-                if (a.quiet) {
-                    const bool q = L.ev == 0;
-                    a.quiet[(int64_t)slot * a.n_crus + i] = q ? 1 : 0;
-                    if (!q) a.busy[(int64_t)slot * a.n_crus + atomicAdd(&a.busy_n[slot], 1)] = (int)i;
+            }
+            if (!__any_sync(0xffffffffu, m >= 0)) break;
+            const uint32_t lcc0 = c.lcc, fl0 = c.flags;
+            dev::IterInfo<double> f;
+            bool ran = false, done = false;
+            if (m >= 0 && !pend) {
+                if (L.surely_last(c, cc, sk, svf, rng, a.dt)) {
+                    L.finish(c, cc, sv, rng, a.dt, var ? &f : nullptr);
+                    ran = done = true;
+                } else {
+                    pend = true;
                 }
-                ev += (unsigned int)L.ev;
-                m = -1;
+            }
+            const unsigned pm = __ballot_sync(0xffffffffu, pend);
+            if (pm && (qc >= qe || __popc(pm) >= dev::kDefer) && pend) {
+                done = L.iterate(c, cc, sv, nullptr, rng, a.dt, a.event_cap, err, var ? &f : nullptr);
+                ran = true;
+                pend = false;
+            }
+            if (ran) {
+                after(m, f, lcc0, fl0, done);
+                if (done) m = -1;
             }
         }
     }
@@ -982,7 +1077,7 @@ int gw_grad_create(const gw_grad_desc *d, gw_grad **out) {
     {
         int per_sm = 1;
         cudaDeviceGetAttribute(&g->sm_count, cudaDevAttrMultiProcessorCount, d->device);
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ssa, kBlk, 0) != cudaSuccess) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ssa<false>, kBlk, 0) != cudaSuccess) {
             cudaGetLastError();
             per_sm = 1;
         }
@@ -1136,7 +1231,7 @@ int gw_grad_forward(gw_grad *g, double *V_samples) {
     cudaEventRecord(g->ev0, g->stream);
     for (int64_t s = 0; s < g->n_steps; ++s) {
         if (s % g->ck_every == 0 && (rc = g->save(s / g->ck_every))) return rc;
-        k_ssa<<<g->n_blocks, kBlk, 0, g->stream>>>(a, s, 0);
+        k_ssa<false><<<g->n_blocks, kBlk, 0, g->stream>>>(a, s, 0);
         k_global<<<g->n_cells, kOdeLanes, global_layout().total, g->stream>>>(a, s, 0, 0);
     }
     cudaEventRecord(g->ev1, g->stream);
@@ -1192,7 +1287,7 @@ int gw_grad_backward(gw_grad *g, const double *dL_dV, double *sens) {
         if ((rc = g->restore(k))) return rc;
         if ((rc = g->cuda(cudaMemsetAsync(g->busy_n.p, 0, g->busy_n.n, g->stream), "gw_grad_backward"))) return rc;
         for (int64_t s = s0; s < s1; ++s) {
-            k_ssa<<<g->n_blocks, kBlk, 0, g->stream>>>(a, s, (int)(s - s0));
+            k_ssa<false><<<g->n_blocks, kBlk, 0, g->stream>>>(a, s, (int)(s - s0));
             k_global<<<g->n_cells, kOdeLanes, global_layout().total, g->stream>>>(a, s, (int)(s - s0), 0);
         }
         for (int64_t s = s1 - 1; s >= s0; --s) {
@@ -1371,7 +1466,7 @@ int gw_grad_replay(gw_grad *g, int n_var, const int32_t *src_cell, const gw_para
     va.regime = dreg.as<unsigned long long>();
     cudaEventRecord(g->ev0, g->stream);
     for (int64_t s = 0; s < g->n_steps; ++s) {
-        k_ssa<<<nb, kBlk, 0, g->stream>>>(a, s, 0);
+        k_ssa<true><<<nb, kBlk, 0, g->stream>>>(a, s, 0);
         k_global<<<n_var, kOdeLanes, global_layout().total, g->stream>>>(a, s, 0, 0);
         k_global<<<n_var, kOdeLanes, global_layout().total, g->stream>>>(va, s, 0, 1);
     }

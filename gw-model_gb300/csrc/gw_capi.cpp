@@ -1367,6 +1367,39 @@ int gw_math_check(const double *x, int64_t n, double *exp_out, double *log_out) 
     return GW_OK;
 }
 
+int gw_screen_check(const gw_params *p, int nCRU, int64_t n, const uint32_t *chan, const double *cass,
+                    const double *sv, const double *t, const double *dt, uint64_t seed, int32_t *out,
+                    double *jump) {
+    if (!p || nCRU < 1 || !chan || !cass || !sv || !t || !dt || !out || !jump || n < 0 || n > (int64_t)1 << 24)
+        return fail(nullptr, GW_ERR_INVALID_ARGUMENT, "bad arguments to gw_screen_check");
+    if (n == 0) return GW_OK;
+    CellStatic C;
+    make_cell_static(*p, nCRU, C);
+    DevBuf dc, dch, dx, ds, dtt, ddt, dout, dj;
+    gw_ctx *c = nullptr;
+    CK(c, dc.alloc(sizeof(CellStatic)));
+    CK(c, dch.alloc(sizeof(uint32_t) * 8 * n));
+    CK(c, dx.alloc(sizeof(double) * 4 * n));
+    CK(c, ds.alloc(sizeof(double) * kSvCount * n));
+    CK(c, dtt.alloc(sizeof(double) * n));
+    CK(c, ddt.alloc(sizeof(double) * n));
+    CK(c, dout.alloc(sizeof(int32_t) * 2 * n));
+    CK(c, dj.alloc(sizeof(double) * n));
+    CK(c, cudaMemcpy(dc.p, &C, sizeof(CellStatic), cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(dch.p, chan, sizeof(uint32_t) * 8 * n, cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(dx.p, cass, sizeof(double) * 4 * n, cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(ds.p, sv, sizeof(double) * kSvCount * n, cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(dtt.p, t, sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(ddt.p, dt, sizeof(double) * n, cudaMemcpyHostToDevice));
+    const int e = screen_check_dev(static_cast<const CellStatic *>(dc.p), (int)n, static_cast<const uint32_t *>(dch.p),
+                                   dx.as<double>(), ds.as<double>(), dtt.as<double>(), ddt.as<double>(), seed,
+                                   static_cast<int *>(dout.p), dj.as<double>());
+    if (e != 0) return fail(nullptr, GW_ERR_CUDA, "screen check launch: %s", cudaGetErrorString((cudaError_t)e));
+    CK(c, cudaMemcpy(out, dout.p, sizeof(int32_t) * 2 * n, cudaMemcpyDeviceToHost));
+    CK(c, cudaMemcpy(jump, dj.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    return GW_OK;
+}
+
 int gw_get_time(gw_ctx *c, int cell, double *t, uint64_t *step) {
     int rc = check_cell(c, cell);
     if (rc) return rc;

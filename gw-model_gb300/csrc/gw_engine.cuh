@@ -767,6 +767,12 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
             float2 *rtab = v.rtab + par * kRateTab;
             if (!FP64)
                 for (int e = (int)threadIdx.x; e < kRateTab; e += n_ssa) build_rate_entry<R>(rtab, cc, sv, e);
+            // FP64: float copies of the step's SSA values for the screen, in the same place and
+            // under the same rule (floats 0..kSvCount-1 of this parity's table)
+            float *svf = reinterpret_cast<float *>(rtab);
+            const float *sk = reinterpret_cast<const float *>(v.rtab) + 64;
+            if (FP64)
+                for (int e = (int)threadIdx.x; e < kSvCount; e += n_ssa) svf[e] = (float)sv[e];
             if (bar_or(2, n_ssa, !ok)) {
                 my_err |= 2;
                 s_stop = s;
@@ -789,7 +795,8 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
             Cru<R> c;
             SsaLane<R, EXACT> sl;
             Stream rng;
-            int m = -1;  // CRU of this lane; -1 none yet, -2 none left
+            int m = -1;         // CRU of this lane; -1 none yet, -2 none left
+            bool pend = false;  // FP64: the lane's next iteration needs the FP64 rates
             for (;;) {
                 const unsigned need = __ballot_sync(0xffffffffu, m == -1);
                 if (need) {
@@ -807,7 +814,35 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
                     }
                 }
                 if (!__any_sync(0xffffffffu, m >= 0)) break;
-                if (m >= 0) {
+                if constexpr (FP64) {
+                    // One iteration per lane and pass: an iteration that the FP32 screen shows to be
+                    // the step's last runs without the FP64 rates (finish); the others wait (pend)
+                    // until kDefer lanes of the warp wait or the warp has no CRUs left to take, and
+                    // then run the FP64 iteration together.
+                    int err = 0;
+                    bool done = false;
+                    if (m >= 0 && !pend) {
+                        if (sl.surely_last(c, cc, sk, svf, rng, dt)) {
+                            sl.finish(c, cc, sv, rng, dt);
+                            done = true;
+                        } else {
+                            pend = true;
+                        }
+                    }
+                    const unsigned pm = __ballot_sync(0xffffffffu, pend);
+                    if (pm && (cursor >= end || __popc(pm) >= kDefer) && pend) {
+                        done = sl.iterate(c, cc, sv, rtab, rng, dt, a.event_cap, err);
+                        pend = false;
+                    }
+                    if (done) {
+                        tile_put(tile[m], c);
+                        my_events += (unsigned long long)sl.ev;
+                        my_err |= err;
+                        acc.add(c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3], sl.jxfer_sum, sl.jtr,
+                                __popc((c.flags >> 4) & 0xFu));
+                        m = -1;
+                    }
+                } else if (m >= 0) {
                     int err = 0;
                     if (sl.iterate(c, cc, sv, rtab, rng, dt, a.event_cap, err)) {
                         tile_put(tile[m], c);
@@ -910,7 +945,9 @@ __global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const __grid_con
         const int cell = v.w.cell;
         if (threadIdx.x == 0) {
             load_ssa_consts<R>(*v.cc, a.cs[cell]);
-
+            // FP64: the screen's constants (SsaLane::surely_last) in the rate-table area, which the
+            // FP64 lane does not otherwise use: floats 64.. of parity 0's table
+            if (FP64) load_screen_consts(reinterpret_cast<float *>(v.rtab) + 64, a.cs[cell]);
         }
         // The leader's warp-partial slots start at zero (slots of warps a CTA does not have stay
         // so); the cell's CTAs write them only after the first cluster barrier of the steps.

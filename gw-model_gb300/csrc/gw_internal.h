@@ -158,5 +158,7 @@ int max_active_clusters_fp32(const LaunchShape &s, bool ode64, int *out);
 int sample_initial_crus_dev(const KernelArgs &a, int cell, int ncru, int fp64, void *stream);
 // The global step's FP64 exp and log on n device inputs (accuracy check).
 int math_check_dev(const double *x, int n, double *ex, double *lg);
+int screen_check_dev(const CellStatic *cs, int n, const uint32_t *chan, const double *cass, const double *sv,
+                     const double *t, const double *dt, uint64_t seed, int *out, double *jump);
 
 }  // namespace gw

@@ -713,6 +713,109 @@ struct IterInfo {
     int act, aj, atr;
 };
 
+// ------------------------------------------------------------------------------------------
+// FP32 screen of the FP64 lane's jump decision (SsaLane::surely_last).
+// ------------------------------------------------------------------------------------------
+// FP64 lanes whose iteration the screen declined wait until this many lanes of their warp do (or
+// the warp has no CRUs left to take), then run the FP64 iteration together.
+constexpr int kDefer = 8;
+
+// Float copies of the rate constants the screen uses; SK_OK is 1 when all of them are
+// non-negative (the error bound assumes sums of non-negative factors in the reciprocals), else the
+// screen declines every iteration.
+enum ScreenConst {
+    SK_K12, SK_K21, SK_K23, SK_K32, SK_K34, SK_K43, SK_K45, SK_K54, SK_K56, SK_K65, SK_K25, SK_K52,
+    SK_KFCLCH, SK_KBCLCH, SK_GAM, SK_OK = SK_GAM + 5, SK_COUNT
+};
+__device__ __forceinline__ void load_screen_consts(float *sk, const CellStatic &s) {
+    const gw_params &p = s.p;
+    sk[SK_K12] = (float)p.k12; sk[SK_K21] = (float)p.k21; sk[SK_K23] = (float)p.k23; sk[SK_K32] = (float)p.k32;
+    sk[SK_K34] = (float)p.k34; sk[SK_K43] = (float)p.k43; sk[SK_K45] = (float)p.k45; sk[SK_K54] = (float)p.k54;
+    sk[SK_K56] = (float)p.k56; sk[SK_K65] = (float)p.k65; sk[SK_K25] = (float)p.k25; sk[SK_K52] = (float)p.k52;
+    sk[SK_KFCLCH] = (float)p.kfClCh; sk[SK_KBCLCH] = (float)p.kbClCh;
+    sk[SK_GAM + 0] = (float)s.gamma0; sk[SK_GAM + 1] = (float)s.gamma0a; sk[SK_GAM + 2] = (float)s.gamma0a2;
+    sk[SK_GAM + 3] = (float)s.gamma0a3; sk[SK_GAM + 4] = (float)s.gamma0a4;
+    bool ok = true;
+    for (int i = 0; i < SK_OK; ++i) ok = ok && sk[i] >= 0.f;
+    sk[SK_OK] = ok ? 1.f : 0.f;
+}
+
+// f = d with its significand truncated to 24 bits (|f - d| <= 2^-23 |d|), by integer operations
+// (an FP64 -> FP32 conversion would take the FP64 pipe); false unless d is zero or in the normal
+// FP32 range.
+__device__ __forceinline__ bool f32_trunc(double d, float &f) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+    const uint32_t e = (hi >> 20) & 0x7FFu;
+    const bool zero = (b << 1) == 0ull;
+    f = zero ? 0.f : __uint_as_float((hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
+    return zero || (e > 896u && e < 1151u);
+}
+
+// Signed byte j of a RyR plane word as a float: the byte, biased by 128, becomes the low byte of
+// the bit pattern of 2^23 + 128 + n.
+__device__ __forceinline__ float count_f(uint32_t w, int j) {
+    return __uint_as_float(__byte_perm(w ^ 0x80808080u, 0x4B000000u, (uint32_t)j | 0x7540u)) - 8388736.f;
+}
+
+// The 17 rates of subunit j as subunit_rates computes them (same regimes and formulas, FP32),
+// added to T and their magnitudes to A.  x: CaSS of the subunit (FP32), xb: its FP64 bits.
+template <typename R>
+__device__ __forceinline__ void screen_subunit(const Cru<R> &s, int j, float x, long long xb, const SsaConsts<R> &c,
+                                               const float *sk, const float *svf, float &T, float &A) {
+    const int st = byte_u(s.lcc, j);
+    const uint32_t w = c.lcct[st & 15];
+    float l0 = svf[w & 0xFFu], l1 = svf[(w >> 8) & 0xFFu], l2 = svf[(w >> 16) & 0xFFu];
+    const int kin = (int)(w >> 24);
+    if (kin < 3) {
+        const float gx = sk[SK_GAM + st - 1] * x;
+        if (kin == 1) l1 = gx; else l2 = gx;
+    }
+    const float inact = ((s.flags >> j) & 1u) == 0u ? svf[SV_INACT0] : svf[SV_INACT1];
+    const float clch = ((s.flags >> (4 + j)) & 1u) == 0u ? sk[SK_KFCLCH] * x : sk[SK_KBCLCH];
+    const float R0 = count_f(s.ryr[0], j), R1 = count_f(s.ryr[1], j), R2 = count_f(s.ryr[2], j);
+    const float R3 = count_f(s.ryr[3], j), R4 = count_f(s.ryr[4], j), R5 = count_f(s.ryr[5], j);
+    const float R23 = R2 + R3, R45 = R4 + R5;  // exact: small integers
+    const float x2 = x * x;
+    float r[12];
+    r[0] = R0 * sk[SK_K12] * x2;
+    r[1] = R1 * sk[SK_K23] * x2;
+    r[2] = R1 * sk[SK_K25] * x2;
+    r[6] = R1 * sk[SK_K21];
+    // x > 3.685e-2 and x > 1.15e-4 of the FP64 code, on the bit patterns
+    if (xb > __double_as_longlong(3.685e-2)) {
+        const float tau34 = __fdividef(1.f, sk[SK_K34] * x2 + sk[SK_K43]);
+        r[3] = 0.f;
+        r[4] = R23 * sk[SK_K45] * sk[SK_K34] * x2 * tau34;
+        r[7] = R23 * sk[SK_K32] * sk[SK_K43] * tau34;
+        r[8] = 0.f;
+    } else {
+        r[3] = R2 * sk[SK_K34] * x2;
+        r[4] = R3 * sk[SK_K45];
+        r[7] = R2 * sk[SK_K32];
+        r[8] = R3 * sk[SK_K43];
+    }
+    if (xb > __double_as_longlong(1.15e-4)) {
+        const float eq56 = __fdividef(sk[SK_K65], sk[SK_K56] * x2 + sk[SK_K65]);
+        r[5] = 0.f;
+        r[9] = R45 * sk[SK_K52] * eq56;
+        r[10] = R45 * sk[SK_K54] * x2 * eq56;
+        r[11] = 0.f;
+    } else {
+        r[5] = R4 * sk[SK_K56] * x2;
+        r[9] = R4 * sk[SK_K52];
+        r[10] = R4 * sk[SK_K54] * x2;
+        r[11] = R5 * sk[SK_K65];
+    }
+    T += ((l0 + l1) + (l2 + inact)) + clch;
+    A += ((fabsf(l0) + fabsf(l1)) + (fabsf(l2) + fabsf(inact))) + fabsf(clch);
+#pragma unroll
+    for (int q = 0; q < 12; ++q) {
+        T += r[q];
+        A += fabsf(r[q]);
+    }
+}
+
 template <typename R, bool EXACT>
 struct SsaLane {
     R t;          // time reached within the global step
@@ -733,14 +836,11 @@ struct SsaLane {
         }
     }
 
-    // One iteration of the event loop; true when the CRU's step is complete (the jump passed the
-    // end of the step, or the event cap was exceeded, which sets err).
-    __device__ __forceinline__ bool iterate(Cru<R> &s, const SsaConsts<R> &c, const R *sv, const float2 *tab,
-                                            Stream &rng, R dt, int cap, int &err, IterInfo<R> *info = nullptr) {
+    // update_fluxes (SSA.tpp:37-45): Jtr (kept in jtr), Jiss and Jxfer of the CRU's current state.
+    __device__ __forceinline__ void fluxes(const Cru<R> &s, const SsaConsts<R> &c, const R *sv, R (&jxfer)[4],
+                                           R (&jiss)[4]) {
         const R Cai = sv[SV_CAI], CaNSR = sv[SV_CANSR];
         const R Cai_lo = EXACT ? (R)0 : sv[SV_CAI_LO], CaNSR_lo = EXACT ? (R)0 : sv[SV_CANSR_LO];
-        R jxfer[4], jiss[4];
-        // update_fluxes (SSA.tpp:37-45)
         if (EXACT) {
             jtr = c.rtr * (CaNSR - s.cajsr);
         } else {
@@ -757,6 +857,14 @@ struct SsaLane {
             else
                 jxfer[j] = c.rxfer * ((s.cass[j] - Cai) - Cai_lo);
         }
+    }
+
+    // One iteration of the event loop; true when the CRU's step is complete (the jump passed the
+    // end of the step, or the event cap was exceeded, which sets err).
+    __device__ __forceinline__ bool iterate(Cru<R> &s, const SsaConsts<R> &c, const R *sv, const float2 *tab,
+                                            Stream &rng, R dt, int cap, int &err, IterInfo<R> *info = nullptr) {
+        R jxfer[4], jiss[4];
+        fluxes(s, c, sv, jxfer, jiss);
         // update_rates (SSA.tpp:48-56): only the subunit totals are kept here.
         R sub[4];
         const uint32_t iw = EXACT ? 0u : rate_index_word(s.lcc, s.flags);
@@ -778,7 +886,26 @@ struct SsaLane {
             jump = __fdividef(-logf((float)u0), (float)total);
         const bool last = !(t + jump < dt);
         const R h = last ? (dt - t) : jump;
+        return advance(s, c, sv, rng, h, last, jump, sub, total, jxfer, jiss, cap, err, info);
+    }
 
+    // The step's last iteration of a CRU whose jump is known to pass the end of the step (see
+    // surely_last): iterate() without the rate evaluation and the jump draw, which such an
+    // iteration does not use.  Same expressions in the same order, so the same results.
+    __device__ __forceinline__ void finish(Cru<R> &s, const SsaConsts<R> &c, const R *sv, Stream &rng, R dt,
+                                           IterInfo<R> *info = nullptr) {
+        R jxfer[4], jiss[4];
+        fluxes(s, c, sv, jxfer, jiss);
+        const R none[4] = {(R)0, (R)0, (R)0, (R)0};
+        int err = 0;
+        advance(s, c, sv, rng, dt - t, true, (R)0, none, (R)0, jxfer, jiss, 0, err, info);
+    }
+
+    // The iteration once its sub-step h is known: update_CaSS with its re-splits, the event choice
+    // (not on the last iteration), update_CaJSR and the transition.
+    __device__ __forceinline__ bool advance(Cru<R> &s, const SsaConsts<R> &c, const R *sv, Stream &rng, R h,
+                                            bool last, R jump, const R (&sub)[4], R total, const R (&jxfer)[4],
+                                            const R (&jiss)[4], int cap, int &err, IterInfo<R> *info) {
         // update_CaSS (SSA.tpp:87-99), first pass: new values and threshold crossings.
         R tmp[4];
         int kind[4];
@@ -853,6 +980,49 @@ struct SsaLane {
             return true;
         }
         return false;
+    }
+
+    // FP32 screen of the next FP64 iteration (EXACT, R = double): true only if that iteration is
+    // certainly the step's last, i.e. its jump -log(u0) / total passes dt - t.  An FP64 iteration
+    // spends most of its FP64 instructions on the 68 rates and the log and division of the jump
+    // time, which the last iteration does not otherwise use; an FP64 instruction takes a warp
+    // scheduler's FP64 pipe for ~64 cycles, an FP32 one for one or two.  The screen evaluates the
+    // rates in FP32 from CaSS truncated to FP32 and float copies of the constants (sk) and the
+    // step's SSA values (svf):
+    //   T = their sum, A = the sum of their magnitudes.  Every rate is a product of at most five
+    //   factors with at most one reciprocal, so it is within ~2e-6 of the FP64 rate relative to
+    //   itself; the sum adds at most 67 roundings of 2^-24 of A: |T - total| <= 7e-6 A.  The
+    //   regime tests (CaSS above 3.685e-2 and 1.15e-4) compare the FP64 bit patterns as integers,
+    //   which orders non-negative doubles exactly as the FP64 compare does, so both sides take the
+    //   same branches (a NaN fails the screen through T).
+    //   u0 = max(w >> 11, 1) 2^-53 <= ((w >> 40) + 1) 2^-24 = u_hi, exact in FP32.
+    // The FP64 iteration finds the jump past the end when -log(u0) >= total (dt - t) (1 + 1e-5)
+    // and total > 0: then jump = -log(u0) / total, both rounded to within a few ulp, exceeds the
+    // exact dt - t, and t + jump rounds to at least dt.  The screen asks for
+    //   T - 1e-4 A > 0  and  u_hi <= 0.9999 exp(-(T + 1e-4 A) h (1 + 2e-5)),
+    // h = dt - t truncated to FP32, with __expf's relative error (~4e-6 for arguments below 88)
+    // inside the 1e-4 margin.  It declines (and the FP64 iteration decides) in the few cases within
+    // those margins, and on every iteration that has an event.
+    __device__ __forceinline__ bool surely_last(const Cru<R> &s, const SsaConsts<R> &c, const float *sk,
+                                                const float *svf, Stream &rng, R dt) {
+        static_assert(sizeof(R) == 8 && EXACT, "the screen is for the FP64 lane");
+        float T = 0.f, A = 0.f;
+        bool ok = true;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const long long xb = __double_as_longlong(s.cass[j]);
+            float x;
+            ok &= f32_trunc(s.cass[j], x);
+            screen_subunit(s, j, x, xb, c, sk, svf, T, A);
+        }
+        uint32_t hi, lo;
+        rng.words(k, hi, lo);
+        const float u_hi = __uint2float_rn((hi >> 8) + 1u) * 0x1p-24f;
+        float h;
+        ok &= f32_trunc(dt - t, h);
+        const float Thi = fmaf(1e-4f, A, T), Tlo = fmaf(-1e-4f, A, T);
+        const float X = Thi * h * 1.00002f;
+        return ok && sk[SK_OK] != 0.f && Tlo > 0.f && u_hi <= __expf(-X) * 0.9999f;
     }
 };
 

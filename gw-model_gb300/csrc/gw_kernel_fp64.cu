@@ -34,7 +34,57 @@ __global__ void math_check_kernel(const double *x, int n, double *ex, double *lg
     ex[i] = math64::exp(x[i], T);
     lg[i] = math64::log(x[i], T);
 }
+// The FP64 lane's FP32 screen (SsaLane::surely_last) beside the FP64 iteration's own decision, for
+// n given CRU states, step values, times and step lengths (draw 0 of stream (seed, cell 0, CRU i,
+// step 0)): out[2i] the screen's verdict, out[2i+1] whether the FP64 iteration was the step's last,
+// jump[i] its jump time when it was not.
+__global__ void screen_check_kernel(const CellStatic *cs, int n, const uint32_t *chan, const double *cass,
+                                    const double *sv, const double *t, const double *dt, uint64_t seed, int *out,
+                                    double *jump) {
+    __shared__ SsaConsts<double> cc;
+    __shared__ float sk[SK_COUNT];
+    if (threadIdx.x == 0) {
+        load_ssa_consts<double>(cc, *cs);
+        load_screen_consts(sk, *cs);
+    }
+    __syncthreads();
+    const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= n) return;
+    Cru<double> c;
+    c.lcc = chan[8 * (int64_t)i];
+    c.flags = chan[8 * (int64_t)i + 1];
+    for (int q = 0; q < 6; ++q) c.ryr[q] = chan[8 * (int64_t)i + 2 + q];
+    for (int j = 0; j < 4; ++j) {
+        c.cass[j] = cass[4 * (int64_t)i + j];
+        c.jlcc[j] = 0.0;
+    }
+    c.cajsr = 1.0;
+    c.cajsr_lo = 0.f;
+    const double *svi = sv + (int64_t)kSvCount * i;
+    float svf[kSvCount];
+    for (int e = 0; e < kSvCount; ++e) svf[e] = (float)svi[e];
+    Stream rng;
+    rng.open(seed, 0u, (uint32_t)i, 0ull, 0u);
+    SsaLane<double, true> L;
+    L.begin(c, cc);
+    L.t = t[i];
+    const bool sc = L.surely_last(c, cc, sk, svf, rng, dt[i]);
+    IterInfo<double> f;
+    int err = 0;
+    L.iterate(c, cc, svi, nullptr, rng, dt[i], 1 << 30, err, &f);
+    out[2 * (int64_t)i] = sc ? 1 : 0;
+    out[2 * (int64_t)i + 1] = f.act == 0 ? 1 : 0;
+    jump[i] = f.act == 0 ? 0.0 : f.h;
+}
 }  // namespace dev
+
+int screen_check_dev(const CellStatic *cs, int n, const uint32_t *chan, const double *cass, const double *sv,
+                     const double *t, const double *dt, uint64_t seed, int *out, double *jump) {
+    if (n <= 0) return 0;
+    const int threads = 128;
+    dev::screen_check_kernel<<<(n + threads - 1) / threads, threads>>>(cs, n, chan, cass, sv, t, dt, seed, out, jump);
+    return (int)cudaGetLastError();
+}
 
 int math_check_dev(const double *x, int n, double *ex, double *lg) {
     if (n <= 0) return 0;

@@ -125,6 +125,8 @@ _SIGS = {
     "gw_autotune": ([_P(GwEnsembleDesc), C.c_int, _P(C.c_int), _P(C.c_int), _P(C.c_double)], C.c_int),
     "gw_default_shape": ([_P(GwEnsembleDesc), _P(C.c_int), _P(C.c_int)], C.c_int),
     "gw_math_check": ([_P(C.c_double), C.c_int64, _P(C.c_double), _P(C.c_double)], C.c_int),
+    "gw_screen_check": ([_P(GwParams), C.c_int, C.c_int64, _P(C.c_uint32), _P(C.c_double), _P(C.c_double),
+                         _P(C.c_double), _P(C.c_double), C.c_uint64, _P(C.c_int32), _P(C.c_double)], C.c_int),
     "gw_get_time": ([C.c_void_p, C.c_int, _P(C.c_double), _P(C.c_uint64)], C.c_int),
     "gw_set_time": ([C.c_void_p, C.c_int, C.c_double, C.c_uint64], C.c_int),
     "gw_get_stats": ([C.c_void_p, _P(GwStats)], C.c_int),

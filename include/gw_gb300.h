@@ -267,6 +267,18 @@ int gw_run_noalloc(gw_ctx *ctx, double dt, int64_t n_steps, int record_every, gw
  * error against a reference libm can be checked. */
 int gw_math_check(const double *x, int64_t n, double *exp_out, double *log_out);
 
+/* Diagnostic, no counterpart in the reference: the FP32 screen that lets the FP64 SSA lane skip
+ * the FP64 rates of an iteration that is certainly the step's last, beside the FP64 iteration's
+ * own decision, for n CRU states on the current device.  Per case i: chan[8i..8i+7] = LCC states,
+ * flags, RyR planes 0-5 (the engine's packing, gw_get_crus' words); cass[4i..4i+3]; sv[40i..40i+39]
+ * the step's SSA values (index 0 must be 0); t[i] the time reached within the step; dt[i] the step.
+ * The draw is draw 0 of the stream (seed, cell 0, CRU i, step 0).  out[2i] = 1 if the screen
+ * declared the iteration last, out[2i+1] = 1 if the FP64 iteration was last; jump[i] its jump
+ * time when it was not (else 0).  The screen is sound if out[2i] = 1 implies out[2i+1] = 1. */
+int gw_screen_check(const gw_params *p, int nCRU, int64_t n, const uint32_t *chan, const double *cass,
+                    const double *sv, const double *t, const double *dt, uint64_t seed, int32_t *out,
+                    double *jump);
+
 int gw_get_time(gw_ctx *ctx, int cell, double *t, uint64_t *step);
 /* Restores a cell's accumulated time and global step index (the RNG counter).  With the globals,
  * the CRU arrays including JLCC, and the flux carry, this resumes a run bit for bit; the reference
