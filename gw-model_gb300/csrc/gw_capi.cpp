@@ -27,6 +27,7 @@ namespace {
 constexpr double kFaraday = 96.5;   // common.hpp:9
 constexpr double kGasConst = 8.314; // common.hpp:10
 constexpr int kMaxSsaWarps = 12;    // + kOdeWarps ODE warps = 512 threads per CTA
+constexpr int kMaxSsaWarpsFp64 = 4; // FP64: + kOdeWarps = 256 threads (the FP64 engine's launch bound)
 
 thread_local std::string g_create_error;
 // cudaMalloc calls of this library in this process (gw_stats.device_allocs); every device
@@ -223,7 +224,7 @@ int plan_shape(gw_ctx *c, int cluster_req, int tile_req) {
     if (need > C)
         return fail(c, GW_ERR_UNSUPPORTED, "a cell of %d CRUs needs %d CTAs of %d CRUs but the cluster has %d",
                     max_n, need, tile, C);
-    c->ssa_warps = std::min(kMaxSsaWarps, tile / 32);
+    c->ssa_warps = std::min(c->precision == GW_PRECISION_FP64 ? kMaxSsaWarpsFp64 : kMaxSsaWarps, tile / 32);
     c->tile_cap = tile;
     // Pack cells (first-fit decreasing on CTA count) into clusters of C CTAs.
     std::vector<int> order(c->n_cells);

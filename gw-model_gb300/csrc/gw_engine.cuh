@@ -42,6 +42,7 @@ struct OdeShared {
 };
 
 constexpr int kMaxThreads = 512;  // SSA warps + ODE warps per CTA (128 registers per thread)
+constexpr int kMaxThreadsFp64 = 256;  // FP64 instance: at most 4 SSA warps, up to 255 registers
 constexpr int kMaxWarps = kMaxThreads / 32;
 
 struct SmemLayout {
@@ -929,7 +930,7 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
 // CTA and the SSA warps.  Both parts end with one more cluster barrier, so that no CTA exits
 // while another may still write into its shared memory.
 template <bool FP64, bool ODE64>
-__global__ void __launch_bounds__(kMaxThreads, 1) engine_kernel(const __grid_constant__ KernelArgs a) {
+__global__ void __launch_bounds__(FP64 ? kMaxThreadsFp64 : kMaxThreads, 1) engine_kernel(const __grid_constant__ KernelArgs a) {
     using R = typename std::conditional<FP64, double, float>::type;
     const CtaView<FP64, ODE64> v(a);
     // The partials' mbarriers (one arrival per phase: the ODE thread's expect_tx) are initialised

@@ -137,8 +137,10 @@ def test_fp64_launch_shape_independent(oracle, shape):
 
 def test_fp64_leader_with_and_without_ssa(oracle):
     """A cell over several CTAs of at least 1,024 CRUs each keeps SSA work on its leader CTA (the
-    split 12 : 16 warps); thinner cells give the leader none (the other parity cases).  Both are the
-    oracle's trajectory: 2,400 CRUs over two CTAs of up to 1,216."""
+    split 4 : 8 warps, FP64 CTAs having at most 4 SSA warps); thinner cells give the leader none (the
+    other parity cases).  Both are the oracle's trajectory: 2,400 CRUs over two CTAs of up to 1,216,
+    i.e. ~200 CRUs per SSA warp, which takes the FP64 lane's screened and deferred iterations over
+    several passes."""
     m, (g, s, st) = run_pair(oracle, 2400, 300, 6, "fp64", cluster_ctas=2, cta_crus=1216)
     assert st["ctas"] == 2
     for k in CHANNELS:
