@@ -380,48 +380,94 @@ __global__ void __launch_bounds__(kBlk, VAR ? 1 : kSsaBlocksPerSm) k_ssa(const G
     // CRUs left, then they run the FP64 iteration together.
     __syncthreads();
     const int nq = min(qn, kQCap);
-    const int nwu = min(nw, (nq + 31) >> 5);
-    if (warp < nwu) {
-        int qc = (int)((int64_t)nq * warp / nwu);
-        const int qe = (int)((int64_t)nq * (warp + 1) / nwu);
-        m = -1;
-        bool pend = false;  // the lane's next iteration needs the FP64 rates
-        for (;;) {
-            const unsigned need = __ballot_sync(0xffffffffu, m == -1);
-            if (need) {
-                const int nm = qc + __popc(need & ((1u << lane) - 1u));
-                qc += __popc(need);
-                if (m == -1) {
-                    if (nm < qe) {
-                        m = q[nm];
-                        fetch(m, false);
-                        pend = true;
+    if constexpr (!VAR) {
+        // Four lanes per queued CRU (SsaLane::iterate_group: one subunit's rates per lane), eight
+        // CRUs per warp at a time: the queue is the tail of the block's step, so its FP64
+        // iterations are taken at a third of their single-lane latency.
+        const int j = lane & 3, base = lane & ~3;
+        const int nwu = min(nw, (nq + 7) >> 3);
+        if (warp < nwu) {
+            int qc = (int)((int64_t)nq * warp / nwu);
+            const int qe = (int)((int64_t)nq * (warp + 1) / nwu);
+            m = -1;
+            bool first = false;  // the CRU's first iteration (declined by the screen in pass 1)
+            for (;;) {
+                const unsigned need = __ballot_sync(0xffffffffu, m == -1 && j == 0);
+                if (need) {
+                    const int nm = qc + __popc(need & ((1u << base) - 1u));
+                    qc += __popc(need);
+                    if (m == -1) {
+                        if (nm < qe) {
+                            m = q[nm];
+                            fetch(m, false);
+                            first = true;
+                        } else {
+                            m = -2;
+                        }
+                    }
+                }
+                if (!__any_sync(0xffffffffu, m >= 0)) break;
+                if (m >= 0) {
+                    bool done;
+                    if (!first && L.surely_last(c, cc, sk, svf, rng, a.dt)) {
+                        L.finish(c, cc, sv, rng, a.dt);
+                        done = true;
                     } else {
-                        m = -2;
+                        done = L.iterate_group(c, cc, sv, rng, a.dt, a.event_cap, err);
+                    }
+                    first = false;
+                    if (done) {
+                        if (j == 0) after(m, dev::IterInfo<double>{}, 0u, 0u, true);
+                        m = -1;
                     }
                 }
             }
-            if (!__any_sync(0xffffffffu, m >= 0)) break;
-            const uint32_t lcc0 = c.lcc, fl0 = c.flags;
-            dev::IterInfo<double> f;
-            bool ran = false, done = false;
-            if (m >= 0 && !pend) {
-                if (L.surely_last(c, cc, sk, svf, rng, a.dt)) {
-                    L.finish(c, cc, sv, rng, a.dt, var ? &f : nullptr);
-                    ran = done = true;
-                } else {
-                    pend = true;
+        }
+    }
+    if constexpr (VAR) {
+        const int nwu = min(nw, (nq + 31) >> 5);
+        if (warp < nwu) {
+            int qc = (int)((int64_t)nq * warp / nwu);
+            const int qe = (int)((int64_t)nq * (warp + 1) / nwu);
+            m = -1;
+            bool pend = false;  // the lane's next iteration needs the FP64 rates
+            for (;;) {
+                const unsigned need = __ballot_sync(0xffffffffu, m == -1);
+                if (need) {
+                    const int nm = qc + __popc(need & ((1u << lane) - 1u));
+                    qc += __popc(need);
+                    if (m == -1) {
+                        if (nm < qe) {
+                            m = q[nm];
+                            fetch(m, false);
+                            pend = true;
+                        } else {
+                            m = -2;
+                        }
+                    }
                 }
-            }
-            const unsigned pm = __ballot_sync(0xffffffffu, pend);
-            if (pm && (qc >= qe || __popc(pm) >= dev::kDefer) && pend) {
-                done = L.iterate(c, cc, sv, nullptr, rng, a.dt, a.event_cap, err, var ? &f : nullptr);
-                ran = true;
-                pend = false;
-            }
-            if (ran) {
-                after(m, f, lcc0, fl0, done);
-                if (done) m = -1;
+                if (!__any_sync(0xffffffffu, m >= 0)) break;
+                const uint32_t lcc0 = c.lcc, fl0 = c.flags;
+                dev::IterInfo<double> f;
+                bool ran = false, done = false;
+                if (m >= 0 && !pend) {
+                    if (L.surely_last(c, cc, sk, svf, rng, a.dt)) {
+                        L.finish(c, cc, sv, rng, a.dt, var ? &f : nullptr);
+                        ran = done = true;
+                    } else {
+                        pend = true;
+                    }
+                }
+                const unsigned pm = __ballot_sync(0xffffffffu, pend);
+                if (pm && (qc >= qe || __popc(pm) >= dev::kDefer) && pend) {
+                    done = L.iterate(c, cc, sv, nullptr, rng, a.dt, a.event_cap, err, var ? &f : nullptr);
+                    ran = true;
+                    pend = false;
+                }
+                if (ran) {
+                    after(m, f, lcc0, fl0, done);
+                    if (done) m = -1;
+                }
             }
         }
     }

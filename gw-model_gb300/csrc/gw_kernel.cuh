@@ -607,13 +607,23 @@ __device__ __forceinline__ int crossing(const Cru<R> &s, int j, R x, R x_new, ui
 // the iteration with draws kk, kk+1, kk+2: act 1 LCC, 2 inactivation toggle, 3 RyR, 4 ClCh
 // toggle; aj the subunit, atr the transition.
 template <typename R, bool EXACT>
+__device__ __forceinline__ void select_transition(const Rates<R> &r, R subr, Stream &rng, uint32_t &kk, int &act,
+                                                  int &atr);
+template <typename R, bool EXACT>
 __device__ __forceinline__ void select_event(const Cru<R> &s, const SsaConsts<R> &c, const R *sv, const R (&sub)[4],
                                              R total, Stream &rng, uint32_t &kk, int &act, int &aj, int &atr) {
     const R us = rng.uniform<R>(kk++) * total;
     aj = scan_weights<R, 4, !EXACT>(sub, us);
     Rates<R> r;
     const R sr = subunit_rates<R>(s, aj, pick4(s.cass, aj), c, sv, r);
-    const R subr = EXACT ? pick4(sub, aj) : sr;
+    select_transition<R, EXACT>(r, EXACT ? pick4(sub, aj) : sr, rng, kk, act, atr);
+}
+
+// sample_new_state's choice within subunit aj (SSA.tpp:262-283) from its rates r and total subr,
+// with draws kk, kk+1: act 1 LCC, 2 inactivation toggle, 3 RyR, 4 ClCh toggle; atr the transition.
+template <typename R, bool EXACT>
+__device__ __forceinline__ void select_transition(const Rates<R> &r, R subr, Stream &rng, uint32_t &kk, int &act,
+                                                  int &atr) {
     const R sum_lcc = r.lcc[0] + r.lcc[1] + r.lcc[2];
     R sum_ryr;
     if (EXACT) {
@@ -901,32 +911,38 @@ struct SsaLane {
         advance(s, c, sv, rng, dt - t, true, (R)0, none, (R)0, jxfer, jiss, 0, err, info);
     }
 
+    // update_CaSS (SSA.tpp:87-99), first pass, for subunit j: its new CaSS (tmp_j) and threshold
+    // crossing (kind_j; a positive count of the re-split pair adds its draws to D).
+    __device__ __forceinline__ void cass_update(const Cru<R> &s, const SsaConsts<R> &c, int j, R h,
+                                                const R (&jxfer)[4], const R (&jiss)[4], R &tmp_j, int &kind_j,
+                                                uint32_t &D) const {
+        // (pick4: j may be a lane's own subunit, and a register array indexed by a value known only
+        // at run time would go to local memory)
+        const R x = pick4(s.cass, j);
+        R beta;
+        if (EXACT) {
+            beta = (R)1.0 / ((R)1 + (c.BSR_const / ((c.KBSR + x) * (c.KBSR + x))) +
+                             (c.BSL_const / ((c.KBSL + x) * (c.KBSL + x))));
+        } else {
+            const R u = (c.KBSR + x) * (c.KBSR + x), v = (c.KBSL + x) * (c.KBSL + x);
+            const R uv = u * v;
+            beta = __fdividef((float)uv, (float)(uv + c.BSR_const * v + c.BSL_const * u));
+        }
+        const R d = h * (pick4(s.jlcc, j) + pick4(jrel, j) - pick4(jxfer, j) + pick4(jiss, j)) * beta;
+        tmp_j = x + d;
+        kind_j = crossing<R>(s, j, x, tmp_j, D);
+    }
+
     // The iteration once its sub-step h is known: update_CaSS with its re-splits, the event choice
     // (not on the last iteration), update_CaJSR and the transition.
     __device__ __forceinline__ bool advance(Cru<R> &s, const SsaConsts<R> &c, const R *sv, Stream &rng, R h,
                                             bool last, R jump, const R (&sub)[4], R total, const R (&jxfer)[4],
                                             const R (&jiss)[4], int cap, int &err, IterInfo<R> *info) {
-        // update_CaSS (SSA.tpp:87-99), first pass: new values and threshold crossings.
         R tmp[4];
         int kind[4];
         uint32_t D = 0;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const R x = s.cass[j];
-            R beta;
-            if (EXACT) {
-                beta = (R)1.0 / ((R)1 + (c.BSR_const / ((c.KBSR + x) * (c.KBSR + x))) +
-                                 (c.BSL_const / ((c.KBSL + x) * (c.KBSL + x))));
-            } else {
-                const R u = (c.KBSR + x) * (c.KBSR + x), v = (c.KBSL + x) * (c.KBSL + x);
-                const R uv = u * v;
-                beta = __fdividef((float)uv, (float)(uv + c.BSR_const * v + c.BSL_const * u));
-            }
-            const R d = h * (s.jlcc[j] + jrel[j] - jxfer[j] + jiss[j]) * beta;
-            tmp[j] = x + d;
-            kind[j] = crossing<R>(s, j, x, tmp[j], D);
-        }
-
+        for (int j = 0; j < 4; ++j) cass_update(s, c, j, h, jxfer, jiss, tmp[j], kind[j], D);
         // Event selection from the rates of the start of this iteration, draws k+D+1, k+D+2, k+D+3.
         uint32_t kk = k + 1u + D;
         int act = 0, aj = 0, atr = 0;
@@ -934,12 +950,18 @@ struct SsaLane {
             t += jump;
             select_event<R, EXACT>(s, c, sv, sub, total, rng, kk, act, aj, atr);
         }
-        // update_CaSS second pass, then commit.
+        return conclude(s, c, sv, rng, h, last, tmp, kind, D, kk, act, aj, atr, jxfer, cap, err, info);
+    }
+
+    // The iteration's end: update_CaSS's second pass and commit, update_CaJSR (SSA.hpp:68-71), the
+    // transition, and the loop state.
+    __device__ __forceinline__ bool conclude(Cru<R> &s, const SsaConsts<R> &c, const R *sv, Stream &rng, R h,
+                                             bool last, const R (&tmp)[4], const int (&kind)[4], uint32_t D,
+                                             uint32_t kk, int act, int aj, int atr, const R (&jxfer)[4], int cap,
+                                             int &err, IterInfo<R> *info) {
         if (D > 0 || kind[0] || kind[1] || kind[2] || kind[3]) resplit_crossed<R>(s, c, kind, rng, k);
 #pragma unroll
         for (int j = 0; j < 4; ++j) s.cass[j] = tmp[j];
-
-        // update_CaJSR (SSA.hpp:68-71)
         {
             const R x = s.cajsr;
             R beta;
@@ -963,7 +985,6 @@ struct SsaLane {
                 s.cajsr_lo = err_;
             }
         }
-
         // Apply the transition to the updated state.
         if (act != 0) apply_event<R>(s, c, sv, act, aj, atr, jrel);
         if (info) {
@@ -980,6 +1001,62 @@ struct SsaLane {
             return true;
         }
         return false;
+    }
+
+    // iterate() by the four lanes of a group (lanes 4g .. 4g+3 of the warp, every one holding the
+    // same CRU and lane state; EXACT, R = double): lane j = lane & 3 evaluates the 17 rates and the
+    // CaSS update of subunit j, the group exchanges them by shuffles, and the rest runs on the four
+    // lanes alike.  Same expressions in the same order as iterate(), hence the same results on every
+    // lane; an FP64 warp instruction costs the same whatever its active lanes, so the iteration takes
+    // about a third of the FP64 instructions of one lane's.  The four lanes must call it together.
+    __device__ __forceinline__ bool iterate_group(Cru<R> &s, const SsaConsts<R> &c, const R *sv, Stream &rng, R dt,
+                                                  int cap, int &err) {
+        static_assert(sizeof(R) == 8 && EXACT, "the group iteration is for the FP64 lane");
+        const int lane = (int)(threadIdx.x & 31u), j = lane & 3, base = lane & ~3;
+        const unsigned gm = 0xFu << base;
+        R jxfer[4], jiss[4];
+        fluxes(s, c, sv, jxfer, jiss);
+        Rates<R> rj;
+        const R sj = subunit_rates<R>(s, j, pick4(s.cass, j), c, sv, rj);
+        R sub[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) sub[q] = __shfl_sync(gm, sj, base + q);
+        const R total = sub[0] + sub[1] + sub[2] + sub[3];
+        const R u0 = rng.uniform<R>(k);
+        const R jump = -log(u0) / total;
+        const bool last = !(t + jump < dt);
+        const R h = last ? (dt - t) : jump;
+        R tj;
+        int kj;
+        uint32_t Dj = 0;
+        cass_update(s, c, j, h, jxfer, jiss, tj, kj, Dj);
+        R tmp[4];
+        int kind[4];
+        uint32_t D = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            tmp[q] = __shfl_sync(gm, tj, base + q);
+            kind[q] = __shfl_sync(gm, kj, base + q);
+            D += __shfl_sync(gm, Dj, base + q);
+        }
+        uint32_t kk = k + 1u + D;
+        int act = 0, aj = 0, atr = 0;
+        if (!last) {
+            t += jump;
+            // select_event with the drawn subunit's rates from its lane
+            const R us = rng.uniform<R>(kk++) * total;
+            aj = scan_weights<R, 4, false>(sub, us);
+            const int src = base + aj;
+            Rates<R> r;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) r.lcc[q] = __shfl_sync(gm, rj.lcc[q], src);
+            r.inact = __shfl_sync(gm, rj.inact, src);
+#pragma unroll
+            for (int q = 0; q < 12; ++q) r.ryr[q] = __shfl_sync(gm, rj.ryr[q], src);
+            r.clch = __shfl_sync(gm, rj.clch, src);
+            select_transition<R, true>(r, pick4(sub, aj), rng, kk, act, atr);
+        }
+        return conclude(s, c, sv, rng, h, last, tmp, kind, D, kk, act, aj, atr, jxfer, cap, err, nullptr);
     }
 
     // FP32 screen of the next FP64 iteration (EXACT, R = double): true only if that iteration is
