@@ -46,8 +46,12 @@ constexpr int kMaxThreadsFp64 = 256;  // FP64 instance: at most 4 SSA warps, up 
 constexpr int kMaxWarps = kMaxThreads / 32;
 
 struct SmemLayout {
-    size_t cc, sv, ode, prog, x, math, svs, rtab, part, mbar, tile, total;
+    size_t cc, sv, ode, prog, x, math, svs, rtab, part, mbar, fq, tile, total;
 };
+
+// FP64: CRUs of a CTA whose first iteration of a step waits for the four-lane pass (the queue
+// holds their tile indices; a CTA with more such CRUs in a step runs the rest on their own lanes).
+constexpr int kEngQCap = 256;
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
@@ -75,6 +79,8 @@ __host__ __device__ inline SmemLayout smem_layout(int tile_cap, int max_cta_cell
     o += align16((size_t)2 * max_cta_cell * kMaxWarps * sizeof(Partial));
     L.mbar = o;  // mbarriers: the warp partials of steps of parity 0 and 1 (leader CTA), then the
     o += 32;     // per-step SSA values of parity 0 and 1 (every CTA)
+    L.fq = o;    // FP64: the queue's two counters (by step parity), then kEngQCap tile indices
+    o += sizeof(R) == 8 ? align16((size_t)(4 + kEngQCap) * sizeof(int)) : 0;
     L.tile = o;  // TileRec<R> per CRU
     o += align16((size_t)tile_cap * sizeof(TileRec<R>));
     L.total = o;
@@ -505,6 +511,7 @@ struct CtaView {
     void *svstage;
     Partial *part;
     float2 *rtab;
+    int *fq;        // FP64: queue counters [2] (+2 unused), then the queue
     uint32_t mbar;  // shared address of the partials' mbarrier of parity 0 (parity 1 at +8); the
                     // SSA values' mbarriers of parity 0 and 1 at +16 and +24
     TileRec<R> *tile;
@@ -531,6 +538,7 @@ struct CtaView {
         svstage = smem + L.svs;
         part = reinterpret_cast<Partial *>(smem + L.part);
         rtab = reinterpret_cast<float2 *>(smem + L.rtab);
+        fq = reinterpret_cast<int *>(smem + L.fq);
         mbar = smem_addr(smem + L.mbar);
         tile = reinterpret_cast<TileRec<R> *>(smem + L.tile);
         off = OdeOffsets{(uint32_t)L.prog, (uint32_t)L.x, (uint32_t)L.ode, (uint32_t)L.math, (uint32_t)L.svs};
@@ -796,62 +804,146 @@ __device__ __forceinline__ void ssa_warps(const KernelArgs &a, uint64_t step0) {
             Cru<R> c;
             SsaLane<R, EXACT> sl;
             Stream rng;
-            int m = -1;         // CRU of this lane; -1 none yet, -2 none left
-            bool pend = false;  // FP64: the lane's next iteration needs the FP64 rates
-            for (;;) {
-                const unsigned need = __ballot_sync(0xffffffffu, m == -1);
-                if (need) {
-                    const int nm = cursor + __popc(need & ((1u << lane) - 1u));
-                    cursor += __popc(need);
-                    if (m == -1) {
-                        if (nm < end) {
-                            m = nm;
-                            tile_get(c, tile[m]);
-                            rng.open(a.seed, (uint32_t)(a.cell_base + cell), (uint32_t)(w.cru_begin + m), step0 + s, 0);
-                            sl.begin(c, cc);
-                        } else {
-                            m = -2;
+            int m = -1;  // CRU of this lane; -1 none yet, -2 none left
+            if constexpr (FP64) {
+                // Pass 1: the warp's CRUs, one iteration per lane and pass.  An iteration that the
+                // FP32 screen shows to be the step's last runs without the FP64 rates (finish); a
+                // CRU whose first iteration it declines (an event in the step) goes, untouched in
+                // the tile, to the CTA's queue, and its lane takes the next CRU.
+                int *qn = v.fq + par;
+                int *q = v.fq + 4;
+                if (threadIdx.x == 0) v.fq[par ^ 1] = 0;  // step s-1's count: every reader has passed
+                                                          // bar_or(2) of this step
+                bool fresh = false;
+                for (;;) {
+                    const unsigned need = __ballot_sync(0xffffffffu, m == -1);
+                    if (need) {
+                        const int nm = cursor + __popc(need & ((1u << lane) - 1u));
+                        cursor += __popc(need);
+                        if (m == -1) {
+                            if (nm < end) {
+                                m = nm;
+                                tile_get(c, tile[m]);
+                                rng.open(a.seed, (uint32_t)(a.cell_base + cell), (uint32_t)(w.cru_begin + m),
+                                         step0 + s, 0);
+                                sl.begin(c, cc);
+                                fresh = true;
+                            } else {
+                                m = -2;
+                            }
                         }
                     }
-                }
-                if (!__any_sync(0xffffffffu, m >= 0)) break;
-                if constexpr (FP64) {
-                    // One iteration per lane and pass: an iteration that the FP32 screen shows to be
-                    // the step's last runs without the FP64 rates (finish); the others wait (pend)
-                    // until kDefer lanes of the warp wait or the warp has no CRUs left to take, and
-                    // then run the FP64 iteration together.
-                    int err = 0;
-                    bool done = false;
-                    if (m >= 0 && !pend) {
+                    if (!__any_sync(0xffffffffu, m >= 0)) break;
+                    if (m >= 0) {
+                        int err = 0;
+                        bool done = false;
                         if (sl.surely_last(c, cc, sk, svf, rng, dt)) {
                             sl.finish(c, cc, sv, rng, dt);
                             done = true;
                         } else {
-                            pend = true;
+                            const int qs = fresh ? atomicAdd(qn, 1) : kEngQCap;
+                            if (qs < kEngQCap) {
+                                q[qs] = m;
+                                m = -1;
+                            } else {  // the queue is full, or the CRU is past its first iteration
+                                done = sl.iterate(c, cc, sv, rtab, rng, dt, a.event_cap, err);
+                            }
+                        }
+                        fresh = false;
+                        if (done) {
+                            tile_put(tile[m], c);
+                            my_events += (unsigned long long)sl.ev;
+                            my_err |= err;
+                            acc.add(c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3], sl.jxfer_sum, sl.jtr,
+                                    __popc((c.flags >> 4) & 0xFu));
+                            m = -1;
                         }
                     }
-                    const unsigned pm = __ballot_sync(0xffffffffu, pend);
-                    if (pm && (cursor >= end || __popc(pm) >= kDefer) && pend) {
-                        done = sl.iterate(c, cc, sv, rtab, rng, dt, a.event_cap, err);
-                        pend = false;
+                }
+                // Pass 2: the queued CRUs on four lanes each (SsaLane::iterate_group: one subunit's
+                // rates per lane), eight per warp at a time, over the CTA's SSA warps.
+                ssa_bar(n_ssa);
+                const int nq = min(*qn, kEngQCap);
+                const int jq = lane & 3, base = lane & ~3;
+                const int nwu = min(nsw, (nq + 7) >> 3);
+                if (warp < nwu) {
+                    int qc = (int)((int64_t)nq * warp / nwu);
+                    const int qe = (int)((int64_t)nq * (warp + 1) / nwu);
+                    m = -1;
+                    bool first = false;
+                    for (;;) {
+                        const unsigned need = __ballot_sync(0xffffffffu, m == -1 && jq == 0);
+                        if (need) {
+                            const int nm = qc + __popc(need & ((1u << base) - 1u));
+                            qc += __popc(need);
+                            if (m == -1) {
+                                if (nm < qe) {
+                                    m = q[nm];
+                                    tile_get(c, tile[m]);
+                                    rng.open(a.seed, (uint32_t)(a.cell_base + cell), (uint32_t)(w.cru_begin + m),
+                                             step0 + s, 0);
+                                    sl.begin(c, cc);
+                                    first = true;
+                                } else {
+                                    m = -2;
+                                }
+                            }
+                        }
+                        if (!__any_sync(0xffffffffu, m >= 0)) break;
+                        if (m >= 0) {
+                            int err = 0;
+                            bool done;
+                            if (!first && sl.surely_last(c, cc, sk, svf, rng, dt)) {
+                                sl.finish(c, cc, sv, rng, dt);
+                                done = true;
+                            } else {
+                                done = sl.iterate_group(c, cc, sv, rng, dt, a.event_cap, err);
+                            }
+                            first = false;
+                            if (done) {
+                                if (jq == 0) {
+                                    tile_put(tile[m], c);
+                                    my_events += (unsigned long long)sl.ev;
+                                    my_err |= err;
+                                    acc.add(c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3], sl.jxfer_sum, sl.jtr,
+                                            __popc((c.flags >> 4) & 0xFu));
+                                }
+                                m = -1;
+                            }
+                        }
                     }
-                    if (done) {
-                        tile_put(tile[m], c);
-                        my_events += (unsigned long long)sl.ev;
-                        my_err |= err;
-                        acc.add(c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3], sl.jxfer_sum, sl.jtr,
-                                __popc((c.flags >> 4) & 0xFu));
-                        m = -1;
+                }
+                // the records read the warps' tile ranges, which pass 2 may have written elsewhere
+                if (rec_ok && (cell == a.tr_cell || a.tr_sums != nullptr)) ssa_bar(n_ssa);
+            } else {
+                for (;;) {
+                    const unsigned need = __ballot_sync(0xffffffffu, m == -1);
+                    if (need) {
+                        const int nm = cursor + __popc(need & ((1u << lane) - 1u));
+                        cursor += __popc(need);
+                        if (m == -1) {
+                            if (nm < end) {
+                                m = nm;
+                                tile_get(c, tile[m]);
+                                rng.open(a.seed, (uint32_t)(a.cell_base + cell), (uint32_t)(w.cru_begin + m),
+                                         step0 + s, 0);
+                                sl.begin(c, cc);
+                            } else {
+                                m = -2;
+                            }
+                        }
                     }
-                } else if (m >= 0) {
-                    int err = 0;
-                    if (sl.iterate(c, cc, sv, rtab, rng, dt, a.event_cap, err)) {
-                        tile_put(tile[m], c);
-                        my_events += (unsigned long long)sl.ev;
-                        my_err |= err;
-                        acc.add(c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3], sl.jxfer_sum, sl.jtr,
-                                __popc((c.flags >> 4) & 0xFu));
-                        m = -1;
+                    if (!__any_sync(0xffffffffu, m >= 0)) break;
+                    if (m >= 0) {
+                        int err = 0;
+                        if (sl.iterate(c, cc, sv, rtab, rng, dt, a.event_cap, err)) {
+                            tile_put(tile[m], c);
+                            my_events += (unsigned long long)sl.ev;
+                            my_err |= err;
+                            acc.add(c.jlcc[0] + c.jlcc[1] + c.jlcc[2] + c.jlcc[3], sl.jxfer_sum, sl.jtr,
+                                    __popc((c.flags >> 4) & 0xFu));
+                            m = -1;
+                        }
                     }
                 }
             }
@@ -948,7 +1040,11 @@ __global__ void __launch_bounds__(FP64 ? kMaxThreadsFp64 : kMaxThreads, 1) engin
             load_ssa_consts<R>(*v.cc, a.cs[cell]);
             // FP64: the screen's constants (SsaLane::surely_last) in the rate-table area, which the
             // FP64 lane does not otherwise use: floats 64.. of parity 0's table
-            if (FP64) load_screen_consts(reinterpret_cast<float *>(v.rtab) + 64, a.cs[cell]);
+            if (FP64) {
+                load_screen_consts(reinterpret_cast<float *>(v.rtab) + 64, a.cs[cell]);
+                v.fq[0] = 0;
+                v.fq[1] = 0;
+            }
         }
         // The leader's warp-partial slots start at zero (slots of warps a CTA does not have stay
         // so); the cell's CTAs write them only after the first cluster barrier of the steps.
